@@ -1,0 +1,186 @@
+/*
+ * so4_gb300.h -- C ABI of the GB300-native SO(4)/SNAP bispectrum path.
+ *
+ * Replaces the numeric core of PyXtal_FF's descriptor
+ *   pyxtal_ff/descriptors/SO4.py   SO4_Bispectrum.calculate          :171-209
+ *                                  build_neighbor_list                :211-287
+ *                                  get_bispectrum_components          :1256-1730
+ *   pyxtal_ff/descriptors/SNAP.py  (same, weights / rfac0 variant)   :200-1762
+ * and the contraction its consumers apply to dxdr / rdxdr
+ *   pyxtal_ff/models/neuralnetwork.py:492 (forces), :497,:677-678 (stress).
+ *
+ * Conventions
+ *  - Every entry point returns an int status (enum so4_status); nothing throws
+ *    across the ABI.  Device-side failures are reported through a status word
+ *    in the caller's workspace, read back by so4_status_read().
+ *  - Pointers named d_* are device pointers; h_* are host pointers.  All device
+ *    buffers are allocated by the caller.  No entry point allocates device
+ *    memory except so4_tables_create (the constant tables it owns).
+ *  - `stream` is a cudaStream_t passed as void*.  Every launch is ordered on it;
+ *    no entry point synchronises the host except so4_tables_create/destroy.
+ *  - Atoms of many structures are concatenated; a structure's atoms are
+ *    contiguous.  Every atom is a centre (the reference's atom_ids prefix is a
+ *    slice of the outputs).  seq rows hold structure-local atom indices, as
+ *    the reference's seq does.
+ *  - "half layout": for each 2j = l in 0..twol the rows mb = 0..floor(l/2) of
+ *    the (l+1)x(l+1) Wigner-U block, all l+1 columns, stored as (re, im).
+ *    idxu_half entries in total (155 at twol = 8).
+ */
+#ifndef SO4_GB300_H
+#define SO4_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum so4_status {
+    SO4_OK = 0,
+    SO4_ERR_ARG = 1,          /* invalid argument (reference: ValueError)            */
+    SO4_ERR_UNSUPPORTED = 2,  /* valid but not supported (reference: NotImplementedError) */
+    SO4_ERR_CUDA = 3,         /* a CUDA runtime call failed                         */
+    SO4_ERR_CAPACITY = 4,     /* an image offset or count exceeds the encodable range */
+    SO4_ERR_NONFINITE = 5,    /* NaN/Inf in positions or cell                       */
+    SO4_ERR_WORKSPACE = 6,    /* workspace smaller than the size query returned     */
+    SO4_ERR_NO_NEIGHBOR = 7,  /* an atom has no neighbour image (reference raises ValueError, SO4.py:275) */
+    SO4_ERR_REVERSE = 8       /* an image has no reverse image (asymmetric list)    */
+};
+
+/* Maximum 2*lmax the kernels are compiled for (lmax <= 6). */
+#define SO4_TWOL_MAX 12
+
+typedef struct so4_tables so4_tables;
+
+/* Parameters of one evaluation (SO4.py:22-158, SNAP.py:22-187).
+ * cutoff_id: 1 cosine, 2 tanh, 3 poly1, 4 poly2, 5 poly3, 6 poly4, 7 exp (SO4.py:134-154).
+ * rfac0: 1 for SO4.py (psi = pi r / rc), the SNAP rfac0 otherwise (psi = rfac0 pi r / rc). */
+typedef struct {
+    int twol;
+    int cutoff_id;
+    double rcut;
+    double rfac0;
+} so4_params;
+
+/* Per-structure geometry record, filled on the host by so4_geometry() and copied
+ * to the device by the caller.  f = r . inv  gives fractional coordinates. */
+typedef struct {
+    double cell[9];
+    double inv[9];
+    double vol;
+    int nbin[3];
+    int mshift[3];
+    int pbc[3];
+    int bin_base;
+    int atom_base;
+    int natoms;
+} so4_geom;
+
+/* ------------------------------------------------------------------ tables */
+
+/* FP64 Clebsch-Gordan list, rootpq and index tables for one twol, built on the
+ * host exactly as the reference builds them (SO4.py:410-480, 831-838,
+ * 1265-1396; angular_momentum.py:9-190) and copied to the device once.
+ * normalize_u selects u_norm = 4 pi / sqrt(l+1) (SO4.py:1304-1311). */
+int so4_tables_create(int twol, int normalize_u, so4_tables **out);
+int so4_tables_destroy(so4_tables *t);
+/* sizes[0..5] = idxu, idxu_half, idxz, nB, idxcg, number of Z blocks */
+int so4_tables_sizes(const so4_tables *t, int *sizes);
+/* host copies of the reference-visible tables (any pointer may be NULL):
+ * cglist[idxcg] f64, idxb[nB*3], idxz[idxz*10], idxu_block[twol+1],
+ * idxz_block[(twol+1)^3], idxcg_block[(twol+1)^3] -- same values and order as
+ * the reference's arrays. */
+int so4_tables_export(const so4_tables *t, double *h_cglist, int *h_idxb, int *h_idxz,
+                      int *h_idxu_block, int *h_idxz_block, int *h_idxcg_block);
+
+/* ------------------------------------------------------------ neighbours */
+/* Replaces ase.neighborlist.NeighborList(rc/2 per atom, bothways, no self) and
+ * the (i, sorted unique j) grouping of SO4.py:211-287: an image (j, o) of
+ * centre i is kept when |pos[j] + o.cell - pos[i]| < rcut, (i, 0) excluded;
+ * images are sorted by (j, o) and every centre gets an (i, i) pair. */
+
+/* Host: geometry records for nstruct structures.  h_cells[9*s] row-major
+ * (rows a1, a2, a3), h_pbc[3*s], h_atom_ptr[nstruct+1].  Writes h_geom[nstruct]
+ * and the total number of bins.  Fails with SO4_ERR_ARG on a singular cell
+ * with periodic axes and SO4_ERR_NONFINITE on NaN/Inf. */
+int so4_geometry(const double *h_cells, const int *h_pbc, const int *h_atom_ptr, int nstruct,
+                 double rcut, so4_geom *h_geom, int *h_nbins_total);
+
+/* Workspace bytes for so4_nl_count / so4_nl_fill / so4_nl_pairs. */
+size_t so4_nl_workspace_size(int natoms, int nbins_total, int64_t nimg);
+
+/* Pass 1: bins the atoms and counts the images of every centre.
+ * d_pos[3*natoms] f64, d_atom_struct[natoms] i32.  Writes d_img_ptr[natoms+1]
+ * (exclusive scan; the host reads d_img_ptr[natoms] = nimg). */
+int so4_nl_count(const so4_geom *d_geom, int nstruct, int nbins_total, const double *d_pos,
+                 const int *d_atom_struct, int natoms, double rcut, int32_t *d_img_ptr,
+                 void *d_work, size_t work_bytes, void *stream);
+
+/* Pass 2: writes the sorted images of every centre: d_img_j[nimg],
+ * d_img_off[3*nimg] (integer cell offsets), d_img_r[3*nimg] (the image vectors,
+ * (pos[j] + (o0 a1 + o1 a2) + o2 a3) - pos[i] in FP64 with every operation
+ * separately rounded) and the pair counts as an exclusive scan d_pair_ptr[natoms+1]. */
+int so4_nl_fill(const so4_geom *d_geom, int nstruct, int nbins_total, const double *d_pos,
+                const int *d_atom_struct, int natoms, double rcut, const int32_t *d_img_ptr,
+                int64_t nimg, int32_t *d_img_j, int32_t *d_img_off, double *d_img_r,
+                int32_t *d_pair_ptr, void *d_work, size_t work_bytes, void *stream);
+
+/* Pass 3: d_seq[2*npair] (i64, structure-local (i, j)), d_pair_img[npair+1]
+ * (images of pair p are [pair_img[p], pair_img[p+1])), d_nsite[natoms] (the
+ * (i, i) pair of each centre), d_img_pair[nimg] and d_img_rev[nimg] (index of
+ * the image (i, -o) in the list of j). */
+int so4_nl_pairs(const so4_geom *d_geom, int nstruct, const int *d_atom_struct, int natoms,
+                 const int32_t *d_img_ptr, int64_t nimg, const int32_t *d_img_j,
+                 const int32_t *d_img_off, const int32_t *d_pair_ptr, int64_t npair,
+                 int64_t *d_seq, int32_t *d_pair_img, int32_t *d_nsite, int32_t *d_img_pair,
+                 int32_t *d_img_rev, void *d_work, size_t work_bytes, void *stream);
+
+/* Reads the device status word of a workspace (synchronises `stream`). */
+int so4_status_read(const void *d_work, size_t work_bytes, void *stream, int *h_status);
+
+/* ------------------------------------------------------------- plain path */
+/* B, dB/dr per (i, j) pair and the per-pair virial, as the reference returns
+ * them (SO4.py:190-199): x = blist.real, dxdr, rdxdr = -bstress / vol.
+ * precision 0 = FP64 throughout, 1 = FP32 arithmetic with FP64 tables and
+ * FP32 outputs.  d_w_nb[natoms]: neighbour weight of each atom (SO4: atomic
+ * number; SNAP: weights[symbol]); d_w_site[natoms]: site weight (SO4: atomic
+ * number; SNAP: 1).  want_deriv / want_stress as the reference's flags; dxdr
+ * and rdxdr may be NULL when not wanted.  Output element type is double
+ * (precision 0) or float (precision 1). */
+size_t so4_plain_workspace_size(const so4_tables *t, int natoms);
+int so4_plain(const so4_tables *t, const so4_params *p, int precision, const so4_geom *d_geom,
+              const int *d_atom_struct, int natoms, const double *d_pos, const double *d_w_nb,
+              const double *d_w_site, const int32_t *d_img_ptr, const int32_t *d_img_j,
+              const double *d_img_r, const int32_t *d_pair_ptr, const int32_t *d_pair_img,
+              const int32_t *d_nsite, int want_deriv, int want_stress, void *d_x, void *d_dxdr,
+              void *d_rdxdr, void *d_work, size_t work_bytes, void *stream);
+
+/* ------------------------------------------------------------ adjoint path */
+/* Forward (FP32): U_tot per centre in the half layout (d_utot[natoms*idxu_half*2]
+ * f32, kept for the adjoint) and B (d_x[natoms*nB] f32). */
+int so4_forward32(const so4_tables *t, const so4_params *p, int natoms, const double *d_w_nb,
+                  const double *d_w_site, const int32_t *d_img_ptr, const int32_t *d_img_j,
+                  const double *d_img_r, float *d_utot, float *d_x, void *stream);
+
+/* Adjoint (FP32 arithmetic, FP64 accumulation of forces and virial): given
+ * beta = dE/dB (d_beta[natoms*nB] f32) and the forward's d_utot, writes
+ *   d_forces[natoms*3] f64 = -dE/dr,
+ *   d_virial[nstruct*9] f64 = sum over images of r (x) dE/dr_image (eV),
+ * without materialising dB/dr.  The reference's contracted stress is
+ * -virial/vol in Voigt order (xx,yy,zz,xy,xz,yz) x 160.21766 GPa.
+ * Uses scratch from d_work (so4_adjoint_workspace_size). */
+size_t so4_adjoint_workspace_size(const so4_tables *t, int natoms, int64_t nimg);
+int so4_adjoint32(const so4_tables *t, const so4_params *p, int nstruct, const int *d_atom_struct,
+                  const int *d_atom_ptr, int natoms, const double *d_w_nb, const int32_t *d_img_ptr,
+                  const int32_t *d_img_j, const double *d_img_r, const int32_t *d_img_rev,
+                  int64_t nimg, const float *d_utot, const float *d_beta, double *d_forces,
+                  double *d_virial, void *d_work, size_t work_bytes, void *stream);
+
+/* Library version string. */
+const char *so4_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SO4_GB300_H */

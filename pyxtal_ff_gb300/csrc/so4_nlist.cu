@@ -1,0 +1,479 @@
+// so4_nlist.cu -- cell-list neighbour search and (i, j) grouping.
+//
+// Replaces ase.neighborlist.NeighborList(rc/2 per atom, self_interaction=False,
+// bothways=True, skin=0) and the grouping loop of
+// pyxtal_ff/descriptors/SO4.py:211-287:
+//   - every periodic image (j, o) with |pos[j] + o.cell - pos[i]| < rcut is a
+//     neighbour of centre i, except (i, o = 0);
+//   - the images of centre i are sorted by (j, o0, o1, o2); the pairs are the
+//     sorted unique j plus a forced (i, i) pair (SO4.py:250-266).
+// Atoms are binned on wrapped fractional coordinates (a bin is at least rcut
+// thick along every periodic axis); the bin-offset range covers every image
+// within rcut however small the cell is.  The image vector is evaluated from
+// the ORIGINAL positions and the integer offset with every FP64 operation
+// separately rounded, so it is reproducible bit for bit on any host.
+#include <cmath>
+#include <cstring>
+
+#include "so4_common.cuh"
+
+namespace {
+
+constexpr int OFF_BIAS = 512;  // image offsets are packed in 10 bits each
+constexpr int OFF_MAX = 511;
+
+struct NLWork {
+    int *status;
+    int *bin_cnt;    // nbins + 1
+    int *bin_start;  // nbins + 1
+    int *bin_cur;    // nbins
+    int *bin_atoms;  // natoms
+    int *atom_bin;   // natoms
+    int *atom_shift; // 3 natoms
+    int *cnt;        // natoms (image or pair counts)
+    unsigned long long *keys;  // nimg
+};
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+size_t carve(NLWork &w, void *base, int natoms, int nbins, int64_t nimg) {
+    char *p = (char *)base;
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        char *q = p ? p + off : nullptr;
+        off += align256(bytes);
+        return (void *)q;
+    };
+    w.status = (int *)take(SO4_WS_HEADER);
+    w.bin_cnt = (int *)take(sizeof(int) * (nbins + 1));
+    w.bin_start = (int *)take(sizeof(int) * (nbins + 1));
+    w.bin_cur = (int *)take(sizeof(int) * (nbins + 1));
+    w.bin_atoms = (int *)take(sizeof(int) * (natoms + 1));
+    w.atom_bin = (int *)take(sizeof(int) * (natoms + 1));
+    w.atom_shift = (int *)take(sizeof(int) * 3 * (natoms + 1));
+    w.cnt = (int *)take(sizeof(int) * (natoms + 1));
+    w.keys = (unsigned long long *)take(sizeof(unsigned long long) * (nimg + 1));
+    return off;
+}
+
+__device__ __forceinline__ void flag(int *status, int code) { atomicOr(status, 1 << code); }
+
+// fractional coordinate k of a Cartesian point: f_k = sum_c r_c inv[c][k]
+__device__ __forceinline__ double frac_k(const so4_geom &g, const double *r, int k) {
+    return __dadd_rn(__dadd_rn(__dmul_rn(r[0], g.inv[k]), __dmul_rn(r[1], g.inv[3 + k])), __dmul_rn(r[2], g.inv[6 + k]));
+}
+
+// image vector (pos[j] + ((o0 a1 + o1 a2) + o2 a3)) - pos[i], every op rounded
+__device__ __forceinline__ void image_vec(const so4_geom &g, const double *pi, const double *pj, int o0, int o1,
+                                          int o2, double *r) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        double sc = __dadd_rn(__dadd_rn(__dmul_rn((double)o0, g.cell[c]), __dmul_rn((double)o1, g.cell[3 + c])),
+                              __dmul_rn((double)o2, g.cell[6 + c]));
+        r[c] = __dsub_rn(__dadd_rn(pj[c], sc), pi[c]);
+    }
+}
+
+__device__ __forceinline__ double norm_rn(const double *r) {
+    return __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(r[0], r[0]), __dmul_rn(r[1], r[1])), __dmul_rn(r[2], r[2])));
+}
+
+__global__ void k_bin(const so4_geom *geom, const double *pos, const int *astruct, int natoms, NLWork w) {
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= natoms) return;
+    const so4_geom &g = geom[astruct[a]];
+    const double r[3] = {pos[3 * a], pos[3 * a + 1], pos[3 * a + 2]};
+    if (!isfinite(r[0]) || !isfinite(r[1]) || !isfinite(r[2])) flag(w.status, SO4_ERR_NONFINITE);
+    int b[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        double f = frac_k(g, r, k);
+        int sh = 0;
+        int bk = 0;
+        if (g.pbc[k]) {
+            double fl = floor(f);
+            if (!isfinite(fl)) fl = 0.0;
+            sh = -(int)fl;
+            f = f - fl;
+            bk = (int)floor(f * g.nbin[k]);
+            bk = min(max(bk, 0), g.nbin[k] - 1);
+        }
+        b[k] = bk;
+        w.atom_shift[3 * a + k] = sh;
+    }
+    const int bin = g.bin_base + (b[0] * g.nbin[1] + b[1]) * g.nbin[2] + b[2];
+    w.atom_bin[a] = bin;
+    atomicAdd(&w.bin_cnt[bin], 1);
+}
+
+__global__ void k_bin_fill(const int *astruct, int natoms, NLWork w) {
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= natoms) return;
+    const int bin = w.atom_bin[a];
+    const int slot = atomicAdd(&w.bin_cur[bin], 1);
+    w.bin_atoms[w.bin_start[bin] + slot] = a;
+}
+
+// single-CTA exclusive scan: out[0..n] from in[0..n-1]
+__global__ void k_scan(const int *in, int *out, int n) {
+    __shared__ int sums[1024];
+    const int t = threadIdx.x;
+    const int per = (n + blockDim.x - 1) / blockDim.x;
+    const int lo = min(n, t * per), hi = min(n, lo + per);
+    int s = 0;
+    for (int q = lo; q < hi; ++q) s += in[q];
+    sums[t] = s;
+    __syncthreads();
+    for (int d = 1; d < blockDim.x; d <<= 1) {
+        int v = (t >= d) ? sums[t - d] : 0;
+        __syncthreads();
+        sums[t] += v;
+        __syncthreads();
+    }
+    int run = (t == 0) ? 0 : sums[t - 1];
+    for (int q = lo; q < hi; ++q) {
+        const int v = in[q];
+        out[q] = run;
+        run += v;
+    }
+    if (t == blockDim.x - 1) out[n] = sums[t];
+}
+
+__global__ void k_set_int(int *p, int v) { *p = v; }
+
+// One warp per centre.  MODE 0: count images into w.cnt.  MODE 1: write the
+// packed (j, o) keys into w.keys[img_ptr[a] ...] (unsorted).
+template <int MODE>
+__global__ void k_scan_images(const so4_geom *geom, const double *pos, const int *astruct, int natoms,
+                              double rcut, const int32_t *img_ptr, NLWork w) {
+    const int lane = threadIdx.x & 31;
+    const int a = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (a >= natoms) return;
+    const so4_geom &g = geom[astruct[a]];
+    const double pi[3] = {pos[3 * a], pos[3 * a + 1], pos[3 * a + 2]};
+    const int lb = w.atom_bin[a] - g.bin_base;
+    const int bi[3] = {lb / (g.nbin[1] * g.nbin[2]), (lb / g.nbin[2]) % g.nbin[1], lb % g.nbin[2]};
+    const int si[3] = {w.atom_shift[3 * a], w.atom_shift[3 * a + 1], w.atom_shift[3 * a + 2]};
+    const int n0 = 2 * g.mshift[0] + 1, n1 = 2 * g.mshift[1] + 1, n2 = 2 * g.mshift[2] + 1;
+    const int nq = n0 * n1 * n2;
+    int base = 0;
+    if (MODE == 1) base = img_ptr[a];
+    for (int pass = 0; pass < MODE + 1; ++pass) {
+        int mine = 0;
+        for (int q = lane; q < nq; q += 32) {
+            const int d[3] = {q / (n1 * n2) - g.mshift[0], (q / n2) % n1 - g.mshift[1], q % n2 - g.mshift[2]};
+            int tb[3], img[3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const int t = bi[k] + d[k];
+                const int nb = g.nbin[k];
+                const int wk = ((t % nb) + nb) % nb;
+                tb[k] = wk;
+                img[k] = (t - wk) / nb;
+            }
+            const int bin = g.bin_base + (tb[0] * g.nbin[1] + tb[1]) * g.nbin[2] + tb[2];
+            for (int s = w.bin_start[bin]; s < w.bin_start[bin + 1]; ++s) {
+                const int j = w.bin_atoms[s];
+                const int o[3] = {img[0] + w.atom_shift[3 * j] - si[0], img[1] + w.atom_shift[3 * j + 1] - si[1],
+                                  img[2] + w.atom_shift[3 * j + 2] - si[2]};
+                if (j == a && o[0] == 0 && o[1] == 0 && o[2] == 0) continue;
+                const double pj[3] = {pos[3 * j], pos[3 * j + 1], pos[3 * j + 2]};
+                double r[3];
+                image_vec(g, pi, pj, o[0], o[1], o[2], r);
+                if (!(norm_rn(r) < rcut)) continue;
+                if (MODE == 1 && pass == 1) {
+                    if (abs(o[0]) > OFF_MAX || abs(o[1]) > OFF_MAX || abs(o[2]) > OFF_MAX) {
+                        flag(w.status, SO4_ERR_CAPACITY);
+                        continue;
+                    }
+                    const unsigned long long key = ((unsigned long long)(unsigned)j << 30) |
+                                                   ((unsigned long long)(o[0] + OFF_BIAS) << 20) |
+                                                   ((unsigned long long)(o[1] + OFF_BIAS) << 10) |
+                                                   (unsigned long long)(o[2] + OFF_BIAS);
+                    w.keys[base + mine] = key;
+                }
+                ++mine;
+            }
+        }
+        if (MODE == 0) {
+            int tot = mine;
+#pragma unroll
+            for (int d = 16; d > 0; d >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, d);
+            if (lane == 0) {
+                w.cnt[a] = tot;
+                if (tot == 0) flag(w.status, SO4_ERR_NO_NEIGHBOR);
+            }
+        } else if (pass == 0) {
+            // exclusive prefix of the lane counts -> write offsets for pass 1
+            int incl = mine;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                int v = __shfl_up_sync(0xffffffffu, incl, d);
+                if (lane >= d) incl += v;
+            }
+            base = img_ptr[a] + incl - mine;
+        }
+    }
+}
+
+// One warp per centre: rank-sort the keys, write the sorted images and count pairs.
+__global__ void k_sort(const so4_geom *geom, const double *pos, const int *astruct, int natoms,
+                       const int32_t *img_ptr, int32_t *img_j, int32_t *img_off, double *img_r, NLWork w) {
+    const int lane = threadIdx.x & 31;
+    const int a = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (a >= natoms) return;
+    const so4_geom &g = geom[astruct[a]];
+    const int p0 = img_ptr[a], p1 = img_ptr[a + 1];
+    const double pi[3] = {pos[3 * a], pos[3 * a + 1], pos[3 * a + 2]};
+    for (int q = p0 + lane; q < p1; q += 32) {
+        const unsigned long long kq = w.keys[q];
+        int rank = 0;
+        for (int p = p0; p < p1; ++p) rank += (w.keys[p] < kq) ? 1 : 0;
+        const int dst = p0 + rank;
+        const int j = (int)(kq >> 30);
+        const int o0 = (int)((kq >> 20) & 1023) - OFF_BIAS;
+        const int o1 = (int)((kq >> 10) & 1023) - OFF_BIAS;
+        const int o2 = (int)(kq & 1023) - OFF_BIAS;
+        img_j[dst] = j;
+        img_off[3 * dst] = o0;
+        img_off[3 * dst + 1] = o1;
+        img_off[3 * dst + 2] = o2;
+        const double pj[3] = {pos[3 * j], pos[3 * j + 1], pos[3 * j + 2]};
+        double r[3];
+        image_vec(g, pi, pj, o0, o1, o2, r);
+        img_r[3 * dst] = r[0];
+        img_r[3 * dst + 1] = r[1];
+        img_r[3 * dst + 2] = r[2];
+    }
+    __syncwarp();
+    __threadfence_block();
+    int uniq = 0, self = 0;
+    for (int q = p0 + lane; q < p1; q += 32) {
+        const int j = img_j[q];
+        if (q == p0 || img_j[q - 1] != j) ++uniq;
+        if (j == a) self = 1;
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+        uniq += __shfl_xor_sync(0xffffffffu, uniq, d);
+        self |= __shfl_xor_sync(0xffffffffu, self, d);
+    }
+    if (lane == 0) w.cnt[a] = uniq + (self ? 0 : 1);
+}
+
+// One thread per centre: emit its pairs in (sorted j, with (i,i) forced) order.
+__global__ void k_pairs(const so4_geom *geom, const int *astruct, int natoms, const int32_t *img_ptr,
+                        const int32_t *img_j, const int32_t *pair_ptr, int64_t *seq, int32_t *pair_img,
+                        int32_t *nsite, int32_t *img_pair) {
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= natoms) return;
+    const int base = geom[astruct[a]].atom_base;
+    int p = pair_ptr[a];
+    int m = img_ptr[a];
+    const int me = img_ptr[a + 1];
+    bool self_done = false;
+    while (m < me || !self_done) {
+        const int j = (m < me) ? img_j[m] : 0x7fffffff;
+        if (!self_done && a < j) {
+            seq[2 * p] = a - base;
+            seq[2 * p + 1] = a - base;
+            pair_img[p] = m;
+            nsite[a] = p;
+            ++p;
+            self_done = true;
+            continue;
+        }
+        seq[2 * p] = a - base;
+        seq[2 * p + 1] = j - base;
+        pair_img[p] = m;
+        if (j == a) {
+            nsite[a] = p;
+            self_done = true;
+        }
+        while (m < me && img_j[m] == j) {
+            img_pair[m] = p;
+            ++m;
+        }
+        ++p;
+    }
+}
+
+// One thread per image: index of the reverse image (i, -o) in the list of j.
+__global__ void k_rev(const int *astruct, int natoms, const int32_t *img_ptr, const int32_t *img_j,
+                      const int32_t *img_off, const int32_t *img_pair, int64_t nimg, const int64_t *seq,
+                      const so4_geom *geom, int32_t *img_rev, NLWork w) {
+    const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= nimg) return;
+    const int j = img_j[m];
+    const int p = img_pair[m];
+    const int a = (int)seq[2 * p] + geom[astruct[j]].atom_base;
+    const int t0 = -img_off[3 * m], t1 = -img_off[3 * m + 1], t2 = -img_off[3 * m + 2];
+    int lo = img_ptr[j], hi = img_ptr[j + 1] - 1, found = -1;
+    while (lo <= hi) {
+        const int mid = (lo + hi) >> 1;
+        const int jj = img_j[mid];
+        const int c0 = img_off[3 * mid], c1 = img_off[3 * mid + 1], c2 = img_off[3 * mid + 2];
+        int cmp;
+        if (jj != a) cmp = jj < a ? -1 : 1;
+        else if (c0 != t0) cmp = c0 < t0 ? -1 : 1;
+        else if (c1 != t1) cmp = c1 < t1 ? -1 : 1;
+        else if (c2 != t2) cmp = c2 < t2 ? -1 : 1;
+        else cmp = 0;
+        if (cmp == 0) {
+            found = mid;
+            break;
+        }
+        if (cmp < 0) lo = mid + 1;
+        else hi = mid - 1;
+    }
+    if (found < 0) flag(w.status, SO4_ERR_REVERSE);
+    img_rev[m] = found < 0 ? (int32_t)m : found;
+}
+
+}  // namespace
+
+extern "C" int so4_geometry(const double *h_cells, const int *h_pbc, const int *h_atom_ptr, int nstruct, double rcut,
+                            so4_geom *h_geom, int *h_nbins_total) {
+    if (!h_cells || !h_pbc || !h_atom_ptr || !h_geom || nstruct < 0) return SO4_ERR_ARG;
+    if (!(rcut > 0.0) || !std::isfinite(rcut)) return SO4_ERR_ARG;
+    long long nbins = 0;
+    for (int s = 0; s < nstruct; ++s) {
+        so4_geom &g = h_geom[s];
+        std::memset(&g, 0, sizeof g);
+        const double *m = h_cells + 9 * s;
+        for (int q = 0; q < 9; ++q) {
+            if (!std::isfinite(m[q])) return SO4_ERR_NONFINITE;
+            g.cell[q] = m[q];
+        }
+        int np = 0;
+        for (int k = 0; k < 3; ++k) {
+            g.pbc[k] = h_pbc[3 * s + k] ? 1 : 0;
+            np += g.pbc[k];
+        }
+        const double det = m[0] * (m[4] * m[8] - m[5] * m[7]) - m[1] * (m[3] * m[8] - m[5] * m[6]) +
+                           m[2] * (m[3] * m[7] - m[4] * m[6]);
+        g.vol = std::fabs(det);
+        if (!(std::fabs(det) > 1e-300)) {
+            if (np) return SO4_ERR_ARG;
+            for (int q = 0; q < 9; ++q) g.inv[q] = (q % 4 == 0) ? 1.0 : 0.0;
+        } else {
+            g.inv[0] = (m[4] * m[8] - m[5] * m[7]) / det;
+            g.inv[1] = (m[2] * m[7] - m[1] * m[8]) / det;
+            g.inv[2] = (m[1] * m[5] - m[2] * m[4]) / det;
+            g.inv[3] = (m[5] * m[6] - m[3] * m[8]) / det;
+            g.inv[4] = (m[0] * m[8] - m[2] * m[6]) / det;
+            g.inv[5] = (m[2] * m[3] - m[0] * m[5]) / det;
+            g.inv[6] = (m[3] * m[7] - m[4] * m[6]) / det;
+            g.inv[7] = (m[1] * m[6] - m[0] * m[7]) / det;
+            g.inv[8] = (m[0] * m[4] - m[1] * m[3]) / det;
+        }
+        for (int k = 0; k < 3; ++k) {
+            if (g.pbc[k]) {
+                const double cn =
+                    std::sqrt(g.inv[k] * g.inv[k] + g.inv[3 + k] * g.inv[3 + k] + g.inv[6 + k] * g.inv[6 + k]);
+                const double d = 1.0 / cn;  // spacing of the lattice planes normal to axis k
+                int nb = (int)std::floor(d / rcut);
+                nb = std::max(1, std::min(nb, 256));
+                g.nbin[k] = nb;
+                g.mshift[k] = (int)std::floor(rcut * nb / d + 1e-9) + 1;
+                if (g.mshift[k] > OFF_MAX / 2) return SO4_ERR_CAPACITY;
+            } else {
+                g.nbin[k] = 1;
+                g.mshift[k] = 0;
+            }
+        }
+        g.bin_base = (int)nbins;
+        nbins += (long long)g.nbin[0] * g.nbin[1] * g.nbin[2];
+        if (nbins > (1LL << 30)) return SO4_ERR_CAPACITY;
+        g.atom_base = h_atom_ptr[s];
+        g.natoms = h_atom_ptr[s + 1] - h_atom_ptr[s];
+        if (g.natoms < 0) return SO4_ERR_ARG;
+    }
+    if (h_nbins_total) *h_nbins_total = (int)nbins;
+    return SO4_OK;
+}
+
+extern "C" size_t so4_nl_workspace_size(int natoms, int nbins_total, int64_t nimg) {
+    NLWork w;
+    return carve(w, nullptr, natoms, nbins_total, nimg);
+}
+
+extern "C" int so4_nl_count(const so4_geom *d_geom, int nstruct, int nbins, const double *d_pos, const int *d_astruct,
+                            int natoms, double rcut, int32_t *d_img_ptr, void *d_work, size_t work_bytes,
+                            void *stream) {
+    if (natoms < 0 || nstruct < 0 || nbins < 0 || !d_work) return SO4_ERR_ARG;
+    NLWork w;
+    if (carve(w, nullptr, natoms, nbins, 0) > work_bytes) return SO4_ERR_WORKSPACE;
+    carve(w, d_work, natoms, nbins, 0);
+    cudaStream_t st = (cudaStream_t)stream;
+    SO4_CUDA_TRY(cudaMemsetAsync(w.status, 0, sizeof(int), st));
+    if (natoms == 0) {
+        k_set_int<<<1, 1, 0, st>>>(d_img_ptr, 0);
+        return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
+    }
+    SO4_CUDA_TRY(cudaMemsetAsync(w.bin_cnt, 0, sizeof(int) * (nbins + 1), st));
+    SO4_CUDA_TRY(cudaMemsetAsync(w.bin_cur, 0, sizeof(int) * (nbins + 1), st));
+    const int tb = 256;
+    k_bin<<<(natoms + tb - 1) / tb, tb, 0, st>>>(d_geom, d_pos, d_astruct, natoms, w);
+    k_scan<<<1, 1024, 0, st>>>(w.bin_cnt, w.bin_start, nbins);
+    k_bin_fill<<<(natoms + tb - 1) / tb, tb, 0, st>>>(d_astruct, natoms, w);
+    const int warps = 8;
+    k_scan_images<0><<<(natoms + warps - 1) / warps, 32 * warps, 0, st>>>(d_geom, d_pos, d_astruct, natoms, rcut,
+                                                                          nullptr, w);
+    k_scan<<<1, 1024, 0, st>>>(w.cnt, d_img_ptr, natoms);
+    return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
+}
+
+extern "C" int so4_nl_fill(const so4_geom *d_geom, int nstruct, int nbins, const double *d_pos, const int *d_astruct,
+                           int natoms, double rcut, const int32_t *d_img_ptr, int64_t nimg, int32_t *d_img_j,
+                           int32_t *d_img_off, double *d_img_r, int32_t *d_pair_ptr, void *d_work,
+                           size_t work_bytes, void *stream) {
+    if (natoms < 0 || nstruct < 0 || nimg < 0 || !d_work) return SO4_ERR_ARG;
+    if (nimg > 0x7fffffff) return SO4_ERR_CAPACITY;
+    NLWork w;
+    if (carve(w, nullptr, natoms, nbins, nimg) > work_bytes) return SO4_ERR_WORKSPACE;
+    carve(w, d_work, natoms, nbins, nimg);
+    cudaStream_t st = (cudaStream_t)stream;
+    if (natoms == 0) {
+        k_set_int<<<1, 1, 0, st>>>(d_pair_ptr, 0);
+        return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
+    }
+    const int warps = 8;
+    const int grid = (natoms + warps - 1) / warps;
+    k_scan_images<1><<<grid, 32 * warps, 0, st>>>(d_geom, d_pos, d_astruct, natoms, rcut, d_img_ptr, w);
+    k_sort<<<grid, 32 * warps, 0, st>>>(d_geom, d_pos, d_astruct, natoms, d_img_ptr, d_img_j, d_img_off, d_img_r, w);
+    k_scan<<<1, 1024, 0, st>>>(w.cnt, d_pair_ptr, natoms);
+    return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
+}
+
+extern "C" int so4_nl_pairs(const so4_geom *d_geom, int nstruct, const int *d_astruct, int natoms,
+                            const int32_t *d_img_ptr, int64_t nimg, const int32_t *d_img_j, const int32_t *d_img_off,
+                            const int32_t *d_pair_ptr, int64_t npair, int64_t *d_seq, int32_t *d_pair_img,
+                            int32_t *d_nsite, int32_t *d_img_pair, int32_t *d_img_rev, void *d_work,
+                            size_t work_bytes, void *stream) {
+    if (natoms < 0 || nstruct < 0 || nimg < 0 || npair < 0 || !d_work) return SO4_ERR_ARG;
+    if (work_bytes < SO4_WS_HEADER) return SO4_ERR_WORKSPACE;
+    NLWork w;
+    std::memset(&w, 0, sizeof w);
+    w.status = (int *)d_work;
+    cudaStream_t st = (cudaStream_t)stream;
+    k_set_int<<<1, 1, 0, st>>>(d_pair_img + npair, (int)nimg);
+    if (natoms == 0) return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
+    const int tb = 128;
+    k_pairs<<<(natoms + tb - 1) / tb, tb, 0, st>>>(d_geom, d_astruct, natoms, d_img_ptr, d_img_j, d_pair_ptr, d_seq,
+                                                   d_pair_img, d_nsite, d_img_pair);
+    if (nimg > 0 && d_img_rev)
+        k_rev<<<(unsigned)((nimg + 255) / 256), 256, 0, st>>>(d_astruct, natoms, d_img_ptr, d_img_j, d_img_off,
+                                                              d_img_pair, nimg, d_seq, d_geom, d_img_rev, w);
+    return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
+}
+
+extern "C" int so4_status_read(const void *d_work, size_t work_bytes, void *stream, int *h_status) {
+    if (!d_work || !h_status || work_bytes < sizeof(int)) return SO4_ERR_ARG;
+    int v = 0;
+    cudaStream_t st = (cudaStream_t)stream;
+    SO4_CUDA_TRY(cudaMemcpyAsync(&v, d_work, sizeof(int), cudaMemcpyDeviceToHost, st));
+    SO4_CUDA_TRY(cudaStreamSynchronize(st));
+    *h_status = v;
+    return SO4_OK;
+}

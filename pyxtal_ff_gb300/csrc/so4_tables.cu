@@ -1,0 +1,325 @@
+// so4_tables.cu -- FP64 Clebsch-Gordan list, rootpq and index tables (host),
+// copied once to the device.  The loops follow the reference:
+//   factorial table / deltacg     pyxtal_ff/descriptors/angular_momentum.py:9-190
+//   init_clebsch_gordan           pyxtal_ff/descriptors/SO4.py:410-480
+//   init_rootpqarray              SO4.py:831-838
+//   idxcg/idxu/idxb/idxz tables   SO4.py:1265-1396
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+
+#include "so4_common.cuh"
+
+namespace {
+
+// n! as the reference tabulates it: exact up to 20!, rounded to 15 significant
+// decimal digits above (angular_momentum.py:14-182).
+double factorial_ref(int n) {
+    static double tab[40];
+    static bool ready = false;
+    if (!ready) {
+        unsigned __int128 f = 1;
+        for (int k = 0; k < 40; ++k) {
+            if (k > 0) f *= (unsigned __int128)k;
+            if (k <= 20) {
+                tab[k] = (double)(uint64_t)f;
+            } else if (k <= 34) {
+                std::string s;
+                unsigned __int128 t = f;
+                while (t > 0) {
+                    s.insert(s.begin(), (char)('0' + (int)(t % 10)));
+                    t /= 10;
+                }
+                std::string m = s.substr(0, 15);
+                bool carry = s[15] >= '5';
+                for (int q = 14; q >= 0 && carry; --q) {
+                    if (m[q] == '9') {
+                        m[q] = '0';
+                    } else {
+                        m[q]++;
+                        carry = false;
+                    }
+                }
+                int e10 = (int)s.size() - 1;
+                if (carry) {
+                    m = "1" + m.substr(0, 14);
+                    e10++;
+                }
+                std::string sci = m.substr(0, 1) + "." + m.substr(1) + "e" + std::to_string(e10);
+                tab[k] = std::strtod(sci.c_str(), nullptr);
+            } else {
+                tab[k] = NAN;
+            }
+        }
+        ready = true;
+    }
+    return (n >= 0 && n < 40) ? tab[n] : NAN;
+}
+
+double deltacg(int l1, int l2, int l) {
+    double s = factorial_ref((l1 + l2 + l) / 2 + 1);
+    return std::sqrt(factorial_ref((l1 + l2 - l) / 2) * factorial_ref((l1 - l2 + l) / 2) *
+                     factorial_ref((-l1 + l2 + l) / 2) / s);
+}
+
+int b3(int ld, int a, int b, int c) { return (a * ld + b) * ld + c; }
+
+template <typename T>
+int upload(T **dst, const std::vector<T> &src) {
+    size_t bytes = sizeof(T) * (src.empty() ? 1 : src.size());
+    if (cudaMalloc((void **)dst, bytes) != cudaSuccess) return SO4_ERR_CUDA;
+    if (!src.empty() && cudaMemcpy(*dst, src.data(), sizeof(T) * src.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+        return SO4_ERR_CUDA;
+    return SO4_OK;
+}
+
+void free_device(so4_tables *t) {
+    cudaFree(t->d_cg64);
+    cudaFree(t->d_cg32);
+    cudaFree(t->d_rootpq64);
+    cudaFree(t->d_rootpq32);
+    cudaFree(t->d_z);
+    cudaFree(t->d_b);
+    cudaFree(t->d_blk);
+    cudaFree(t->d_yblk_ptr);
+    cudaFree(t->d_yblk);
+}
+
+}  // namespace
+
+extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
+    if (!out) return SO4_ERR_ARG;
+    *out = nullptr;
+    if (twol < 0) return SO4_ERR_ARG;
+    if (twol > SO4_TWOL_MAX) return SO4_ERR_UNSUPPORTED;
+    so4_tables *t = new so4_tables();
+    const int ld = twol + 1;
+    t->twol = twol;
+    t->ldim = ld;
+    t->normalize_u = normalize_u ? 1 : 0;
+
+    // idxcg_block and CG list (SO4.py:1269-1285, 410-480)
+    t->idxcg_block.assign(ld * ld * ld, 0);
+    int n = 0;
+    for (int l1 = 0; l1 < ld; ++l1)
+        for (int l2 = 0; l2 <= l1; ++l2)
+            for (int l = l1 - l2; l <= std::min(twol, l1 + l2); l += 2) {
+                t->idxcg_block[b3(ld, l1, l2, l)] = n;
+                n += (l1 + 1) * (l2 + 1);
+            }
+    t->n_cg = n;
+    t->cglist.assign(n, 0.0);
+    n = 0;
+    for (int l1 = 0; l1 < ld; ++l1)
+        for (int l2 = 0; l2 <= l1; ++l2)
+            for (int l = l1 - l2; l <= std::min(twol, l1 + l2); l += 2)
+                for (int m1 = 0; m1 <= l1; ++m1) {
+                    const int aa2 = 2 * m1 - l1;
+                    for (int m2 = 0; m2 <= l2; ++m2) {
+                        const int bb2 = 2 * m2 - l2;
+                        const int m = (aa2 + bb2 + l) / 2;
+                        if (m < 0 || m > l) {
+                            t->cglist[n++] = 0.0;
+                            continue;
+                        }
+                        double sum = 0.0;
+                        const int zlo = std::max(0, std::max(-(l - l2 + aa2) / 2, -(l - l1 - bb2) / 2));
+                        const int zhi = std::min((l1 + l2 - l) / 2, std::min((l1 - aa2) / 2, (l2 + bb2) / 2));
+                        for (int z = zlo; z <= zhi; ++z) {
+                            const double ifac = (z % 2 == 0) ? 1.0 : -1.0;
+                            sum += ifac / (factorial_ref(z) * factorial_ref((l1 + l2 - l) / 2 - z) *
+                                           factorial_ref((l1 - aa2) / 2 - z) * factorial_ref((l2 + bb2) / 2 - z) *
+                                           factorial_ref((l - l2 + aa2) / 2 + z) *
+                                           factorial_ref((l - l1 - bb2) / 2 + z));
+                        }
+                        const int cc2 = 2 * m - l;
+                        const double dcg = deltacg(l1, l2, l);
+                        const double sfaccg =
+                            std::sqrt(factorial_ref((l1 + aa2) / 2) * factorial_ref((l1 - aa2) / 2) *
+                                      factorial_ref((l2 + bb2) / 2) * factorial_ref((l2 - bb2) / 2) *
+                                      factorial_ref((l + cc2) / 2) * factorial_ref((l - cc2) / 2) * (double)(l + 1));
+                        t->cglist[n++] = sum * dcg * sfaccg;
+                    }
+                }
+
+    // U offsets: full and half layouts, u_norm per level (SO4.py:1288-1311)
+    t->idxu_block.assign(ld, 0);
+    t->h_block.assign(ld + 1, 0);
+    t->unorm_l.assign(ld, 1.0);
+    int nu = 0, nh = 0;
+    for (int l = 0; l < ld; ++l) {
+        t->idxu_block[l] = nu;
+        t->h_block[l] = nh;
+        nu += (l + 1) * (l + 1);
+        nh += (l / 2 + 1) * (l + 1);
+        if (normalize_u) t->unorm_l[l] = 4 * SO4_PI / std::sqrt((double)(l + 1));
+    }
+    t->h_block[ld] = nh;
+    t->n_u = nu;
+    t->n_half = nh;
+
+    // idxb (SO4.py:1314-1327)
+    for (int l1 = 0; l1 < ld; ++l1)
+        for (int l2 = 0; l2 <= l1; ++l2)
+            for (int l = l1 - l2; l <= std::min(twol, l1 + l2); l += 2)
+                if (l >= l1) {
+                    t->idxb.push_back(l1);
+                    t->idxb.push_back(l2);
+                    t->idxb.push_back(l);
+                }
+    t->n_b = (int)t->idxb.size() / 3;
+
+    // idxz and idxz_block (SO4.py:1329-1395), plus the device entry list
+    t->idxz_block.assign(ld * ld * ld, 0);
+    std::vector<ZEnt> zent;
+    std::vector<ZBlk> blks;
+    n = 0;
+    for (int l1 = 0; l1 < ld; ++l1)
+        for (int l2 = 0; l2 <= l1; ++l2)
+            for (int l = l1 - l2; l <= std::min(twol, l1 + l2); l += 2) {
+                t->idxz_block[b3(ld, l1, l2, l)] = n;
+                ZBlk bk;
+                std::memset(&bk, 0, sizeof bk);
+                bk.l1 = l1;
+                bk.l2 = l2;
+                bk.l = l;
+                bk.z0 = n;
+                for (int mb = 0; 2 * mb <= l; ++mb)
+                    for (int ma = 0; ma <= l; ++ma) {
+                        int q[10];
+                        q[0] = l1;
+                        q[1] = l2;
+                        q[2] = l;
+                        q[3] = std::max(0, (2 * ma - l - l2 + l1) / 2);
+                        q[4] = (2 * ma - l - (2 * q[3] - l1) + l2) / 2;
+                        q[5] = std::min(l1, (2 * ma - l + l2 + l1) / 2) - q[3] + 1;
+                        q[6] = std::max(0, (2 * mb - l - l2 + l1) / 2);
+                        q[7] = (2 * mb - l - (2 * q[6] - l1) + l2) / 2;
+                        q[8] = std::min(l1, (2 * mb - l + l2 + l1) / 2) - q[6] + 1;
+                        q[9] = t->idxu_block[l] + (l + 1) * mb + ma;
+                        for (int c = 0; c < 10; ++c) t->idxz.push_back(q[c]);
+                        ZEnt z;
+                        const int cgbase = t->idxcg_block[b3(ld, l1, l2, l)];
+                        z.na = q[5];
+                        z.nb = q[8];
+                        z.ma1min = q[3];
+                        z.ma2max = q[4];
+                        z.cga = cgbase + q[3] * (l2 + 1) + q[4];
+                        z.cgb = cgbase + q[6] * (l2 + 1) + q[7];
+                        z.u1 = t->idxu_block[l1] + (l1 + 1) * q[6];
+                        z.u2 = t->idxu_block[l2] + (l2 + 1) * q[7];
+                        z.l1 = l1;
+                        z.l2 = l2;
+                        z.jh = t->h_block[l] + (l + 1) * mb + ma;
+                        z.blk = (int)blks.size();
+                        zent.push_back(z);
+                        n++;
+                    }
+                bk.n = n - bk.z0;
+                blks.push_back(bk);
+            }
+    t->n_z = n;
+    t->n_blk = (int)blks.size();
+
+    // bispectrum components and the roles of each Z block in dB/dr (SO4.py:1113-1227)
+    std::vector<BEnt> bent(t->n_b);
+    for (int k = 0; k < t->n_b; ++k) {
+        const int l1 = t->idxb[3 * k], l2 = t->idxb[3 * k + 1], l = t->idxb[3 * k + 2];
+        BEnt &b = bent[k];
+        b.l1 = l1;
+        b.l2 = l2;
+        b.l = l;
+        b.lam[0] = l;
+        b.lam[1] = l1;
+        b.lam[2] = l2;
+        b.z[0] = t->idxz_block[b3(ld, l1, l2, l)];
+        b.z[1] = t->idxz_block[b3(ld, l, l2, l1)];
+        b.z[2] = t->idxz_block[b3(ld, l, l1, l2)];
+        b.fac[0] = 2.0;
+        b.fac[1] = 2.0 * ((double)(l + 1) / (l1 + 1.0));
+        b.fac[2] = 2.0 * ((double)(l + 1) / (l2 + 1.0));
+        for (int s = 0; s < 3; ++s) {
+            b.h[s] = t->h_block[b.lam[s]];
+            b.cnt[s] = section_count(b.lam[s]);
+        }
+        const int blk_of[3] = {b.z[0], b.z[1], b.z[2]};
+        for (int s = 0; s < 3; ++s) {
+            for (auto &bk : blks)
+                if (bk.z0 == blk_of[s]) {
+                    bk.role_k[bk.nrole] = k;
+                    bk.role_f[bk.nrole] = b.fac[s];
+                    bk.nrole++;
+                }
+        }
+    }
+    // blocks grouped by their third index (the level of Y they feed)
+    std::vector<int> yptr(ld + 1, 0), ylist;
+    for (int lam = 0; lam < ld; ++lam) {
+        yptr[lam] = (int)ylist.size();
+        for (int bi = 0; bi < t->n_blk; ++bi)
+            if (blks[bi].l == lam) ylist.push_back(bi);
+    }
+    yptr[ld] = (int)ylist.size();
+
+    std::vector<double> rp64(ld * ld, 0.0);
+    std::vector<float> rp32(ld * ld, 0.f);
+    for (int p = 1; p < ld; ++p)
+        for (int q = 1; q < ld; ++q) {
+            rp64[p * ld + q] = std::sqrt((double)p / (double)q);
+            rp32[p * ld + q] = (float)rp64[p * ld + q];
+        }
+    std::vector<float> cg32(t->cglist.begin(), t->cglist.end());
+
+    int rc = SO4_OK;
+    if (!rc) rc = upload(&t->d_cg64, t->cglist);
+    if (!rc) rc = upload(&t->d_cg32, cg32);
+    if (!rc) rc = upload(&t->d_rootpq64, rp64);
+    if (!rc) rc = upload(&t->d_rootpq32, rp32);
+    if (!rc) rc = upload(&t->d_z, zent);
+    if (!rc) rc = upload(&t->d_b, bent);
+    if (!rc) rc = upload(&t->d_blk, blks);
+    if (!rc) rc = upload(&t->d_yblk_ptr, yptr);
+    if (!rc) rc = upload(&t->d_yblk, ylist);
+    if (rc) {
+        free_device(t);
+        delete t;
+        return rc;
+    }
+    *out = t;
+    return SO4_OK;
+}
+
+extern "C" int so4_tables_destroy(so4_tables *t) {
+    if (!t) return SO4_OK;
+    free_device(t);
+    delete t;
+    return SO4_OK;
+}
+
+extern "C" int so4_tables_sizes(const so4_tables *t, int *s) {
+    if (!t || !s) return SO4_ERR_ARG;
+    s[0] = t->n_u;
+    s[1] = t->n_half;
+    s[2] = t->n_z;
+    s[3] = t->n_b;
+    s[4] = t->n_cg;
+    s[5] = t->n_blk;
+    return SO4_OK;
+}
+
+extern "C" int so4_tables_export(const so4_tables *t, double *cg, int *idxb, int *idxz, int *idxu_block,
+                                 int *idxz_block, int *idxcg_block) {
+    if (!t) return SO4_ERR_ARG;
+    const size_t l3 = (size_t)t->ldim * t->ldim * t->ldim;
+    if (cg) std::memcpy(cg, t->cglist.data(), sizeof(double) * t->n_cg);
+    if (idxb) std::memcpy(idxb, t->idxb.data(), sizeof(int) * t->idxb.size());
+    if (idxz) std::memcpy(idxz, t->idxz.data(), sizeof(int) * t->idxz.size());
+    if (idxu_block) std::memcpy(idxu_block, t->idxu_block.data(), sizeof(int) * t->ldim);
+    if (idxz_block) std::memcpy(idxz_block, t->idxz_block.data(), sizeof(int) * l3);
+    if (idxcg_block) std::memcpy(idxcg_block, t->idxcg_block.data(), sizeof(int) * l3);
+    return SO4_OK;
+}
+
+extern "C" const char *so4_version(void) { return "so4_gb300 0.1.0 (sm_103a)"; }

@@ -1,0 +1,246 @@
+"""Host orchestration of the CUDA path: device tables, the GPU neighbour list and
+the descriptor / adjoint launches.  Device memory comes from torch (the caller
+side of the C ABI); the library itself allocates nothing but its tables.
+
+A batch is any list of structures: their atoms are concatenated, structure s
+owning atoms [atom_ptr[s], atom_ptr[s+1]).  Every launch goes on torch's current
+CUDA stream.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import Geom, Params, check, lib
+
+CUTOFF_IDS = {"cosine": 1, "tanh": 2, "poly1": 3, "poly2": 4, "poly3": 5, "poly4": 6, "exp": 7}
+
+
+def _stream():
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _ptr(t):
+    return C.c_void_p(t.data_ptr()) if t is not None else C.c_void_p(0)
+
+
+def require_cuda():
+    """Raise unless a CUDA device is present: the path has no CPU fallback."""
+    if not torch.cuda.is_available():
+        raise RuntimeError("pyxtal_ff_gb300 needs a CUDA GPU (GB300, sm_103a); there is no CPU fallback")
+
+
+# ---------------------------------------------------------------------- tables
+class Tables:
+    """Device-resident CG / rootpq / index tables for one (twol, normalize_U)."""
+
+    def __init__(self, twol, normalize_u=False):
+        h = C.c_void_p()
+        check(lib().so4_tables_create(int(twol), int(bool(normalize_u)), C.byref(h)), "so4_tables_create")
+        self.handle = h
+        s = (C.c_int * 6)()
+        check(lib().so4_tables_sizes(h, s), "so4_tables_sizes")
+        self.twol = int(twol)
+        self.n_u, self.n_half, self.n_z, self.nB, self.n_cg, self.n_blk = [int(v) for v in s]
+
+    def export(self):
+        ld = self.twol + 1
+        cg = np.zeros(self.n_cg)
+        idxb = np.zeros((self.nB, 3), np.int32)
+        idxz = np.zeros((self.n_z, 10), np.int32)
+        iub = np.zeros(ld, np.int32)
+        izb = np.zeros((ld, ld, ld), np.int32)
+        icb = np.zeros((ld, ld, ld), np.int32)
+        check(lib().so4_tables_export(self.handle, cg.ctypes.data, idxb.ctypes.data, idxz.ctypes.data,
+                                      iub.ctypes.data, izb.ctypes.data, icb.ctypes.data), "so4_tables_export")
+        return dict(cglist=cg, idxb=idxb, idxz=idxz, idxu_block=iub, idxz_block=izb, idxcg_block=icb)
+
+    def __del__(self):
+        try:
+            if self.handle:
+                lib().so4_tables_destroy(self.handle)
+                self.handle = None
+        except Exception:
+            pass
+
+
+_TABLES = {}
+
+
+def tables(twol, normalize_u=False):
+    key = (int(twol), bool(normalize_u), torch.cuda.current_device())
+    t = _TABLES.get(key)
+    if t is None:
+        t = Tables(twol, normalize_u)
+        _TABLES[key] = t
+    return t
+
+
+def params(twol, rcut, rfac0, cutoff):
+    return Params(int(twol), CUTOFF_IDS[cutoff], float(rcut), float(rfac0))
+
+
+# ---------------------------------------------------------------- neighbours
+@dataclass
+class Neighbors:
+    natoms: int
+    nstruct: int
+    nimg: int
+    npair: int
+    atom_ptr: np.ndarray       # host (S+1,)
+    vol: np.ndarray            # host (S,)
+    geom: torch.Tensor         # device bytes
+    nbins: int
+    atom_struct: torch.Tensor  # (N,) i32
+    atom_ptr_dev: torch.Tensor  # (S+1,) i32
+    img_ptr: torch.Tensor      # (N+1,) i32
+    img_j: torch.Tensor        # (M,) i32
+    img_off: torch.Tensor      # (M,3) i32
+    img_r: torch.Tensor        # (M,3) f64
+    pair_ptr: torch.Tensor     # (N+1,) i32
+    seq: torch.Tensor          # (P,2) i64
+    pair_img: torch.Tensor     # (P+1,) i32
+    nsite: torch.Tensor        # (N,) i32
+    img_pair: torch.Tensor     # (M,) i32
+    img_rev: torch.Tensor      # (M,) i32
+    no_neighbor: bool          # some atom has no image within rcut
+
+
+def geometry(cells, pbc, atom_ptr, rcut):
+    cells = np.ascontiguousarray(np.asarray(cells, dtype=np.float64).reshape(-1, 9))
+    pbc = np.ascontiguousarray(np.asarray(pbc, dtype=np.int32).reshape(-1, 3))
+    atom_ptr = np.ascontiguousarray(np.asarray(atom_ptr, dtype=np.int32))
+    S = len(cells)
+    geo = (Geom * max(S, 1))()
+    nb = C.c_int()
+    rc = lib().so4_geometry(cells.ctypes.data, pbc.ctypes.data, atom_ptr.ctypes.data, S, float(rcut), geo,
+                            C.byref(nb))
+    if rc == _lib.SO4_ERR_NONFINITE:
+        raise ValueError("cell contains NaN or Inf")
+    if rc == _lib.SO4_ERR_ARG:
+        raise ValueError("singular cell with periodic boundary conditions, or invalid rcut")
+    check(rc, "so4_geometry")
+    raw = np.frombuffer(bytes(geo), dtype=np.uint8)[: C.sizeof(Geom) * S]
+    vol = np.array([geo[s].vol for s in range(S)])
+    return raw, vol, int(nb.value)
+
+
+def build_neighbors(pos, cells, pbc, atom_ptr, rcut, device="cuda", workspace=None):
+    """GPU neighbour list of a batch.  pos: (N,3) f64 tensor on the device (or a
+    numpy array), cells (S,3,3), pbc (S,3), atom_ptr (S+1,) host arrays."""
+    L = lib()
+    dev = torch.device(device)
+    if not isinstance(pos, torch.Tensor):
+        pos = torch.from_numpy(np.ascontiguousarray(pos, dtype=np.float64))
+    pos = pos.to(dev, dtype=torch.float64).contiguous()
+    atom_ptr = np.asarray(atom_ptr, dtype=np.int64)
+    N, S = int(atom_ptr[-1]), len(atom_ptr) - 1
+    if pos.shape != (N, 3):
+        raise ValueError("positions must be (N,3) for N = atom_ptr[-1]")
+    raw, vol, nbins = geometry(cells, pbc, atom_ptr, rcut)
+    geom = torch.from_numpy(raw.copy()).to(dev)
+    counts = np.diff(atom_ptr)
+    atom_struct = torch.from_numpy(np.repeat(np.arange(S, dtype=np.int32), counts)).to(dev)
+    atom_ptr_dev = torch.from_numpy(atom_ptr.astype(np.int32)).to(dev)
+    st = _stream()
+    est_m = max(64 * N, 1)
+    ws_bytes = L.so4_nl_workspace_size(N, nbins, est_m)
+    ws = workspace if (workspace is not None and workspace.numel() >= ws_bytes) else torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
+    img_ptr = torch.empty(N + 1, dtype=torch.int32, device=dev)
+    check(L.so4_nl_count(_ptr(geom), S, nbins, _ptr(pos), _ptr(atom_struct), N, float(rcut), _ptr(img_ptr),
+                         _ptr(ws), ws.numel(), st), "so4_nl_count")
+    M = int(img_ptr[N].item())
+    need = L.so4_nl_workspace_size(N, nbins, M)
+    if need > ws.numel():
+        ws2 = torch.empty(need, dtype=torch.uint8, device=dev)
+        ws2[: ws.numel()].copy_(ws)
+        ws = ws2
+    img_j = torch.empty(max(M, 1), dtype=torch.int32, device=dev)
+    img_off = torch.empty((max(M, 1), 3), dtype=torch.int32, device=dev)
+    img_r = torch.empty((max(M, 1), 3), dtype=torch.float64, device=dev)
+    pair_ptr = torch.empty(N + 1, dtype=torch.int32, device=dev)
+    check(L.so4_nl_fill(_ptr(geom), S, nbins, _ptr(pos), _ptr(atom_struct), N, float(rcut), _ptr(img_ptr), M,
+                        _ptr(img_j), _ptr(img_off), _ptr(img_r), _ptr(pair_ptr), _ptr(ws), ws.numel(), st),
+          "so4_nl_fill")
+    P = int(pair_ptr[N].item())
+    seq = torch.empty((max(P, 1), 2), dtype=torch.int64, device=dev)
+    pair_img = torch.empty(P + 1, dtype=torch.int32, device=dev)
+    nsite = torch.empty(max(N, 1), dtype=torch.int32, device=dev)
+    img_pair = torch.empty(max(M, 1), dtype=torch.int32, device=dev)
+    img_rev = torch.empty(max(M, 1), dtype=torch.int32, device=dev)
+    check(L.so4_nl_pairs(_ptr(geom), S, _ptr(atom_struct), N, _ptr(img_ptr), M, _ptr(img_j), _ptr(img_off),
+                         _ptr(pair_ptr), P, _ptr(seq), _ptr(pair_img), _ptr(nsite), _ptr(img_pair), _ptr(img_rev),
+                         _ptr(ws), ws.numel(), st), "so4_nl_pairs")
+    status = C.c_int()
+    check(L.so4_status_read(_ptr(ws), ws.numel(), st, C.byref(status)), "so4_status_read")
+    bits = status.value
+    if bits & (1 << _lib.SO4_ERR_NONFINITE):
+        raise ValueError("positions contain NaN or Inf")
+    for code in (_lib.SO4_ERR_CAPACITY, _lib.SO4_ERR_REVERSE):
+        if bits & (1 << code):
+            raise _lib.SO4Error(code, "neighbour list")
+    return Neighbors(N, S, M, P, atom_ptr, vol, geom, nbins, atom_struct, atom_ptr_dev, img_ptr, img_j[:M],
+                     img_off[:M], img_r[:M], pair_ptr, seq[:P], pair_img, nsite[:N], img_pair[:M], img_rev[:M],
+                     bool(bits & (1 << _lib.SO4_ERR_NO_NEIGHBOR)))
+
+
+# ----------------------------------------------------------------- compute
+def site_weights(kind, numbers, symbols, weights=None):
+    """(w_nb, w_site) per atom: SO4.py uses atomic numbers for both
+    (SO4.py:244, 271); SNAP.py uses weights[symbol] and 1 (SNAP.py:273, 299-301)."""
+    numbers = np.asarray(numbers)
+    if kind == "SO4":
+        w = numbers.astype(np.float64)
+        return w, w.copy()
+    w_nb = np.array([float(weights[s]) for s in symbols], dtype=np.float64)
+    return w_nb, np.ones(len(numbers), dtype=np.float64)
+
+
+def plain(tab, prm, nb: Neighbors, pos, w_nb, w_site, precision=0, want_deriv=True, want_stress=True):
+    """x (N,nB), dxdr (P,nB,3), rdxdr (P,nB,3,3) on the device; FP64 (precision 0) or FP32 (1)."""
+    dev = pos.device
+    dt = torch.float64 if precision == 0 else torch.float32
+    x = torch.empty((max(nb.natoms, 1), tab.nB), dtype=dt, device=dev)
+    dxdr = torch.empty((max(nb.npair, 1), tab.nB, 3), dtype=dt, device=dev) if want_deriv else None
+    rdxdr = torch.empty((max(nb.npair, 1), tab.nB, 3, 3), dtype=dt, device=dev) if (want_deriv and want_stress) else None
+    ws = torch.empty(lib().so4_plain_workspace_size(tab.handle, nb.natoms), dtype=torch.uint8, device=dev)
+    check(lib().so4_plain(tab.handle, C.byref(prm), int(precision), _ptr(nb.geom), _ptr(nb.atom_struct), nb.natoms,
+                          _ptr(pos), _ptr(w_nb), _ptr(w_site), _ptr(nb.img_ptr), _ptr(nb.img_j), _ptr(nb.img_r),
+                          _ptr(nb.pair_ptr), _ptr(nb.pair_img), _ptr(nb.nsite), int(want_deriv),
+                          int(want_deriv and want_stress), _ptr(x), _ptr(dxdr), _ptr(rdxdr), _ptr(ws), ws.numel(),
+                          _stream()), "so4_plain")
+    x = x[: nb.natoms]
+    if dxdr is not None:
+        dxdr = dxdr[: nb.npair]
+    if rdxdr is not None:
+        rdxdr = rdxdr[: nb.npair]
+    return x, dxdr, rdxdr
+
+
+def forward32(tab, prm, nb: Neighbors, w_nb, w_site):
+    """FP32 B (N,nB) and U_tot (N, n_half, 2) for the adjoint."""
+    dev = w_nb.device
+    x = torch.empty((max(nb.natoms, 1), tab.nB), dtype=torch.float32, device=dev)
+    utot = torch.empty((max(nb.natoms, 1), tab.n_half, 2), dtype=torch.float32, device=dev)
+    check(lib().so4_forward32(tab.handle, C.byref(prm), nb.natoms, _ptr(w_nb), _ptr(w_site), _ptr(nb.img_ptr),
+                              _ptr(nb.img_j), _ptr(nb.img_r), _ptr(utot), _ptr(x), _stream()), "so4_forward32")
+    return x[: nb.natoms], utot[: nb.natoms]
+
+
+def adjoint32(tab, prm, nb: Neighbors, w_nb, utot, beta, workspace=None):
+    """forces (N,3) f64 = -dE/dr and virial (S,3,3) f64 = sum r (x) dE/dr, for beta = dE/dB."""
+    dev = utot.device
+    beta = beta.to(torch.float32).contiguous()
+    forces = torch.empty((max(nb.natoms, 1), 3), dtype=torch.float64, device=dev)
+    virial = torch.empty((max(nb.nstruct, 1), 3, 3), dtype=torch.float64, device=dev)
+    need = lib().so4_adjoint_workspace_size(tab.handle, nb.natoms, nb.nimg)
+    ws = workspace if (workspace is not None and workspace.numel() >= need) else torch.empty(need, dtype=torch.uint8, device=dev)
+    check(lib().so4_adjoint32(tab.handle, C.byref(prm), nb.nstruct, _ptr(nb.atom_struct), _ptr(nb.atom_ptr_dev),
+                              nb.natoms, _ptr(w_nb), _ptr(nb.img_ptr), _ptr(nb.img_j), _ptr(nb.img_r),
+                              _ptr(nb.img_rev), nb.nimg, _ptr(utot), _ptr(beta), _ptr(forces), _ptr(virial),
+                              _ptr(ws), ws.numel(), _stream()), "so4_adjoint32")
+    return forces[: nb.natoms], virial[: nb.nstruct]

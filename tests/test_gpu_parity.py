@@ -1,0 +1,164 @@
+"""Parity of the CUDA path with the reference (golden vectors) and with the oracle.
+
+Tolerances (relative = max|a-b| / max|b| per output array):
+  FP64 path vs reference goldens / oracle   1e-10
+  FP32 plain path vs FP64 oracle            x 2e-5, dxdr 2e-4, rdxdr 2e-4
+  FP32 adjoint forces / virial vs oracle    2e-4 relative, and the absolute
+                                            force error is reported
+The neighbour list is compared bit for bit (indices, offsets and FP64 vectors).
+"""
+import numpy as np
+import pytest
+import torch
+
+from oracle import oracle as O
+from pyxtal_ff_gb300 import engine
+from pyxtal_ff_gb300 import structures as S
+from pyxtal_ff_gb300.descriptors.SNAP import SO4_Bispectrum as SNAP
+from pyxtal_ff_gb300.descriptors.SO4 import SO4_Bispectrum as SO4
+from tests import goldens as G
+
+pytestmark = pytest.mark.gpu
+
+
+def _dropin(meta):
+    kw = G.descriptor_kwargs(meta)
+    kind = kw.pop("kind")
+    cutoff = kw.pop("cutoff")
+    atom_ids = kw.pop("atom_ids", None)
+    common = dict(lmax=kw["lmax"], rcut=kw["rcut"], derivative=kw["derivative"], stress=kw["stress"],
+                  normalize_U=kw["normalize_U"], cutoff_function=cutoff)
+    if kind == "SO4":
+        return SO4(**common), atom_ids
+    return SNAP(kw["weights"], rfac0=kw["rfac0"], **common), atom_ids
+
+
+@pytest.mark.parametrize("name", G.names())
+def test_dropin_matches_reference_goldens(cuda_device, name):
+    atoms, meta, d = G.load(name)
+    desc, atom_ids = _dropin(meta)
+    out = desc.calculate(atoms, atom_ids=atom_ids)
+    errs = G.compare_to_golden(out, d, tol=1e-10)
+    assert out["elements"] == list(atoms.symbols)
+    assert isinstance(out["x"], np.ndarray) and out["x"].dtype == np.float64
+    if meta["derivative"]:
+        assert out["seq"].dtype == np.int64
+    else:
+        assert "seq" not in out and out["dxdr"] is None
+    print(name, errs)
+
+
+def _batch_arrays(structs):
+    pos = np.concatenate([s.positions for s in structs])
+    cells = np.stack([s.get_cell() for s in structs])
+    pbc = np.stack([np.asarray(s.pbc, dtype=np.int32) for s in structs])
+    ptr = np.concatenate([[0], np.cumsum([len(s) for s in structs])])
+    return pos, cells, pbc, ptr
+
+
+@pytest.mark.parametrize("rc", [3.0, 4.9, 6.5])
+def test_neighbor_list_bit_exact_vs_oracle(cuda_device, rc):
+    rng = np.random.default_rng(7)
+    structs = [S.diamond_si(1, 1, 1, sigma=0.1, strain=0.05, rng=rng),
+               S.diamond_si(2, 1, 1, sigma=0.1, strain=0.05, rng=rng),
+               S.sio2_random(n_si=8, seed=3), S.nacl_cluster(3.0),
+               S.diamond_si(3, 3, 2, sigma=0.1, rng=rng)]
+    pos, cells, pbc, ptr = _batch_arrays(structs)
+    nb = engine.build_neighbors(pos, cells, pbc, ptr, rc)
+    seq_all, pimg = nb.seq.cpu().numpy(), nb.pair_img.cpu().numpy()
+    img_ptr = nb.img_ptr.cpu().numpy()
+    pair_ptr = nb.pair_ptr.cpu().numpy()
+    for s, st in enumerate(structs):
+        a0, a1 = ptr[s], ptr[s + 1]
+        onl = O.NeighborList(st.positions, st.get_cell(), np.asarray(st.pbc, dtype=np.int32), rc)
+        m0, m1 = img_ptr[a0], img_ptr[a1]
+        assert np.array_equal(nb.img_j[m0:m1].cpu().numpy() - a0, onl.img_j)
+        assert np.array_equal(nb.img_off[m0:m1].cpu().numpy(), onl.img_off)
+        assert np.array_equal(nb.img_r[m0:m1].cpu().numpy().view(np.int64), onl.img_r.view(np.int64))
+        p0, p1 = pair_ptr[a0], pair_ptr[a1]
+        assert np.array_equal(seq_all[p0:p1], onl.seq)
+        assert np.array_equal(pimg[p0:p1] - m0, onl.pair_img[:-1])
+        assert np.array_equal(nb.nsite[a0:a1].cpu().numpy() - p0, onl.nsite)
+    rev = nb.img_rev.cpu().numpy()
+    assert np.array_equal(rev[rev], np.arange(len(rev)))
+    assert not nb.no_neighbor
+
+
+def test_isolated_atom_raises_like_reference(cuda_device):
+    atoms = S.Atoms([14, 14, 14], [[1, 1, 1], [2.5, 1, 1], [9, 9, 9]], 20 * np.eye(3))
+    with pytest.raises(ValueError):
+        SO4(lmax=2, rcut=3.0).calculate(atoms)
+
+
+def test_nonfinite_positions_raise(cuda_device):
+    atoms = S.Atoms([14, 14], [[1, 1, 1], [np.nan, 1, 1]], 10 * np.eye(3))
+    with pytest.raises(ValueError):
+        SO4(lmax=2, rcut=3.0).calculate(atoms)
+
+
+def _plain_batch(structs, lmax, rc, precision, kind="SNAP", weights=None, rfac0=1.0):
+    pos, cells, pbc, ptr = _batch_arrays(structs)
+    numbers = np.concatenate([s.numbers for s in structs])
+    symbols = sum([list(s.symbols) for s in structs], [])
+    tab = engine.tables(2 * lmax)
+    prm = engine.params(2 * lmax, rc, rfac0, "cosine")
+    pos_d = torch.from_numpy(pos).cuda()
+    nb = engine.build_neighbors(pos_d, cells, pbc, ptr, rc)
+    w_nb, w_site = engine.site_weights(kind, numbers, symbols, weights)
+    w_nb, w_site = torch.from_numpy(w_nb).cuda(), torch.from_numpy(w_site).cuda()
+    return nb, engine.plain(tab, prm, nb, pos_d, w_nb, w_site, precision=precision)
+
+
+def test_fp32_plain_vs_fp64_oracle_batched(cuda_device):
+    structs = S.si_batch(6, seed=1)
+    nb, (x, dxdr, rdxdr) = _plain_batch(structs, 3, 4.9, precision=1, weights={"Si": 1.0})
+    ptr = nb.atom_ptr
+    pptr = nb.pair_ptr.cpu().numpy()
+    for s, st in enumerate(structs):
+        ref = O.descriptor(st, kind="SNAP", lmax=3, rcut=4.9, weights={"Si": 1.0}, rfac0=1.0, stress=True)
+        a0, a1 = ptr[s], ptr[s + 1]
+        p0, p1 = pptr[a0], pptr[a1]
+        assert G.rel_err(x[a0:a1].cpu().numpy(), ref["x"]) < 2e-5
+        assert G.rel_err(dxdr[p0:p1].cpu().numpy(), ref["dxdr"]) < 2e-4
+        assert G.rel_err(rdxdr[p0:p1].cpu().numpy(), ref["rdxdr"]) < 2e-4
+
+
+def test_fp64_plain_batched_vs_oracle(cuda_device):
+    structs = S.si_batch(4, seed=2) + [S.sio2_random(n_si=8, seed=4)]
+    w = {"Si": 1.0, "O": 0.5}
+    nb, (x, dxdr, rdxdr) = _plain_batch(structs, 4, 5.0, precision=0, weights=w, rfac0=0.99363)
+    ptr = nb.atom_ptr
+    pptr = nb.pair_ptr.cpu().numpy()
+    for s, st in enumerate(structs):
+        ref = O.descriptor(st, kind="SNAP", lmax=4, rcut=5.0, weights=w, rfac0=0.99363, stress=True)
+        a0, a1 = ptr[s], ptr[s + 1]
+        p0, p1 = pptr[a0], pptr[a1]
+        assert G.rel_err(x[a0:a1].cpu().numpy(), ref["x"]) < 1e-10
+        assert G.rel_err(dxdr[p0:p1].cpu().numpy(), ref["dxdr"]) < 1e-10
+        assert G.rel_err(rdxdr[p0:p1].cpu().numpy(), ref["rdxdr"]) < 1e-10
+
+
+@pytest.mark.parametrize("lmax,rc,w", [(3, 4.9, {"Si": 1.0}), (4, 5.0, {"Si": 1.0, "O": 0.5})])
+def test_adjoint_fp32_vs_oracle_contraction(cuda_device, lmax, rc, w):
+    structs = [S.diamond_si(2, 2, 1, sigma=0.1, rng=np.random.default_rng(5)), S.sio2_random(n_si=8, seed=9)]
+    pos, cells, pbc, ptr = _batch_arrays(structs)
+    numbers = np.concatenate([s.numbers for s in structs])
+    symbols = sum([list(s.symbols) for s in structs], [])
+    tab = engine.tables(2 * lmax)
+    prm = engine.params(2 * lmax, rc, 0.99363, "cosine")
+    nb = engine.build_neighbors(torch.from_numpy(pos).cuda(), cells, pbc, ptr, rc)
+    w_nb, w_site = engine.site_weights("SNAP", numbers, symbols, w)
+    w_nb, w_site = torch.from_numpy(w_nb).cuda(), torch.from_numpy(w_site).cuda()
+    x, utot = engine.forward32(tab, prm, nb, w_nb, w_site)
+    beta = np.random.default_rng(6).normal(0, 0.01, size=(len(pos), tab.nB))
+    forces, virial = engine.adjoint32(tab, prm, nb, w_nb, utot, torch.from_numpy(beta).float().cuda())
+    forces, virial = forces.cpu().numpy(), virial.cpu().numpy()
+    for s, st in enumerate(structs):
+        a0, a1 = ptr[s], ptr[s + 1]
+        ref = O.forces_virial(st, beta[a0:a1], kind="SNAP", lmax=lmax, rcut=rc, weights=w, rfac0=0.99363)
+        assert G.rel_err(x[a0:a1].cpu().numpy(), ref["x"]) < 2e-5
+        ef = G.rel_err(forces[a0:a1], ref["forces"])
+        ev = G.rel_err(virial[s] / nb.vol[s], ref["virial"])
+        print("lmax", lmax, "struct", s, "force rel", ef, "abs", np.abs(forces[a0:a1] - ref["forces"]).max(),
+              "virial rel", ev)
+        assert ef < 2e-4 and ev < 2e-4
