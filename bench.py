@@ -1,0 +1,379 @@
+"""Benchmark of the SO4 energy + forces + stress path on one GB300 (or N replicas).
+
+Workload: diamond-Si 20x20x10 supercell (32,000 atoms, a = 5.43 A, Gaussian
+displacement sigma = 0.1 A, seed 5), SO4 lmax = 4, rcut = 5.0 A, cosine cutoff,
+unit Si weight, psi = pi r / rcut; energy from a fixed linear model with
+coefficients ~ N(0, 0.01) (seed 6).  One step = GPU neighbour list + FP32
+forward (U_tot, B) + model + FP32 adjoint (forces, virial), with the positions
+already in HBM.  The FP64 plain dB/dr path (NL + B, dxdr, rdxdr + the
+consumers' contraction) is timed on the same structure and is the error
+reference.  `e2e` is the same metric through SO4Calculator.compute() from
+pinned host positions, with the H2D copy and the D2H read of energy, forces
+and stress inside the timed region.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+LMAX, RCUT, SEED_POS, SEED_COEF = 4, 5.0, 5, 6
+METRIC = "SO4 atoms/s w/ forces+stress: FP32 adjoint vs plain FP64 dB/dr, 1 GB300; err vs FP64"
+CONFIG = {"workload": "diamond-Si 20x20x10 (32000 atoms), SO4 lmax=4, rcut=5.0 A, energy+forces+stress, "
+                      "linear model N(0,0.01)", "structures": 1, "atoms": 32000, "lmax": LMAX, "rcut": RCUT,
+          "neighbor_list": "in step", "l2": "flushed between steps (512 MiB write)"}
+
+
+def workload():
+    from pyxtal_ff_gb300 import structures as S
+    atoms = S.diamond_si(20, 20, 10, sigma=0.1, rng=np.random.default_rng(SEED_POS))
+    from pyxtal_ff_gb300.flops import sizes
+    nB = sizes(2 * LMAX)["nB"]
+    coef = np.random.default_rng(SEED_COEF).normal(0.0, 0.01, size=nB)
+    return atoms, coef
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+# ----------------------------------------------------------------- clocks
+class Clocks:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        if self.proc is None:
+            return out
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                rows.append((float(f[1]), float(f[2]), float(f[3]), f[5:9]))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return out
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i, v in enumerate(r[3]) if v.lower() == "active"})
+        load = [r for r in rows if r[2] > 250.0] or rows
+        out.update(sm_mhz=float(np.median([r[0] for r in load])), sm_max_mhz=max(r[1] for r in rows),
+                   reasons=reasons, samples=len(rows), power_w_max=max(r[2] for r in rows))
+        return out
+
+
+# ----------------------------------------------------------------- peaks
+def measured_peaks(torch):
+    """Measured denominators: HBM from MEASURED_PEAKS.json; FP32 / FP64 CUDA-core rates
+    measured here with cuBLAS SGEMM (TF32 off) / DGEMM, since that file has none."""
+    peaks = {}
+    try:
+        peaks.update(json.load(open(os.path.join(HERE, "MEASURED_PEAKS.json"))))
+        peaks["source"] = "MEASURED_PEAKS.json"
+    except Exception:
+        peaks.update(hbm_gbs=6800.0, source="fallback")
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    for name, dt, n in (("fp32_tflops", torch.float32, 8192), ("fp64_tflops", torch.float64, 4096)):
+        a = torch.randn(n, n, device="cuda", dtype=dt)
+        b = torch.randn(n, n, device="cuda", dtype=dt)
+        for _ in range(2):
+            a @ b
+        torch.cuda.synchronize()
+        best = 1e9
+        for _ in range(5):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            a @ b
+            e1.record()
+            torch.cuda.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+        peaks[name] = 2.0 * n ** 3 / (best * 1e-3) / 1e12
+        del a, b
+    torch.backends.cuda.matmul.allow_tf32 = prev
+    return peaks
+
+
+# ----------------------------------------------------------------- CPU side
+def cpu_run(atoms, coef, nthreads):
+    """The oracle (C restatement of the reference path, FP64) on every centre of the
+    workload: energy, forces and the contracted virial."""
+    from oracle import oracle as O
+    t0 = time.perf_counter()
+    beta = np.broadcast_to(coef, (len(atoms), len(coef)))
+    O.forces_virial(atoms, beta, kind="SNAP", lmax=LMAX, rcut=RCUT, weights={"Si": 1.0}, rfac0=1.0,
+                    nthreads=nthreads)
+    return time.perf_counter() - t0
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return
+    atoms, coef = workload()
+    nth = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_run(atoms, coef, nth)
+    times = [cpu_run(atoms, coef, nth) for _ in range(args.steps)]
+    t = float(np.sum(times))
+    value = len(atoms) * args.steps / t
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "atoms/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded)", "config": CONFIG,
+            "cpu_baseline": {"value": value, "unit": "atoms/s", "cores": nth, "kind": "port",
+                             "sample": "all 32000 centres of the workload per step (oracle, OpenMP)"},
+            "e2e": {"value": value, "unit": "atoms/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------- GPU side
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--quick", action="store_true",
+                    help="device-resident steps only (no e2e, FP64, CPU or peak legs); for profiler runs")
+    args = ap.parse_args()
+    ws, rank, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+        return
+
+    import torch
+    import torch.distributed as dist
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if ws > 1:
+        dist.init_process_group("nccl", device_id=dev)
+
+    def barrier():
+        if ws > 1:
+            dist.barrier()
+
+    def max_over_ranks(v):
+        if ws == 1:
+            return v
+        t = torch.tensor([v], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    from pyxtal_ff_gb300 import _lib, engine, flops
+    from pyxtal_ff_gb300.calculator import Batch, LinearModel, SO4Calculator, contract_plain
+
+    atoms, coef = workload()
+    batch = Batch([atoms])
+    calc = SO4Calculator(lmax=LMAX, rcut=RCUT, kind="SNAP", weights={"Si": 1.0}, rfac0=1.0, device=dev)
+    model = LinearModel(coef).to(dev)
+    calc.prepare(batch)
+    pos_dev = torch.from_numpy(batch.positions).to(dev)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    tab, prm = calc.tables, calc.params
+    L = _lib.lib()
+
+    stage_names = ["neighbors", "forward32", "model", "adjoint_y32", "adjoint_deidrj32", "gather"]
+
+    def device_step(ev=None):
+        """One step with the inputs in HBM; ev: list of events recorded between stages."""
+        def mark(i):
+            if ev is not None:
+                ev[i].record()
+        mark(0)
+        nb = calc.neighbors(batch, pos_dev)
+        mark(1)
+        x, utot = engine.forward32(tab, prm, nb, calc._w_nb, calc._w_site)
+        mark(2)
+        xg = x.detach().requires_grad_(True)
+        with torch.enable_grad():
+            e_atom = model(xg, calc._species)
+            beta, = torch.autograd.grad(e_atom.sum(), xg)
+        mark(3)
+        out = engine.adjoint32_staged(tab, prm, nb, calc._w_nb, utot, beta, mark=mark, first=3)
+        energy = e_atom.detach().double().sum()
+        mark(6)
+        return energy, out
+
+    # ---- warm-up
+    for _ in range(args.warmup):
+        device_step()
+    torch.cuda.synchronize()
+
+    # ---- device-resident timed region
+    clocks = Clocks(local)
+    nev = len(stage_names) + 1
+    stage_ms = np.zeros(len(stage_names))
+    step_ms = []
+    barrier()
+    torch.cuda.synchronize()
+    launches0 = L.so4_launch_count()
+    clocks.start()
+    for _ in range(args.steps):
+        flush.zero_()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(nev)]
+        device_step(ev)
+        ev[-1].synchronize()
+        step_ms.append(ev[0].elapsed_time(ev[-1]))
+        stage_ms += np.array([ev[i].elapsed_time(ev[i + 1]) for i in range(nev - 1)])
+    torch.cuda.synchronize()
+    barrier()
+    clk = clocks.stop()
+    launches = (L.so4_launch_count() - launches0) // args.steps
+    t_dev = max_over_ranks(float(np.sum(step_ms)))
+    natoms = len(atoms)
+    value = ws * natoms * args.steps / (t_dev * 1e-3)
+    stage_ms /= args.steps
+    if args.quick:
+        if rank == 0:
+            print(json.dumps({"quick": True, "value": value, "unit": "atoms/s", "ms_per_step": t_dev / args.steps,
+                              "stages_ms": dict(zip(stage_names, stage_ms.tolist())),
+                              "gpu_launches": int(launches)}), flush=True)
+        if ws > 1:
+            dist.destroy_process_group()
+        return
+
+    # ---- e2e through the public API, host buffers
+    pos_host = torch.from_numpy(batch.positions.copy()).pin_memory()
+    out_e = torch.empty(1, dtype=torch.float64).pin_memory()
+    out_f = torch.empty((natoms, 3), dtype=torch.float64).pin_memory()
+    out_s = torch.empty((1, 6), dtype=torch.float64).pin_memory()
+    for _ in range(2):
+        calc.compute(batch, model, positions=pos_host)
+    torch.cuda.synchronize()
+    barrier()
+    t_e2e = 0.0
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res = calc.compute(batch, model, positions=pos_host)
+        out_e.copy_(res["energy"], non_blocking=True)
+        out_f.copy_(res["forces"], non_blocking=True)
+        out_s.copy_(res["stress"], non_blocking=True)
+        torch.cuda.synchronize()
+        t_e2e += time.perf_counter() - t0
+    t_e2e = max_over_ranks(t_e2e)
+    e2e = {"value": ws * natoms * args.steps / t_e2e, "unit": "atoms/s",
+           "h2d_bytes_per_step": int(pos_host.numel() * 8),
+           "d2h_bytes_per_step": int(out_e.numel() * 8 + out_f.numel() * 8 + out_s.numel() * 8),
+           "ms_per_step": 1e3 * t_e2e / args.steps}
+
+    # ---- plain FP64 dB/dr path on the same structure + errors of the FP32 path
+    coef_t = torch.as_tensor(coef, dtype=torch.float64, device=dev)
+
+    def plain_step():
+        d = calc.descriptors(batch, pos_dev, precision="fp64")
+        beta64 = coef_t.expand(natoms, -1)
+        c = contract_plain(d["x"], d["dxdr"], d["rdxdr"], d["seq"], d["pair_ptr"], batch.atom_ptr, beta64,
+                           batch.volumes)
+        return d, c
+    plain_step()
+    torch.cuda.synchronize()
+    t64 = []
+    for _ in range(2):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        d64, c64 = plain_step()
+        e1.record()
+        e1.synchronize()
+        t64.append(e0.elapsed_time(e1))
+    ms64 = max_over_ranks(float(np.mean(t64)))
+    stress64 = c64["stress"]  # rdxdr already carries 1/vol
+    res = calc.compute(batch, model)
+    e64 = float((d64["x"].double() @ coef_t).sum())
+    err = {"force_max_abs_eV_per_A": float((res["forces"] - c64["forces"]).abs().max()),
+           "force_max_rel": float((res["forces"] - c64["forces"]).abs().max() / c64["forces"].abs().max()),
+           "stress_max_abs_GPa": float((res["stress"] - stress64).abs().max()),
+           "energy_rel": abs(float(res["energy"].sum()) - e64) / abs(e64),
+           "B_max_rel": float((res["x"].double() - d64["x"]).abs().max() / d64["x"].abs().max())}
+    del d64, c64
+    fp64 = {"ms_per_step": ms64, "atoms_per_s": ws * natoms / (ms64 * 1e-3),
+            "speedup_fp32_adjoint_over_fp64_plain": ms64 / (t_dev / args.steps)}
+
+    # ---- roofline of the dominant kernel (live CUDA events of the timed region)
+    nb = calc.neighbors(batch, pos_dev)
+    kf = flops.kernel_flops(2 * LMAX, nb.natoms, nb.nimg)
+    peaks = measured_peaks(torch)
+    i_dom = int(np.argmax(stage_ms))
+    dom = stage_names[i_dom]
+    if dom in kf:
+        achieved = kf[dom] / (stage_ms[i_dom] * 1e-3) / 1e12
+        roof = {"kernel": dom, "bound": "fp32", "achieved": achieved, "peak": peaks["fp32_tflops"],
+                "unit": "TFLOP/s", "frac": achieved / peaks["fp32_tflops"], "traffic": None,
+                "peak_source": "cuBLAS SGEMM (TF32 off) measured in this run"}
+    else:
+        roof = {"kernel": dom, "bound": "latency", "achieved": None, "peak": None, "unit": None, "frac": None,
+                "traffic": None}
+    kernels = {}
+    for i, nme in enumerate(stage_names):
+        k = {"ms": float(stage_ms[i])}
+        if nme in kf:
+            k["tflops"] = kf[nme] / (stage_ms[i] * 1e-3) / 1e12
+            k["frac_fp32"] = k["tflops"] / peaks["fp32_tflops"]
+        kernels[nme] = k
+    kernels["plain_fp64"] = {"ms": ms64, "tflops_fp64_incl_nl_contraction": kf["plain"] / (ms64 * 1e-3) / 1e12,
+                             "frac_fp64": kf["plain"] / (ms64 * 1e-3) / 1e12 / peaks["fp64_tflops"]}
+
+    # ---- CPU baseline (the oracle, all host threads), rank 0 only
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        nth = os.cpu_count() or 1
+        tcpu = cpu_run(atoms, coef, nth)
+        cpu = {"value": natoms / tcpu, "unit": "atoms/s", "cores": nth, "kind": "port",
+               "sample": "all 32000 centres of the workload, one evaluation (oracle, OpenMP, FP64)"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "atoms/s", "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": t_dev / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 tables and reductions)",
+                "data": "synthetic (seeded diamond-Si, sigma 0.1 A)", "config": CONFIG,
+                "pairs_per_s": ws * (nb.npair) * args.steps / (t_dev * 1e-3),
+                "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": int(launches),
+                "fp64_plain": fp64, "err_vs_fp64": err, "kernels": kernels,
+                "peaks": {k: peaks[k] for k in ("hbm_gbs", "fp32_tflops", "fp64_tflops") if k in peaks}}
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

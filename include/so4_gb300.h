@@ -177,6 +177,24 @@ int so4_adjoint32(const so4_tables *t, const so4_params *p, int nstruct, const i
                   int64_t nimg, const float *d_utot, const float *d_beta, double *d_forces,
                   double *d_virial, void *d_work, size_t work_bytes, void *stream);
 
+/* The three stages so4_adjoint32 runs, for callers that keep their own buffers:
+ *   so4_adjoint_y32      Y[natoms*idxu_half*2] f32 from U_tot and beta (one CTA per centre);
+ *   so4_adjoint_deidrj32 g[nimg*3] f32 = dE/dr of every image and the per-centre
+ *                        virial vatom[natoms*9] f64 (U and dU by the recursion, contracted with Y);
+ *   so4_adjoint_gather   forces[natoms*3] f64 = sum_m (g_m - g_rev(m)) and the
+ *                        per-structure virial[nstruct*9] f64, in a fixed order. */
+int so4_adjoint_y32(const so4_tables *t, int natoms, const float *d_utot, const float *d_beta, float *d_y,
+                    void *stream);
+int so4_adjoint_deidrj32(const so4_tables *t, const so4_params *p, int natoms, const double *d_w_nb,
+                         const int32_t *d_img_ptr, const int32_t *d_img_j, const double *d_img_r,
+                         const float *d_y, float *d_g, double *d_vatom, void *stream);
+int so4_adjoint_gather(int natoms, int nstruct, const int *d_atom_ptr, const int32_t *d_img_ptr,
+                       const int32_t *d_img_rev, const float *d_g, const double *d_vatom, double *d_forces,
+                       double *d_virial, void *stream);
+
+/* Number of kernels this library has launched since it was loaded. */
+long long so4_launch_count(void);
+
 /* Library version string. */
 const char *so4_version(void);
 

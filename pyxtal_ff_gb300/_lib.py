@@ -88,6 +88,10 @@ def lib():
                            _i, _i, _vp, _vp, _vp, _vp, _sz, _vp]),
         "so4_forward32": (_i, [_vp, C.POINTER(Params), _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
         "so4_adjoint_workspace_size": (_sz, [_vp, _i, _i64]),
+        "so4_adjoint_y32": (_i, [_vp, _i, _vp, _vp, _vp, _vp]),
+        "so4_adjoint_deidrj32": (_i, [_vp, C.POINTER(Params), _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+        "so4_adjoint_gather": (_i, [_i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+        "so4_launch_count": (C.c_longlong, []),
         "so4_adjoint32": (_i, [_vp, C.POINTER(Params), _i, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _i64, _vp, _vp,
                                _vp, _vp, _vp, _sz, _vp]),
     }
@@ -103,5 +107,6 @@ def exported_symbols():
     """Names the C ABI header declares (used by the load test)."""
     hdr = os.path.join(os.path.dirname(build_ext.HERE), "include", "so4_gb300.h")
     import re
-    names = re.findall(r"^\s*(?:int|size_t|const char \*)\s*\**\s*(so4_\w+)\s*\(", open(hdr).read(), re.M)
+    names = re.findall(r"^\s*(?:int|size_t|long long|const char \*)\s*\**\s*(so4_\w+)\s*\(", open(hdr).read(),
+                       re.M)
     return sorted(set(names))

@@ -1,0 +1,181 @@
+"""Batched energy / forces / stress on the GPU (the public API of the adjoint path).
+
+``SO4Calculator`` evaluates many structures in one pass: the GPU neighbour list,
+the FP32 forward (U_tot, B), a per-atom energy model on B, and the FP32 adjoint
+that turns beta = dE/dB into forces and the virial without forming dB/dr.  It is
+the batched counterpart of what the reference does per structure in
+pyxtal_ff/calculator/__init__.py:22-73 (compute_descriptor, then
+NeuralNetwork.calculate_properties :579-678, which contracts dxdr and rdxdr with
+dE/dx).  Stress follows the reference's convention:
+  stress_voigt (GPa) = -(1/V) sum_images r (x) dE/dr in (xx, yy, zz, xy, xz, yz) x 160.21766.
+
+``LinearModel`` is E_i = B_i . c[species_i] + b[species_i] (the reference's
+order-1 PolynomialRegression, pyxtal_ff/models/polynomialregression.py:374).
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import engine
+from .structures import as_arrays
+
+EV_A3_TO_GPA = 160.21766208
+VOIGT = [0, 4, 8, 1, 2, 5]
+
+
+class LinearModel(torch.nn.Module):
+    """Per-species linear energy on B: E_i = B_i . coef[s_i] + bias[s_i]."""
+
+    def __init__(self, coef, bias=None):
+        super().__init__()
+        coef = torch.as_tensor(coef, dtype=torch.float32)
+        if coef.dim() == 1:
+            coef = coef[None]
+        self.coef = torch.nn.Parameter(coef)
+        b = torch.zeros(coef.shape[0]) if bias is None else torch.as_tensor(bias, dtype=torch.float32).reshape(-1)
+        self.bias = torch.nn.Parameter(b)
+
+    def forward(self, x, species):
+        return (x * self.coef[species]).sum(-1) + self.bias[species]
+
+
+class Batch:
+    """Host description of a batch of structures (cells, pbc, atom ranges, species)."""
+
+    def __init__(self, structures, species_order=None):
+        pos, cells, pbcs, nums, syms = [], [], [], [], []
+        for s in structures:
+            p, c, b, n, y = as_arrays(s)
+            pos.append(p)
+            cells.append(c)
+            pbcs.append(b)
+            nums.append(n)
+            syms.extend(y)
+        self.positions = np.ascontiguousarray(np.concatenate(pos)) if pos else np.zeros((0, 3))
+        self.cells = np.stack(cells) if cells else np.zeros((0, 3, 3))
+        self.pbc = np.stack(pbcs).astype(np.int32) if pbcs else np.zeros((0, 3), np.int32)
+        self.numbers = np.concatenate(nums) if nums else np.zeros(0, np.int64)
+        self.symbols = syms
+        self.atom_ptr = np.concatenate([[0], np.cumsum([len(p) for p in pos])]).astype(np.int64)
+        self.volumes = np.abs(np.linalg.det(self.cells)) if len(cells) else np.zeros(0)
+        order = species_order or sorted(set(syms))
+        self.species_order = list(order)
+        idx = {s: i for i, s in enumerate(self.species_order)}
+        self.species = np.array([idx[s] for s in syms], dtype=np.int64)
+
+    @property
+    def natoms(self):
+        return int(self.atom_ptr[-1])
+
+    @property
+    def nstruct(self):
+        return len(self.atom_ptr) - 1
+
+
+class SO4Calculator:
+    """Energy, forces and stress of many structures with the FP32 adjoint kernels.
+
+    kind="SO4": neighbour and site weights are atomic numbers, psi = pi r / rcut
+    (pyxtal_ff/descriptors/SO4.py).  kind="SNAP": weights[symbol] and 1,
+    psi = rfac0 pi r / rcut (pyxtal_ff/descriptors/SNAP.py).
+    """
+
+    def __init__(self, lmax=3, rcut=3.5, kind="SO4", weights=None, rfac0=0.99363, cutoff_function="cosine",
+                 normalize_U=False, device="cuda"):
+        engine.require_cuda()
+        if kind not in ("SO4", "SNAP"):
+            raise ValueError("kind must be 'SO4' or 'SNAP'")
+        if kind == "SNAP" and not isinstance(weights, dict):
+            raise TypeError("weights must be a dictionary")
+        self.kind = kind
+        self.weights = weights
+        self.lmax = lmax
+        self.twol = int(round(2 * lmax))
+        self.rcut = float(rcut)
+        self.rfac0 = 1.0 if kind == "SO4" else float(rfac0)
+        self.cutoff_function = cutoff_function
+        self.device = torch.device(device)
+        with torch.cuda.device(self.device):
+            self.tables = engine.tables(self.twol, normalize_U)
+        self.params = engine.params(self.twol, self.rcut, self.rfac0, cutoff_function)
+        self._ws = None
+        self._batch_key = None
+
+    @property
+    def nB(self):
+        return self.tables.nB
+
+    def prepare(self, batch: Batch):
+        """Upload the per-atom weights and species of a batch (once per batch layout)."""
+        key = id(batch)
+        if key != self._batch_key:
+            w_nb, w_site = engine.site_weights(self.kind, batch.numbers, batch.symbols, self.weights)
+            self._w_nb = torch.from_numpy(w_nb).to(self.device)
+            self._w_site = torch.from_numpy(w_site).to(self.device)
+            self._species = torch.from_numpy(batch.species).to(self.device)
+            self._struct = torch.from_numpy(np.repeat(np.arange(batch.nstruct), np.diff(batch.atom_ptr))).to(self.device)
+            self._vol = torch.from_numpy(batch.volumes).to(self.device)
+            self._batch_key = key
+        return self
+
+    def neighbors(self, batch: Batch, positions):
+        return engine.build_neighbors(positions, batch.cells, batch.pbc, batch.atom_ptr, self.rcut, device=self.device)
+
+    def descriptors(self, batch: Batch, positions=None, precision="fp64", derivative=True, stress=True):
+        """Plain path for a batch: x, dxdr, rdxdr, seq on the device."""
+        self.prepare(batch)
+        pos = self._positions(batch, positions)
+        nb = self.neighbors(batch, pos)
+        x, dxdr, rdxdr = engine.plain(self.tables, self.params, nb, pos, self._w_nb, self._w_site,
+                                      precision=0 if precision == "fp64" else 1, want_deriv=derivative,
+                                      want_stress=stress)
+        return dict(x=x, dxdr=dxdr, rdxdr=rdxdr, seq=nb.seq, pair_ptr=nb.pair_ptr, neighbors=nb)
+
+    def _positions(self, batch, positions):
+        if positions is None:
+            positions = batch.positions
+        if isinstance(positions, np.ndarray):
+            positions = torch.from_numpy(np.ascontiguousarray(positions, dtype=np.float64))
+        return positions.to(self.device, dtype=torch.float64, non_blocking=True).contiguous()
+
+    def compute(self, batch: Batch, model, positions=None):
+        """Energy (S,) f64, forces (N,3) f64, virial (S,3,3) f64, stress (S,6) GPa and B."""
+        self.prepare(batch)
+        pos = self._positions(batch, positions)
+        nb = self.neighbors(batch, pos)
+        x, utot = engine.forward32(self.tables, self.params, nb, self._w_nb, self._w_site)
+        xg = x.detach().requires_grad_(True)
+        with torch.enable_grad():
+            e_atom = model(xg, self._species)
+            beta, = torch.autograd.grad(e_atom.sum(), xg)
+        need = engine.lib().so4_adjoint_workspace_size(self.tables.handle, nb.natoms, nb.nimg)
+        if self._ws is None or self._ws.numel() < need:
+            self._ws = torch.empty(int(need * 1.25) + 4096, dtype=torch.uint8, device=self.device)
+        forces, virial = engine.adjoint32(self.tables, self.params, nb, self._w_nb, utot, beta, workspace=self._ws)
+        energy = torch.zeros(batch.nstruct, dtype=torch.float64, device=self.device)
+        energy.index_add_(0, self._struct, e_atom.detach().double())
+        stress = -(virial.reshape(-1, 9)[:, VOIGT] / self._vol[:, None]) * EV_A3_TO_GPA
+        return dict(energy=energy, forces=forces, virial=virial, stress=stress, x=x, neighbors=nb)
+
+
+def contract_plain(x, dxdr, rdxdr, seq, pair_ptr, atom_ptr, beta, volumes):
+    """Forces and stress from the plain path's dxdr / rdxdr, as the reference's
+    consumers contract them (neuralnetwork.py:492, 497, 677-678), in FP64:
+      F_m = -sum_i beta_i . dxdr_dense[i, m],  stress = -sum_i beta_i . rdxdr_atom[i] x 160.21766."""
+    dev = dxdr.device
+    atom_ptr_t = torch.as_tensor(np.asarray(atom_ptr), device=dev)
+    natoms = int(atom_ptr[-1])
+    centre = torch.repeat_interleave(torch.arange(natoms, device=dev), (pair_ptr[1:] - pair_ptr[:-1]).long())
+    struct = torch.repeat_interleave(torch.arange(len(atom_ptr) - 1, device=dev), (atom_ptr_t[1:] - atom_ptr_t[:-1]))
+    base = atom_ptr_t[:-1][struct[centre]]
+    j = seq[:, 1] + base
+    b = beta.double()[centre]
+    contrib = torch.einsum("pk,pkc->pc", b, dxdr.double())
+    forces = torch.zeros((natoms, 3), dtype=torch.float64, device=dev).index_add_(0, j, -contrib)
+    vir_pair = torch.einsum("pk,pkab->pab", b, rdxdr.double())
+    vir = torch.zeros((len(atom_ptr) - 1, 3, 3), dtype=torch.float64, device=dev).index_add_(0, struct[centre], vir_pair)
+    stress = -(vir.reshape(-1, 9)[:, VOIGT]) * EV_A3_TO_GPA
+    energy = torch.zeros(len(atom_ptr) - 1, dtype=torch.float64, device=dev).index_add_(
+        0, struct, (beta.double() * x.double()).sum(-1))
+    return dict(forces=forces, stress=stress, energy=energy)

@@ -309,6 +309,7 @@ extern "C" int so4_forward32(const so4_tables *t, const so4_params *p, int natom
     int rc = set_smem(k_forward32, smem);
     if (rc) return rc;
     k_forward32<<<natoms, NWF * 32, smem, (cudaStream_t)stream>>>(A);
+    so4_count_launch();
     return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
 }
 
@@ -318,6 +319,79 @@ extern "C" size_t so4_adjoint_workspace_size(const so4_tables *t, int natoms, in
     return carve_adj(w, nullptr, natoms, t->n_half, nimg);
 }
 
+extern "C" int so4_adjoint_y32(const so4_tables *t, int natoms, const float *d_utot, const float *d_beta, float *d_y,
+                               void *stream) {
+    if (!t || natoms < 0 || !d_utot || !d_beta || !d_y) return SO4_ERR_ARG;
+    if (natoms == 0) return SO4_OK;
+    YArgs Y;
+    Y.natoms = natoms;
+    Y.nh = t->n_half;
+    Y.nu = t->n_u;
+    Y.nz = t->n_z;
+    Y.nB = t->n_b;
+    Y.nblk = t->n_blk;
+    Y.utot = d_utot;
+    Y.beta = d_beta;
+    Y.cg = t->d_cg32;
+    Y.zent = t->d_z;
+    Y.blk = t->d_blk;
+    Y.yptr = t->d_yblk_ptr;
+    Y.ylist = t->d_yblk;
+    fill_small_tables(t, Y.st);
+    Y.Y = (float2 *)d_y;
+    const size_t smy = sizeof(cx<float>) * ((size_t)t->n_half + t->n_u + t->n_z) + sizeof(float) * ((t->n_blk + 3) & ~3);
+    int rc = set_smem(k_yi, smy);
+    if (rc) return rc;
+    k_yi<<<natoms, NWY * 32, smy, (cudaStream_t)stream>>>(Y);
+    so4_count_launch();
+    return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
+}
+
+extern "C" int so4_adjoint_deidrj32(const so4_tables *t, const so4_params *p, int natoms, const double *d_w_nb,
+                                    const int32_t *d_img_ptr, const int32_t *d_img_j, const double *d_img_r,
+                                    const float *d_y, float *d_g, double *d_vatom, void *stream) {
+    if (!t || !p || natoms < 0 || !d_y || !d_g || !d_vatom) return SO4_ERR_ARG;
+    if (p->twol != t->twol || !(p->rcut > 0.0) || !(p->rfac0 > 0.0)) return SO4_ERR_ARG;
+    if (p->cutoff_id < 1 || p->cutoff_id > 7) return SO4_ERR_UNSUPPORTED;
+    if (natoms == 0) return SO4_OK;
+    DArgs D;
+    D.prm = *p;
+    D.natoms = natoms;
+    D.nh = t->n_half;
+    D.w_nb = d_w_nb;
+    D.img_r = d_img_r;
+    D.img_ptr = d_img_ptr;
+    D.img_j = d_img_j;
+    D.rootpq = t->d_rootpq32;
+    fill_small_tables(t, D.st);
+    D.Y = (const float2 *)d_y;
+    D.g = d_g;
+    D.vatom = d_vatom;
+    const size_t smd =
+        sizeof(float) * rootpq_floats(t->ldim) + sizeof(cx<float>) * ((size_t)t->n_half + (size_t)NWD * 4 * t->n_half);
+    int rc = set_smem(k_deidrj, smd);
+    if (rc) return rc;
+    k_deidrj<<<natoms, NWD * 32, smd, (cudaStream_t)stream>>>(D);
+    so4_count_launch();
+    return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
+}
+
+extern "C" int so4_adjoint_gather(int natoms, int nstruct, const int *d_atom_ptr, const int32_t *d_img_ptr,
+                                  const int32_t *d_img_rev, const float *d_g, const double *d_vatom, double *d_forces,
+                                  double *d_virial, void *stream) {
+    if (natoms < 0 || nstruct < 0) return SO4_ERR_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (natoms > 0) {
+        k_gather<<<(natoms + 127) / 128, 128, 0, st>>>(natoms, d_img_ptr, d_img_rev, d_g, d_forces);
+        so4_count_launch();
+    }
+    if (nstruct > 0) {
+        k_virial<<<nstruct, 256, 0, st>>>(d_atom_ptr, d_vatom, d_virial);
+        so4_count_launch();
+    }
+    return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
+}
+
 extern "C" int so4_adjoint32(const so4_tables *t, const so4_params *p, int nstruct, const int *d_atom_struct,
                              const int *d_atom_ptr, int natoms, const double *d_w_nb, const int32_t *d_img_ptr,
                              const int32_t *d_img_j, const double *d_img_r, const int32_t *d_img_rev, int64_t nimg,
@@ -325,55 +399,14 @@ extern "C" int so4_adjoint32(const so4_tables *t, const so4_params *p, int nstru
                              void *d_work, size_t work_bytes, void *stream) {
     (void)d_atom_struct;
     if (!t || !p || natoms < 0 || nstruct < 0 || nimg < 0 || !d_work) return SO4_ERR_ARG;
-    if (p->twol != t->twol || !(p->rcut > 0.0) || !(p->rfac0 > 0.0)) return SO4_ERR_ARG;
-    if (p->cutoff_id < 1 || p->cutoff_id > 7) return SO4_ERR_UNSUPPORTED;
     AdjWork w;
     if (carve_adj(w, nullptr, natoms, t->n_half, nimg) > work_bytes) return SO4_ERR_WORKSPACE;
     carve_adj(w, d_work, natoms, t->n_half, nimg);
-    cudaStream_t st = (cudaStream_t)stream;
-    if (natoms > 0) {
-        YArgs Y;
-        Y.natoms = natoms;
-        Y.nh = t->n_half;
-        Y.nu = t->n_u;
-        Y.nz = t->n_z;
-        Y.nB = t->n_b;
-        Y.nblk = t->n_blk;
-        Y.utot = d_utot;
-        Y.beta = d_beta;
-        Y.cg = t->d_cg32;
-        Y.zent = t->d_z;
-        Y.blk = t->d_blk;
-        Y.yptr = t->d_yblk_ptr;
-        Y.ylist = t->d_yblk;
-        fill_small_tables(t, Y.st);
-        Y.Y = w.Y;
-        const size_t smy =
-            sizeof(cx<float>) * ((size_t)t->n_half + t->n_u + t->n_z) + sizeof(float) * ((t->n_blk + 3) & ~3);
-        int rc = set_smem(k_yi, smy);
-        if (rc) return rc;
-        k_yi<<<natoms, NWY * 32, smy, st>>>(Y);
-
-        DArgs D;
-        D.prm = *p;
-        D.natoms = natoms;
-        D.nh = t->n_half;
-        D.w_nb = d_w_nb;
-        D.img_r = d_img_r;
-        D.img_ptr = d_img_ptr;
-        D.img_j = d_img_j;
-        D.rootpq = t->d_rootpq32;
-        fill_small_tables(t, D.st);
-        D.Y = w.Y;
-        D.g = w.g;
-        D.vatom = w.vatom;
-        const size_t smd = sizeof(float) * rootpq_floats(t->ldim) +
-                           sizeof(cx<float>) * ((size_t)t->n_half + (size_t)NWD * 4 * t->n_half);
-        rc = set_smem(k_deidrj, smd);
-        if (rc) return rc;
-        k_deidrj<<<natoms, NWD * 32, smd, st>>>(D);
-        k_gather<<<(natoms + 127) / 128, 128, 0, st>>>(natoms, d_img_ptr, d_img_rev, w.g, d_forces);
-    }
-    if (nstruct > 0) k_virial<<<nstruct, 256, 0, st>>>(d_atom_ptr, w.vatom, d_virial);
-    return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
+    int rc = so4_adjoint_y32(t, natoms, d_utot, d_beta, (float *)w.Y, stream);
+    if (rc) return rc;
+    rc = so4_adjoint_deidrj32(t, p, natoms, d_w_nb, d_img_ptr, d_img_j, d_img_r, (const float *)w.Y, w.g, w.vatom,
+                              stream);
+    if (rc) return rc;
+    return so4_adjoint_gather(natoms, nstruct, d_atom_ptr, d_img_ptr, d_img_rev, w.g, w.vatom, d_forces, d_virial,
+                              stream);
 }

@@ -359,3 +359,6 @@ __host__ __device__ __forceinline__ int section_count(int lam) {
 
 // status word at the start of every workspace
 #define SO4_WS_HEADER 256
+
+// number of kernels this library has launched (so4_launch_count)
+void so4_count_launch(int n = 1);

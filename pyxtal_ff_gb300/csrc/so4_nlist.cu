@@ -409,18 +409,24 @@ extern "C" int so4_nl_count(const so4_geom *d_geom, int nstruct, int nbins, cons
     SO4_CUDA_TRY(cudaMemsetAsync(w.status, 0, sizeof(int), st));
     if (natoms == 0) {
         k_set_int<<<1, 1, 0, st>>>(d_img_ptr, 0);
+        so4_count_launch();
         return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
     }
     SO4_CUDA_TRY(cudaMemsetAsync(w.bin_cnt, 0, sizeof(int) * (nbins + 1), st));
     SO4_CUDA_TRY(cudaMemsetAsync(w.bin_cur, 0, sizeof(int) * (nbins + 1), st));
     const int tb = 256;
     k_bin<<<(natoms + tb - 1) / tb, tb, 0, st>>>(d_geom, d_pos, d_astruct, natoms, w);
+    so4_count_launch();
     k_scan<<<1, 1024, 0, st>>>(w.bin_cnt, w.bin_start, nbins);
+    so4_count_launch();
     k_bin_fill<<<(natoms + tb - 1) / tb, tb, 0, st>>>(d_astruct, natoms, w);
+    so4_count_launch();
     const int warps = 8;
     k_scan_images<0><<<(natoms + warps - 1) / warps, 32 * warps, 0, st>>>(d_geom, d_pos, d_astruct, natoms, rcut,
                                                                           nullptr, w);
+    so4_count_launch();
     k_scan<<<1, 1024, 0, st>>>(w.cnt, d_img_ptr, natoms);
+    so4_count_launch();
     return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
 }
 
@@ -436,13 +442,17 @@ extern "C" int so4_nl_fill(const so4_geom *d_geom, int nstruct, int nbins, const
     cudaStream_t st = (cudaStream_t)stream;
     if (natoms == 0) {
         k_set_int<<<1, 1, 0, st>>>(d_pair_ptr, 0);
+        so4_count_launch();
         return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
     }
     const int warps = 8;
     const int grid = (natoms + warps - 1) / warps;
     k_scan_images<1><<<grid, 32 * warps, 0, st>>>(d_geom, d_pos, d_astruct, natoms, rcut, d_img_ptr, w);
+    so4_count_launch();
     k_sort<<<grid, 32 * warps, 0, st>>>(d_geom, d_pos, d_astruct, natoms, d_img_ptr, d_img_j, d_img_off, d_img_r, w);
+    so4_count_launch();
     k_scan<<<1, 1024, 0, st>>>(w.cnt, d_pair_ptr, natoms);
+    so4_count_launch();
     return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
 }
 
@@ -458,13 +468,17 @@ extern "C" int so4_nl_pairs(const so4_geom *d_geom, int nstruct, const int *d_as
     w.status = (int *)d_work;
     cudaStream_t st = (cudaStream_t)stream;
     k_set_int<<<1, 1, 0, st>>>(d_pair_img + npair, (int)nimg);
+    so4_count_launch();
     if (natoms == 0) return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
     const int tb = 128;
     k_pairs<<<(natoms + tb - 1) / tb, tb, 0, st>>>(d_geom, d_astruct, natoms, d_img_ptr, d_img_j, d_pair_ptr, d_seq,
                                                    d_pair_img, d_nsite, d_img_pair);
-    if (nimg > 0 && d_img_rev)
+    so4_count_launch();
+    if (nimg > 0 && d_img_rev) {
         k_rev<<<(unsigned)((nimg + 255) / 256), 256, 0, st>>>(d_astruct, natoms, d_img_ptr, d_img_j, d_img_off,
                                                               d_img_pair, nimg, d_seq, d_geom, d_img_rev, w);
+        so4_count_launch();
+    }
     return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
 }
 

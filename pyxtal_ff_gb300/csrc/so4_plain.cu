@@ -204,6 +204,7 @@ int launch_plain(const PlainArgs<T> &A, size_t smem, cudaStream_t st) {
     auto kern = k_plain<T, NW, KS>;
     if (smem > 48 * 1024) SO4_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     kern<<<A.natoms, NW * 32, smem, st>>>(A);
+    so4_count_launch();
     return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
 }
 

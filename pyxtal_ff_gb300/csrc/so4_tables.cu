@@ -323,3 +323,8 @@ extern "C" int so4_tables_export(const so4_tables *t, double *cg, int *idxb, int
 }
 
 extern "C" const char *so4_version(void) { return "so4_gb300 0.1.0 (sm_103a)"; }
+
+#include <atomic>
+static std::atomic<long long> g_launches{0};
+void so4_count_launch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+extern "C" long long so4_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }

@@ -244,3 +244,27 @@ def adjoint32(tab, prm, nb: Neighbors, w_nb, utot, beta, workspace=None):
                               _ptr(nb.img_rev), nb.nimg, _ptr(utot), _ptr(beta), _ptr(forces), _ptr(virial),
                               _ptr(ws), ws.numel(), _stream()), "so4_adjoint32")
     return forces[: nb.natoms], virial[: nb.nstruct]
+
+
+def adjoint32_staged(tab, prm, nb: Neighbors, w_nb, utot, beta, mark=None, first=0):
+    """adjoint32 as its three C-ABI stages (Y build, per-image contraction, gather) with
+    caller-visible buffers; mark(i) is called between stages (for timing)."""
+    dev = utot.device
+    beta = beta.to(torch.float32).contiguous()
+    N, M = nb.natoms, nb.nimg
+    y = torch.empty((max(N, 1), tab.n_half, 2), dtype=torch.float32, device=dev)
+    g = torch.empty((max(M, 1), 3), dtype=torch.float32, device=dev)
+    vatom = torch.empty((max(N, 1), 9), dtype=torch.float64, device=dev)
+    forces = torch.empty((max(N, 1), 3), dtype=torch.float64, device=dev)
+    virial = torch.empty((max(nb.nstruct, 1), 3, 3), dtype=torch.float64, device=dev)
+    L, st = lib(), _stream()
+    check(L.so4_adjoint_y32(tab.handle, N, _ptr(utot), _ptr(beta), _ptr(y), st), "so4_adjoint_y32")
+    if mark:
+        mark(first + 1)
+    check(L.so4_adjoint_deidrj32(tab.handle, C.byref(prm), N, _ptr(w_nb), _ptr(nb.img_ptr), _ptr(nb.img_j),
+                                 _ptr(nb.img_r), _ptr(y), _ptr(g), _ptr(vatom), st), "so4_adjoint_deidrj32")
+    if mark:
+        mark(first + 2)
+    check(L.so4_adjoint_gather(N, nb.nstruct, _ptr(nb.atom_ptr_dev), _ptr(nb.img_ptr), _ptr(nb.img_rev), _ptr(g),
+                               _ptr(vatom), _ptr(forces), _ptr(virial), st), "so4_adjoint_gather")
+    return forces[:N], virial[: nb.nstruct]

@@ -1,0 +1,130 @@
+"""Algorithmic floating-point work of each kernel, counted from the index tables.
+
+Convention: complex multiply 6 flop, complex add 2, real x complex 2, and
+Re(conj(a) b) 4 (two multiply-adds); a fused multiply-add counts 2.  The loops
+counted are the reference's (pyxtal_ff/descriptors/SO4.py), not the kernels'
+own bookkeeping:
+
+  U     per image   the recursion over the left-half rows of every level
+                    (compute_uarray_recursive :888-906): per entry, each of its
+                    one or two terms is a complex multiply and a real scaling
+                    (8), plus 2 per extra term;
+  dU    per image   the same entries, three components, each term
+                    conj(da) U + conj(a) dU scaled (16 per component), plus 6
+                    per extra term (compute_duarray_recursive :950-968);
+  Utot  per image   (w U) sfac accumulated: 6 per half entry (add_uarraytot);
+  Z     per atom    sum_ib [na (2 + 6 + 2) + 4] per Z entry (compute_zi);
+  B     per atom    4 per summed entry + 2 per component (compute_bi);
+  dB    per image   per component k, three sections of 4 dot products
+                    (sfac dU_c and r^ U against Z) = 16 per summed entry,
+                    plus 18 for the virial outer product (compute_dbidrj :1113-1227
+                    and the bstress update :1466-1468);
+  Y     per atom    4 flop per (Z entry, role) plus the Z entries themselves;
+  dE    per image   U + dU + 4 dot products against Y (16 per half entry).
+"""
+from __future__ import annotations
+
+
+def _blocks(twol):
+    for l1 in range(twol + 1):
+        for l2 in range(l1 + 1):
+            for l in range(l1 - l2, min(twol, l1 + l2) + 1, 2):
+                yield l1, l2, l
+
+
+def sizes(twol):
+    n_half = sum((l // 2 + 1) * (l + 1) for l in range(twol + 1))
+    n_u = sum((l + 1) ** 2 for l in range(twol + 1))
+    nB = sum(1 for (l1, l2, l) in _blocks(twol) if l >= l1)
+    n_z = sum((l // 2 + 1) * (l + 1) for (l1, l2, l) in _blocks(twol))
+    return dict(n_half=n_half, n_u=n_u, nB=nB, n_z=n_z)
+
+
+def _section(lam):
+    return ((lam + 1) // 2) * (lam + 1) + ((lam // 2 + 1) if lam % 2 == 0 else 0)
+
+
+def per_image_u(twol):
+    f = 0
+    for l in range(1, twol + 1):
+        for mb in range(l // 2 + 1):
+            for ma in range(l + 1):
+                t = (ma > 0) + (ma < l)
+                f += 8 * t + 2 * (t - 1)
+    return f
+
+
+def per_image_du(twol):
+    f = 0
+    for l in range(1, twol + 1):
+        for mb in range(l // 2 + 1):
+            for ma in range(l + 1):
+                t = (ma > 0) + (ma < l)
+                f += 3 * 16 * t + 6 * (t - 1)
+    return f
+
+
+def per_atom_z(twol):
+    f = 0
+    for (l1, l2, l) in _blocks(twol):
+        for mb in range(l // 2 + 1):
+            for ma in range(l + 1):
+                ma1min = max(0, (2 * ma - l - l2 + l1) // 2)
+                na = min(l1, (2 * ma - l + l2 + l1) // 2) - ma1min + 1
+                mb1min = max(0, (2 * mb - l - l2 + l1) // 2)
+                nb = min(l1, (2 * mb - l + l2 + l1) // 2) - mb1min + 1
+                f += nb * (na * 10 + 4)
+    return f
+
+
+def per_atom_z_b_blocks(twol):
+    """Z work restricted to the blocks B reads (l >= l1)."""
+    f = 0
+    for (l1, l2, l) in _blocks(twol):
+        if l < l1:
+            continue
+        for mb in range(l // 2 + 1):
+            for ma in range(l + 1):
+                ma1min = max(0, (2 * ma - l - l2 + l1) // 2)
+                na = min(l1, (2 * ma - l + l2 + l1) // 2) - ma1min + 1
+                mb1min = max(0, (2 * mb - l - l2 + l1) // 2)
+                nb = min(l1, (2 * mb - l + l2 + l1) // 2) - mb1min + 1
+                f += nb * (na * 10 + 4)
+    return f
+
+
+def per_atom_b(twol):
+    return sum(4 * _section(l) + 2 for (l1, l2, l) in _blocks(twol) if l >= l1)
+
+
+def per_image_db(twol):
+    f = 0
+    for (l1, l2, l) in _blocks(twol):
+        if l < l1:
+            continue
+        f += 16 * (_section(l) + _section(l1) + _section(l2)) + 3 * 6 + 18
+    return f
+
+
+def per_atom_y(twol):
+    roles = 0
+    for (l1, l2, l) in _blocks(twol):
+        if l < l1:
+            continue
+        roles += 3
+    n = sizes(twol)
+    # each Y entry gathers one complex scale-add per contributing block entry
+    return 4 * n["n_z"] + 2 * roles
+
+
+def kernel_flops(twol, natoms, nimg):
+    """Algorithmic flops of one launch of each kernel for a batch."""
+    n = sizes(twol)
+    u, du, z = per_image_u(twol), per_image_du(twol), per_atom_z(twol)
+    utot_img = u + 6 * n["n_half"]
+    return {
+        "forward32": natoms * (z + per_atom_b(twol)) + nimg * utot_img,
+        "adjoint_y32": natoms * (z + per_atom_y(twol)),
+        "adjoint_deidrj32": nimg * (u + du + 16 * n["n_half"] + 24),
+        "plain": natoms * (z + per_atom_b(twol)) + nimg * (utot_img + u + du + per_image_db(twol)),
+    }
