@@ -45,7 +45,8 @@ enum so4_status {
     SO4_ERR_NONFINITE = 5,    /* NaN/Inf in positions or cell                       */
     SO4_ERR_WORKSPACE = 6,    /* workspace smaller than the size query returned     */
     SO4_ERR_NO_NEIGHBOR = 7,  /* an atom has no neighbour image (reference raises ValueError, SO4.py:275) */
-    SO4_ERR_REVERSE = 8       /* an image has no reverse image (asymmetric list)    */
+    SO4_ERR_REVERSE = 8,      /* an image has no reverse image (asymmetric list)    */
+    SO4_ERR_TOO_LARGE = 9     /* problem needs more than the fixed scratch of so4_adjoint32_noalloc */
 };
 
 /* Maximum 2*lmax the kernels are compiled for (lmax <= 6). */
@@ -191,6 +192,21 @@ int so4_adjoint_deidrj32(const so4_tables *t, const so4_params *p, int natoms, c
 int so4_adjoint_gather(int natoms, int nstruct, const int *d_atom_ptr, const int32_t *d_img_ptr,
                        const int32_t *d_img_rev, const float *d_g, const double *d_vatom, double *d_forces,
                        double *d_virial, void *stream);
+
+/* so4_adjoint32 for callers that cannot allocate device memory.  No counterpart
+ * in the reference (whose CPU code has no device allocator to avoid).
+ * Same arguments as so4_adjoint32 without the workspace: the scratch comes from
+ * a fixed array of SO4_NOALLOC_SCRATCH_BYTES that every GPU loading the library
+ * holds until exit.  Problems whose so4_adjoint_workspace_size() exceeds it
+ * return SO4_ERR_TOO_LARGE.  The first call on each device looks up the
+ * array's address (make it before any stream capture); calls that overlap on
+ * the GPU race on the shared array.  Allocates nothing. */
+#define SO4_NOALLOC_SCRATCH_BYTES (64u << 20)
+int so4_adjoint32_noalloc(const so4_tables *t, const so4_params *p, int nstruct, const int *d_atom_struct,
+                          const int *d_atom_ptr, int natoms, const double *d_w_nb, const int32_t *d_img_ptr,
+                          const int32_t *d_img_j, const double *d_img_r, const int32_t *d_img_rev,
+                          int64_t nimg, const float *d_utot, const float *d_beta, double *d_forces,
+                          double *d_virial, void *stream);
 
 /* Number of kernels this library has launched since it was loaded. */
 long long so4_launch_count(void);

@@ -19,6 +19,7 @@ SO4_ERR_NONFINITE = 5
 SO4_ERR_WORKSPACE = 6
 SO4_ERR_NO_NEIGHBOR = 7
 SO4_ERR_REVERSE = 8
+SO4_ERR_TOO_LARGE = 9
 
 _MESSAGES = {
     SO4_ERR_ARG: "invalid argument",
@@ -29,6 +30,7 @@ _MESSAGES = {
     SO4_ERR_WORKSPACE: "workspace too small",
     SO4_ERR_NO_NEIGHBOR: "an atom has no neighbour within rcut",
     SO4_ERR_REVERSE: "neighbour list is not symmetric",
+    SO4_ERR_TOO_LARGE: "problem exceeds the fixed 64 MiB scratch of so4_adjoint32_noalloc",
 }
 
 
@@ -92,6 +94,8 @@ def lib():
         "so4_adjoint_deidrj32": (_i, [_vp, C.POINTER(Params), _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
         "so4_adjoint_gather": (_i, [_i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
         "so4_launch_count": (C.c_longlong, []),
+        "so4_adjoint32_noalloc": (_i, [_vp, C.POINTER(Params), _i, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _i64, _vp,
+                                       _vp, _vp, _vp, _vp]),
         "so4_adjoint32": (_i, [_vp, C.POINTER(Params), _i, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _i64, _vp, _vp,
                                _vp, _vp, _vp, _sz, _vp]),
     }

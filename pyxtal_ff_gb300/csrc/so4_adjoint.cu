@@ -410,3 +410,72 @@ extern "C" int so4_adjoint32(const so4_tables *t, const so4_params *p, int nstru
     return so4_adjoint_gather(natoms, nstruct, d_atom_ptr, d_img_ptr, d_img_rev, w.g, w.vatom, d_forces, d_virial,
                               stream);
 }
+
+// ---------------------------------------------------------------------------
+// so4_adjoint32_noalloc: the adjoint with its scratch in a fixed device array.
+//
+// Some callers cannot allocate device memory at the moment they need forces:
+// an MD engine's force plugin that is handed only its input and output
+// buffers, code running while another allocator owns the whole of HBM (a
+// pre-reserved pool), or a path that must not call cudaMalloc because that
+// call can synchronise the device or fail under memory pressure mid-run.  For
+// them this entry point takes the adjoint's scratch (Y, the per-image dE/dr
+// and the per-atom virials) from g_noalloc_scratch below instead of a
+// caller-provided workspace.  It calls no cudaMalloc, no cudaFree and no
+// allocating library routine.
+//
+// Limit: the scratch one call needs is so4_adjoint_workspace_size(t, natoms,
+// nimg) bytes; problems needing more than SO4_NOALLOC_SCRATCH_BYTES (64 MiB,
+// e.g. 32,000 atoms with ~900k images at lmax 4) are rejected with
+// SO4_ERR_TOO_LARGE.  The array lives on every GPU that loads this library,
+// until the process exits.
+//
+// Every call on a device uses the same array and leaves its contents behind.
+// Nothing in it needs to start at zero: each byte a kernel reads was written
+// earlier in the same call.  Calls that overlap on the GPU (different streams,
+// or host threads sharing a device) race on the array; serialise them.
+//
+// The device address of the array is looked up with cudaGetSymbolAddress the
+// first time the entry point runs on each device (with that device current);
+// that first call should come before any stream capture.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[SO4_NOALLOC_SCRATCH_BYTES];
+
+#include <mutex>
+
+namespace {
+constexpr int kNoallocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void *g_noalloc_ptr[kNoallocMaxDevices] = {nullptr};
+}  // namespace
+
+extern "C" int so4_adjoint32_noalloc(const so4_tables *t, const so4_params *p, int nstruct, const int *d_atom_struct,
+                                     const int *d_atom_ptr, int natoms, const double *d_w_nb,
+                                     const int32_t *d_img_ptr, const int32_t *d_img_j, const double *d_img_r,
+                                     const int32_t *d_img_rev, int64_t nimg, const float *d_utot,
+                                     const float *d_beta, double *d_forces, double *d_virial, void *stream) {
+    (void)d_atom_struct;
+    if (!t || !p || natoms < 0 || nstruct < 0 || nimg < 0) return SO4_ERR_ARG;
+    AdjWork w;
+    if (carve_adj(w, nullptr, natoms, t->n_half, nimg) > (size_t)SO4_NOALLOC_SCRATCH_BYTES) return SO4_ERR_TOO_LARGE;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return SO4_ERR_CUDA;
+    if (dev < 0 || dev >= kNoallocMaxDevices) return SO4_ERR_UNSUPPORTED;
+    void *scratch = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_noalloc_mu);
+        if (!g_noalloc_ptr[dev]) {
+            void *q = nullptr;
+            if (cudaGetSymbolAddress(&q, g_noalloc_scratch) != cudaSuccess || !q) return SO4_ERR_CUDA;
+            g_noalloc_ptr[dev] = q;
+        }
+        scratch = g_noalloc_ptr[dev];
+    }
+    carve_adj(w, scratch, natoms, t->n_half, nimg);
+    int rc = so4_adjoint_y32(t, natoms, d_utot, d_beta, (float *)w.Y, stream);
+    if (rc) return rc;
+    rc = so4_adjoint_deidrj32(t, p, natoms, d_w_nb, d_img_ptr, d_img_j, d_img_r, (const float *)w.Y, w.g, w.vatom,
+                              stream);
+    if (rc) return rc;
+    return so4_adjoint_gather(natoms, nstruct, d_atom_ptr, d_img_ptr, d_img_rev, w.g, w.vatom, d_forces, d_virial,
+                              stream);
+}
