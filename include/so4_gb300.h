@@ -188,7 +188,7 @@ int so4_adjoint_y32(const so4_tables *t, int natoms, const float *d_utot, const 
                     void *stream);
 int so4_adjoint_deidrj32(const so4_tables *t, const so4_params *p, int natoms, const double *d_w_nb,
                          const int32_t *d_img_ptr, const int32_t *d_img_j, const double *d_img_r,
-                         const float *d_y, float *d_g, double *d_vatom, void *stream);
+                         int64_t nimg, const float *d_y, float *d_g, double *d_vatom, void *stream);
 int so4_adjoint_gather(int natoms, int nstruct, const int *d_atom_ptr, const int32_t *d_img_ptr,
                        const int32_t *d_img_rev, const float *d_g, const double *d_vatom, double *d_forces,
                        double *d_virial, void *stream);

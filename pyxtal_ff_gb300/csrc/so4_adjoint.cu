@@ -15,11 +15,12 @@
 #include <algorithm>
 
 #include "so4_atom.cuh"
+#include "so4_rowchain.cuh"
+#include "so4_zlanes.cuh"
 
 namespace {
 
 constexpr int NWF = 4;  // warps per CTA, forward
-constexpr int NWY = 4;  // warps per CTA, Y build
 constexpr int NWD = 8;  // warps per CTA, per-image contraction
 
 struct AdjWork {
@@ -46,31 +47,39 @@ size_t carve_adj(AdjWork &w, void *base, int natoms, int nh, int64_t nimg) {
     return off;
 }
 
+template <typename K>
+int set_smem(K kern, size_t smem) {
+    if (smem > 227 * 1024) return SO4_ERR_UNSUPPORTED;
+    if (smem > 48 * 1024)
+        SO4_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    return SO4_OK;
+}
+
 struct FwdArgs {
     so4_params prm;
-    int natoms, nh, nu, nz, nB;
+    float psi_fac, rc32;  // rfac0 pi / rcut and rcut in FP32, set on the host
+    int natoms, nh, nu, nz, nB, nzB;
     const double *w_nb, *w_site, *img_r;
     const int32_t *img_ptr, *img_j;
     const float *cg, *rootpq;
-    const ZEnt *zent;
+    const ZEnt *zent, *zentB;
     const BEnt *bent;
     SmallTables st;
     float *utot, *x;
 };
 
-__global__ void __launch_bounds__(NWF * 32) k_forward32(FwdArgs A) {
+// U_tot of one centre per CTA (half layout, to global).
+__global__ void __launch_bounds__(NWF * 32) k_utot32(FwdArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ SmallTables st;
     const int tid = threadIdx.x;
     const int a = blockIdx.x;
     if (tid == 0) st = A.st;
     const int ldim = A.st.twol + 1;
-    const int nh = A.nh, nu = A.nu, nz = A.nz;
+    const int nh = A.nh;
     float *rootpq = (float *)smem_raw;
     cx<float> *Uh = (cx<float> *)(rootpq + ((ldim * ldim + 1) & ~1));
-    cx<float> *Uf = Uh + nh;
-    cx<float> *Z = Uf + nu;
-    cx<float> *W = Z + nz;  // per warp: H[nh], P[nh]
+    cx<float> *W = Uh + nh;  // per warp: H[nh], P[nh]
     for (int q = tid; q < ldim * ldim; q += NWF * 32) rootpq[q] = A.rootpq[q];
     __syncthreads();
     const float rc = (float)A.prm.rcut;
@@ -79,69 +88,176 @@ __global__ void __launch_bounds__(NWF * 32) k_forward32(FwdArgs A) {
                            psi_fac, A.prm.cutoff_id, nh, W, W + nh, 2 * nh, Uh);
     float2 *ug = (float2 *)A.utot + (size_t)a * nh;
     for (int e = tid; e < nh; e += NWF * 32) ug[e] = make_float2(Uh[e].re, Uh[e].im);
-    block_expand<float, NWF>(st, Uh, nu, Uf);
-    block_z<float, NWF>(A.zent, nz, A.cg, Uf, Z);
-    block_b<float, NWF, float>(A.bent, A.nB, Uh, Z, A.x + (size_t)a * A.nB);
 }
 
-struct YArgs {
-    int natoms, nh, nu, nz, nB, nblk;
-    const float *utot, *beta, *cg;
-    const ZEnt *zent;
+// U_tot with the row-chain recursion: one warp per centre, RowChain<TWOL>::IPW
+// images per round.  Each lane accumulates w_j sfac U over its images for its
+// chain's rows; the image groups are then added through shared memory in group
+// order, the self term f_c(0) w_site is put on the diagonal and u_norm applied
+// (SO4.py:1480-1505, 560-597).
+template <int TWOL, int NW>
+__global__ void __launch_bounds__(NW * 32) k_utot_rc(FwdArgs A) {
+    using RC = RowChain<TWOL>;
+    constexpr int W = TWOL + 1, NACC = acc_block(TWOL + 1);
+    extern __shared__ __align__(16) float ut_smem[];  // [NW][32][2 * NACC]
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int a = blockIdx.x * NW + wid;
+    const int grp = lane / RC::NCH, mb = lane - grp * RC::NCH;
+    float accr[NACC], acci[NACC];
+#pragma unroll
+    for (int q = 0; q < NACC; ++q) accr[q] = acci[q] = 0.f;
+    if (a < A.natoms) {
+        const int m0 = A.img_ptr[a], m1 = A.img_ptr[a + 1];
+        for (int base = m0; base < m1; base += RC::IPW) {
+            const int m = base + grp;
+            float x = 1.f, y = 0.f, z = 0.f, wsf = 0.f;
+            if (grp < RC::IPW && m < m1) {
+                x = (float)A.img_r[3 * m];
+                y = (float)A.img_r[3 * m + 1];
+                z = (float)A.img_r[3 * m + 2];
+                const float rr = sqrtf(x * x + y * y + z * z);
+                if (rr >= 1e-8f) {
+                    float sf, dsf;
+                    cutoff_fn<float>(A.prm.cutoff_id, rr, A.rc32, sf, dsf);
+                    wsf = (float)A.w_nb[A.img_j[m]] * sf;
+                } else {
+                    x = 1.f;
+                    y = z = 0.f;
+                }
+            }
+            const float r = sqrtf(x * x + y * y + z * z);
+            CK<float> ck;
+            make_ck<float, false>(x, y, z, r, A.psi_fac * r, ck);
+            float ur[W], ui[W], dr[3][W], di[3][W];
+#pragma unroll
+            for (int q = 0; q < W; ++q) ur[q] = ui[q] = 0.f;
+            ur[0] = 1.f;
+            if (mb == 0) accr[0] += wsf;
+            RcUtot<TWOL, 1>::run(mb, ck, wsf, ur, ui, dr, di, accr, acci);
+        }
+    }
+    float *sw = ut_smem + (size_t)wid * 32 * 2 * NACC;
+#pragma unroll
+    for (int q = 0; q < NACC; ++q) {
+        sw[lane * 2 * NACC + 2 * q] = accr[q];
+        sw[lane * 2 * NACC + 2 * q + 1] = acci[q];
+    }
+    __syncwarp();
+    if (a >= A.natoms) return;
+    float f0, df0;
+    cutoff_fn<float>(A.prm.cutoff_id, 0.f, A.rc32, f0, df0);
+    const float selfw = f0 * (float)A.w_site[a];
+    float2 *ug = (float2 *)A.utot + (size_t)a * A.nh;
+    for (int e = lane; e < A.nh; e += 32) {
+        int L = 0;
+        while (L < TWOL && half_block(L + 1) <= e) ++L;
+        const int off = e - half_block(L);
+        const int row = off / (L + 1), ma = off - row * (L + 1);
+        float sr = 0.f, si = 0.f;
+        for (int g = 0; g < RC::IPW; ++g) {
+            const float *src = sw + (g * RC::NCH + row) * 2 * NACC + 2 * (acc_block(L) + ma);
+            sr += src[0];
+            si += src[1];
+        }
+        if (ma == row) sr += selfw;
+        const float un = (float)A.st.unorm[L];
+        ug[e] = make_float2(sr * un, si * un);
+    }
+}
+
+template <int TWOL>
+int launch_utot_rc(const FwdArgs &A, cudaStream_t st) {
+    constexpr int NW = 4;
+    const size_t smem = sizeof(float) * NW * 32 * 2 * acc_block(TWOL + 1);
+    int rc = set_smem(k_utot_rc<TWOL, NW>, smem);
+    if (rc) return rc;
+    k_utot_rc<TWOL, NW><<<(A.natoms + NW - 1) / NW, NW * 32, smem, st>>>(A);
+    so4_count_launch();
+    return SO4_OK;
+}
+
+struct ZLArgs {
+    int natoms, nh, nu, nB, nblk, nunit;
+    const float2 *utot;
+    const int *fmap, *term_ptr;
+    const int4 *unit, *seg;
+    const ZTerm *terms;
+    const BEnt *bent;
     const ZBlk *blk;
     const int *yptr, *ylist;
+    const float *beta;
     SmallTables st;
-    float2 *Y;
+    float *x;    // B out  (k_zb32)
+    float2 *Y;   // Y out  (k_zy32)
 };
 
-__global__ void __launch_bounds__(NWY * 32) k_yi(YArgs A) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ SmallTables st;
-    const int tid = threadIdx.x;
-    const int a = blockIdx.x;
-    if (tid == 0) st = A.st;
-    const int nh = A.nh, nu = A.nu, nz = A.nz;
-    cx<float> *Uh = (cx<float> *)smem_raw;
-    cx<float> *Uf = Uh + nh;
-    cx<float> *Z = Uf + nu;
-    float *coef = (float *)(Z + nz);
-    const float2 *ug = (const float2 *)A.utot + (size_t)a * nh;
-    for (int e = tid; e < nh; e += NWY * 32) Uh[e] = mk<float>(ug[e].x, ug[e].y);
-    const float *bt = A.beta + (size_t)a * A.nB;
-    for (int b = tid; b < A.nblk; b += NWY * 32) {
-        const ZBlk bk = A.blk[b];
+// B_k = 2 Re sum' conj(U_l) Z(l1,l2,l) for 32 atoms per CTA (compute_bi, SO4.py:1071-1111)
+__global__ void __launch_bounds__(256) k_zb32(ZLArgs A) {
+    extern __shared__ __align__(16) float2 zl_smem[];
+    __shared__ int s_unit;
+    const int lane = threadIdx.x & 31;
+    const int a0 = blockIdx.x * 32;
+    float2 *Uf = zl_smem;
+    if (threadIdx.x == 0) s_unit = 0;
+    zl_load_utot(A.utot, A.fmap, a0, A.natoms, A.nh, A.nu, Uf);
+    __syncthreads();
+    for (int u = zl_next(&s_unit); u < A.nunit; u = zl_next(&s_unit)) {
+        const int4 un = __ldg(A.unit + u);
+        float acc = 0.f;
+        int4 sg = (un.y < un.z) ? __ldg(A.seg + un.y) : make_int4(0, 0, 0, 1);
+        for (int q = un.y; q < un.z; ++q) {
+            const int4 cur = sg;
+            if (q + 1 < un.z) sg = __ldg(A.seg + q + 1);
+            const float2 z = zl_entry(A.terms, cur.x, cur.y, Uf, lane);
+            const float2 ul = Uf[cur.z * ZL_PITCH + lane];
+            const float v = ul.x * z.x + ul.y * z.y;
+            acc += (cur.w == 2) ? 0.5f * v : v;
+        }
+        if (a0 + lane < A.natoms) A.x[(size_t)(a0 + lane) * A.nB + un.x] = 2.f * acc;
+    }
+}
+
+// Y for 32 atoms per CTA: Y_lam[e] = u_norm w_mid sum_{blocks (a,b,lam)} coef_block Z_block[e]
+__global__ void __launch_bounds__(256) k_zy32(ZLArgs A) {
+    extern __shared__ __align__(16) float2 zl_smem[];
+    __shared__ int s_unit;
+    const int lane = threadIdx.x & 31;
+    const int a0 = blockIdx.x * 32;
+    float2 *Uf = zl_smem;
+    float *coef = (float *)(Uf + (size_t)A.nu * ZL_PITCH);  // [nblk][33]
+    if (threadIdx.x == 0) s_unit = 0;
+    zl_load_utot(A.utot, A.fmap, a0, A.natoms, A.nh, A.nu, Uf);
+    for (int idx = threadIdx.x; idx < 32 * A.nblk; idx += blockDim.x) {
+        const int l = idx / A.nblk, b = idx - l * A.nblk;
+        const int a = a0 + l;
         float c = 0.f;
-        for (int r = 0; r < bk.nrole; ++r) c += (float)bk.role_f[r] * bt[bk.role_k[r]];
-        coef[b] = c;
+        if (a < A.natoms) {
+            const ZBlk &bk = A.blk[b];
+            for (int r = 0; r < bk.nrole; ++r) c += (float)bk.role_f[r] * __ldg(A.beta + (size_t)a * A.nB + bk.role_k[r]);
+        }
+        coef[b * ZL_PITCH + l] = c;
     }
     __syncthreads();
-    block_expand<float, NWY>(st, Uh, nu, Uf);
-    block_z<float, NWY>(A.zent, nz, A.cg, Uf, Z);
-    const int ldim = st.twol + 1;
-    float2 *Yg = A.Y + (size_t)a * nh;
-    for (int e = tid; e < nh; e += NWY * 32) {
-        const int lam = level_of(st.h_block, ldim, e);
-        const int off = e - st.h_block[lam];
-        const int mb = off / (lam + 1), ma = off - mb * (lam + 1);
-        float wmid = 1.f;
-        if (2 * mb == lam) wmid = (2 * ma < lam) ? 1.f : ((2 * ma == lam) ? 0.5f : 0.f);
+    for (int u = zl_next(&s_unit); u < A.nunit; u = zl_next(&s_unit)) {
+        const int4 un = __ldg(A.unit + u);
         float yr = 0.f, yi = 0.f;
-        if (wmid != 0.f) {
-            for (int q = A.yptr[lam]; q < A.yptr[lam + 1]; ++q) {
-                const int b = A.ylist[q];
-                const float c = coef[b];
-                const cx<float> zv = Z[A.blk[b].z0 + off];
-                yr += c * zv.re;
-                yi += c * zv.im;
-            }
+        int4 sg = (un.y < un.z) ? __ldg(A.seg + un.y) : make_int4(0, 0, 0, 0);
+        for (int q = un.y; q < un.z; ++q) {
+            const int4 cur = sg;
+            if (q + 1 < un.z) sg = __ldg(A.seg + q + 1);
+            const float2 z = zl_entry(A.terms, cur.x, cur.y, Uf, lane);
+            const float c = coef[cur.z * ZL_PITCH + lane];
+            yr += c * z.x;
+            yi += c * z.y;
         }
-        const float s = (float)st.unorm[lam] * wmid;
-        Yg[e] = make_float2(s * yr, s * yi);
+        const float s = __int_as_float(un.w);
+        if (a0 + lane < A.natoms) A.Y[(size_t)(a0 + lane) * A.nh + un.x] = make_float2(s * yr, s * yi);
     }
 }
 
 struct DArgs {
     so4_params prm;
+    float psi_fac, rc32;  // rfac0 pi / rcut and rcut in FP32, set on the host
     int natoms, nh;
     const double *w_nb, *img_r;
     const int32_t *img_ptr, *img_j;
@@ -157,7 +273,7 @@ struct DArgs {
 __global__ void __launch_bounds__(NWD * 32) k_deidrj(DArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ SmallTables st;
-    __shared__ double vred[NWD][9];
+    __shared__ float vred[NWD][9];
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const int a = blockIdx.x;
     if (tid == 0) st = A.st;
@@ -173,13 +289,12 @@ __global__ void __launch_bounds__(NWD * 32) k_deidrj(DArgs A) {
     __syncthreads();
     const float rc = (float)A.prm.rcut;
     const float psi_fac = (float)(A.prm.rfac0 * SO4_PI / A.prm.rcut);
-    double vw[9];
-#pragma unroll
-    for (int q = 0; q < 9; ++q) vw[q] = 0.0;
+    // virial of this centre: lane q < 9 accumulates component q = 3a + b of sum r_a g_b
+    float vq = 0.f;
+    const int qa = (lane < 9) ? lane / 3 : 0, qb = (lane < 9) ? lane % 3 : 0;
     const int m0 = A.img_ptr[a], m1 = A.img_ptr[a + 1];
     for (int m = m0 + wid; m < m1; m += NWD) {
-        const double xd = A.img_r[3 * m], yd = A.img_r[3 * m + 1], zd = A.img_r[3 * m + 2];
-        const float x = (float)xd, y = (float)yd, z = (float)zd;
+        const float x = (float)A.img_r[3 * m], y = (float)A.img_r[3 * m + 1], z = (float)A.img_r[3 * m + 2];
         const float r = sqrtf(x * x + y * y + z * z);
         if (r < 1e-8f) {
             if (lane == 0) A.g[3 * m] = A.g[3 * m + 1] = A.g[3 * m + 2] = 0.f;
@@ -214,21 +329,116 @@ __global__ void __launch_bounds__(NWD * 32) k_deidrj(DArgs A) {
             A.g[3 * m + 1] = gy;
             A.g[3 * m + 2] = gz;
         }
-        const double rv[3] = {xd, yd, zd}, gv[3] = {gx, gy, gz};
-#pragma unroll
-        for (int p = 0; p < 3; ++p)
-#pragma unroll
-            for (int q = 0; q < 3; ++q) vw[3 * p + q] += rv[p] * gv[q];
+        const float ra = (qa == 0) ? x : ((qa == 1) ? y : z);
+        const float gb = (qb == 0) ? gx : ((qb == 1) ? gy : gz);
+        vq += ra * gb;
         __syncwarp();
     }
-    if (lane == 0)
-        for (int q = 0; q < 9; ++q) vred[wid][q] = vw[q];
+    if (lane < 9) vred[wid][lane] = vq;
     __syncthreads();
     if (tid < 9) {
         double s = 0.0;
-        for (int w = 0; w < NWD; ++w) s += vred[w][tid];
+        for (int w = 0; w < NWD; ++w) s += (double)vred[w][tid];
         A.vatom[9 * (size_t)a + tid] = s;
     }
+}
+
+// Per-image dE/dr with the register-resident row-chain recursion.  Images are
+// flattened over all centres (load balance independent of the per-atom count):
+// warp w takes images [w*IPW, (w+1)*IPW), lane = image_in_warp * NCH + mb.
+template <int TWOL>
+__global__ void __launch_bounds__(256) k_deidrj_rc(DArgs A, int64_t nimg) {
+    using RC = RowChain<TWOL>;
+    constexpr int W = TWOL + 1;
+    const int lane = threadIdx.x & 31;
+    const int64_t wg = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int grp = lane / RC::NCH, mb = lane - grp * RC::NCH;
+    const int64_t m = wg * RC::IPW + grp;
+    const bool valid = (grp < RC::IPW) && (m < nimg);
+    float x = 1.f, y = 0.f, z = 0.f, wj = 0.f;
+    int centre = 0;
+    if (valid) {
+        x = (float)A.img_r[3 * m];
+        y = (float)A.img_r[3 * m + 1];
+        z = (float)A.img_r[3 * m + 2];
+        wj = (float)A.w_nb[A.img_j[m]];
+        centre = centre_of(A.img_ptr, A.natoms, (int)m);
+    }
+    float r = sqrtf(x * x + y * y + z * z);
+    const bool skip = !(r >= 1e-8f);  // SO4.py:1441 skips r < 1e-8
+    if (skip) {
+        x = 1.f;
+        y = z = 0.f;
+        r = 1.f;
+    }
+    CK<float> ck;
+    make_ck<float, true>(x, y, z, r, A.psi_fac * r, ck);
+    float ur[W], ui[W], dr[3][W], di[3][W];
+#pragma unroll
+    for (int q = 0; q < W; ++q) {
+        ur[q] = ui[q] = 0.f;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) dr[c][q] = di[c][q] = 0.f;
+    }
+    ur[0] = 1.f;
+    const float2 *Y = A.Y + (size_t)centre * A.nh;
+    float su = (mb == 0) ? __ldg(Y).x : 0.f;  // level 0: U = 1, dU = 0
+    float sc[3] = {0.f, 0.f, 0.f};
+    RcDeidrj<TWOL, 1>::run(mb, ck, Y, ur, ui, dr, di, su, sc);
+    // sum the chains of each image into its mb == 0 lane
+    float tu = su, t0 = sc[0], t1 = sc[1], t2 = sc[2];
+#pragma unroll
+    for (int k = 1; k < RC::NCH; ++k) {
+        const float a0 = __shfl_down_sync(0xffffffffu, su, k);
+        const float a1 = __shfl_down_sync(0xffffffffu, sc[0], k);
+        const float a2 = __shfl_down_sync(0xffffffffu, sc[1], k);
+        const float a3 = __shfl_down_sync(0xffffffffu, sc[2], k);
+        tu += a0;
+        t0 += a1;
+        t1 += a2;
+        t2 += a3;
+    }
+    if (valid && mb == 0) {
+        float sf, dsf;
+        cutoff_fn<float>(A.prm.cutoff_id, r, A.rc32, sf, dsf);
+        float gx = wj * (sf * t0 + dsf * (x / r) * tu);
+        float gy = wj * (sf * t1 + dsf * (y / r) * tu);
+        float gz = wj * (sf * t2 + dsf * (z / r) * tu);
+        if (skip) gx = gy = gz = 0.f;
+        A.g[3 * m] = gx;
+        A.g[3 * m + 1] = gy;
+        A.g[3 * m + 2] = gz;
+    }
+}
+
+// per-centre virial sum_{images m of i} r_m (x) g_m in FP64
+__global__ void k_vatom(int natoms, const int32_t *img_ptr, const double *img_r, const float *g, double *vatom) {
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= natoms) return;
+    double v[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) v[q] = 0.0;
+    for (int m = img_ptr[a]; m < img_ptr[a + 1]; ++m) {
+        const double r[3] = {img_r[3 * m], img_r[3 * m + 1], img_r[3 * m + 2]};
+        const double gg[3] = {g[3 * m], g[3 * m + 1], g[3 * m + 2]};
+#pragma unroll
+        for (int p = 0; p < 3; ++p)
+#pragma unroll
+            for (int q = 0; q < 3; ++q) v[3 * p + q] += r[p] * gg[q];
+    }
+#pragma unroll
+    for (int q = 0; q < 9; ++q) vatom[9 * (size_t)a + q] = v[q];
+}
+
+template <int TWOL>
+int launch_deidrj_rc(const DArgs &D, int64_t nimg, cudaStream_t st) {
+    using RC = RowChain<TWOL>;
+    if (nimg <= 0) return SO4_OK;
+    const int64_t warps = (nimg + RC::IPW - 1) / RC::IPW;
+    const int64_t blocks = (warps + 7) / 8;
+    k_deidrj_rc<TWOL><<<(unsigned)blocks, 256, 0, st>>>(D, nimg);
+    so4_count_launch();
+    return SO4_OK;
 }
 
 // F_i = sum over images m of i of (g_m - g_rev(m))  (FP64 accumulation)
@@ -247,36 +457,57 @@ __global__ void k_gather(int natoms, const int32_t *img_ptr, const int32_t *img_
     forces[3 * a + 2] = f2;
 }
 
-// per-structure virial: fixed-order block reduction of the per-atom virials
-__global__ void k_virial(const int *atom_ptr, const double *vatom, double *virial) {
-    __shared__ double red[256];
-    const int s = blockIdx.x, t = threadIdx.x;
+// per-structure virial: fixed-order reduction of the per-atom virials
+// (each thread sums a strided subset of atoms, then warp shuffles and a
+// 32-entry shared-memory stage; the order never depends on timing)
+__global__ void __launch_bounds__(1024) k_virial(const int *atom_ptr, const double *vatom, double *virial) {
+    __shared__ double red[32][9];
+    const int s = blockIdx.x, t = threadIdx.x, lane = t & 31, wid = t >> 5;
     const int a0 = atom_ptr[s], a1 = atom_ptr[s + 1];
-    for (int q = 0; q < 9; ++q) {
-        double acc = 0.0;
-        for (int a = a0 + t; a < a1; a += blockDim.x) acc += vatom[9 * (size_t)a + q];
-        red[t] = acc;
-        __syncthreads();
-        for (int d = blockDim.x / 2; d > 0; d >>= 1) {
-            if (t < d) red[t] += red[t + d];
-            __syncthreads();
-        }
-        if (t == 0) virial[9 * s + q] = red[0];
-        __syncthreads();
+    double acc[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) acc[q] = 0.0;
+    for (int a = a0 + t; a < a1; a += blockDim.x) {
+#pragma unroll
+        for (int q = 0; q < 9; ++q) acc[q] += vatom[9 * (size_t)a + q];
     }
-}
-
-template <typename K>
-int set_smem(K kern, size_t smem) {
-    if (smem > 227 * 1024) return SO4_ERR_UNSUPPORTED;
-    if (smem > 48 * 1024)
-        SO4_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    return SO4_OK;
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) acc[q] += __shfl_down_sync(0xffffffffu, acc[q], d);
+    }
+    if (lane == 0)
+#pragma unroll
+        for (int q = 0; q < 9; ++q) red[wid][q] = acc[q];
+    __syncthreads();
+    if (t < 9) {
+        double v = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v += red[w][t];
+        virial[9 * s + t] = v;
+    }
 }
 
 size_t rootpq_floats(int ldim) { return (size_t)((ldim * ldim + 1) & ~1); }
 
 }  // namespace
+
+static ZLArgs zl_args(const so4_tables *t, int natoms) {
+    ZLArgs Z;
+    Z.natoms = natoms;
+    Z.nh = t->n_half;
+    Z.nu = t->n_u;
+    Z.nB = t->n_b;
+    Z.nblk = t->n_blk;
+    Z.fmap = t->d_fmap;
+    Z.term_ptr = t->d_term_ptr;
+    Z.terms = t->d_terms;
+    Z.bent = t->d_b;
+    Z.blk = t->d_blk;
+    Z.yptr = t->d_yblk_ptr;
+    Z.ylist = t->d_yblk;
+    fill_small_tables(t, Z.st);
+    return Z;
+}
 
 extern "C" int so4_forward32(const so4_tables *t, const so4_params *p, int natoms, const double *d_w_nb,
                              const double *d_w_site, const int32_t *d_img_ptr, const int32_t *d_img_j,
@@ -285,6 +516,7 @@ extern "C" int so4_forward32(const so4_tables *t, const so4_params *p, int natom
     if (p->twol != t->twol || !(p->rcut > 0.0) || !(p->rfac0 > 0.0)) return SO4_ERR_ARG;
     if (p->cutoff_id < 1 || p->cutoff_id > 7) return SO4_ERR_UNSUPPORTED;
     if (natoms == 0) return SO4_OK;
+    cudaStream_t st = (cudaStream_t)stream;
     FwdArgs A;
     A.prm = *p;
     A.natoms = natoms;
@@ -300,15 +532,42 @@ extern "C" int so4_forward32(const so4_tables *t, const so4_params *p, int natom
     A.cg = t->d_cg32;
     A.rootpq = t->d_rootpq32;
     A.zent = t->d_z;
+    A.zentB = t->d_zB;
+    A.nzB = t->n_zB;
     A.bent = t->d_b;
     fill_small_tables(t, A.st);
     A.utot = d_utot;
     A.x = d_x;
-    const size_t smem = sizeof(float) * rootpq_floats(t->ldim) +
-                        sizeof(cx<float>) * ((size_t)t->n_half + t->n_u + t->n_z + (size_t)NWF * 2 * t->n_half);
-    int rc = set_smem(k_forward32, smem);
+    A.psi_fac = (float)(p->rfac0 * SO4_PI / p->rcut);
+    A.rc32 = (float)p->rcut;
+    int rc = SO4_OK;
+    switch (t->twol) {
+        case 2: rc = launch_utot_rc<2>(A, st); break;
+        case 4: rc = launch_utot_rc<4>(A, st); break;
+        case 6: rc = launch_utot_rc<6>(A, st); break;
+        case 8: rc = launch_utot_rc<8>(A, st); break;
+        case 10: rc = launch_utot_rc<10>(A, st); break;
+        case 12: rc = launch_utot_rc<12>(A, st); break;
+        default: {
+            const size_t smu =
+                sizeof(float) * rootpq_floats(t->ldim) + sizeof(cx<float>) * ((size_t)t->n_half * (1 + 2 * NWF));
+            rc = set_smem(k_utot32, smu);
+            if (rc) return rc;
+            k_utot32<<<natoms, NWF * 32, smu, st>>>(A);
+            so4_count_launch();
+        }
+    }
     if (rc) return rc;
-    k_forward32<<<natoms, NWF * 32, smem, (cudaStream_t)stream>>>(A);
+    ZLArgs Z = zl_args(t, natoms);
+    Z.utot = (const float2 *)d_utot;
+    Z.unit = t->d_bunit;
+    Z.seg = t->d_bseg;
+    Z.nunit = t->n_b;
+    Z.x = d_x;
+    const size_t smz = sizeof(float2) * (size_t)t->n_u * ZL_PITCH;
+    rc = set_smem(k_zb32, smz);
+    if (rc) return rc;
+    k_zb32<<<(natoms + 31) / 32, 256, smz, st>>>(Z);
     so4_count_launch();
     return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
 }
@@ -323,34 +582,25 @@ extern "C" int so4_adjoint_y32(const so4_tables *t, int natoms, const float *d_u
                                void *stream) {
     if (!t || natoms < 0 || !d_utot || !d_beta || !d_y) return SO4_ERR_ARG;
     if (natoms == 0) return SO4_OK;
-    YArgs Y;
-    Y.natoms = natoms;
-    Y.nh = t->n_half;
-    Y.nu = t->n_u;
-    Y.nz = t->n_z;
-    Y.nB = t->n_b;
-    Y.nblk = t->n_blk;
-    Y.utot = d_utot;
-    Y.beta = d_beta;
-    Y.cg = t->d_cg32;
-    Y.zent = t->d_z;
-    Y.blk = t->d_blk;
-    Y.yptr = t->d_yblk_ptr;
-    Y.ylist = t->d_yblk;
-    fill_small_tables(t, Y.st);
-    Y.Y = (float2 *)d_y;
-    const size_t smy = sizeof(cx<float>) * ((size_t)t->n_half + t->n_u + t->n_z) + sizeof(float) * ((t->n_blk + 3) & ~3);
-    int rc = set_smem(k_yi, smy);
+    ZLArgs Z = zl_args(t, natoms);
+    Z.utot = (const float2 *)d_utot;
+    Z.unit = t->d_yunit;
+    Z.seg = t->d_yseg;
+    Z.nunit = t->n_half;
+    Z.beta = d_beta;
+    Z.Y = (float2 *)d_y;
+    const size_t smz = sizeof(float2) * (size_t)t->n_u * ZL_PITCH + sizeof(float) * (size_t)t->n_blk * ZL_PITCH;
+    int rc = set_smem(k_zy32, smz);
     if (rc) return rc;
-    k_yi<<<natoms, NWY * 32, smy, (cudaStream_t)stream>>>(Y);
+    k_zy32<<<(natoms + 31) / 32, 256, smz, (cudaStream_t)stream>>>(Z);
     so4_count_launch();
     return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
 }
 
 extern "C" int so4_adjoint_deidrj32(const so4_tables *t, const so4_params *p, int natoms, const double *d_w_nb,
                                     const int32_t *d_img_ptr, const int32_t *d_img_j, const double *d_img_r,
-                                    const float *d_y, float *d_g, double *d_vatom, void *stream) {
-    if (!t || !p || natoms < 0 || !d_y || !d_g || !d_vatom) return SO4_ERR_ARG;
+                                    int64_t nimg, const float *d_y, float *d_g, double *d_vatom, void *stream) {
+    if (!t || !p || natoms < 0 || nimg < 0 || !d_y || !d_g || !d_vatom) return SO4_ERR_ARG;
     if (p->twol != t->twol || !(p->rcut > 0.0) || !(p->rfac0 > 0.0)) return SO4_ERR_ARG;
     if (p->cutoff_id < 1 || p->cutoff_id > 7) return SO4_ERR_UNSUPPORTED;
     if (natoms == 0) return SO4_OK;
@@ -364,14 +614,32 @@ extern "C" int so4_adjoint_deidrj32(const so4_tables *t, const so4_params *p, in
     D.img_j = d_img_j;
     D.rootpq = t->d_rootpq32;
     fill_small_tables(t, D.st);
+    D.psi_fac = (float)(p->rfac0 * SO4_PI / p->rcut);
+    D.rc32 = (float)p->rcut;
     D.Y = (const float2 *)d_y;
     D.g = d_g;
     D.vatom = d_vatom;
-    const size_t smd =
-        sizeof(float) * rootpq_floats(t->ldim) + sizeof(cx<float>) * ((size_t)t->n_half + (size_t)NWD * 4 * t->n_half);
-    int rc = set_smem(k_deidrj, smd);
+    cudaStream_t st = (cudaStream_t)stream;
+    int rc = SO4_OK;
+    switch (t->twol) {
+        case 2: rc = launch_deidrj_rc<2>(D, nimg, st); break;
+        case 4: rc = launch_deidrj_rc<4>(D, nimg, st); break;
+        case 6: rc = launch_deidrj_rc<6>(D, nimg, st); break;
+        case 8: rc = launch_deidrj_rc<8>(D, nimg, st); break;
+        case 10: rc = launch_deidrj_rc<10>(D, nimg, st); break;
+        case 12: rc = launch_deidrj_rc<12>(D, nimg, st); break;
+        default: {
+            const size_t smd = sizeof(float) * rootpq_floats(t->ldim) +
+                               sizeof(cx<float>) * ((size_t)t->n_half + (size_t)NWD * 4 * t->n_half);
+            rc = set_smem(k_deidrj, smd);
+            if (rc) return rc;
+            k_deidrj<<<natoms, NWD * 32, smd, st>>>(D);
+            so4_count_launch();
+            return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
+        }
+    }
     if (rc) return rc;
-    k_deidrj<<<natoms, NWD * 32, smd, (cudaStream_t)stream>>>(D);
+    k_vatom<<<(natoms + 127) / 128, 128, 0, st>>>(natoms, d_img_ptr, d_img_r, d_g, d_vatom);
     so4_count_launch();
     return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
 }
@@ -386,7 +654,7 @@ extern "C" int so4_adjoint_gather(int natoms, int nstruct, const int *d_atom_ptr
         so4_count_launch();
     }
     if (nstruct > 0) {
-        k_virial<<<nstruct, 256, 0, st>>>(d_atom_ptr, d_vatom, d_virial);
+        k_virial<<<nstruct, 1024, 0, st>>>(d_atom_ptr, d_vatom, d_virial);
         so4_count_launch();
     }
     return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
@@ -404,7 +672,7 @@ extern "C" int so4_adjoint32(const so4_tables *t, const so4_params *p, int nstru
     carve_adj(w, d_work, natoms, t->n_half, nimg);
     int rc = so4_adjoint_y32(t, natoms, d_utot, d_beta, (float *)w.Y, stream);
     if (rc) return rc;
-    rc = so4_adjoint_deidrj32(t, p, natoms, d_w_nb, d_img_ptr, d_img_j, d_img_r, (const float *)w.Y, w.g, w.vatom,
+    rc = so4_adjoint_deidrj32(t, p, natoms, d_w_nb, d_img_ptr, d_img_j, d_img_r, nimg, (const float *)w.Y, w.g, w.vatom,
                               stream);
     if (rc) return rc;
     return so4_adjoint_gather(natoms, nstruct, d_atom_ptr, d_img_ptr, d_img_rev, w.g, w.vatom, d_forces, d_virial,
@@ -473,7 +741,7 @@ extern "C" int so4_adjoint32_noalloc(const so4_tables *t, const so4_params *p, i
     carve_adj(w, scratch, natoms, t->n_half, nimg);
     int rc = so4_adjoint_y32(t, natoms, d_utot, d_beta, (float *)w.Y, stream);
     if (rc) return rc;
-    rc = so4_adjoint_deidrj32(t, p, natoms, d_w_nb, d_img_ptr, d_img_j, d_img_r, (const float *)w.Y, w.g, w.vatom,
+    rc = so4_adjoint_deidrj32(t, p, natoms, d_w_nb, d_img_ptr, d_img_j, d_img_r, nimg, (const float *)w.Y, w.g, w.vatom,
                               stream);
     if (rc) return rc;
     return so4_adjoint_gather(natoms, nstruct, d_atom_ptr, d_img_ptr, d_img_rev, w.g, w.vatom, d_forces, d_virial,

@@ -103,6 +103,16 @@ __device__ void block_z(const ZEnt *zent, int nz, const T *cg, const cx<T> *Uf, 
     __syncthreads();
 }
 
+// The Z entries of a list (e.g. only the blocks B reads), each to its own slot.
+template <typename T, int NW>
+__device__ void block_z_list(const ZEnt *list, int n, const T *cg, const cx<T> *Uf, cx<T> *Z) {
+    for (int q = threadIdx.x; q < n; q += NW * 32) {
+        const ZEnt ze = list[q];
+        Z[ze.jz] = z_entry<T>(ze, cg, Uf);
+    }
+    __syncthreads();
+}
+
 // B_k = 2 Re sum' conj(U_l) Z(l1,l2,l) (compute_bi, SO4.py:1071-1111).
 template <typename T, int NW, typename TO>
 __device__ void block_b(const BEnt *bent, int nB, const cx<T> *Uh, const cx<T> *Z, TO *x) {

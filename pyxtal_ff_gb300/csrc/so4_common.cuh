@@ -61,6 +61,7 @@ struct ZEnt {
     int l1, l2;          // row strides - 1
     int jh;              // half offset of (l, mb, ma)
     int blk;             // Z block index
+    int jz;              // index of this entry in the full Z list
 };
 
 // One bispectrum component k = (l1, l2, l), l >= l1 >= l2 (SO4.py:1314-1327),
@@ -84,6 +85,14 @@ struct ZBlk {
     double role_f[3];
 };
 
+// One product term of a Z entry: Z += c * U[i1] * U[i2] with c = cg_a * cg_b
+// and i1, i2 offsets in the full layout (compute_zi's two CG sums, SO4.py:1047-1066,
+// flattened into one list).
+struct ZTerm {
+    float c;
+    unsigned short i1, i2;
+};
+
 struct so4_tables {
     int twol, ldim, normalize_u;
     int n_u, n_half, n_z, n_b, n_cg, n_blk;
@@ -98,10 +107,23 @@ struct so4_tables {
     double *d_rootpq64 = nullptr;  // ldim x ldim
     float *d_rootpq32 = nullptr;
     ZEnt *d_z = nullptr;
+    ZEnt *d_zB = nullptr;       // entries of the blocks B reads (l >= l1)
+    int n_zB = 0;
     BEnt *d_b = nullptr;
     ZBlk *d_blk = nullptr;
     int *d_yblk_ptr = nullptr;  // ldim + 1 : blocks grouped by their third index
     int *d_yblk = nullptr;      // n_blk
+    // flattened Z terms and the work orders of the atoms-across-lanes kernels
+    ZTerm *d_terms = nullptr;
+    int *d_term_ptr = nullptr;  // n_z + 1
+    int *d_fmap = nullptr;      // n_u: full entry -> half source | conj << 15 | negate << 14
+    // work units of the atoms-across-lanes kernels, most expensive first:
+    //   B unit {k, seg0, seg1, 0},       B segment {t0, t1, full index of U_l[e], weight 1 or 2 (= 1/2)}
+    //   Y unit {half e, seg0, seg1, bits of u_norm w_mid},  Y segment {t0, t1, block, 0}
+    int4 *d_bunit = nullptr, *d_bseg = nullptr;
+    int4 *d_yunit = nullptr, *d_yseg = nullptr;
+    int n_terms = 0;
+    std::vector<int> term_ptr;
 };
 
 // Table data every kernel stages into shared memory at start.

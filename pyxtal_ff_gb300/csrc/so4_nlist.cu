@@ -31,6 +31,7 @@ struct NLWork {
     int *atom_bin;   // natoms
     int *atom_shift; // 3 natoms
     int *cnt;        // natoms (image or pair counts)
+    float4 *pos32;   // natoms: FP32 copy of the positions for the prefilter
     unsigned long long *keys;  // nimg
 };
 
@@ -52,6 +53,7 @@ size_t carve(NLWork &w, void *base, int natoms, int nbins, int64_t nimg) {
     w.atom_bin = (int *)take(sizeof(int) * (natoms + 1));
     w.atom_shift = (int *)take(sizeof(int) * 3 * (natoms + 1));
     w.cnt = (int *)take(sizeof(int) * (natoms + 1));
+    w.pos32 = (float4 *)take(sizeof(float4) * (natoms + 1));
     w.keys = (unsigned long long *)take(sizeof(unsigned long long) * (nimg + 1));
     return off;
 }
@@ -103,6 +105,7 @@ __global__ void k_bin(const so4_geom *geom, const double *pos, const int *astruc
     }
     const int bin = g.bin_base + (b[0] * g.nbin[1] + b[1]) * g.nbin[2] + b[2];
     w.atom_bin[a] = bin;
+    w.pos32[a] = make_float4((float)r[0], (float)r[1], (float)r[2], 0.f);
     atomicAdd(&w.bin_cnt[bin], 1);
 }
 
@@ -142,76 +145,98 @@ __global__ void k_scan(const int *in, int *out, int n) {
 __global__ void k_set_int(int *p, int v) { *p = v; }
 
 // One warp per centre.  MODE 0: count images into w.cnt.  MODE 1: write the
-// packed (j, o) keys into w.keys[img_ptr[a] ...] (unsorted).
+// packed (j, o) keys into w.keys[img_ptr[a] ...] (unsorted; slots are taken with
+// a shared-memory counter, the order is fixed later by k_sort).
+// Each candidate is classified in FP32 with a margin delta that bounds the FP32
+// rounding of the image vector (about 6 ulp of the magnitudes involved, here
+// taken 8x larger plus an absolute 1e-5 A): |r| > rcut + delta is surely out,
+// |r| < rcut - delta surely in, and only the band in between is decided by the
+// exact FP64 test, so the accepted set is exactly the FP64 one while FP64 work
+// (1/64 of the FP32 rate on this GPU) is almost never issued.
 template <int MODE>
 __global__ void k_scan_images(const so4_geom *geom, const double *pos, const int *astruct, int natoms,
                               double rcut, const int32_t *img_ptr, NLWork w) {
-    const int lane = threadIdx.x & 31;
+    __shared__ int s_cnt[8];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int a = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (MODE == 1 && lane == 0) s_cnt[wib] = 0;
+    __syncwarp();
     if (a >= natoms) return;
     const so4_geom &g = geom[astruct[a]];
     const double pi[3] = {pos[3 * a], pos[3 * a + 1], pos[3 * a + 2]};
+    const float4 pi32 = w.pos32[a];
+    float c32[9], amax = 0.f;
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+        c32[q] = (float)g.cell[q];
+        amax = fmaxf(amax, fabsf(c32[q]));
+    }
+    const float rc32 = (float)rcut;
+    const float pimag = fmaxf(fabsf(pi32.x), fmaxf(fabsf(pi32.y), fabsf(pi32.z)));
     const int lb = w.atom_bin[a] - g.bin_base;
     const int bi[3] = {lb / (g.nbin[1] * g.nbin[2]), (lb / g.nbin[2]) % g.nbin[1], lb % g.nbin[2]};
     const int si[3] = {w.atom_shift[3 * a], w.atom_shift[3 * a + 1], w.atom_shift[3 * a + 2]};
-    const int n0 = 2 * g.mshift[0] + 1, n1 = 2 * g.mshift[1] + 1, n2 = 2 * g.mshift[2] + 1;
-    const int nq = n0 * n1 * n2;
-    int base = 0;
-    if (MODE == 1) base = img_ptr[a];
-    for (int pass = 0; pass < MODE + 1; ++pass) {
-        int mine = 0;
-        for (int q = lane; q < nq; q += 32) {
-            const int d[3] = {q / (n1 * n2) - g.mshift[0], (q / n2) % n1 - g.mshift[1], q % n2 - g.mshift[2]};
-            int tb[3], img[3];
+    const int n1 = 2 * g.mshift[1] + 1, n2 = 2 * g.mshift[2] + 1;
+    const int nq = (2 * g.mshift[0] + 1) * n1 * n2;
+    const int base = (MODE == 1) ? img_ptr[a] : 0;
+    int mine = 0;
+    for (int q = lane; q < nq; q += 32) {
+        const int d[3] = {q / (n1 * n2) - g.mshift[0], (q / n2) % n1 - g.mshift[1], q % n2 - g.mshift[2]};
+        int tb[3], img[3];
 #pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                const int t = bi[k] + d[k];
-                const int nb = g.nbin[k];
-                const int wk = ((t % nb) + nb) % nb;
-                tb[k] = wk;
-                img[k] = (t - wk) / nb;
-            }
-            const int bin = g.bin_base + (tb[0] * g.nbin[1] + tb[1]) * g.nbin[2] + tb[2];
-            for (int s = w.bin_start[bin]; s < w.bin_start[bin + 1]; ++s) {
-                const int j = w.bin_atoms[s];
-                const int o[3] = {img[0] + w.atom_shift[3 * j] - si[0], img[1] + w.atom_shift[3 * j + 1] - si[1],
-                                  img[2] + w.atom_shift[3 * j + 2] - si[2]};
-                if (j == a && o[0] == 0 && o[1] == 0 && o[2] == 0) continue;
+        for (int k = 0; k < 3; ++k) {
+            const int t = bi[k] + d[k];
+            const int nb = g.nbin[k];
+            const int wk = ((t % nb) + nb) % nb;
+            tb[k] = wk;
+            img[k] = (t - wk) / nb;
+        }
+        const int bin = g.bin_base + (tb[0] * g.nbin[1] + tb[1]) * g.nbin[2] + tb[2];
+        for (int s = w.bin_start[bin]; s < w.bin_start[bin + 1]; ++s) {
+            const int j = w.bin_atoms[s];
+            const int o[3] = {img[0] + w.atom_shift[3 * j] - si[0], img[1] + w.atom_shift[3 * j + 1] - si[1],
+                              img[2] + w.atom_shift[3 * j + 2] - si[2]};
+            if (j == a && o[0] == 0 && o[1] == 0 && o[2] == 0) continue;
+            // FP32 prefilter
+            const float4 pj32 = w.pos32[j];
+            const float f0 = (float)o[0], f1 = (float)o[1], f2 = (float)o[2];
+            const float rx = (pj32.x + (f0 * c32[0] + f1 * c32[3] + f2 * c32[6])) - pi32.x;
+            const float ry = (pj32.y + (f0 * c32[1] + f1 * c32[4] + f2 * c32[7])) - pi32.y;
+            const float rz = (pj32.z + (f0 * c32[2] + f1 * c32[5] + f2 * c32[8])) - pi32.z;
+            const float mag = pimag + fmaxf(fabsf(pj32.x), fmaxf(fabsf(pj32.y), fabsf(pj32.z))) +
+                              (fabsf(f0) + fabsf(f1) + fabsf(f2)) * amax;
+            const float delta = 2e-6f * mag + 1e-5f;
+            const float d2 = rx * rx + ry * ry + rz * rz;
+            const float hi = rc32 + delta, lo = rc32 - delta;
+            if (d2 > hi * hi) continue;            // surely outside
+            if (!(lo > 0.f && d2 < lo * lo)) {     // within the rounding band: decide in FP64
                 const double pj[3] = {pos[3 * j], pos[3 * j + 1], pos[3 * j + 2]};
                 double r[3];
                 image_vec(g, pi, pj, o[0], o[1], o[2], r);
                 if (!(norm_rn(r) < rcut)) continue;
-                if (MODE == 1 && pass == 1) {
-                    if (abs(o[0]) > OFF_MAX || abs(o[1]) > OFF_MAX || abs(o[2]) > OFF_MAX) {
-                        flag(w.status, SO4_ERR_CAPACITY);
-                        continue;
-                    }
-                    const unsigned long long key = ((unsigned long long)(unsigned)j << 30) |
-                                                   ((unsigned long long)(o[0] + OFF_BIAS) << 20) |
-                                                   ((unsigned long long)(o[1] + OFF_BIAS) << 10) |
-                                                   (unsigned long long)(o[2] + OFF_BIAS);
-                    w.keys[base + mine] = key;
+            }
+            if (MODE == 1) {
+                if (abs(o[0]) > OFF_MAX || abs(o[1]) > OFF_MAX || abs(o[2]) > OFF_MAX) {
+                    flag(w.status, SO4_ERR_CAPACITY);
+                    continue;
                 }
-                ++mine;
+                const unsigned long long key = ((unsigned long long)(unsigned)j << 30) |
+                                               ((unsigned long long)(o[0] + OFF_BIAS) << 20) |
+                                               ((unsigned long long)(o[1] + OFF_BIAS) << 10) |
+                                               (unsigned long long)(o[2] + OFF_BIAS);
+                const int slot = atomicAdd(&s_cnt[wib], 1);
+                w.keys[base + slot] = key;
             }
+            ++mine;
         }
-        if (MODE == 0) {
-            int tot = mine;
+    }
+    if (MODE == 0) {
+        int tot = mine;
 #pragma unroll
-            for (int d = 16; d > 0; d >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, d);
-            if (lane == 0) {
-                w.cnt[a] = tot;
-                if (tot == 0) flag(w.status, SO4_ERR_NO_NEIGHBOR);
-            }
-        } else if (pass == 0) {
-            // exclusive prefix of the lane counts -> write offsets for pass 1
-            int incl = mine;
-#pragma unroll
-            for (int d = 1; d < 32; d <<= 1) {
-                int v = __shfl_up_sync(0xffffffffu, incl, d);
-                if (lane >= d) incl += v;
-            }
-            base = img_ptr[a] + incl - mine;
+        for (int d = 16; d > 0; d >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, d);
+        if (lane == 0) {
+            w.cnt[a] = tot;
+            if (tot == 0) flag(w.status, SO4_ERR_NO_NEIGHBOR);
         }
     }
 }

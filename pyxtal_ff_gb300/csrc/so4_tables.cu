@@ -9,6 +9,8 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <algorithm>
+#include <utility>
 
 #include "so4_common.cuh"
 
@@ -81,10 +83,18 @@ void free_device(so4_tables *t) {
     cudaFree(t->d_rootpq64);
     cudaFree(t->d_rootpq32);
     cudaFree(t->d_z);
+    cudaFree(t->d_zB);
     cudaFree(t->d_b);
     cudaFree(t->d_blk);
     cudaFree(t->d_yblk_ptr);
     cudaFree(t->d_yblk);
+    cudaFree(t->d_terms);
+    cudaFree(t->d_fmap);
+    cudaFree(t->d_term_ptr);
+    cudaFree(t->d_bunit);
+    cudaFree(t->d_bseg);
+    cudaFree(t->d_yunit);
+    cudaFree(t->d_yseg);
 }
 
 }  // namespace
@@ -214,6 +224,7 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
                         z.l2 = l2;
                         z.jh = t->h_block[l] + (l + 1) * mb + ma;
                         z.blk = (int)blks.size();
+                        z.jz = n;
                         zent.push_back(z);
                         n++;
                     }
@@ -271,13 +282,115 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
             rp32[p * ld + q] = (float)rp64[p * ld + q];
         }
     std::vector<float> cg32(t->cglist.begin(), t->cglist.end());
+    std::vector<ZEnt> zentB;
+    for (const ZEnt &z : zent) {
+        const ZBlk &bk = blks[z.blk];
+        if (bk.l >= bk.l1) zentB.push_back(z);
+    }
+    t->n_zB = (int)zentB.size();
+
+    // flattened Z terms (full-layout offsets) and cost-ordered work lists
+    std::vector<ZTerm> terms;
+    t->term_ptr.assign(t->n_z + 1, 0);
+    for (int jz = 0; jz < t->n_z; ++jz) {
+        const int *q = &t->idxz[10 * jz];
+        const int l1 = q[0], l2 = q[1], l = q[2];
+        const int cgbase = t->idxcg_block[b3(ld, l1, l2, l)];
+        t->term_ptr[jz] = (int)terms.size();
+        for (int ib = 0; ib < q[8]; ++ib) {
+            const int mb1 = q[6] + ib, mb2 = q[7] - ib;
+            const double cgb = t->cglist[cgbase + mb1 * (l2 + 1) + mb2];
+            for (int ia = 0; ia < q[5]; ++ia) {
+                const int ma1 = q[3] + ia, ma2 = q[4] - ia;
+                const double cga = t->cglist[cgbase + ma1 * (l2 + 1) + ma2];
+                ZTerm zt;
+                zt.c = (float)(cga * cgb);
+                zt.i1 = (unsigned short)(t->idxu_block[l1] + mb1 * (l1 + 1) + ma1);
+                zt.i2 = (unsigned short)(t->idxu_block[l2] + mb2 * (l2 + 1) + ma2);
+                terms.push_back(zt);
+            }
+        }
+    }
+    t->term_ptr[t->n_z] = (int)terms.size();
+    t->n_terms = (int)terms.size();
+    auto zcost = [&](int jz) { return t->term_ptr[jz + 1] - t->term_ptr[jz]; };
+    // B units: one per component k, a segment per summed entry of its block
+    std::vector<std::pair<long, int>> bc, yc;
+    for (int k = 0; k < t->n_b; ++k) {
+        long c = 0;
+        for (int e = 0; e < bent[k].cnt[0]; ++e) c += zcost(bent[k].z[0] + e);
+        bc.push_back({-c, k});
+    }
+    std::stable_sort(bc.begin(), bc.end());
+    std::vector<int4> bunit, bseg;
+    for (auto &v : bc) {
+        const int k = v.second;
+        const BEnt &be = bent[k];
+        const int s0 = (int)bseg.size();
+        for (int e = 0; e < be.cnt[0]; ++e) {
+            const int jz = be.z[0] + e;
+            const int half = ((be.lam[0] % 2) == 0 && e == be.cnt[0] - 1) ? 2 : 1;
+            bseg.push_back(make_int4(t->term_ptr[jz], t->term_ptr[jz + 1], t->idxu_block[be.lam[0]] + e, half));
+        }
+        bunit.push_back(make_int4(k, s0, (int)bseg.size(), 0));
+    }
+    // Y units: one per half-layout entry (lam, off), a segment per block (a, b, lam)
+    for (int lam = 0; lam < ld; ++lam)
+        for (int off = 0; off < (lam / 2 + 1) * (lam + 1); ++off) {
+            long c = 0;
+            for (int qq = yptr[lam]; qq < yptr[lam + 1]; ++qq) c += zcost(blks[ylist[qq]].z0 + off);
+            yc.push_back({-c, t->h_block[lam] + off});
+        }
+    std::stable_sort(yc.begin(), yc.end());
+    std::vector<int4> yunit, yseg;
+    for (auto &v : yc) {
+        const int e = v.second;
+        int lam = 0;
+        while (lam + 1 < ld && t->h_block[lam + 1] <= e) ++lam;
+        const int off = e - t->h_block[lam];
+        const int mb = off / (lam + 1), ma = off - mb * (lam + 1);
+        double wmid = 1.0;
+        if (2 * mb == lam) wmid = (2 * ma < lam) ? 1.0 : ((2 * ma == lam) ? 0.5 : 0.0);
+        const float scale = (float)(t->unorm_l[lam] * wmid);
+        int bits;
+        std::memcpy(&bits, &scale, sizeof bits);
+        const int s0 = (int)yseg.size();
+        if (wmid != 0.0)
+            for (int qq = yptr[lam]; qq < yptr[lam + 1]; ++qq) {
+                const int b = ylist[qq];
+                const int jz = blks[b].z0 + off;
+                yseg.push_back(make_int4(t->term_ptr[jz], t->term_ptr[jz + 1], b, 0));
+            }
+        yunit.push_back(make_int4(e, s0, (int)yseg.size(), bits));
+    }
+
+    std::vector<int> fmap(t->n_u);
+    for (int l = 0; l < ld; ++l)
+        for (int mb = 0; mb <= l; ++mb)
+            for (int ma = 0; ma <= l; ++ma) {
+                const int f = t->idxu_block[l] + mb * (l + 1) + ma;
+                if (2 * mb <= l) {
+                    fmap[f] = t->h_block[l] + mb * (l + 1) + ma;
+                } else {
+                    const int src = t->h_block[l] + (l - mb) * (l + 1) + (l - ma);
+                    fmap[f] = src | (1 << 15) | ((((mb + ma) & 1) ? 1 : 0) << 14);
+                }
+            }
 
     int rc = SO4_OK;
+    if (!rc) rc = upload(&t->d_fmap, fmap);
+    if (!rc) rc = upload(&t->d_terms, terms);
+    if (!rc) rc = upload(&t->d_term_ptr, t->term_ptr);
+    if (!rc) rc = upload(&t->d_bunit, bunit);
+    if (!rc) rc = upload(&t->d_bseg, bseg);
+    if (!rc) rc = upload(&t->d_yunit, yunit);
+    if (!rc) rc = upload(&t->d_yseg, yseg);
     if (!rc) rc = upload(&t->d_cg64, t->cglist);
     if (!rc) rc = upload(&t->d_cg32, cg32);
     if (!rc) rc = upload(&t->d_rootpq64, rp64);
     if (!rc) rc = upload(&t->d_rootpq32, rp32);
     if (!rc) rc = upload(&t->d_z, zent);
+    if (!rc) rc = upload(&t->d_zB, zentB);
     if (!rc) rc = upload(&t->d_b, bent);
     if (!rc) rc = upload(&t->d_blk, blks);
     if (!rc) rc = upload(&t->d_yblk_ptr, yptr);

@@ -262,7 +262,7 @@ def adjoint32_staged(tab, prm, nb: Neighbors, w_nb, utot, beta, mark=None, first
     if mark:
         mark(first + 1)
     check(L.so4_adjoint_deidrj32(tab.handle, C.byref(prm), N, _ptr(w_nb), _ptr(nb.img_ptr), _ptr(nb.img_j),
-                                 _ptr(nb.img_r), _ptr(y), _ptr(g), _ptr(vatom), st), "so4_adjoint_deidrj32")
+                                 _ptr(nb.img_r), M, _ptr(y), _ptr(g), _ptr(vatom), st), "so4_adjoint_deidrj32")
     if mark:
         mark(first + 2)
     check(L.so4_adjoint_gather(N, nb.nstruct, _ptr(nb.atom_ptr_dev), _ptr(nb.img_ptr), _ptr(nb.img_rev), _ptr(g),
