@@ -193,6 +193,19 @@ int so4_adjoint_gather(int natoms, int nstruct, const int *d_atom_ptr, const int
                        const int32_t *d_img_rev, const float *d_g, const double *d_vatom, double *d_forces,
                        double *d_virial, void *stream);
 
+/* The adjoint's backward: the Jacobian-vector product of B (FP32),
+ *   d_dB[natoms*nB] = sum_{images m of i} dB_i/dr_m . dr_m,  dr_m = (v_j - v_i) + G_s^T r_m,
+ * for per-atom vectors d_v[natoms*3] (f64, may be NULL) and per-structure
+ * matrices d_G[nstruct*9] (f64, row-major G_ab, may be NULL; then d_atom_struct
+ * is not read).  With v = -dL/dF and G = dL/dW it gives dL/dbeta for the forces
+ * and virial of so4_adjoint32, i.e. the gradient a force/stress loss sends back
+ * into an energy model.  Scratch: so4_jvp_workspace_size() bytes. */
+size_t so4_jvp_workspace_size(const so4_tables *t, int natoms);
+int so4_jvp32(const so4_tables *t, const so4_params *p, const int *d_atom_struct, int natoms,
+              const double *d_w_nb, const int32_t *d_img_ptr, const int32_t *d_img_j, const double *d_img_r,
+              const float *d_utot, const double *d_v, const double *d_G, float *d_dB, void *d_work,
+              size_t work_bytes, void *stream);
+
 /* so4_adjoint32 for callers that cannot allocate device memory.  No counterpart
  * in the reference (whose CPU code has no device allocator to avoid).
  * Same arguments as so4_adjoint32 without the workspace: the scratch comes from

@@ -122,6 +122,8 @@ struct so4_tables {
     //   Y unit {half e, seg0, seg1, bits of u_norm w_mid},  Y segment {t0, t1, block, 0}
     int4 *d_bunit = nullptr, *d_bseg = nullptr;
     int4 *d_yunit = nullptr, *d_yseg = nullptr;
+    //   JVP unit {k, seg0, seg1, 0},     JVP segment {t0, t1, half index of dU_lam[e], bits of fac_s w_e}
+    int4 *d_junit = nullptr, *d_jseg = nullptr;
     int n_terms = 0;
     std::vector<int> term_ptr;
 };

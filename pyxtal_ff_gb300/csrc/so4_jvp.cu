@@ -1,0 +1,232 @@
+// so4_jvp.cu -- the adjoint's backward: the Jacobian-vector product of B.
+//
+// For a displacement field given per image as dr_m = (v_j - v_i) + G_s^T r_m
+// (v: per-atom vectors, G: a per-structure 3x3 matrix), returns
+//   dB_i = sum_{images m of i} (dB_i/dr_m) . dr_m
+// with dB/dr in the reference's form (compute_dbidrj, pyxtal_ff/descriptors/SO4.py:1113-1227):
+//   dB_k = Re [2 S(l; dU, Z(l1,l2,l)) + 2 (l+1)/(l1+1) S(l1; dU, Z(l,l2,l1)) + 2 (l+1)/(l2+1) S(l2; dU, Z(l,l1,l2))]
+// where dU is the tangent of U_tot, sum_m u_norm w_j (sfac dU_m . dr_m + dsfac (r^ . dr_m) U_m)
+// (dudr, :1001-1018).  With v = -dL/dF and G = dL/dW this is dL/dbeta of the
+// adjoint's forces F and virial W, which is how forces enter a training loss.
+#include <algorithm>
+
+#include "so4_atom.cuh"
+#include "so4_rowchain.cuh"
+#include "so4_zlanes.cuh"
+
+namespace {
+
+template <typename K>
+int set_smem_j(K kern, size_t smem) {
+    if (smem > 227 * 1024) return SO4_ERR_UNSUPPORTED;
+    if (smem > 48 * 1024)
+        SO4_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    return SO4_OK;
+}
+
+struct JArgs {
+    int cutoff_id, natoms, nh, nu, nB;
+    float psi_fac, rc32;
+    const int *astruct;
+    const double *w_nb, *img_r, *v, *G;
+    const int32_t *img_ptr, *img_j;
+    const float2 *utot;
+    const int *fmap;
+    const ZTerm *terms;
+    const int4 *unit, *seg;
+    SmallTables st;
+    float2 *dU;
+    float *dB;
+};
+
+// tangent of U_tot, one warp per centre (same layout as k_utot_rc)
+template <int TWOL, int NW>
+__global__ void __launch_bounds__(NW * 32) k_jvp_du_rc(JArgs A) {
+    using RC = RowChain<TWOL>;
+    constexpr int W = TWOL + 1, NACC = acc_block(TWOL + 1);
+    extern __shared__ __align__(16) float jv_smem[];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int a = blockIdx.x * NW + wid;
+    const int grp = lane / RC::NCH, mb = lane - grp * RC::NCH;
+    float accr[NACC], acci[NACC];
+#pragma unroll
+    for (int q = 0; q < NACC; ++q) accr[q] = acci[q] = 0.f;
+    if (a < A.natoms) {
+        const int m0 = A.img_ptr[a], m1 = A.img_ptr[a + 1];
+        float vi[3] = {0.f, 0.f, 0.f}, G[9];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) G[q] = 0.f;
+        if (A.v)
+            for (int c = 0; c < 3; ++c) vi[c] = (float)A.v[3 * a + c];
+        if (A.G) {
+            const int s = A.astruct[a];
+            for (int q = 0; q < 9; ++q) G[q] = (float)A.G[9 * s + q];
+        }
+        for (int base = m0; base < m1; base += RC::IPW) {
+            const int m = base + grp;
+            float x = 1.f, y = 0.f, z = 0.f, a_du = 0.f, ax = 0.f, ay = 0.f, az = 0.f;
+            if (grp < RC::IPW && m < m1) {
+                x = (float)A.img_r[3 * m];
+                y = (float)A.img_r[3 * m + 1];
+                z = (float)A.img_r[3 * m + 2];
+                const float rr = sqrtf(x * x + y * y + z * z);
+                if (rr >= 1e-8f) {
+                    const int j = A.img_j[m];
+                    float d[3] = {0.f, 0.f, 0.f};
+                    if (A.v)
+                        for (int c = 0; c < 3; ++c) d[c] = (float)A.v[3 * j + c] - vi[c];
+                    // dr_b += sum_a G_ab r_a
+                    d[0] += G[0] * x + G[3] * y + G[6] * z;
+                    d[1] += G[1] * x + G[4] * y + G[7] * z;
+                    d[2] += G[2] * x + G[5] * y + G[8] * z;
+                    float sf, dsf;
+                    cutoff_fn<float>(A.cutoff_id, rr, A.rc32, sf, dsf);
+                    const float w = (float)A.w_nb[A.img_j[m]];
+                    a_du = w * dsf * (x * d[0] + y * d[1] + z * d[2]) / rr;
+                    ax = w * sf * d[0];
+                    ay = w * sf * d[1];
+                    az = w * sf * d[2];
+                } else {
+                    x = 1.f;
+                    y = z = 0.f;
+                }
+            }
+            const float r = sqrtf(x * x + y * y + z * z);
+            CK<float> ck;
+            make_ck<float, true>(x, y, z, r, A.psi_fac * r, ck);
+            float ur[W], ui[W], dr[3][W], di[3][W];
+#pragma unroll
+            for (int q = 0; q < W; ++q) {
+                ur[q] = ui[q] = 0.f;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) dr[c][q] = di[c][q] = 0.f;
+            }
+            ur[0] = 1.f;
+            if (mb == 0) accr[0] += a_du;  // level 0: U = 1, dU = 0
+            RcJvp<TWOL, 1>::run(mb, ck, a_du, ax, ay, az, ur, ui, dr, di, accr, acci);
+        }
+    }
+    float *sw = jv_smem + (size_t)wid * 32 * 2 * NACC;
+#pragma unroll
+    for (int q = 0; q < NACC; ++q) {
+        sw[lane * 2 * NACC + 2 * q] = accr[q];
+        sw[lane * 2 * NACC + 2 * q + 1] = acci[q];
+    }
+    __syncwarp();
+    if (a >= A.natoms) return;
+    float2 *out = A.dU + (size_t)a * A.nh;
+    for (int e = lane; e < A.nh; e += 32) {
+        int L = 0;
+        while (L < TWOL && half_block(L + 1) <= e) ++L;
+        const int off = e - half_block(L);
+        const int row = off / (L + 1), ma = off - row * (L + 1);
+        float sr = 0.f, si = 0.f;
+        for (int g = 0; g < RC::IPW; ++g) {
+            const float *src = sw + (g * RC::NCH + row) * 2 * NACC + 2 * (acc_block(L) + ma);
+            sr += src[0];
+            si += src[1];
+        }
+        const float un = (float)A.st.unorm[L];
+        out[e] = make_float2(sr * un, si * un);
+    }
+}
+
+// dB_k = sum_{sections s, entries e} fac_s w_e Re(conj(dU[e]) Z_s[e]) for 32 atoms per CTA
+__global__ void __launch_bounds__(256) k_zjvp32(JArgs A) {
+    extern __shared__ __align__(16) float2 zl_smem[];
+    __shared__ int s_unit;
+    const int lane = threadIdx.x & 31;
+    const int a0 = blockIdx.x * 32;
+    float2 *Uf = zl_smem;
+    if (threadIdx.x == 0) s_unit = 0;
+    zl_load_utot(A.utot, A.fmap, a0, A.natoms, A.nh, A.nu, Uf);
+    __syncthreads();
+    const int a = a0 + lane;
+    const float2 *dU = A.dU + (size_t)min(a, A.natoms - 1) * A.nh;
+    for (int u = zl_next(&s_unit); u < A.nB; u = zl_next(&s_unit)) {
+        const int4 un = __ldg(A.unit + u);
+        float acc = 0.f;
+        int4 sg = (un.y < un.z) ? __ldg(A.seg + un.y) : make_int4(0, 0, 0, 0);
+        for (int q = un.y; q < un.z; ++q) {
+            const int4 cur = sg;
+            if (q + 1 < un.z) sg = __ldg(A.seg + q + 1);
+            const float2 z = zl_entry(A.terms, cur.x, cur.y, Uf, lane);
+            const float2 d = __ldg(dU + cur.z);
+            acc += __int_as_float(cur.w) * (d.x * z.x + d.y * z.y);
+        }
+        if (a < A.natoms) A.dB[(size_t)a * A.nB + un.x] = acc;
+    }
+}
+
+template <int TWOL>
+int launch_jvp_du(const JArgs &A, cudaStream_t st) {
+    constexpr int NW = 4;
+    const size_t smem = sizeof(float) * NW * 32 * 2 * acc_block(TWOL + 1);
+    int rc = set_smem_j(k_jvp_du_rc<TWOL, NW>, smem);
+    if (rc) return rc;
+    k_jvp_du_rc<TWOL, NW><<<(A.natoms + NW - 1) / NW, NW * 32, smem, st>>>(A);
+    so4_count_launch();
+    return SO4_OK;
+}
+
+size_t a256j(size_t x) { return (x + 255) & ~(size_t)255; }
+
+}  // namespace
+
+extern "C" size_t so4_jvp_workspace_size(const so4_tables *t, int natoms) {
+    if (!t) return 0;
+    return a256j(SO4_WS_HEADER) + a256j(sizeof(float2) * (size_t)t->n_half * (natoms + 1));
+}
+
+extern "C" int so4_jvp32(const so4_tables *t, const so4_params *p, const int *d_atom_struct, int natoms,
+                         const double *d_w_nb, const int32_t *d_img_ptr, const int32_t *d_img_j, const double *d_img_r,
+                         const float *d_utot, const double *d_v, const double *d_G, float *d_dB, void *d_work,
+                         size_t work_bytes, void *stream) {
+    if (!t || !p || natoms < 0 || !d_utot || !d_dB || !d_work) return SO4_ERR_ARG;
+    if (p->twol != t->twol || !(p->rcut > 0.0) || !(p->rfac0 > 0.0)) return SO4_ERR_ARG;
+    if (p->cutoff_id < 1 || p->cutoff_id > 7) return SO4_ERR_UNSUPPORTED;
+    if (d_G && !d_atom_struct) return SO4_ERR_ARG;
+    if (so4_jvp_workspace_size(t, natoms) > work_bytes) return SO4_ERR_WORKSPACE;
+    if (natoms == 0) return SO4_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    JArgs A;
+    A.cutoff_id = p->cutoff_id;
+    A.natoms = natoms;
+    A.nh = t->n_half;
+    A.nu = t->n_u;
+    A.nB = t->n_b;
+    A.psi_fac = (float)(p->rfac0 * SO4_PI / p->rcut);
+    A.rc32 = (float)p->rcut;
+    A.astruct = d_atom_struct;
+    A.w_nb = d_w_nb;
+    A.img_r = d_img_r;
+    A.v = d_v;
+    A.G = d_G;
+    A.img_ptr = d_img_ptr;
+    A.img_j = d_img_j;
+    A.utot = (const float2 *)d_utot;
+    A.fmap = t->d_fmap;
+    A.terms = t->d_terms;
+    A.unit = t->d_junit;
+    A.seg = t->d_jseg;
+    fill_small_tables(t, A.st);
+    A.dU = (float2 *)((char *)d_work + a256j(SO4_WS_HEADER));
+    A.dB = d_dB;
+    int rc;
+    switch (t->twol) {
+        case 2: rc = launch_jvp_du<2>(A, st); break;
+        case 4: rc = launch_jvp_du<4>(A, st); break;
+        case 6: rc = launch_jvp_du<6>(A, st); break;
+        case 8: rc = launch_jvp_du<8>(A, st); break;
+        case 10: rc = launch_jvp_du<10>(A, st); break;
+        case 12: rc = launch_jvp_du<12>(A, st); break;
+        default: return SO4_ERR_UNSUPPORTED;
+    }
+    if (rc) return rc;
+    const size_t smz = sizeof(float2) * (size_t)t->n_u * ZL_PITCH;
+    rc = set_smem_j(k_zjvp32, smz);
+    if (rc) return rc;
+    k_zjvp32<<<(natoms + 31) / 32, 256, smz, st>>>(A);
+    so4_count_launch();
+    return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
+}

@@ -80,6 +80,17 @@ __device__ __forceinline__ double norm_rn(const double *r) {
     return __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(r[0], r[0]), __dmul_rn(r[1], r[1])), __dmul_rn(r[2], r[2])));
 }
 
+// Exact membership test |r| < rcut in FP64.  Kept out of line so the compiler
+// cannot if-convert it into the FP32 loop: FP64 runs at 1/64 of the FP32 rate
+// here, and the test is needed only for the rare candidates in the rounding band.
+__device__ __noinline__ bool exact_inside(const so4_geom &g, const double *pi, const double *pos, int j, int o0, int o1,
+                                          int o2, double rcut) {
+    const double pj[3] = {pos[3 * j], pos[3 * j + 1], pos[3 * j + 2]};
+    double r[3];
+    image_vec(g, pi, pj, o0, o1, o2, r);
+    return norm_rn(r) < rcut;
+}
+
 __global__ void k_bin(const so4_geom *geom, const double *pos, const int *astruct, int natoms, NLWork w) {
     const int a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= natoms) return;
@@ -210,10 +221,7 @@ __global__ void k_scan_images(const so4_geom *geom, const double *pos, const int
             const float hi = rc32 + delta, lo = rc32 - delta;
             if (d2 > hi * hi) continue;            // surely outside
             if (!(lo > 0.f && d2 < lo * lo)) {     // within the rounding band: decide in FP64
-                const double pj[3] = {pos[3 * j], pos[3 * j + 1], pos[3 * j + 2]};
-                double r[3];
-                image_vec(g, pi, pj, o[0], o[1], o[2], r);
-                if (!(norm_rn(r) < rcut)) continue;
+                if (!exact_inside(g, pi, pos, j, o[0], o[1], o[2], rcut)) continue;
             }
             if (MODE == 1) {
                 if (abs(o[0]) > OFF_MAX || abs(o[1]) > OFF_MAX || abs(o[2]) > OFF_MAX) {

@@ -229,3 +229,32 @@ struct RcUtot<TWOL, TWOL + 1> {
                                                float (&)[3][TWOL + 1], float (&)[3][TWOL + 1],
                                                float (&)[acc_block(TWOL + 1)], float (&)[acc_block(TWOL + 1)]) {}
 };
+
+// Levels L..TWOL with derivatives; after each level the lane adds the
+// directional derivative of its row along the image displacement dr_m,
+//   w (sfac sum_c dU_c dr_c + dsfac (r^ . dr) U),
+// into its accumulator (the tangent of U_tot used by the JVP).
+template <int TWOL, int L>
+struct RcJvp {
+    __device__ __forceinline__ static void run(int mb, const CK<float> &ck, float a_du, float a_dx, float a_dy,
+                                               float a_dz, float (&ur)[TWOL + 1], float (&ui)[TWOL + 1],
+                                               float (&dr)[3][TWOL + 1], float (&di)[3][TWOL + 1],
+                                               float (&accr)[acc_block(TWOL + 1)], float (&acci)[acc_block(TWOL + 1)]) {
+        if ((L & 1) == 0) rc_start<TWOL, L, true>(mb, ur, ui, dr, di);
+        rc_level<TWOL, L, true>(mb, ck, ur, ui, dr, di);
+        if (2 * mb <= L) {
+#pragma unroll
+            for (int ma = 0; ma <= L; ++ma) {
+                accr[acc_block(L) + ma] += a_du * ur[ma] + a_dx * dr[0][ma] + a_dy * dr[1][ma] + a_dz * dr[2][ma];
+                acci[acc_block(L) + ma] += a_du * ui[ma] + a_dx * di[0][ma] + a_dy * di[1][ma] + a_dz * di[2][ma];
+            }
+        }
+        RcJvp<TWOL, L + 1>::run(mb, ck, a_du, a_dx, a_dy, a_dz, ur, ui, dr, di, accr, acci);
+    }
+};
+template <int TWOL>
+struct RcJvp<TWOL, TWOL + 1> {
+    __device__ __forceinline__ static void run(int, const CK<float> &, float, float, float, float, float (&)[TWOL + 1],
+                                               float (&)[TWOL + 1], float (&)[3][TWOL + 1], float (&)[3][TWOL + 1],
+                                               float (&)[acc_block(TWOL + 1)], float (&)[acc_block(TWOL + 1)]) {}
+};

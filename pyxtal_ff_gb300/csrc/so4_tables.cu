@@ -95,6 +95,8 @@ void free_device(so4_tables *t) {
     cudaFree(t->d_bseg);
     cudaFree(t->d_yunit);
     cudaFree(t->d_yseg);
+    cudaFree(t->d_junit);
+    cudaFree(t->d_jseg);
 }
 
 }  // namespace
@@ -364,6 +366,32 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
         yunit.push_back(make_int4(e, s0, (int)yseg.size(), bits));
     }
 
+    // JVP units: one per component k, a segment per summed entry of each of its three sections
+    std::vector<std::pair<long, int>> jc;
+    for (int k = 0; k < t->n_b; ++k) {
+        long c = 0;
+        for (int sct = 0; sct < 3; ++sct)
+            for (int e = 0; e < bent[k].cnt[sct]; ++e) c += zcost(bent[k].z[sct] + e);
+        jc.push_back({-c, k});
+    }
+    std::stable_sort(jc.begin(), jc.end());
+    std::vector<int4> junit, jseg;
+    for (auto &v : jc) {
+        const int k = v.second;
+        const BEnt &be = bent[k];
+        const int s0 = (int)jseg.size();
+        for (int sct = 0; sct < 3; ++sct)
+            for (int e = 0; e < be.cnt[sct]; ++e) {
+                const int jz = be.z[sct] + e;
+                const double w = (((be.lam[sct] % 2) == 0) && e == be.cnt[sct] - 1) ? 0.5 : 1.0;
+                const float f = (float)(be.fac[sct] * w);
+                int bits;
+                std::memcpy(&bits, &f, sizeof bits);
+                jseg.push_back(make_int4(t->term_ptr[jz], t->term_ptr[jz + 1], be.h[sct] + e, bits));
+            }
+        junit.push_back(make_int4(k, s0, (int)jseg.size(), 0));
+    }
+
     std::vector<int> fmap(t->n_u);
     for (int l = 0; l < ld; ++l)
         for (int mb = 0; mb <= l; ++mb)
@@ -385,6 +413,8 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
     if (!rc) rc = upload(&t->d_bseg, bseg);
     if (!rc) rc = upload(&t->d_yunit, yunit);
     if (!rc) rc = upload(&t->d_yseg, yseg);
+    if (!rc) rc = upload(&t->d_junit, junit);
+    if (!rc) rc = upload(&t->d_jseg, jseg);
     if (!rc) rc = upload(&t->d_cg64, t->cglist);
     if (!rc) rc = upload(&t->d_cg32, cg32);
     if (!rc) rc = upload(&t->d_rootpq64, rp64);

@@ -268,3 +268,17 @@ def adjoint32_staged(tab, prm, nb: Neighbors, w_nb, utot, beta, mark=None, first
     check(L.so4_adjoint_gather(N, nb.nstruct, _ptr(nb.atom_ptr_dev), _ptr(nb.img_ptr), _ptr(nb.img_rev), _ptr(g),
                                _ptr(vatom), _ptr(forces), _ptr(virial), st), "so4_adjoint_gather")
     return forces[:N], virial[: nb.nstruct]
+
+
+def jvp32(tab, prm, nb: Neighbors, w_nb, utot, v=None, G=None, workspace=None):
+    """dB (N, nB) f32: the JVP of B along dr_m = (v_j - v_i) + G_s^T r_m (v (N,3), G (S,3,3) f64)."""
+    dev = utot.device
+    dB = torch.empty((max(nb.natoms, 1), tab.nB), dtype=torch.float32, device=dev)
+    need = lib().so4_jvp_workspace_size(tab.handle, nb.natoms)
+    ws = workspace if (workspace is not None and workspace.numel() >= need) else torch.empty(need, dtype=torch.uint8, device=dev)
+    v = v.to(torch.float64).contiguous() if v is not None else None
+    G = G.to(torch.float64).contiguous() if G is not None else None
+    check(lib().so4_jvp32(tab.handle, C.byref(prm), _ptr(nb.atom_struct), nb.natoms, _ptr(w_nb), _ptr(nb.img_ptr),
+                          _ptr(nb.img_j), _ptr(nb.img_r), _ptr(utot), _ptr(v), _ptr(G), _ptr(dB), _ptr(ws), ws.numel(),
+                          _stream()), "so4_jvp32")
+    return dB[: nb.natoms]
