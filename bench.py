@@ -171,6 +171,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-train", action="store_true", help="skip the training-step leg")
     ap.add_argument("--quick", action="store_true",
                     help="device-resident steps only (no e2e, FP64, CPU or peak legs); for profiler runs")
     args = ap.parse_args()
@@ -355,6 +356,29 @@ def main():
     kernels["plain_fp64"] = {"ms": ms64, "tflops_fp64_incl_nl_contraction": kf["plain"] / (ms64 * 1e-3) / 1e12,
                              "frac_fp64": kf["plain"] / (ms64 * 1e-3) / 1e12 / peaks["fp64_tflops"]}
 
+    # ---- force-matching training step (512 Si structures of 8-64 atoms, lmax 3), extra line item
+    train = None
+    if not args.no_train:
+        from pyxtal_ff_gb300 import structures as S
+        from pyxtal_ff_gb300.train import ForceMatching
+        tstructs = S.si_batch(512, seed=4, sizes=range(1, 9), max_cells=8, strain=0.04, sigma=0.1)
+        fm = ForceMatching(tstructs, lmax=3, rcut=4.9, seed=4)
+        for _ in range(2):
+            fm.step()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        nstep = 5
+        e0.record()
+        for _ in range(nstep):
+            fm.step()
+        e1.record()
+        e1.synchronize()
+        tms = e0.elapsed_time(e1) / nstep
+        train = {"workload": "512 Si structures (8-64 atoms, 22256 atoms), SO4 lmax 3, rcut 4.9, MLP 30-30 tanh, "
+                             "loss MSE(E/atom)+0.1 MSE(F), Adam; B and U_tot held on device",
+                 "ms_per_step": tms, "atoms_per_s": fm.batch.natoms / (tms * 1e-3)}
+        del fm
+
     # ---- CPU baseline (the oracle, all host threads), rank 0 only
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -370,7 +394,7 @@ def main():
                 "data": "synthetic (seeded diamond-Si, sigma 0.1 A)", "config": CONFIG,
                 "pairs_per_s": ws * (nb.npair) * args.steps / (t_dev * 1e-3),
                 "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": int(launches),
-                "fp64_plain": fp64, "err_vs_fp64": err, "kernels": kernels,
+                "fp64_plain": fp64, "err_vs_fp64": err, "kernels": kernels, "train_step": train,
                 "peaks": {k: peaks[k] for k in ("hbm_gbs", "fp32_tflops", "fp64_tflops") if k in peaks}}
         print(json.dumps(line), flush=True)
     if ws > 1:
