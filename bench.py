@@ -30,7 +30,8 @@ LMAX, RCUT, SEED_POS, SEED_COEF = 4, 5.0, 5, 6
 METRIC = "SO4 atoms/s w/ forces+stress: FP32 adjoint vs plain FP64 dB/dr, 1 GB300; err vs FP64"
 CONFIG = {"workload": "diamond-Si 20x20x10 (32000 atoms), SO4 lmax=4, rcut=5.0 A, energy+forces+stress, "
                       "linear model N(0,0.01)", "structures": 1, "atoms": 32000, "lmax": LMAX, "rcut": RCUT,
-          "neighbor_list": "in step", "l2": "flushed between steps (512 MiB write)"}
+          "neighbor_list": "in step", "l2": "flushed between steps (512 MiB write)",
+          "path": "FP32 fused linear forward + adjoint (Z once for B and Y), FP64 force/virial reductions"}
 
 
 def workload():
@@ -211,27 +212,24 @@ def main():
     tab, prm = calc.tables, calc.params
     L = _lib.lib()
 
-    stage_names = ["neighbors", "forward32", "model", "adjoint_y32", "adjoint_deidrj32", "gather"]
+    stage_names = ["neighbors", "utot32", "linear_by32", "adjoint_deidrj32", "gather_energy"]
+    beta_dev = model.coef.detach()[calc._species].contiguous()
+    bias0 = float(model.bias.detach()[0])
 
     def device_step(ev=None):
-        """One step with the inputs in HBM; ev: list of events recorded between stages."""
+        """One step with the inputs in HBM: neighbour list, U_tot, the fused B + Y pass of the
+        linear energy, per-image dE/dr, forces / virial gather and the energy; ev: events
+        recorded between the stages."""
         def mark(i):
             if ev is not None:
                 ev[i].record()
         mark(0)
         nb = calc.neighbors(batch, pos_dev)
         mark(1)
-        x, utot = engine.forward32(tab, prm, nb, calc._w_nb, calc._w_site)
-        mark(2)
-        xg = x.detach().requires_grad_(True)
-        with torch.enable_grad():
-            e_atom = model(xg, calc._species)
-            beta, = torch.autograd.grad(e_atom.sum(), xg)
-        mark(3)
-        out = engine.adjoint32_staged(tab, prm, nb, calc._w_nb, utot, beta, mark=mark, first=3)
-        energy = e_atom.detach().double().sum()
-        mark(6)
-        return energy, out
+        x, forces, virial = engine.linear_staged(tab, prm, nb, calc._w_nb, calc._w_site, beta_dev, mark=mark, first=1)
+        energy = ((x * beta_dev).sum(-1).double()).sum() + bias0
+        mark(5)
+        return energy, forces, virial
 
     # ---- warm-up
     for _ in range(args.warmup):

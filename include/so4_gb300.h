@@ -86,7 +86,8 @@ typedef struct {
  * normalize_u selects u_norm = 4 pi / sqrt(l+1) (SO4.py:1304-1311). */
 int so4_tables_create(int twol, int normalize_u, so4_tables **out);
 int so4_tables_destroy(so4_tables *t);
-/* sizes[0..5] = idxu, idxu_half, idxz, nB, idxcg, number of Z blocks */
+/* sizes[0..7] = idxu, idxu_half, idxz, nB, idxcg, number of Z blocks,
+ * B-section entries per atom (scratch of so4_linear_by32), flattened Z terms */
 int so4_tables_sizes(const so4_tables *t, int *sizes);
 /* host copies of the reference-visible tables (any pointer may be NULL):
  * cglist[idxcg] f64, idxb[nB*3], idxz[idxz*10], idxu_block[twol+1],
@@ -118,7 +119,9 @@ int so4_nl_count(const so4_geom *d_geom, int nstruct, int nbins_total, const dou
                  const int *d_atom_struct, int natoms, double rcut, int32_t *d_img_ptr,
                  void *d_work, size_t work_bytes, void *stream);
 
-/* Pass 2: writes the sorted images of every centre: d_img_j[nimg],
+/* Pass 2: writes the sorted images of every centre: d_img_j[nimg] (nimg is the
+ * capacity of the image arrays; past it nothing is written and the status gets
+ * SO4_ERR_CAPACITY, so a caller may pass an estimate and retry with more),
  * d_img_off[3*nimg] (integer cell offsets), d_img_r[3*nimg] (the image vectors,
  * (pos[j] + (o0 a1 + o1 a2) + o2 a3) - pos[i] in FP64 with every operation
  * separately rounded) and the pair counts as an exclusive scan d_pair_ptr[natoms+1]. */
@@ -127,7 +130,8 @@ int so4_nl_fill(const so4_geom *d_geom, int nstruct, int nbins_total, const doub
                 int64_t nimg, int32_t *d_img_j, int32_t *d_img_off, double *d_img_r,
                 int32_t *d_pair_ptr, void *d_work, size_t work_bytes, void *stream);
 
-/* Pass 3: d_seq[2*npair] (i64, structure-local (i, j)), d_pair_img[npair+1]
+/* Pass 3 (npair: capacity of the pair arrays, as nimg above):
+ * d_seq[2*npair] (i64, structure-local (i, j)), d_pair_img[npair+1]
  * (images of pair p are [pair_img[p], pair_img[p+1])), d_nsite[natoms] (the
  * (i, i) pair of each centre), d_img_pair[nimg] and d_img_rev[nimg] (index of
  * the image (i, -o) in the list of j). */
@@ -136,6 +140,11 @@ int so4_nl_pairs(const so4_geom *d_geom, int nstruct, const int *d_atom_struct, 
                  const int32_t *d_img_off, const int32_t *d_pair_ptr, int64_t npair,
                  int64_t *d_seq, int32_t *d_pair_img, int32_t *d_nsite, int32_t *d_img_pair,
                  int32_t *d_img_rev, void *d_work, size_t work_bytes, void *stream);
+
+/* One synchronising read of {total images, total pairs, status bits} after the
+ * three passes (d_pair_ptr may be NULL after pass 1 only). */
+int so4_nl_summary(const int32_t *d_img_ptr, const int32_t *d_pair_ptr, int natoms, const void *d_work,
+                   size_t work_bytes, void *stream, int *h_summary);
 
 /* Reads the device status word of a workspace (synchronises `stream`). */
 int so4_status_read(const void *d_work, size_t work_bytes, void *stream, int *h_status);
@@ -192,6 +201,25 @@ int so4_adjoint_deidrj32(const so4_tables *t, const so4_params *p, int natoms, c
 int so4_adjoint_gather(int natoms, int nstruct, const int *d_atom_ptr, const int32_t *d_img_ptr,
                        const int32_t *d_img_rev, const float *d_g, const double *d_vatom, double *d_forces,
                        double *d_virial, void *stream);
+
+/* Forward and adjoint in one call for an energy linear in B (beta = dE/dB does not
+ * depend on B, e.g. the reference's order-1 polynomial regression,
+ * pyxtal_ff/models/polynomialregression.py:374): writes d_x (B, natoms*nB f32),
+ * d_forces and d_virial as so4_forward32 + so4_adjoint32 would, with every Z entry
+ * computed once for both B and Y.  Scratch: so4_linear_workspace_size() bytes. */
+size_t so4_linear_workspace_size(const so4_tables *t, int natoms, int64_t nimg);
+/* Its stages: U_tot alone (the first half of so4_forward32), then B and Y from U_tot
+ * and beta in one pass (d_bc: sizes[6] * natoms floats of scratch, entry-major). */
+int so4_utot32(const so4_tables *t, const so4_params *p, int natoms, const double *d_w_nb,
+               const double *d_w_site, const int32_t *d_img_ptr, const int32_t *d_img_j,
+               const double *d_img_r, float *d_utot, void *stream);
+int so4_linear_by32(const so4_tables *t, int natoms, const float *d_utot, const float *d_beta, float *d_x,
+                    float *d_y, float *d_bc, void *stream);
+int so4_adjoint_linear32(const so4_tables *t, const so4_params *p, int nstruct, const int *d_atom_struct,
+                         const int *d_atom_ptr, int natoms, const double *d_w_nb, const double *d_w_site,
+                         const int32_t *d_img_ptr, const int32_t *d_img_j, const double *d_img_r,
+                         const int32_t *d_img_rev, int64_t nimg, const float *d_beta, float *d_x,
+                         double *d_forces, double *d_virial, void *d_work, size_t work_bytes, void *stream);
 
 /* The adjoint's backward: the Jacobian-vector product of B (FP32),
  *   d_dB[natoms*nB] = sum_{images m of i} dB_i/dr_m . dr_m,  dr_m = (v_j - v_i) + G_s^T r_m,

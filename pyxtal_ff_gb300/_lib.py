@@ -85,6 +85,7 @@ def lib():
         "so4_nl_pairs": (_i, [_vp, _i, _vp, _i, _vp, _i64, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp, _vp, _vp,
                               _sz, _vp]),
         "so4_status_read": (_i, [_vp, _sz, _vp, C.POINTER(_i)]),
+        "so4_nl_summary": (_i, [_vp, _vp, _i, _vp, _sz, _vp, C.POINTER(_i)]),
         "so4_plain_workspace_size": (_sz, [_vp, _i]),
         "so4_plain": (_i, [_vp, C.POINTER(Params), _i, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
                            _i, _i, _vp, _vp, _vp, _vp, _sz, _vp]),
@@ -95,6 +96,11 @@ def lib():
         "so4_adjoint_gather": (_i, [_i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
         "so4_launch_count": (C.c_longlong, []),
         "so4_jvp_workspace_size": (_sz, [_vp, _i]),
+        "so4_linear_workspace_size": (_sz, [_vp, _i, _i64]),
+        "so4_utot32": (_i, [_vp, C.POINTER(Params), _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+        "so4_linear_by32": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _vp, _vp]),
+        "so4_adjoint_linear32": (_i, [_vp, C.POINTER(Params), _i, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _i64,
+                                      _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
         "so4_jvp32": (_i, [_vp, C.POINTER(Params), _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
         "so4_adjoint32_noalloc": (_i, [_vp, C.POINTER(Params), _i, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _i64, _vp,
                                        _vp, _vp, _vp, _vp]),

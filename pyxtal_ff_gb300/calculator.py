@@ -144,6 +144,19 @@ class SO4Calculator:
         self.prepare(batch)
         pos = self._positions(batch, positions)
         nb = self.neighbors(batch, pos)
+        if isinstance(model, LinearModel):
+            # beta = dE/dB does not depend on B: forward and adjoint in one fused pass
+            beta = model.coef.detach()[self._species]
+            need = engine.lib().so4_linear_workspace_size(self.tables.handle, nb.natoms, nb.nimg)
+            if self._ws is None or self._ws.numel() < need:
+                self._ws = torch.empty(int(need * 1.25) + 4096, dtype=torch.uint8, device=self.device)
+            x, forces, virial = engine.adjoint_linear32(self.tables, self.params, nb, self._w_nb, self._w_site, beta,
+                                                        workspace=self._ws)
+            e_atom = (x * beta).sum(-1) + model.bias.detach()[self._species]
+            energy = torch.zeros(batch.nstruct, dtype=torch.float64, device=self.device)
+            energy.index_add_(0, self._struct, e_atom.double())
+            stress = -(virial.reshape(-1, 9)[:, VOIGT] / self._vol[:, None]) * EV_A3_TO_GPA
+            return dict(energy=energy, forces=forces, virial=virial, stress=stress, x=x, neighbors=nb)
         x, utot = engine.forward32(self.tables, self.params, nb, self._w_nb, self._w_site)
         xg = x.detach().requires_grad_(True)
         with torch.enable_grad():

@@ -186,9 +186,12 @@ struct ZLArgs {
     const ZBlk *blk;
     const int *yptr, *ylist;
     const float *beta;
+    const int *bpos;  // fused path: start of each component's B-section entries
+    int nbsec;
     SmallTables st;
-    float *x;    // B out  (k_zb32)
-    float2 *Y;   // Y out  (k_zy32)
+    float *x;    // B out  (k_zb32, k_zby32)
+    float2 *Y;   // Y out  (k_zy32, k_zby32)
+    float *bc;   // fused path: per-atom B-section contributions [natoms][nbsec]
 };
 
 // B_k = 2 Re sum' conj(U_l) Z(l1,l2,l) for 32 atoms per CTA (compute_bi, SO4.py:1071-1111)
@@ -208,7 +211,7 @@ __global__ void __launch_bounds__(256) k_zb32(ZLArgs A) {
         for (int q = un.y; q < un.z; ++q) {
             const int4 cur = sg;
             if (q + 1 < un.z) sg = __ldg(A.seg + q + 1);
-            const float2 z = zl_entry(A.terms, cur.x, cur.y, Uf, lane);
+            const float2 z = zl_entry(A.terms, cur.x, cur.y, Uf + lane);
             const float2 ul = Uf[cur.z * ZL_PITCH + lane];
             const float v = ul.x * z.x + ul.y * z.y;
             acc += (cur.w == 2) ? 0.5f * v : v;
@@ -245,13 +248,73 @@ __global__ void __launch_bounds__(256) k_zy32(ZLArgs A) {
         for (int q = un.y; q < un.z; ++q) {
             const int4 cur = sg;
             if (q + 1 < un.z) sg = __ldg(A.seg + q + 1);
-            const float2 z = zl_entry(A.terms, cur.x, cur.y, Uf, lane);
+            const float2 z = zl_entry(A.terms, cur.x, cur.y, Uf + lane);
             const float c = coef[cur.z * ZL_PITCH + lane];
             yr += c * z.x;
             yi += c * z.y;
         }
         const float s = __int_as_float(un.w);
         if (a0 + lane < A.natoms) A.Y[(size_t)(a0 + lane) * A.nh + un.x] = make_float2(s * yr, s * yi);
+    }
+}
+
+// Fused forward + Y for an energy linear in B (beta known before B): every Z entry
+// is computed once; it feeds Y as in k_zy32 and, when it lies in a B section, its
+// contribution w_e Re(conj(U_l[e]) Z[e]) goes to the atom's scratch row, which is
+// then summed per component in a fixed order: B_k = 2 sum_e (compute_bi, SO4.py:1071-1111).
+// The scratch is [entry][atom] (d_bc holds nbsec * natoms floats).
+__global__ void __launch_bounds__(256) k_zby32(ZLArgs A) {
+    extern __shared__ __align__(16) float2 zl_smem[];
+    __shared__ int s_unit;
+    const int lane = threadIdx.x & 31;
+    const int a0 = blockIdx.x * 32;
+    const int a = a0 + lane;
+    float2 *Uf = zl_smem;
+    float *coef = (float *)(Uf + (size_t)A.nu * ZL_PITCH);  // [nblk][33]
+    if (threadIdx.x == 0) s_unit = 0;
+    zl_load_utot(A.utot, A.fmap, a0, A.natoms, A.nh, A.nu, Uf);
+    for (int idx = threadIdx.x; idx < 32 * A.nblk; idx += blockDim.x) {
+        const int l = idx / A.nblk, b = idx - l * A.nblk;
+        const int aa = a0 + l;
+        float c = 0.f;
+        if (aa < A.natoms) {
+            const ZBlk &bk = A.blk[b];
+            for (int r = 0; r < bk.nrole; ++r) c += (float)bk.role_f[r] * __ldg(A.beta + (size_t)aa * A.nB + bk.role_k[r]);
+        }
+        coef[b * ZL_PITCH + l] = c;
+    }
+    __syncthreads();
+    const int ldim = A.st.twol + 1;
+    for (int u = zl_next(&s_unit); u < A.nunit; u = zl_next(&s_unit)) {
+        const int4 un = __ldg(A.unit + u);
+        const int lam = level_of(A.st.h_block, ldim, un.x);
+        const float2 ul = Uf[(A.st.u_block[lam] + un.x - A.st.h_block[lam]) * ZL_PITCH + lane];
+        float yr = 0.f, yi = 0.f;
+        int4 sg = (un.y < un.z) ? __ldg(A.seg + un.y) : make_int4(0, 0, 0, -1);
+        for (int q = un.y; q < un.z; ++q) {
+            const int4 cur = sg;
+            if (q + 1 < un.z) sg = __ldg(A.seg + q + 1);
+            const float2 z = zl_entry(A.terms, cur.x, cur.y, Uf + lane);
+            const float c = coef[cur.z * ZL_PITCH + lane];
+            yr += c * z.x;
+            yi += c * z.y;
+            if (cur.w >= 0 && a < A.natoms) {
+                // scratch is entry-major, so the 32 lanes (atoms) store one contiguous line
+                const float v = ul.x * z.x + ul.y * z.y;
+                A.bc[(size_t)(cur.w >> 1) * A.natoms + a] = (cur.w & 1) ? 0.5f * v : v;
+            }
+        }
+        const float s = __int_as_float(un.w);
+        if (a < A.natoms) A.Y[(size_t)a * A.nh + un.x] = make_float2(s * yr, s * yi);
+    }
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < 32 * A.nB; idx += blockDim.x) {
+        const int k = idx >> 5, l = idx & 31;
+        const int aa = a0 + l;
+        if (aa >= A.natoms) continue;
+        float acc = 0.f;
+        for (int e = __ldg(A.bpos + k); e < __ldg(A.bpos + k + 1); ++e) acc += A.bc[(size_t)e * A.natoms + aa];
+        A.x[(size_t)aa * A.nB + k] = 2.f * acc;
     }
 }
 
@@ -743,6 +806,116 @@ extern "C" int so4_adjoint32_noalloc(const so4_tables *t, const so4_params *p, i
     if (rc) return rc;
     rc = so4_adjoint_deidrj32(t, p, natoms, d_w_nb, d_img_ptr, d_img_j, d_img_r, nimg, (const float *)w.Y, w.g, w.vatom,
                               stream);
+    if (rc) return rc;
+    return so4_adjoint_gather(natoms, nstruct, d_atom_ptr, d_img_ptr, d_img_rev, w.g, w.vatom, d_forces, d_virial,
+                              stream);
+}
+
+// ---------------------------------------------------------------------------
+// Energy linear in B: forward and adjoint with Z computed once.
+extern "C" size_t so4_linear_workspace_size(const so4_tables *t, int natoms, int64_t nimg) {
+    if (!t) return 0;
+    AdjWork w;
+    size_t s = carve_adj(w, nullptr, natoms, t->n_half, nimg);
+    s += a256(sizeof(float2) * (size_t)natoms * t->n_half + 8);          // U_tot
+    s += a256(sizeof(float) * (size_t)(natoms + 1) * t->n_bsec);          // B-section row
+    return s;
+}
+
+extern "C" int so4_utot32(const so4_tables *t, const so4_params *p, int natoms, const double *d_w_nb,
+                          const double *d_w_site, const int32_t *d_img_ptr, const int32_t *d_img_j,
+                          const double *d_img_r, float *d_utot, void *stream) {
+    if (!t || !p || natoms < 0 || !d_utot) return SO4_ERR_ARG;
+    if (p->twol != t->twol || !(p->rcut > 0.0) || !(p->rfac0 > 0.0)) return SO4_ERR_ARG;
+    if (p->cutoff_id < 1 || p->cutoff_id > 7) return SO4_ERR_UNSUPPORTED;
+    if (natoms == 0) return SO4_OK;
+    FwdArgs A;
+    A.prm = *p;
+    A.natoms = natoms;
+    A.nh = t->n_half;
+    A.nu = t->n_u;
+    A.nz = t->n_z;
+    A.nB = t->n_b;
+    A.w_nb = d_w_nb;
+    A.w_site = d_w_site;
+    A.img_r = d_img_r;
+    A.img_ptr = d_img_ptr;
+    A.img_j = d_img_j;
+    A.cg = t->d_cg32;
+    A.rootpq = t->d_rootpq32;
+    A.zent = t->d_z;
+    A.zentB = t->d_zB;
+    A.nzB = t->n_zB;
+    A.bent = t->d_b;
+    fill_small_tables(t, A.st);
+    A.utot = d_utot;
+    A.x = nullptr;
+    A.psi_fac = (float)(p->rfac0 * SO4_PI / p->rcut);
+    A.rc32 = (float)p->rcut;
+    cudaStream_t st = (cudaStream_t)stream;
+    int rc = SO4_OK;
+    switch (t->twol) {
+        case 2: rc = launch_utot_rc<2>(A, st); break;
+        case 4: rc = launch_utot_rc<4>(A, st); break;
+        case 6: rc = launch_utot_rc<6>(A, st); break;
+        case 8: rc = launch_utot_rc<8>(A, st); break;
+        case 10: rc = launch_utot_rc<10>(A, st); break;
+        case 12: rc = launch_utot_rc<12>(A, st); break;
+        default: {
+            const size_t smu =
+                sizeof(float) * rootpq_floats(t->ldim) + sizeof(cx<float>) * ((size_t)t->n_half * (1 + 2 * NWF));
+            rc = set_smem(k_utot32, smu);
+            if (rc) return rc;
+            k_utot32<<<natoms, NWF * 32, smu, st>>>(A);
+            so4_count_launch();
+        }
+    }
+    if (rc) return rc;
+    return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
+}
+
+extern "C" int so4_linear_by32(const so4_tables *t, int natoms, const float *d_utot, const float *d_beta, float *d_x,
+                               float *d_y, float *d_bc, void *stream) {
+    if (!t || natoms < 0 || !d_utot || !d_beta || !d_x || !d_y || !d_bc) return SO4_ERR_ARG;
+    if (natoms == 0) return SO4_OK;
+    ZLArgs Z = zl_args(t, natoms);
+    Z.utot = (const float2 *)d_utot;
+    Z.unit = t->d_yunit;
+    Z.seg = t->d_yseg;
+    Z.nunit = t->n_half;
+    Z.beta = d_beta;
+    Z.Y = (float2 *)d_y;
+    Z.x = d_x;
+    Z.bpos = t->d_bpos;
+    Z.nbsec = t->n_bsec;
+    Z.bc = d_bc;
+    const size_t smz = sizeof(float2) * (size_t)t->n_u * ZL_PITCH + sizeof(float) * (size_t)t->n_blk * ZL_PITCH;
+    int rc = set_smem(k_zby32, smz);
+    if (rc) return rc;
+    k_zby32<<<(natoms + 31) / 32, 256, smz, (cudaStream_t)stream>>>(Z);
+    so4_count_launch();
+    return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
+}
+
+extern "C" int so4_adjoint_linear32(const so4_tables *t, const so4_params *p, int nstruct, const int *d_atom_struct,
+                                    const int *d_atom_ptr, int natoms, const double *d_w_nb, const double *d_w_site,
+                                    const int32_t *d_img_ptr, const int32_t *d_img_j, const double *d_img_r,
+                                    const int32_t *d_img_rev, int64_t nimg, const float *d_beta, float *d_x,
+                                    double *d_forces, double *d_virial, void *d_work, size_t work_bytes,
+                                    void *stream) {
+    (void)d_atom_struct;
+    if (!t || !p || natoms < 0 || nstruct < 0 || nimg < 0 || !d_work || !d_x) return SO4_ERR_ARG;
+    if (so4_linear_workspace_size(t, natoms, nimg) > work_bytes) return SO4_ERR_WORKSPACE;
+    AdjWork w;
+    const size_t base = carve_adj(w, d_work, natoms, t->n_half, nimg);
+    float *utot = (float *)((char *)d_work + base);
+    float *bc = (float *)((char *)d_work + base + a256(sizeof(float2) * (size_t)natoms * t->n_half + 8));
+    int rc = so4_utot32(t, p, natoms, d_w_nb, d_w_site, d_img_ptr, d_img_j, d_img_r, utot, stream);
+    if (rc) return rc;
+    rc = so4_linear_by32(t, natoms, utot, d_beta, d_x, (float *)w.Y, bc, stream);
+    if (rc) return rc;
+    rc = so4_adjoint_deidrj32(t, p, natoms, d_w_nb, d_img_ptr, d_img_j, d_img_r, nimg, (const float *)w.Y, w.g,
+                              w.vatom, stream);
     if (rc) return rc;
     return so4_adjoint_gather(natoms, nstruct, d_atom_ptr, d_img_ptr, d_img_rev, w.g, w.vatom, d_forces, d_virial,
                               stream);

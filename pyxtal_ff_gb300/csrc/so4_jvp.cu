@@ -150,7 +150,7 @@ __global__ void __launch_bounds__(256) k_zjvp32(JArgs A) {
         for (int q = un.y; q < un.z; ++q) {
             const int4 cur = sg;
             if (q + 1 < un.z) sg = __ldg(A.seg + q + 1);
-            const float2 z = zl_entry(A.terms, cur.x, cur.y, Uf, lane);
+            const float2 z = zl_entry(A.terms, cur.x, cur.y, Uf + lane);
             const float2 d = __ldg(dU + cur.z);
             acc += __int_as_float(cur.w) * (d.x * z.x + d.y * z.y);
         }

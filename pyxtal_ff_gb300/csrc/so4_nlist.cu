@@ -33,6 +33,8 @@ struct NLWork {
     int *cnt;        // natoms (image or pair counts)
     float4 *pos32;   // natoms: FP32 copy of the positions for the prefilter
     unsigned long long *keys;  // nimg
+    int64_t cap_img;           // capacity of the image arrays (fill / sort / rev)
+    int64_t cap_pair;          // capacity of the pair arrays (pairs)
 };
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -128,32 +130,68 @@ __global__ void k_bin_fill(const int *astruct, int natoms, NLWork w) {
     w.bin_atoms[w.bin_start[bin] + slot] = a;
 }
 
-// single-CTA exclusive scan: out[0..n] from in[0..n-1]
-__global__ void k_scan(const int *in, int *out, int n) {
-    __shared__ int sums[1024];
-    const int t = threadIdx.x;
-    const int per = (n + blockDim.x - 1) / blockDim.x;
-    const int lo = min(n, t * per), hi = min(n, lo + per);
-    int s = 0;
-    for (int q = lo; q < hi; ++q) s += in[q];
-    sums[t] = s;
+// single-CTA exclusive scan: out[0..n] from in[0..n-1].  Chunks of 4096 values
+// (four per thread, coalesced), warp-shuffle scans inside, a running carry across chunks.
+__global__ void __launch_bounds__(1024) k_scan(const int *in, int *out, int n) {
+    __shared__ int wsum[32];
+    __shared__ int carry_s;
+    const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+    if (t == 0) carry_s = 0;
     __syncthreads();
-    for (int d = 1; d < blockDim.x; d <<= 1) {
-        int v = (t >= d) ? sums[t - d] : 0;
+    for (int base = 0; base < n; base += 4096) {
+        int v[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int i = base + 4 * t + q;
+            v[q] = (i < n) ? in[i] : 0;
+        }
+        const int tot = v[0] + v[1] + v[2] + v[3];
+        int inc = tot;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, inc, d);
+            if (lane >= d) inc += y;
+        }
+        if (lane == 31) wsum[wid] = inc;
         __syncthreads();
-        sums[t] += v;
+        if (wid == 0) {
+            int w = wsum[lane];
+            int winc = w;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, winc, d);
+                if (lane >= d) winc += y;
+            }
+            wsum[lane] = winc - w;  // exclusive warp offsets
+        }
+        __syncthreads();
+        int run = carry_s + wsum[wid] + inc - tot;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int i = base + 4 * t + q;
+            if (i < n) out[i] = run;
+            run += v[q];
+        }
+        __syncthreads();
+        if (t == 1023) carry_s = run;
         __syncthreads();
     }
-    int run = (t == 0) ? 0 : sums[t - 1];
-    for (int q = lo; q < hi; ++q) {
-        const int v = in[q];
-        out[q] = run;
-        run += v;
-    }
-    if (t == blockDim.x - 1) out[n] = sums[t];
+    if (t == 0) out[n] = carry_s;
 }
 
 __global__ void k_set_int(int *p, int v) { *p = v; }
+
+// pair_img[P] = M (both totals read on the device, clamped to the capacities)
+__global__ void k_sentinel(const int32_t *img_ptr, const int32_t *pair_ptr, int natoms, int32_t *pair_img, NLWork w) {
+    const int64_t P = pair_ptr[natoms], M = img_ptr[natoms];
+    if (P <= w.cap_pair) pair_img[P] = (int32_t)(M <= w.cap_img ? M : w.cap_img);
+}
+
+__global__ void k_summary(const int32_t *img_ptr, const int32_t *pair_ptr, int natoms, const int *status, int *out) {
+    out[0] = natoms > 0 ? img_ptr[natoms] : 0;
+    out[1] = (natoms > 0 && pair_ptr) ? pair_ptr[natoms] : 0;
+    out[2] = *status;
+}
 
 // One warp per centre.  MODE 0: count images into w.cnt.  MODE 1: write the
 // packed (j, o) keys into w.keys[img_ptr[a] ...] (unsorted; slots are taken with
@@ -233,7 +271,8 @@ __global__ void k_scan_images(const so4_geom *geom, const double *pos, const int
                                                ((unsigned long long)(o[1] + OFF_BIAS) << 10) |
                                                (unsigned long long)(o[2] + OFF_BIAS);
                 const int slot = atomicAdd(&s_cnt[wib], 1);
-                w.keys[base + slot] = key;
+                if (base + slot < w.cap_img) w.keys[base + slot] = key;
+                else flag(w.status, SO4_ERR_CAPACITY);
             }
             ++mine;
         }
@@ -257,6 +296,13 @@ __global__ void k_sort(const so4_geom *geom, const double *pos, const int *astru
     if (a >= natoms) return;
     const so4_geom &g = geom[astruct[a]];
     const int p0 = img_ptr[a], p1 = img_ptr[a + 1];
+    if (p1 > w.cap_img) {  // the arrays are too small for this call; the host grows them and retries
+        if (lane == 0) {
+            w.cnt[a] = 1;
+            flag(w.status, SO4_ERR_CAPACITY);
+        }
+        return;
+    }
     const double pi[3] = {pos[3 * a], pos[3 * a + 1], pos[3 * a + 2]};
     for (int q = p0 + lane; q < p1; q += 32) {
         const unsigned long long kq = w.keys[q];
@@ -297,9 +343,13 @@ __global__ void k_sort(const so4_geom *geom, const double *pos, const int *astru
 // One thread per centre: emit its pairs in (sorted j, with (i,i) forced) order.
 __global__ void k_pairs(const so4_geom *geom, const int *astruct, int natoms, const int32_t *img_ptr,
                         const int32_t *img_j, const int32_t *pair_ptr, int64_t *seq, int32_t *pair_img,
-                        int32_t *nsite, int32_t *img_pair) {
+                        int32_t *nsite, int32_t *img_pair, NLWork w) {
     const int a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= natoms) return;
+    if (img_ptr[a + 1] > w.cap_img || pair_ptr[a + 1] > w.cap_pair) {
+        flag(w.status, SO4_ERR_CAPACITY);
+        return;
+    }
     const int base = geom[astruct[a]].atom_base;
     int p = pair_ptr[a];
     int m = img_ptr[a];
@@ -336,7 +386,7 @@ __global__ void k_rev(const int *astruct, int natoms, const int32_t *img_ptr, co
                       const int32_t *img_off, const int32_t *img_pair, int64_t nimg, const int64_t *seq,
                       const so4_geom *geom, int32_t *img_rev, NLWork w) {
     const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (m >= nimg) return;
+    if (m >= nimg || m >= img_ptr[natoms]) return;
     const int j = img_j[m];
     const int p = img_pair[m];
     const int a = (int)seq[2 * p] + geom[astruct[j]].atom_base;
@@ -438,6 +488,8 @@ extern "C" int so4_nl_count(const so4_geom *d_geom, int nstruct, int nbins, cons
     NLWork w;
     if (carve(w, nullptr, natoms, nbins, 0) > work_bytes) return SO4_ERR_WORKSPACE;
     carve(w, d_work, natoms, nbins, 0);
+    w.cap_img = 0;
+    w.cap_pair = 0;
     cudaStream_t st = (cudaStream_t)stream;
     SO4_CUDA_TRY(cudaMemsetAsync(w.status, 0, sizeof(int), st));
     if (natoms == 0) {
@@ -472,6 +524,8 @@ extern "C" int so4_nl_fill(const so4_geom *d_geom, int nstruct, int nbins, const
     NLWork w;
     if (carve(w, nullptr, natoms, nbins, nimg) > work_bytes) return SO4_ERR_WORKSPACE;
     carve(w, d_work, natoms, nbins, nimg);
+    w.cap_img = nimg;
+    w.cap_pair = 0;
     cudaStream_t st = (cudaStream_t)stream;
     if (natoms == 0) {
         k_set_int<<<1, 1, 0, st>>>(d_pair_ptr, 0);
@@ -499,13 +553,19 @@ extern "C" int so4_nl_pairs(const so4_geom *d_geom, int nstruct, const int *d_as
     NLWork w;
     std::memset(&w, 0, sizeof w);
     w.status = (int *)d_work;
+    w.cap_img = nimg;
+    w.cap_pair = npair;
     cudaStream_t st = (cudaStream_t)stream;
-    k_set_int<<<1, 1, 0, st>>>(d_pair_img + npair, (int)nimg);
+    if (natoms == 0) {
+        k_set_int<<<1, 1, 0, st>>>(d_pair_img, 0);
+        so4_count_launch();
+        return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
+    }
+    k_sentinel<<<1, 1, 0, st>>>(d_img_ptr, d_pair_ptr, natoms, d_pair_img, w);
     so4_count_launch();
-    if (natoms == 0) return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
     const int tb = 128;
     k_pairs<<<(natoms + tb - 1) / tb, tb, 0, st>>>(d_geom, d_astruct, natoms, d_img_ptr, d_img_j, d_pair_ptr, d_seq,
-                                                   d_pair_img, d_nsite, d_img_pair);
+                                                   d_pair_img, d_nsite, d_img_pair, w);
     so4_count_launch();
     if (nimg > 0 && d_img_rev) {
         k_rev<<<(unsigned)((nimg + 255) / 256), 256, 0, st>>>(d_astruct, natoms, d_img_ptr, d_img_j, d_img_off,
@@ -522,5 +582,17 @@ extern "C" int so4_status_read(const void *d_work, size_t work_bytes, void *stre
     SO4_CUDA_TRY(cudaMemcpyAsync(&v, d_work, sizeof(int), cudaMemcpyDeviceToHost, st));
     SO4_CUDA_TRY(cudaStreamSynchronize(st));
     *h_status = v;
+    return SO4_OK;
+}
+
+extern "C" int so4_nl_summary(const int32_t *d_img_ptr, const int32_t *d_pair_ptr, int natoms, const void *d_work,
+                              size_t work_bytes, void *stream, int *h_summary) {
+    if (!d_work || !h_summary || work_bytes < SO4_WS_HEADER || natoms < 0) return SO4_ERR_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    int *dev = (int *)d_work + 4;  // header scratch after the status word
+    k_summary<<<1, 1, 0, st>>>(d_img_ptr, d_pair_ptr, natoms, (const int *)d_work, dev);
+    so4_count_launch();
+    SO4_CUDA_TRY(cudaMemcpyAsync(h_summary, dev, 3 * sizeof(int), cudaMemcpyDeviceToHost, st));
+    SO4_CUDA_TRY(cudaStreamSynchronize(st));
     return SO4_OK;
 }

@@ -95,6 +95,7 @@ void free_device(so4_tables *t) {
     cudaFree(t->d_bseg);
     cudaFree(t->d_yunit);
     cudaFree(t->d_yseg);
+    cudaFree(t->d_bpos);
     cudaFree(t->d_junit);
     cudaFree(t->d_jseg);
 }
@@ -307,10 +308,17 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
                 const double cga = t->cglist[cgbase + ma1 * (l2 + 1) + ma2];
                 ZTerm zt;
                 zt.c = (float)(cga * cgb);
-                zt.i1 = (unsigned short)(t->idxu_block[l1] + mb1 * (l1 + 1) + ma1);
-                zt.i2 = (unsigned short)(t->idxu_block[l2] + mb2 * (l2 + 1) + ma2);
+                // offsets pre-scaled by the shared-memory row pitch of the lane-major U layout
+                zt.i1 = (unsigned short)((t->idxu_block[l1] + mb1 * (l1 + 1) + ma1) * 33);
+                zt.i2 = (unsigned short)((t->idxu_block[l2] + mb2 * (l2 + 1) + ma2) * 33);
                 terms.push_back(zt);
             }
+        }
+        if (terms.size() % 2) {  // even length, so two terms load as one 16-byte word
+            ZTerm pad;
+            pad.c = 0.f;
+            pad.i1 = pad.i2 = 0;
+            terms.push_back(pad);
         }
     }
     t->term_ptr[t->n_z] = (int)terms.size();
@@ -336,6 +344,15 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
         }
         bunit.push_back(make_int4(k, s0, (int)bseg.size(), 0));
     }
+    // B component of each block (blocks with l >= l1), and the start of each component's
+    // B-section entries in the fused path's per-atom scratch row
+    std::vector<int> blk_k(t->n_blk, -1), bpos(t->n_b + 1, 0);
+    for (int k = 0; k < t->n_b; ++k) {
+        for (int bi = 0; bi < t->n_blk; ++bi)
+            if (blks[bi].z0 == bent[k].z[0]) blk_k[bi] = k;
+        bpos[k + 1] = bpos[k] + bent[k].cnt[0];
+    }
+    t->n_bsec = bpos[t->n_b];
     // Y units: one per half-layout entry (lam, off), a segment per block (a, b, lam)
     for (int lam = 0; lam < ld; ++lam)
         for (int off = 0; off < (lam / 2 + 1) * (lam + 1); ++off) {
@@ -357,12 +374,18 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
         int bits;
         std::memcpy(&bits, &scale, sizeof bits);
         const int s0 = (int)yseg.size();
-        if (wmid != 0.0)
-            for (int qq = yptr[lam]; qq < yptr[lam + 1]; ++qq) {
-                const int b = ylist[qq];
-                const int jz = blks[b].z0 + off;
-                yseg.push_back(make_int4(t->term_ptr[jz], t->term_ptr[jz + 1], b, 0));
+        for (int qq = yptr[lam]; qq < yptr[lam + 1]; ++qq) {
+            const int b = ylist[qq];
+            const int jz = blks[b].z0 + off;
+            // code of the B-section entry this Z value also feeds (fused linear path), or -1
+            int code = -1;
+            const int k = blk_k[b];
+            if (k >= 0 && off < bent[k].cnt[0]) {
+                const int half = ((lam % 2) == 0 && off == bent[k].cnt[0] - 1) ? 1 : 0;
+                code = 2 * (bpos[k] + off) + half;
             }
+            if (wmid != 0.0 || code >= 0) yseg.push_back(make_int4(t->term_ptr[jz], t->term_ptr[jz + 1], b, code));
+        }
         yunit.push_back(make_int4(e, s0, (int)yseg.size(), bits));
     }
 
@@ -413,6 +436,7 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
     if (!rc) rc = upload(&t->d_bseg, bseg);
     if (!rc) rc = upload(&t->d_yunit, yunit);
     if (!rc) rc = upload(&t->d_yseg, yseg);
+    if (!rc) rc = upload(&t->d_bpos, bpos);
     if (!rc) rc = upload(&t->d_junit, junit);
     if (!rc) rc = upload(&t->d_jseg, jseg);
     if (!rc) rc = upload(&t->d_cg64, t->cglist);
@@ -449,6 +473,8 @@ extern "C" int so4_tables_sizes(const so4_tables *t, int *s) {
     s[3] = t->n_b;
     s[4] = t->n_cg;
     s[5] = t->n_blk;
+    s[6] = t->n_bsec;
+    s[7] = t->n_terms;
     return SO4_OK;
 }
 

@@ -33,28 +33,37 @@ __device__ __forceinline__ void zl_load_utot(const float2 *__restrict__ utot, co
     }
 }
 
-// sum over the terms [t0, t1) of c * U[i1] * U[i2] for this lane's atom
-__device__ __forceinline__ float2 zl_entry(const ZTerm *__restrict__ terms, int t0, int t1, const float2 *Uf, int lane) {
-    float r0 = 0.f, i0 = 0.f, r1 = 0.f, i1 = 0.f;
-    int t = t0;
-    for (; t + 1 < t1; t += 2) {
-        const ZTerm a = terms[t], b = terms[t + 1];
-        const float2 ua = Uf[a.i1 * ZL_PITCH + lane], va = Uf[a.i2 * ZL_PITCH + lane];
-        const float2 ub = Uf[b.i1 * ZL_PITCH + lane], vb = Uf[b.i2 * ZL_PITCH + lane];
-        const float par = ua.x * va.x - ua.y * va.y, pai = ua.x * va.y + ua.y * va.x;
-        const float pbr = ub.x * vb.x - ub.y * vb.y, pbi = ub.x * vb.y + ub.y * vb.x;
-        r0 += a.c * par;
-        i0 += a.c * pai;
-        r1 += b.c * pbr;
-        i1 += b.c * pbi;
+// sum over the terms [t0, t1) of c * U[i1] * U[i2] for this lane's atom.  Ul = Uf + lane;
+// term offsets are pre-scaled by the pitch; lists have even length and start even, so
+// two terms arrive in one 16-byte load.  The term words come from L2 and are the
+// critical latency: each iteration consumes two words while the next two are in flight.
+__device__ __forceinline__ void zl_pair(const int4 w, const float2 *Ul, float &r0, float &i0, float &r1, float &i1) {
+    const float ca = __int_as_float(w.x), cb = __int_as_float(w.z);
+    const float2 ua = Ul[w.y & 0xffff], va = Ul[(unsigned)w.y >> 16];
+    const float2 ub = Ul[w.w & 0xffff], vb = Ul[(unsigned)w.w >> 16];
+    r0 += ca * (ua.x * va.x - ua.y * va.y);
+    i0 += ca * (ua.x * va.y + ua.y * va.x);
+    r1 += cb * (ub.x * vb.x - ub.y * vb.y);
+    i1 += cb * (ub.x * vb.y + ub.y * vb.x);
+}
+
+__device__ __forceinline__ float2 zl_entry(const ZTerm *__restrict__ terms, int t0, int t1, const float2 *Ul) {
+    float r0 = 0.f, i0 = 0.f, r1 = 0.f, i1 = 0.f, r2 = 0.f, i2 = 0.f, r3 = 0.f, i3 = 0.f;
+    const int4 *tp = reinterpret_cast<const int4 *>(terms + t0);
+    const int n2 = (t1 - t0) >> 1;
+    const int4 zero = make_int4(0, 0, 0, 0);
+    int4 wa = (n2 > 0) ? __ldg(tp) : zero;
+    int4 wb = (n2 > 1) ? __ldg(tp + 1) : zero;
+    int q = 0;
+    for (; q + 1 < n2; q += 2) {
+        const int4 ca = wa, cb = wb;
+        wa = (q + 2 < n2) ? __ldg(tp + q + 2) : zero;
+        wb = (q + 3 < n2) ? __ldg(tp + q + 3) : zero;
+        zl_pair(ca, Ul, r0, i0, r1, i1);
+        zl_pair(cb, Ul, r2, i2, r3, i3);
     }
-    if (t < t1) {
-        const ZTerm a = terms[t];
-        const float2 ua = Uf[a.i1 * ZL_PITCH + lane], va = Uf[a.i2 * ZL_PITCH + lane];
-        r0 += a.c * (ua.x * va.x - ua.y * va.y);
-        i0 += a.c * (ua.x * va.y + ua.y * va.x);
-    }
-    return make_float2(r0 + r1, i0 + i1);
+    if (q < n2) zl_pair(wa, Ul, r0, i0, r1, i1);
+    return make_float2((r0 + r1) + (r2 + r3), (i0 + i1) + (i2 + i3));
 }
 
 // next work unit for the calling warp (lane 0 draws from the CTA counter)

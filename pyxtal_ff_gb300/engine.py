@@ -42,10 +42,10 @@ class Tables:
         h = C.c_void_p()
         check(lib().so4_tables_create(int(twol), int(bool(normalize_u)), C.byref(h)), "so4_tables_create")
         self.handle = h
-        s = (C.c_int * 6)()
+        s = (C.c_int * 8)()
         check(lib().so4_tables_sizes(h, s), "so4_tables_sizes")
         self.twol = int(twol)
-        self.n_u, self.n_half, self.n_z, self.nB, self.n_cg, self.n_blk = [int(v) for v in s]
+        self.n_u, self.n_half, self.n_z, self.nB, self.n_cg, self.n_blk, self.n_bsec, self.n_terms = [int(v) for v in s]
 
     def export(self):
         ld = self.twol + 1
@@ -129,9 +129,16 @@ def geometry(cells, pbc, atom_ptr, rcut):
     return raw, vol, int(nb.value)
 
 
+_NL_CAPACITY = {}  # (natoms, nbins, rcut) -> (image capacity, pair capacity) seen last time
+
+
 def build_neighbors(pos, cells, pbc, atom_ptr, rcut, device="cuda", workspace=None):
     """GPU neighbour list of a batch.  pos: (N,3) f64 tensor on the device (or a
-    numpy array), cells (S,3,3), pbc (S,3), atom_ptr (S+1,) host arrays."""
+    numpy array), cells (S,3,3), pbc (S,3), atom_ptr (S+1,) host arrays.
+
+    The image and pair arrays are sized from the counts of the previous call with
+    the same shape (a first call uses an estimate); one synchronising read returns
+    the true totals and the status, and an undersized call is repeated with room."""
     L = lib()
     dev = torch.device(device)
     if not isinstance(pos, torch.Tensor):
@@ -147,45 +154,47 @@ def build_neighbors(pos, cells, pbc, atom_ptr, rcut, device="cuda", workspace=No
     atom_struct = torch.from_numpy(np.repeat(np.arange(S, dtype=np.int32), counts)).to(dev)
     atom_ptr_dev = torch.from_numpy(atom_ptr.astype(np.int32)).to(dev)
     st = _stream()
-    est_m = max(64 * N, 1)
-    ws_bytes = L.so4_nl_workspace_size(N, nbins, est_m)
-    ws = workspace if (workspace is not None and workspace.numel() >= ws_bytes) else torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
-    img_ptr = torch.empty(N + 1, dtype=torch.int32, device=dev)
-    check(L.so4_nl_count(_ptr(geom), S, nbins, _ptr(pos), _ptr(atom_struct), N, float(rcut), _ptr(img_ptr),
-                         _ptr(ws), ws.numel(), st), "so4_nl_count")
-    M = int(img_ptr[N].item())
-    need = L.so4_nl_workspace_size(N, nbins, M)
-    if need > ws.numel():
-        ws2 = torch.empty(need, dtype=torch.uint8, device=dev)
-        ws2[: ws.numel()].copy_(ws)
-        ws = ws2
-    img_j = torch.empty(max(M, 1), dtype=torch.int32, device=dev)
-    img_off = torch.empty((max(M, 1), 3), dtype=torch.int32, device=dev)
-    img_r = torch.empty((max(M, 1), 3), dtype=torch.float64, device=dev)
-    pair_ptr = torch.empty(N + 1, dtype=torch.int32, device=dev)
-    check(L.so4_nl_fill(_ptr(geom), S, nbins, _ptr(pos), _ptr(atom_struct), N, float(rcut), _ptr(img_ptr), M,
-                        _ptr(img_j), _ptr(img_off), _ptr(img_r), _ptr(pair_ptr), _ptr(ws), ws.numel(), st),
-          "so4_nl_fill")
-    P = int(pair_ptr[N].item())
-    seq = torch.empty((max(P, 1), 2), dtype=torch.int64, device=dev)
-    pair_img = torch.empty(P + 1, dtype=torch.int32, device=dev)
-    nsite = torch.empty(max(N, 1), dtype=torch.int32, device=dev)
-    img_pair = torch.empty(max(M, 1), dtype=torch.int32, device=dev)
-    img_rev = torch.empty(max(M, 1), dtype=torch.int32, device=dev)
-    check(L.so4_nl_pairs(_ptr(geom), S, _ptr(atom_struct), N, _ptr(img_ptr), M, _ptr(img_j), _ptr(img_off),
-                         _ptr(pair_ptr), P, _ptr(seq), _ptr(pair_img), _ptr(nsite), _ptr(img_pair), _ptr(img_rev),
-                         _ptr(ws), ws.numel(), st), "so4_nl_pairs")
-    status = C.c_int()
-    check(L.so4_status_read(_ptr(ws), ws.numel(), st, C.byref(status)), "so4_status_read")
-    bits = status.value
+    key = (N, nbins, float(rcut))
+    cap_m, cap_p = _NL_CAPACITY.get(key, (max(64 * N, 1), max(64 * N, 1) + N))
+    summary = (C.c_int * 3)()
+    for _attempt in range(3):
+        ws_bytes = L.so4_nl_workspace_size(N, nbins, cap_m)
+        ws = workspace if (workspace is not None and workspace.numel() >= ws_bytes) else \
+            torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
+        img_ptr = torch.empty(N + 1, dtype=torch.int32, device=dev)
+        check(L.so4_nl_count(_ptr(geom), S, nbins, _ptr(pos), _ptr(atom_struct), N, float(rcut), _ptr(img_ptr),
+                             _ptr(ws), ws.numel(), st), "so4_nl_count")
+        img_j = torch.empty(cap_m, dtype=torch.int32, device=dev)
+        img_off = torch.empty((cap_m, 3), dtype=torch.int32, device=dev)
+        img_r = torch.empty((cap_m, 3), dtype=torch.float64, device=dev)
+        pair_ptr = torch.empty(N + 1, dtype=torch.int32, device=dev)
+        check(L.so4_nl_fill(_ptr(geom), S, nbins, _ptr(pos), _ptr(atom_struct), N, float(rcut), _ptr(img_ptr), cap_m,
+                            _ptr(img_j), _ptr(img_off), _ptr(img_r), _ptr(pair_ptr), _ptr(ws), ws.numel(), st),
+              "so4_nl_fill")
+        seq = torch.empty((cap_p, 2), dtype=torch.int64, device=dev)
+        pair_img = torch.empty(cap_p + 1, dtype=torch.int32, device=dev)
+        nsite = torch.empty(max(N, 1), dtype=torch.int32, device=dev)
+        img_pair = torch.empty(cap_m, dtype=torch.int32, device=dev)
+        img_rev = torch.empty(cap_m, dtype=torch.int32, device=dev)
+        check(L.so4_nl_pairs(_ptr(geom), S, _ptr(atom_struct), N, _ptr(img_ptr), cap_m, _ptr(img_j), _ptr(img_off),
+                             _ptr(pair_ptr), cap_p, _ptr(seq), _ptr(pair_img), _ptr(nsite), _ptr(img_pair),
+                             _ptr(img_rev), _ptr(ws), ws.numel(), st), "so4_nl_pairs")
+        check(L.so4_nl_summary(_ptr(img_ptr), _ptr(pair_ptr), N, _ptr(ws), ws.numel(), st, summary), "so4_nl_summary")
+        M, P, bits = int(summary[0]), int(summary[1]), int(summary[2])
+        if M <= cap_m and P <= cap_p:
+            break
+        cap_m, cap_p = max(cap_m, int(M * 1.25) + 16), max(cap_p, int(P * 1.25) + 16)
+    else:
+        raise _lib.SO4Error(_lib.SO4_ERR_CAPACITY, "neighbour list")
+    _NL_CAPACITY[key] = (max(int(M * 1.1) + 16, 1), max(int(P * 1.1) + 16, 1))
     if bits & (1 << _lib.SO4_ERR_NONFINITE):
         raise ValueError("positions contain NaN or Inf")
-    for code in (_lib.SO4_ERR_CAPACITY, _lib.SO4_ERR_REVERSE):
+    for code in (_lib.SO4_ERR_CAPACITY, _lib.SO4_ERR_REVERSE):  # capacity here: an image offset beyond 511 cells
         if bits & (1 << code):
             raise _lib.SO4Error(code, "neighbour list")
     return Neighbors(N, S, M, P, atom_ptr, vol, geom, nbins, atom_struct, atom_ptr_dev, img_ptr, img_j[:M],
-                     img_off[:M], img_r[:M], pair_ptr, seq[:P], pair_img, nsite[:N], img_pair[:M], img_rev[:M],
-                     bool(bits & (1 << _lib.SO4_ERR_NO_NEIGHBOR)))
+                     img_off[:M], img_r[:M], pair_ptr, seq[:P], pair_img[: P + 1], nsite[:N], img_pair[:M],
+                     img_rev[:M], bool(bits & (1 << _lib.SO4_ERR_NO_NEIGHBOR)))
 
 
 # ----------------------------------------------------------------- compute
@@ -282,3 +291,51 @@ def jvp32(tab, prm, nb: Neighbors, w_nb, utot, v=None, G=None, workspace=None):
                           _ptr(nb.img_j), _ptr(nb.img_r), _ptr(utot), _ptr(v), _ptr(G), _ptr(dB), _ptr(ws), ws.numel(),
                           _stream()), "so4_jvp32")
     return dB[: nb.natoms]
+
+
+def adjoint_linear32(tab, prm, nb: Neighbors, w_nb, w_site, beta, workspace=None):
+    """B (N,nB) f32, forces (N,3) f64 and virial (S,3,3) f64 for an energy linear in B
+    (beta = dE/dB fixed), in one fused pass (Z computed once)."""
+    dev = w_nb.device
+    beta = beta.to(torch.float32).contiguous()
+    x = torch.empty((max(nb.natoms, 1), tab.nB), dtype=torch.float32, device=dev)
+    forces = torch.empty((max(nb.natoms, 1), 3), dtype=torch.float64, device=dev)
+    virial = torch.empty((max(nb.nstruct, 1), 3, 3), dtype=torch.float64, device=dev)
+    need = lib().so4_linear_workspace_size(tab.handle, nb.natoms, nb.nimg)
+    ws = workspace if (workspace is not None and workspace.numel() >= need) else torch.empty(need, dtype=torch.uint8, device=dev)
+    check(lib().so4_adjoint_linear32(tab.handle, C.byref(prm), nb.nstruct, _ptr(nb.atom_struct), _ptr(nb.atom_ptr_dev),
+                                     nb.natoms, _ptr(w_nb), _ptr(w_site), _ptr(nb.img_ptr), _ptr(nb.img_j),
+                                     _ptr(nb.img_r), _ptr(nb.img_rev), nb.nimg, _ptr(beta), _ptr(x), _ptr(forces),
+                                     _ptr(virial), _ptr(ws), ws.numel(), _stream()), "so4_adjoint_linear32")
+    return x[: nb.natoms], forces[: nb.natoms], virial[: nb.nstruct]
+
+
+def linear_staged(tab, prm, nb: Neighbors, w_nb, w_site, beta, mark=None, first=0):
+    """adjoint_linear32 as its C-ABI stages (U_tot; B and Y; per-image dE/dr; gather),
+    with mark(i) called between stages (for timing).  Returns (x, forces, virial)."""
+    dev = w_nb.device
+    beta = beta.to(torch.float32).contiguous()
+    N, M = nb.natoms, nb.nimg
+    utot = torch.empty((max(N, 1), tab.n_half, 2), dtype=torch.float32, device=dev)
+    x = torch.empty((max(N, 1), tab.nB), dtype=torch.float32, device=dev)
+    y = torch.empty((max(N, 1), tab.n_half, 2), dtype=torch.float32, device=dev)
+    bc = torch.empty((tab.n_bsec, max(N, 1)), dtype=torch.float32, device=dev)
+    g = torch.empty((max(M, 1), 3), dtype=torch.float32, device=dev)
+    vatom = torch.empty((max(N, 1), 9), dtype=torch.float64, device=dev)
+    forces = torch.empty((max(N, 1), 3), dtype=torch.float64, device=dev)
+    virial = torch.empty((max(nb.nstruct, 1), 3, 3), dtype=torch.float64, device=dev)
+    L, st = lib(), _stream()
+    check(L.so4_utot32(tab.handle, C.byref(prm), N, _ptr(w_nb), _ptr(w_site), _ptr(nb.img_ptr), _ptr(nb.img_j),
+                       _ptr(nb.img_r), _ptr(utot), st), "so4_utot32")
+    if mark:
+        mark(first + 1)
+    check(L.so4_linear_by32(tab.handle, N, _ptr(utot), _ptr(beta), _ptr(x), _ptr(y), _ptr(bc), st), "so4_linear_by32")
+    if mark:
+        mark(first + 2)
+    check(L.so4_adjoint_deidrj32(tab.handle, C.byref(prm), N, _ptr(w_nb), _ptr(nb.img_ptr), _ptr(nb.img_j),
+                                 _ptr(nb.img_r), M, _ptr(y), _ptr(g), _ptr(vatom), st), "so4_adjoint_deidrj32")
+    if mark:
+        mark(first + 3)
+    check(L.so4_adjoint_gather(N, nb.nstruct, _ptr(nb.atom_ptr_dev), _ptr(nb.img_ptr), _ptr(nb.img_rev), _ptr(g),
+                               _ptr(vatom), _ptr(forces), _ptr(virial), st), "so4_adjoint_gather")
+    return x[:N], forces[:N], virial[: nb.nstruct]

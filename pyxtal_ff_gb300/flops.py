@@ -20,6 +20,7 @@ own bookkeeping:
                     plus 18 for the virial outer product (compute_dbidrj :1113-1227
                     and the bstress update :1466-1468);
   Y     per atom    4 flop per (Z entry, role) plus the Z entries themselves;
+  B+Y   per atom    the fused pass of a linear energy: Z once, then B and Y;
   dE    per image   U + dU + 4 dot products against Y (16 per half entry).
 """
 from __future__ import annotations
@@ -123,6 +124,8 @@ def kernel_flops(twol, natoms, nimg):
     u, du, z = per_image_u(twol), per_image_du(twol), per_atom_z(twol)
     utot_img = u + 6 * n["n_half"]
     return {
+        "utot32": nimg * utot_img,
+        "linear_by32": natoms * (z + per_atom_b(twol) + per_atom_y(twol)),
         "forward32": natoms * (z + per_atom_b(twol)) + nimg * utot_img,
         "adjoint_y32": natoms * (z + per_atom_y(twol)),
         "adjoint_deidrj32": nimg * (u + du + 16 * n["n_half"] + 24),

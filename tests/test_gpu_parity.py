@@ -162,3 +162,32 @@ def test_adjoint_fp32_vs_oracle_contraction(cuda_device, lmax, rc, w):
         print("lmax", lmax, "struct", s, "force rel", ef, "abs", np.abs(forces[a0:a1] - ref["forces"]).max(),
               "virial rel", ev)
         assert ef < 2e-4 and ev < 2e-4
+
+
+def test_fused_linear_path_matches_unfused_and_oracle(cuda_device):
+    structs = [S.diamond_si(2, 2, 1, sigma=0.1, rng=np.random.default_rng(8)), S.sio2_random(n_si=8, seed=10)]
+    pos, cells, pbc, ptr = _batch_arrays(structs)
+    numbers = np.concatenate([s.numbers for s in structs])
+    symbols = sum([list(s.symbols) for s in structs], [])
+    w = {"Si": 1.0, "O": 0.5}
+    tab = engine.tables(8)
+    prm = engine.params(8, 5.0, 0.99363, "cosine")
+    nb = engine.build_neighbors(torch.from_numpy(pos).cuda(), cells, pbc, ptr, 5.0)
+    w_nb, w_site = engine.site_weights("SNAP", numbers, symbols, w)
+    w_nb, w_site = torch.from_numpy(w_nb).cuda(), torch.from_numpy(w_site).cuda()
+    beta = torch.from_numpy(np.random.default_rng(12).normal(0, 0.01, size=(len(pos), tab.nB))).float().cuda()
+    x1, utot = engine.forward32(tab, prm, nb, w_nb, w_site)
+    f1, v1 = engine.adjoint32(tab, prm, nb, w_nb, utot, beta)
+    x2, f2, v2 = engine.adjoint_linear32(tab, prm, nb, w_nb, w_site, beta)
+    x3, f3, v3 = engine.linear_staged(tab, prm, nb, w_nb, w_site, beta)
+    assert G.rel_err(x2.cpu().numpy(), x1.cpu().numpy()) < 1e-5
+    assert G.rel_err(f2.cpu().numpy(), f1.cpu().numpy()) < 1e-5
+    assert G.rel_err(v2.cpu().numpy(), v1.cpu().numpy()) < 1e-5
+    assert torch.equal(x2, x3) and torch.equal(f2, f3) and torch.equal(v2, v3)
+    for s, st in enumerate(structs):
+        a0, a1 = ptr[s], ptr[s + 1]
+        ref = O.forces_virial(st, beta[a0:a1].double().cpu().numpy(), kind="SNAP", lmax=4, rcut=5.0, weights=w,
+                              rfac0=0.99363)
+        assert G.rel_err(x2[a0:a1].cpu().numpy(), ref["x"]) < 2e-5
+        assert G.rel_err(f2[a0:a1].cpu().numpy(), ref["forces"]) < 2e-4
+        assert G.rel_err(v2[s].cpu().numpy() / nb.vol[s], ref["virial"]) < 2e-4
