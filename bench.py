@@ -212,7 +212,7 @@ def main():
     tab, prm = calc.tables, calc.params
     L = _lib.lib()
 
-    stage_names = ["neighbors", "utot32", "linear_by32", "adjoint_deidrj32", "gather_energy"]
+    stage_names = ["neighbors", "utot32", "linear_by32", "adjoint_deidrj32", "gather"]
     beta_dev = model.coef.detach()[calc._species].contiguous()
     bias0 = float(model.bias.detach()[0])
 
@@ -226,8 +226,9 @@ def main():
         mark(0)
         nb = calc.neighbors(batch, pos_dev)
         mark(1)
-        x, forces, virial = engine.linear_staged(tab, prm, nb, calc._w_nb, calc._w_site, beta_dev, mark=mark, first=1)
-        energy = ((x * beta_dev).sum(-1).double()).sum() + bias0
+        x, forces, virial, energy = engine.linear_staged(tab, prm, nb, calc._w_nb, calc._w_site, beta_dev, mark=mark,
+                                                         first=1)
+        energy = energy + bias0
         mark(5)
         return energy, forces, virial
 

@@ -188,38 +188,49 @@ int so4_adjoint32(const so4_tables *t, const so4_params *p, int nstruct, const i
                   double *d_virial, void *d_work, size_t work_bytes, void *stream);
 
 /* The three stages so4_adjoint32 runs, for callers that keep their own buffers:
- *   so4_adjoint_y32      Y[natoms*idxu_half*2] f32 from U_tot and beta (one CTA per centre);
- *   so4_adjoint_deidrj32 g[nimg*3] f32 = dE/dr of every image and the per-centre
- *                        virial vatom[natoms*9] f64 (U and dU by the recursion, contracted with Y);
- *   so4_adjoint_gather   forces[natoms*3] f64 = sum_m (g_m - g_rev(m)) and the
- *                        per-structure virial[nstruct*9] f64, in a fixed order. */
+ *   so4_adjoint_y32      Y[natoms*idxu_half*2] f32 from U_tot and beta (atoms across lanes);
+ *   so4_adjoint_deidrj32 g[nimg*3] f32 = dE/dr of every image (U and dU by the
+ *                        recursion, contracted with Y);
+ *   so4_adjoint_gather   forces[natoms*3] f64 = sum_m (g_m - g_rev(m)), the
+ *                        per-structure virial[nstruct*9] f64 = sum_m r_m (x) g_m and,
+ *                        when d_eatom and d_energy are both non-NULL, energy[nstruct] f64 =
+ *                        the sum of the per-atom d_eatom[natoms] f32 over each structure.
+ *                        All sums have a fixed order (bitwise reproducible).  d_part:
+ *                        so4_gather_workspace_size(natoms) bytes of scratch. */
 int so4_adjoint_y32(const so4_tables *t, int natoms, const float *d_utot, const float *d_beta, float *d_y,
                     void *stream);
 int so4_adjoint_deidrj32(const so4_tables *t, const so4_params *p, int natoms, const double *d_w_nb,
                          const int32_t *d_img_ptr, const int32_t *d_img_j, const double *d_img_r,
-                         int64_t nimg, const float *d_y, float *d_g, double *d_vatom, void *stream);
+                         int64_t nimg, const float *d_y, float *d_g, void *stream);
+size_t so4_gather_workspace_size(int natoms);
 int so4_adjoint_gather(int natoms, int nstruct, const int *d_atom_ptr, const int32_t *d_img_ptr,
-                       const int32_t *d_img_rev, const float *d_g, const double *d_vatom, double *d_forces,
-                       double *d_virial, void *stream);
+                       const int32_t *d_img_rev, const double *d_img_r, const float *d_g,
+                       const float *d_eatom, double *d_part, double *d_forces, double *d_virial,
+                       double *d_energy, void *stream);
 
 /* Forward and adjoint in one call for an energy linear in B (beta = dE/dB does not
  * depend on B, e.g. the reference's order-1 polynomial regression,
  * pyxtal_ff/models/polynomialregression.py:374): writes d_x (B, natoms*nB f32),
  * d_forces and d_virial as so4_forward32 + so4_adjoint32 would, with every Z entry
- * computed once for both B and Y.  Scratch: so4_linear_workspace_size() bytes. */
+ * computed once for both B and Y, and, when d_energy is non-NULL, d_energy[nstruct]
+ * f64 = sum over the structure's atoms of beta_i . B_i (a model's constant term is
+ * the caller's to add).  Scratch: so4_linear_workspace_size() bytes. */
 size_t so4_linear_workspace_size(const so4_tables *t, int natoms, int64_t nimg);
 /* Its stages: U_tot alone (the first half of so4_forward32), then B and Y from U_tot
- * and beta in one pass (d_bc: sizes[6] * natoms floats of scratch, entry-major). */
+ * and beta in one pass (d_bc: sizes[6] * natoms floats of scratch, entry-major;
+ * d_eatom[natoms] f32 = beta_i . B_i, may be NULL), then so4_adjoint_deidrj32 and
+ * so4_adjoint_gather. */
 int so4_utot32(const so4_tables *t, const so4_params *p, int natoms, const double *d_w_nb,
                const double *d_w_site, const int32_t *d_img_ptr, const int32_t *d_img_j,
                const double *d_img_r, float *d_utot, void *stream);
 int so4_linear_by32(const so4_tables *t, int natoms, const float *d_utot, const float *d_beta, float *d_x,
-                    float *d_y, float *d_bc, void *stream);
+                    float *d_y, float *d_bc, float *d_eatom, void *stream);
 int so4_adjoint_linear32(const so4_tables *t, const so4_params *p, int nstruct, const int *d_atom_struct,
                          const int *d_atom_ptr, int natoms, const double *d_w_nb, const double *d_w_site,
                          const int32_t *d_img_ptr, const int32_t *d_img_j, const double *d_img_r,
                          const int32_t *d_img_rev, int64_t nimg, const float *d_beta, float *d_x,
-                         double *d_forces, double *d_virial, void *d_work, size_t work_bytes, void *stream);
+                         double *d_forces, double *d_virial, double *d_energy, void *d_work,
+                         size_t work_bytes, void *stream);
 
 /* The adjoint's backward: the Jacobian-vector product of B (FP32),
  *   d_dB[natoms*nB] = sum_{images m of i} dB_i/dr_m . dr_m,  dr_m = (v_j - v_i) + G_s^T r_m,

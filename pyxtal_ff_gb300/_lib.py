@@ -92,15 +92,16 @@ def lib():
         "so4_forward32": (_i, [_vp, C.POINTER(Params), _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
         "so4_adjoint_workspace_size": (_sz, [_vp, _i, _i64]),
         "so4_adjoint_y32": (_i, [_vp, _i, _vp, _vp, _vp, _vp]),
-        "so4_adjoint_deidrj32": (_i, [_vp, C.POINTER(Params), _i, _vp, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp]),
-        "so4_adjoint_gather": (_i, [_i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+        "so4_adjoint_deidrj32": (_i, [_vp, C.POINTER(Params), _i, _vp, _vp, _vp, _vp, _i64, _vp, _vp, _vp]),
+        "so4_gather_workspace_size": (_sz, [_i]),
+        "so4_adjoint_gather": (_i, [_i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
         "so4_launch_count": (C.c_longlong, []),
         "so4_jvp_workspace_size": (_sz, [_vp, _i]),
         "so4_linear_workspace_size": (_sz, [_vp, _i, _i64]),
         "so4_utot32": (_i, [_vp, C.POINTER(Params), _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
-        "so4_linear_by32": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _vp, _vp]),
+        "so4_linear_by32": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
         "so4_adjoint_linear32": (_i, [_vp, C.POINTER(Params), _i, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _i64,
-                                      _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
+                                      _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
         "so4_jvp32": (_i, [_vp, C.POINTER(Params), _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
         "so4_adjoint32_noalloc": (_i, [_vp, C.POINTER(Params), _i, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _i64, _vp,
                                        _vp, _vp, _vp, _vp]),

@@ -108,15 +108,18 @@ class SO4Calculator:
 
     def prepare(self, batch: Batch):
         """Upload the per-atom weights and species of a batch (once per batch layout)."""
-        key = id(batch)
-        if key != self._batch_key:
+        if batch is not self._batch_key:
             w_nb, w_site = engine.site_weights(self.kind, batch.numbers, batch.symbols, self.weights)
             self._w_nb = torch.from_numpy(w_nb).to(self.device)
             self._w_site = torch.from_numpy(w_site).to(self.device)
             self._species = torch.from_numpy(batch.species).to(self.device)
             self._struct = torch.from_numpy(np.repeat(np.arange(batch.nstruct), np.diff(batch.atom_ptr))).to(self.device)
             self._vol = torch.from_numpy(batch.volumes).to(self.device)
-            self._batch_key = key
+            # atoms of each species per structure: a model's per-species constant, summed exactly
+            counts = np.zeros((batch.nstruct, max(len(batch.species_order), 1)))
+            np.add.at(counts, (np.repeat(np.arange(batch.nstruct), np.diff(batch.atom_ptr)), batch.species), 1.0)
+            self._counts = torch.from_numpy(counts).to(self.device)
+            self._batch_key = batch
         return self
 
     def neighbors(self, batch: Batch, positions):
@@ -150,11 +153,9 @@ class SO4Calculator:
             need = engine.lib().so4_linear_workspace_size(self.tables.handle, nb.natoms, nb.nimg)
             if self._ws is None or self._ws.numel() < need:
                 self._ws = torch.empty(int(need * 1.25) + 4096, dtype=torch.uint8, device=self.device)
-            x, forces, virial = engine.adjoint_linear32(self.tables, self.params, nb, self._w_nb, self._w_site, beta,
-                                                        workspace=self._ws)
-            e_atom = (x * beta).sum(-1) + model.bias.detach()[self._species]
-            energy = torch.zeros(batch.nstruct, dtype=torch.float64, device=self.device)
-            energy.index_add_(0, self._struct, e_atom.double())
+            x, forces, virial, energy = engine.adjoint_linear32(self.tables, self.params, nb, self._w_nb,
+                                                                self._w_site, beta, workspace=self._ws)
+            energy = energy + self._counts @ model.bias.detach().double()
             stress = -(virial.reshape(-1, 9)[:, VOIGT] / self._vol[:, None]) * EV_A3_TO_GPA
             return dict(energy=energy, forces=forces, virial=virial, stress=stress, x=x, neighbors=nb)
         x, utot = engine.forward32(self.tables, self.params, nb, self._w_nb, self._w_site)
@@ -162,12 +163,8 @@ class SO4Calculator:
         with torch.enable_grad():
             e_atom = model(xg, self._species)
             beta, = torch.autograd.grad(e_atom.sum(), xg)
-        need = engine.lib().so4_adjoint_workspace_size(self.tables.handle, nb.natoms, nb.nimg)
-        if self._ws is None or self._ws.numel() < need:
-            self._ws = torch.empty(int(need * 1.25) + 4096, dtype=torch.uint8, device=self.device)
-        forces, virial = engine.adjoint32(self.tables, self.params, nb, self._w_nb, utot, beta, workspace=self._ws)
-        energy = torch.zeros(batch.nstruct, dtype=torch.float64, device=self.device)
-        energy.index_add_(0, self._struct, e_atom.detach().double())
+        forces, virial, energy = engine.adjoint32(self.tables, self.params, nb, self._w_nb, utot, beta,
+                                                  eatom=e_atom.detach())
         stress = -(virial.reshape(-1, 9)[:, VOIGT] / self._vol[:, None]) * EV_A3_TO_GPA
         return dict(energy=energy, forces=forces, virial=virial, stress=stress, x=x, neighbors=nb)
 

@@ -27,10 +27,15 @@ struct AdjWork {
     int *status;
     float2 *Y;       // natoms * n_half
     float *g;        // nimg * 3
-    double *vatom;   // natoms * 9
+    double *part;    // gather_part_doubles(natoms): per-chunk virial + energy partials
 };
 
 size_t a256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+constexpr int GCH = 32;    // atoms per gather chunk (one CTA)
+constexpr int GPART = 10;  // doubles per chunk partial: virial (9) + energy
+
+size_t gather_part_doubles(int natoms) { return (size_t)GPART * ((size_t)(natoms + GCH - 1) / GCH + 1); }
 
 size_t carve_adj(AdjWork &w, void *base, int natoms, int nh, int64_t nimg) {
     char *p = (char *)base;
@@ -43,7 +48,7 @@ size_t carve_adj(AdjWork &w, void *base, int natoms, int nh, int64_t nimg) {
     w.status = (int *)take(SO4_WS_HEADER);
     w.Y = (float2 *)take(sizeof(float2) * (size_t)natoms * nh + 8);
     w.g = (float *)take(sizeof(float) * 3 * (size_t)(nimg + 1));
-    w.vatom = (double *)take(sizeof(double) * 9 * (size_t)(natoms + 1));
+    w.part = (double *)take(sizeof(double) * gather_part_doubles(natoms));
     return off;
 }
 
@@ -191,7 +196,8 @@ struct ZLArgs {
     SmallTables st;
     float *x;    // B out  (k_zb32, k_zby32)
     float2 *Y;   // Y out  (k_zy32, k_zby32)
-    float *bc;   // fused path: per-atom B-section contributions [natoms][nbsec]
+    float *bc;   // fused path: B-section contributions, entry-major [nbsec][natoms]
+    float *eatom;  // fused path: sum_k beta_k B_k per atom (may be null)
 };
 
 // B_k = 2 Re sum' conj(U_l) Z(l1,l2,l) for 32 atoms per CTA (compute_bi, SO4.py:1071-1111)
@@ -308,13 +314,26 @@ __global__ void __launch_bounds__(256) k_zby32(ZLArgs A) {
         if (a < A.natoms) A.Y[(size_t)a * A.nh + un.x] = make_float2(s * yr, s * yi);
     }
     __syncthreads();
+    // B_k, and beta_k B_k kept in shared memory (over the U tiles, no longer read) for the energy
+    float *eb = (float *)zl_smem;  // [nB][33]
     for (int idx = threadIdx.x; idx < 32 * A.nB; idx += blockDim.x) {
         const int k = idx >> 5, l = idx & 31;
         const int aa = a0 + l;
-        if (aa >= A.natoms) continue;
-        float acc = 0.f;
-        for (int e = __ldg(A.bpos + k); e < __ldg(A.bpos + k + 1); ++e) acc += A.bc[(size_t)e * A.natoms + aa];
-        A.x[(size_t)aa * A.nB + k] = 2.f * acc;
+        float acc = 0.f, e = 0.f;
+        if (aa < A.natoms) {
+            for (int q = __ldg(A.bpos + k); q < __ldg(A.bpos + k + 1); ++q) acc += A.bc[(size_t)q * A.natoms + aa];
+            acc *= 2.f;
+            A.x[(size_t)aa * A.nB + k] = acc;
+            e = acc * __ldg(A.beta + (size_t)aa * A.nB + k);
+        }
+        eb[k * ZL_PITCH + l] = e;
+    }
+    if (A.eatom == nullptr) return;
+    __syncthreads();
+    if (threadIdx.x < 32 && a < A.natoms) {
+        float e = 0.f;
+        for (int k = 0; k < A.nB; ++k) e += eb[k * ZL_PITCH + threadIdx.x];
+        A.eatom[a] = e;
     }
 }
 
@@ -328,7 +347,6 @@ struct DArgs {
     SmallTables st;
     const float2 *Y;
     float *g;
-    double *vatom;
 };
 
 // One CTA per centre, warps over its images: U and dU by the recursion, then
@@ -336,7 +354,6 @@ struct DArgs {
 __global__ void __launch_bounds__(NWD * 32) k_deidrj(DArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ SmallTables st;
-    __shared__ float vred[NWD][9];
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const int a = blockIdx.x;
     if (tid == 0) st = A.st;
@@ -352,9 +369,6 @@ __global__ void __launch_bounds__(NWD * 32) k_deidrj(DArgs A) {
     __syncthreads();
     const float rc = (float)A.prm.rcut;
     const float psi_fac = (float)(A.prm.rfac0 * SO4_PI / A.prm.rcut);
-    // virial of this centre: lane q < 9 accumulates component q = 3a + b of sum r_a g_b
-    float vq = 0.f;
-    const int qa = (lane < 9) ? lane / 3 : 0, qb = (lane < 9) ? lane % 3 : 0;
     const int m0 = A.img_ptr[a], m1 = A.img_ptr[a + 1];
     for (int m = m0 + wid; m < m1; m += NWD) {
         const float x = (float)A.img_r[3 * m], y = (float)A.img_r[3 * m + 1], z = (float)A.img_r[3 * m + 2];
@@ -392,17 +406,7 @@ __global__ void __launch_bounds__(NWD * 32) k_deidrj(DArgs A) {
             A.g[3 * m + 1] = gy;
             A.g[3 * m + 2] = gz;
         }
-        const float ra = (qa == 0) ? x : ((qa == 1) ? y : z);
-        const float gb = (qb == 0) ? gx : ((qb == 1) ? gy : gz);
-        vq += ra * gb;
         __syncwarp();
-    }
-    if (lane < 9) vred[wid][lane] = vq;
-    __syncthreads();
-    if (tid < 9) {
-        double s = 0.0;
-        for (int w = 0; w < NWD; ++w) s += (double)vred[w][tid];
-        A.vatom[9 * (size_t)a + tid] = s;
     }
 }
 
@@ -474,25 +478,6 @@ __global__ void __launch_bounds__(256) k_deidrj_rc(DArgs A, int64_t nimg) {
     }
 }
 
-// per-centre virial sum_{images m of i} r_m (x) g_m in FP64
-__global__ void k_vatom(int natoms, const int32_t *img_ptr, const double *img_r, const float *g, double *vatom) {
-    const int a = blockIdx.x * blockDim.x + threadIdx.x;
-    if (a >= natoms) return;
-    double v[9];
-#pragma unroll
-    for (int q = 0; q < 9; ++q) v[q] = 0.0;
-    for (int m = img_ptr[a]; m < img_ptr[a + 1]; ++m) {
-        const double r[3] = {img_r[3 * m], img_r[3 * m + 1], img_r[3 * m + 2]};
-        const double gg[3] = {g[3 * m], g[3 * m + 1], g[3 * m + 2]};
-#pragma unroll
-        for (int p = 0; p < 3; ++p)
-#pragma unroll
-            for (int q = 0; q < 3; ++q) v[3 * p + q] += r[p] * gg[q];
-    }
-#pragma unroll
-    for (int q = 0; q < 9; ++q) vatom[9 * (size_t)a + q] = v[q];
-}
-
 template <int TWOL>
 int launch_deidrj_rc(const DArgs &D, int64_t nimg, cudaStream_t st) {
     using RC = RowChain<TWOL>;
@@ -504,49 +489,168 @@ int launch_deidrj_rc(const DArgs &D, int64_t nimg, cudaStream_t st) {
     return SO4_OK;
 }
 
-// F_i = sum over images m of i of (g_m - g_rev(m))  (FP64 accumulation)
-__global__ void k_gather(int natoms, const int32_t *img_ptr, const int32_t *img_rev, const float *g, double *forces) {
-    const int a = blockIdx.x * blockDim.x + threadIdx.x;
-    if (a >= natoms) return;
-    double f0 = 0.0, f1 = 0.0, f2 = 0.0;
-    for (int m = img_ptr[a]; m < img_ptr[a + 1]; ++m) {
-        const int r = img_rev[m];
-        f0 += (double)g[3 * m] - (double)g[3 * r];
-        f1 += (double)g[3 * m + 1] - (double)g[3 * r + 1];
-        f2 += (double)g[3 * m + 2] - (double)g[3 * r + 2];
-    }
-    forces[3 * a] = f0;
-    forces[3 * a + 1] = f1;
-    forces[3 * a + 2] = f2;
+// ---------------------------------------------------------------------------
+// Gather: forces, per-structure virial and energy in a fixed order.
+//
+// Atoms are cut into chunks of GCH consecutive atoms, one CTA per chunk and
+// GSUB lanes per atom (lanes over the atom's images).  A chunk belongs to the
+// structure of its first atom; the CTA writes forces for all its atoms and the
+// chunk's partial sums (9 virial components + energy, FP64) over the atoms of
+// that structure only.  The structure pass then adds, for structure s, the
+// atoms before its first whole chunk (recomputed from their images) and the
+// partials of the chunks that begin inside s.  Every sum has a fixed order, so
+// results do not depend on scheduling.
+//
+// FP64 runs at a small fraction of the FP32 rate on this GPU, so per-atom sums
+// are FP32: the force sum sum_m g_m - g_rev(m) is compensated (TwoSum, Knuth),
+// which keeps it at FP64 quality despite the cancellation between g_m and
+// g_rev(m); the per-atom virial r (x) g is plain FP32 (its error, ~1e-7 of one
+// atom's virial, is far below the FP32 error already in g), and everything
+// summed across atoms is FP64.
+constexpr int GSUB = 8;  // lanes per atom
+
+__device__ __forceinline__ void two_sum_add(float &hi, float &lo, float b) {
+    const float s = hi + b;
+    const float bb = s - hi;
+    lo += (hi - (s - bb)) + (b - bb);
+    hi = s;
 }
 
-// per-structure virial: fixed-order reduction of the per-atom virials
-// (each thread sums a strided subset of atoms, then warp shuffles and a
-// 32-entry shared-memory stage; the order never depends on timing)
-__global__ void __launch_bounds__(1024) k_virial(const int *atom_ptr, const double *vatom, double *virial) {
-    __shared__ double red[32][9];
-    const int s = blockIdx.x, t = threadIdx.x, lane = t & 31, wid = t >> 5;
-    const int a0 = atom_ptr[s], a1 = atom_ptr[s + 1];
-    double acc[9];
+// s with atom_ptr[s] <= a < atom_ptr[s + 1] (atom_ptr[0] = 0 <= a < atom_ptr[nstruct])
+__device__ __forceinline__ int struct_of(const int *__restrict__ atom_ptr, int nstruct, int a) {
+    int lo = 0, hi = nstruct;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(atom_ptr + mid) <= a)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+// The GSUB-lane group of the calling lane sums over the images m of atom a
+// (a < 0: nothing) g_m - g_rev(m) (FORCES; fh + fl) and r_m (x) g_m (v).  Every
+// lane of the warp must call it (the group reduction shuffles).
+template <bool FORCES>
+__device__ __forceinline__ void group_atom_fv(int a, const int32_t *__restrict__ img_ptr,
+                                              const int32_t *__restrict__ img_rev, const double *__restrict__ img_r,
+                                              const float *__restrict__ g, float (&fh)[3], float (&fl)[3],
+                                              float (&v)[9]) {
 #pragma unroll
-    for (int q = 0; q < 9; ++q) acc[q] = 0.0;
-    for (int a = a0 + t; a < a1; a += blockDim.x) {
+    for (int q = 0; q < 3; ++q) fh[q] = fl[q] = 0.f;
 #pragma unroll
-        for (int q = 0; q < 9; ++q) acc[q] += vatom[9 * (size_t)a + q];
+    for (int q = 0; q < 9; ++q) v[q] = 0.f;
+    if (a >= 0) {
+        const int m1 = __ldg(img_ptr + a + 1);
+        for (int m = __ldg(img_ptr + a) + (int)(threadIdx.x & (GSUB - 1)); m < m1; m += GSUB) {
+            const float gm[3] = {__ldg(g + 3 * (size_t)m), __ldg(g + 3 * (size_t)m + 1), __ldg(g + 3 * (size_t)m + 2)};
+            const float rm[3] = {(float)__ldg(img_r + 3 * (size_t)m), (float)__ldg(img_r + 3 * (size_t)m + 1),
+                                 (float)__ldg(img_r + 3 * (size_t)m + 2)};
+            if (FORCES) {
+                const size_t rv = (size_t)__ldg(img_rev + m);
+#pragma unroll
+                for (int q = 0; q < 3; ++q) {
+                    two_sum_add(fh[q], fl[q], gm[q]);
+                    two_sum_add(fh[q], fl[q], -__ldg(g + 3 * rv + q));
+                }
+            }
+#pragma unroll
+            for (int p = 0; p < 3; ++p)
+#pragma unroll
+                for (int q = 0; q < 3; ++q) v[3 * p + q] = fmaf(rm[p], gm[q], v[3 * p + q]);
+        }
     }
 #pragma unroll
-    for (int q = 0; q < 9; ++q) {
+    for (int d = GSUB / 2; d > 0; d >>= 1) {
+        if (FORCES) {
 #pragma unroll
-        for (int d = 16; d > 0; d >>= 1) acc[q] += __shfl_down_sync(0xffffffffu, acc[q], d);
+            for (int q = 0; q < 3; ++q) {
+                const float oh = __shfl_xor_sync(0xffffffffu, fh[q], d);
+                const float ol = __shfl_xor_sync(0xffffffffu, fl[q], d);
+                two_sum_add(fh[q], fl[q], oh);
+                fl[q] += ol;
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 9; ++q) v[q] += __shfl_xor_sync(0xffffffffu, v[q], d);
     }
-    if (lane == 0)
+}
+
+__global__ void __launch_bounds__(GCH * GSUB) k_gather_fv(int natoms, int nstruct, const int *__restrict__ atom_ptr,
+                                                         const int32_t *__restrict__ img_ptr,
+                                                         const int32_t *__restrict__ img_rev,
+                                                         const double *__restrict__ img_r,
+                                                         const float *__restrict__ g, const float *__restrict__ eatom,
+                                                         double *__restrict__ part, double *__restrict__ forces) {
+    __shared__ float vs[GCH][GPART];
+    __shared__ int s_end;
+    const int c = blockIdx.x;
+    const int slot = threadIdx.x / GSUB;  // atom of the chunk
+    const int a = c * GCH + slot;
+    if (threadIdx.x == 0) s_end = __ldg(atom_ptr + struct_of(atom_ptr, nstruct, c * GCH) + 1);
+    float fh[3], fl[3], v[9];
+    group_atom_fv<true>(a < natoms ? a : -1, img_ptr, img_rev, img_r, g, fh, fl, v);
+    if ((threadIdx.x & (GSUB - 1)) == 0) {
+        if (a < natoms) {
 #pragma unroll
-        for (int q = 0; q < 9; ++q) red[wid][q] = acc[q];
+            for (int q = 0; q < 3; ++q) forces[3 * (size_t)a + q] = (double)fh[q] + (double)fl[q];
+        }
+#pragma unroll
+        for (int q = 0; q < 9; ++q) vs[slot][q] = v[q];
+        vs[slot][9] = (eatom && a < natoms) ? __ldg(eatom + a) : 0.f;
+    }
     __syncthreads();
-    if (t < 9) {
-        double v = 0.0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v += red[w][t];
-        virial[9 * s + t] = v;
+    if (threadIdx.x < GPART) {
+        const int lim = min(natoms, s_end) - c * GCH;  // atoms of the chunk in its first structure
+        double p = 0.0;
+        for (int k = 0; k < GCH && k < lim; ++k) p += (double)vs[k][threadIdx.x];
+        part[(size_t)GPART * c + threadIdx.x] = p;
+    }
+}
+
+// One CTA per structure: virial[s] (9) and energy[s] from the head atoms and the chunk partials.
+constexpr int GSS = GCH * GSUB;  // threads of the structure pass: one group per possible head atom
+__global__ void __launch_bounds__(GSS) k_struct_sum(const int *__restrict__ atom_ptr,
+                                                   const int32_t *__restrict__ img_ptr,
+                                                   const int32_t *__restrict__ img_rev,
+                                                   const double *__restrict__ img_r, const float *__restrict__ g,
+                                                   const float *__restrict__ eatom, const double *__restrict__ part,
+                                                   double *__restrict__ virial, double *__restrict__ energy) {
+    constexpr int NSLOT = GSS / GPART;
+    __shared__ float hv[GCH][GPART];
+    __shared__ double red[NSLOT][GPART];
+    const int s = blockIdx.x, t = threadIdx.x;
+    const int a0 = __ldg(atom_ptr + s), a1 = __ldg(atom_ptr + s + 1);
+    const int c0 = (a0 + GCH - 1) / GCH;                       // first chunk starting inside s
+    const int h1 = min(a1, c0 * GCH);                          // head atoms [a0, h1), fewer than GCH
+    const int c1 = (a1 > c0 * GCH) ? (a1 - 1) / GCH : c0 - 1;  // last chunk starting inside s
+    {
+        const int k = t / GSUB, a = a0 + k;
+        float fh[3], fl[3], v[9];
+        group_atom_fv<false>(a < h1 ? a : -1, img_ptr, img_rev, img_r, g, fh, fl, v);
+        if ((t & (GSUB - 1)) == 0) {
+#pragma unroll
+            for (int q = 0; q < 9; ++q) hv[k][q] = v[q];
+            hv[k][9] = (eatom && a < h1) ? __ldg(eatom + a) : 0.f;
+        }
+    }
+    // chunk partials: thread t < NSLOT * GPART adds component q of chunks c0 + slot, c0 + slot + NSLOT, ...
+    const int q = t % GPART, slot = t / GPART;
+    if (slot < NSLOT) {
+        double acc = 0.0;
+        for (int c = c0 + slot; c <= c1; c += NSLOT) acc += __ldg(part + (size_t)GPART * c + q);
+        red[slot][q] = acc;
+    }
+    __syncthreads();
+    if (t < GPART) {
+        double tot = 0.0;
+        for (int k = 0; k < GCH; ++k) tot += (double)hv[k][t];
+        for (int k = 0; k < NSLOT; ++k) tot += red[k][t];
+        if (t < 9)
+            virial[9 * (size_t)s + t] = tot;
+        else if (energy)
+            energy[s] = tot;
     }
 }
 
@@ -555,7 +659,7 @@ size_t rootpq_floats(int ldim) { return (size_t)((ldim * ldim + 1) & ~1); }
 }  // namespace
 
 static ZLArgs zl_args(const so4_tables *t, int natoms) {
-    ZLArgs Z;
+    ZLArgs Z{};
     Z.natoms = natoms;
     Z.nh = t->n_half;
     Z.nu = t->n_u;
@@ -662,8 +766,8 @@ extern "C" int so4_adjoint_y32(const so4_tables *t, int natoms, const float *d_u
 
 extern "C" int so4_adjoint_deidrj32(const so4_tables *t, const so4_params *p, int natoms, const double *d_w_nb,
                                     const int32_t *d_img_ptr, const int32_t *d_img_j, const double *d_img_r,
-                                    int64_t nimg, const float *d_y, float *d_g, double *d_vatom, void *stream) {
-    if (!t || !p || natoms < 0 || nimg < 0 || !d_y || !d_g || !d_vatom) return SO4_ERR_ARG;
+                                    int64_t nimg, const float *d_y, float *d_g, void *stream) {
+    if (!t || !p || natoms < 0 || nimg < 0 || !d_y || !d_g) return SO4_ERR_ARG;
     if (p->twol != t->twol || !(p->rcut > 0.0) || !(p->rfac0 > 0.0)) return SO4_ERR_ARG;
     if (p->cutoff_id < 1 || p->cutoff_id > 7) return SO4_ERR_UNSUPPORTED;
     if (natoms == 0) return SO4_OK;
@@ -681,7 +785,6 @@ extern "C" int so4_adjoint_deidrj32(const so4_tables *t, const so4_params *p, in
     D.rc32 = (float)p->rcut;
     D.Y = (const float2 *)d_y;
     D.g = d_g;
-    D.vatom = d_vatom;
     cudaStream_t st = (cudaStream_t)stream;
     int rc = SO4_OK;
     switch (t->twol) {
@@ -702,22 +805,31 @@ extern "C" int so4_adjoint_deidrj32(const so4_tables *t, const so4_params *p, in
         }
     }
     if (rc) return rc;
-    k_vatom<<<(natoms + 127) / 128, 128, 0, st>>>(natoms, d_img_ptr, d_img_r, d_g, d_vatom);
-    so4_count_launch();
     return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
 }
 
+extern "C" size_t so4_gather_workspace_size(int natoms) {
+    return natoms < 0 ? 0 : sizeof(double) * gather_part_doubles(natoms);
+}
+
 extern "C" int so4_adjoint_gather(int natoms, int nstruct, const int *d_atom_ptr, const int32_t *d_img_ptr,
-                                  const int32_t *d_img_rev, const float *d_g, const double *d_vatom, double *d_forces,
-                                  double *d_virial, void *stream) {
+                                  const int32_t *d_img_rev, const double *d_img_r, const float *d_g,
+                                  const float *d_eatom, double *d_part, double *d_forces, double *d_virial,
+                                  double *d_energy, void *stream) {
     if (natoms < 0 || nstruct < 0) return SO4_ERR_ARG;
+    if (natoms > 0 && (!d_atom_ptr || !d_img_ptr || !d_img_rev || !d_img_r || !d_g || !d_part || !d_forces))
+        return SO4_ERR_ARG;
+    if (nstruct > 0 && !d_virial) return SO4_ERR_ARG;
+    if (natoms > 0 && nstruct == 0) return SO4_ERR_ARG;
     cudaStream_t st = (cudaStream_t)stream;
     if (natoms > 0) {
-        k_gather<<<(natoms + 127) / 128, 128, 0, st>>>(natoms, d_img_ptr, d_img_rev, d_g, d_forces);
+        k_gather_fv<<<(natoms + GCH - 1) / GCH, GCH * GSUB, 0, st>>>(natoms, nstruct, d_atom_ptr, d_img_ptr, d_img_rev,
+                                                                   d_img_r, d_g, d_eatom, d_part, d_forces);
         so4_count_launch();
     }
     if (nstruct > 0) {
-        k_virial<<<nstruct, 1024, 0, st>>>(d_atom_ptr, d_vatom, d_virial);
+        k_struct_sum<<<nstruct, GSS, 0, st>>>(d_atom_ptr, d_img_ptr, d_img_rev, d_img_r, d_g, d_eatom, d_part,
+                                              d_virial, d_energy);
         so4_count_launch();
     }
     return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
@@ -735,11 +847,11 @@ extern "C" int so4_adjoint32(const so4_tables *t, const so4_params *p, int nstru
     carve_adj(w, d_work, natoms, t->n_half, nimg);
     int rc = so4_adjoint_y32(t, natoms, d_utot, d_beta, (float *)w.Y, stream);
     if (rc) return rc;
-    rc = so4_adjoint_deidrj32(t, p, natoms, d_w_nb, d_img_ptr, d_img_j, d_img_r, nimg, (const float *)w.Y, w.g, w.vatom,
+    rc = so4_adjoint_deidrj32(t, p, natoms, d_w_nb, d_img_ptr, d_img_j, d_img_r, nimg, (const float *)w.Y, w.g,
                               stream);
     if (rc) return rc;
-    return so4_adjoint_gather(natoms, nstruct, d_atom_ptr, d_img_ptr, d_img_rev, w.g, w.vatom, d_forces, d_virial,
-                              stream);
+    return so4_adjoint_gather(natoms, nstruct, d_atom_ptr, d_img_ptr, d_img_rev, d_img_r, w.g, nullptr, w.part,
+                              d_forces, d_virial, nullptr, stream);
 }
 
 // ---------------------------------------------------------------------------
@@ -804,22 +916,34 @@ extern "C" int so4_adjoint32_noalloc(const so4_tables *t, const so4_params *p, i
     carve_adj(w, scratch, natoms, t->n_half, nimg);
     int rc = so4_adjoint_y32(t, natoms, d_utot, d_beta, (float *)w.Y, stream);
     if (rc) return rc;
-    rc = so4_adjoint_deidrj32(t, p, natoms, d_w_nb, d_img_ptr, d_img_j, d_img_r, nimg, (const float *)w.Y, w.g, w.vatom,
+    rc = so4_adjoint_deidrj32(t, p, natoms, d_w_nb, d_img_ptr, d_img_j, d_img_r, nimg, (const float *)w.Y, w.g,
                               stream);
     if (rc) return rc;
-    return so4_adjoint_gather(natoms, nstruct, d_atom_ptr, d_img_ptr, d_img_rev, w.g, w.vatom, d_forces, d_virial,
-                              stream);
+    return so4_adjoint_gather(natoms, nstruct, d_atom_ptr, d_img_ptr, d_img_rev, d_img_r, w.g, nullptr, w.part,
+                              d_forces, d_virial, nullptr, stream);
 }
 
 // ---------------------------------------------------------------------------
 // Energy linear in B: forward and adjoint with Z computed once.
+// linear-path scratch after the adjoint's: U_tot, the B-section rows, the per-atom energy
+static size_t carve_linear(const so4_tables *t, void *base, int natoms, int64_t nimg, AdjWork &w, float **utot,
+                           float **bc, float **eatom) {
+    size_t off = carve_adj(w, base, natoms, t->n_half, nimg);
+    char *p = (char *)base;
+    *utot = p ? (float *)(p + off) : nullptr;
+    off += a256(sizeof(float2) * (size_t)natoms * t->n_half + 8);
+    *bc = p ? (float *)(p + off) : nullptr;
+    off += a256(sizeof(float) * (size_t)(natoms + 1) * t->n_bsec);
+    *eatom = p ? (float *)(p + off) : nullptr;
+    off += a256(sizeof(float) * (size_t)(natoms + 1));
+    return off;
+}
+
 extern "C" size_t so4_linear_workspace_size(const so4_tables *t, int natoms, int64_t nimg) {
     if (!t) return 0;
     AdjWork w;
-    size_t s = carve_adj(w, nullptr, natoms, t->n_half, nimg);
-    s += a256(sizeof(float2) * (size_t)natoms * t->n_half + 8);          // U_tot
-    s += a256(sizeof(float) * (size_t)(natoms + 1) * t->n_bsec);          // B-section row
-    return s;
+    float *u, *b, *e;
+    return carve_linear(t, nullptr, natoms, nimg, w, &u, &b, &e);
 }
 
 extern "C" int so4_utot32(const so4_tables *t, const so4_params *p, int natoms, const double *d_w_nb,
@@ -875,7 +999,7 @@ extern "C" int so4_utot32(const so4_tables *t, const so4_params *p, int natoms, 
 }
 
 extern "C" int so4_linear_by32(const so4_tables *t, int natoms, const float *d_utot, const float *d_beta, float *d_x,
-                               float *d_y, float *d_bc, void *stream) {
+                               float *d_y, float *d_bc, float *d_eatom, void *stream) {
     if (!t || natoms < 0 || !d_utot || !d_beta || !d_x || !d_y || !d_bc) return SO4_ERR_ARG;
     if (natoms == 0) return SO4_OK;
     ZLArgs Z = zl_args(t, natoms);
@@ -889,7 +1013,10 @@ extern "C" int so4_linear_by32(const so4_tables *t, int natoms, const float *d_u
     Z.bpos = t->d_bpos;
     Z.nbsec = t->n_bsec;
     Z.bc = d_bc;
-    const size_t smz = sizeof(float2) * (size_t)t->n_u * ZL_PITCH + sizeof(float) * (size_t)t->n_blk * ZL_PITCH;
+    Z.eatom = d_eatom;
+    // U tiles + per-block coefficients; the epilogue reuses the U tiles for nB x 33 floats
+    const size_t smz = std::max(sizeof(float2) * (size_t)t->n_u, sizeof(float) * (size_t)t->n_b) * ZL_PITCH +
+                       sizeof(float) * (size_t)t->n_blk * ZL_PITCH;
     int rc = set_smem(k_zby32, smz);
     if (rc) return rc;
     k_zby32<<<(natoms + 31) / 32, 256, smz, (cudaStream_t)stream>>>(Z);
@@ -901,22 +1028,21 @@ extern "C" int so4_adjoint_linear32(const so4_tables *t, const so4_params *p, in
                                     const int *d_atom_ptr, int natoms, const double *d_w_nb, const double *d_w_site,
                                     const int32_t *d_img_ptr, const int32_t *d_img_j, const double *d_img_r,
                                     const int32_t *d_img_rev, int64_t nimg, const float *d_beta, float *d_x,
-                                    double *d_forces, double *d_virial, void *d_work, size_t work_bytes,
-                                    void *stream) {
+                                    double *d_forces, double *d_virial, double *d_energy, void *d_work,
+                                    size_t work_bytes, void *stream) {
     (void)d_atom_struct;
     if (!t || !p || natoms < 0 || nstruct < 0 || nimg < 0 || !d_work || !d_x) return SO4_ERR_ARG;
     if (so4_linear_workspace_size(t, natoms, nimg) > work_bytes) return SO4_ERR_WORKSPACE;
     AdjWork w;
-    const size_t base = carve_adj(w, d_work, natoms, t->n_half, nimg);
-    float *utot = (float *)((char *)d_work + base);
-    float *bc = (float *)((char *)d_work + base + a256(sizeof(float2) * (size_t)natoms * t->n_half + 8));
+    float *utot, *bc, *eatom;
+    carve_linear(t, d_work, natoms, nimg, w, &utot, &bc, &eatom);
     int rc = so4_utot32(t, p, natoms, d_w_nb, d_w_site, d_img_ptr, d_img_j, d_img_r, utot, stream);
     if (rc) return rc;
-    rc = so4_linear_by32(t, natoms, utot, d_beta, d_x, (float *)w.Y, bc, stream);
+    rc = so4_linear_by32(t, natoms, utot, d_beta, d_x, (float *)w.Y, bc, d_energy ? eatom : nullptr, stream);
     if (rc) return rc;
     rc = so4_adjoint_deidrj32(t, p, natoms, d_w_nb, d_img_ptr, d_img_j, d_img_r, nimg, (const float *)w.Y, w.g,
-                              w.vatom, stream);
-    if (rc) return rc;
-    return so4_adjoint_gather(natoms, nstruct, d_atom_ptr, d_img_ptr, d_img_rev, w.g, w.vatom, d_forces, d_virial,
                               stream);
+    if (rc) return rc;
+    return so4_adjoint_gather(natoms, nstruct, d_atom_ptr, d_img_ptr, d_img_rev, d_img_r, w.g,
+                              d_energy ? eatom : nullptr, w.part, d_forces, d_virial, d_energy, stream);
 }

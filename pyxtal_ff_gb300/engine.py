@@ -240,10 +240,20 @@ def forward32(tab, prm, nb: Neighbors, w_nb, w_site):
     return x[: nb.natoms], utot[: nb.natoms]
 
 
-def adjoint32(tab, prm, nb: Neighbors, w_nb, utot, beta, workspace=None):
-    """forces (N,3) f64 = -dE/dr and virial (S,3,3) f64 = sum r (x) dE/dr, for beta = dE/dB."""
+def adjoint32(tab, prm, nb: Neighbors, w_nb, utot, beta, workspace=None, eatom=None):
+    """forces (N,3) f64 = -dE/dr and virial (S,3,3) f64 = sum r (x) dE/dr, for beta = dE/dB.
+    With eatom (N,) the per-structure energy (S,) f64 = its fixed-order sum is returned too."""
     dev = utot.device
     beta = beta.to(torch.float32).contiguous()
+    if eatom is not None:
+        y = torch.empty((max(nb.natoms, 1), tab.n_half, 2), dtype=torch.float32, device=dev)
+        g = torch.empty((max(nb.nimg, 1), 3), dtype=torch.float32, device=dev)
+        L, st = lib(), _stream()
+        check(L.so4_adjoint_y32(tab.handle, nb.natoms, _ptr(utot), _ptr(beta), _ptr(y), st), "so4_adjoint_y32")
+        check(L.so4_adjoint_deidrj32(tab.handle, C.byref(prm), nb.natoms, _ptr(w_nb), _ptr(nb.img_ptr),
+                                     _ptr(nb.img_j), _ptr(nb.img_r), nb.nimg, _ptr(y), _ptr(g), st),
+              "so4_adjoint_deidrj32")
+        return gather(nb, g, eatom.to(torch.float32).contiguous())
     forces = torch.empty((max(nb.natoms, 1), 3), dtype=torch.float64, device=dev)
     virial = torch.empty((max(nb.nstruct, 1), 3, 3), dtype=torch.float64, device=dev)
     need = lib().so4_adjoint_workspace_size(tab.handle, nb.natoms, nb.nimg)
@@ -255,6 +265,21 @@ def adjoint32(tab, prm, nb: Neighbors, w_nb, utot, beta, workspace=None):
     return forces[: nb.natoms], virial[: nb.nstruct]
 
 
+def gather(nb: Neighbors, g, eatom=None):
+    """forces (N,3), virial (S,3,3) and, with eatom (N,) f32, energy (S,) -- all f64 and in a
+    fixed summation order -- from the per-image dE/dr g (M,3) f32."""
+    dev = g.device
+    N = nb.natoms
+    forces = torch.empty((max(N, 1), 3), dtype=torch.float64, device=dev)
+    virial = torch.empty((max(nb.nstruct, 1), 3, 3), dtype=torch.float64, device=dev)
+    energy = torch.empty(max(nb.nstruct, 1), dtype=torch.float64, device=dev) if eatom is not None else None
+    part = torch.empty(lib().so4_gather_workspace_size(N), dtype=torch.uint8, device=dev)
+    check(lib().so4_adjoint_gather(N, nb.nstruct, _ptr(nb.atom_ptr_dev), _ptr(nb.img_ptr), _ptr(nb.img_rev),
+                                   _ptr(nb.img_r), _ptr(g), _ptr(eatom), _ptr(part), _ptr(forces), _ptr(virial),
+                                   _ptr(energy), _stream()), "so4_adjoint_gather")
+    return forces[:N], virial[: nb.nstruct], (energy[: nb.nstruct] if energy is not None else None)
+
+
 def adjoint32_staged(tab, prm, nb: Neighbors, w_nb, utot, beta, mark=None, first=0):
     """adjoint32 as its three C-ABI stages (Y build, per-image contraction, gather) with
     caller-visible buffers; mark(i) is called between stages (for timing)."""
@@ -263,20 +288,16 @@ def adjoint32_staged(tab, prm, nb: Neighbors, w_nb, utot, beta, mark=None, first
     N, M = nb.natoms, nb.nimg
     y = torch.empty((max(N, 1), tab.n_half, 2), dtype=torch.float32, device=dev)
     g = torch.empty((max(M, 1), 3), dtype=torch.float32, device=dev)
-    vatom = torch.empty((max(N, 1), 9), dtype=torch.float64, device=dev)
-    forces = torch.empty((max(N, 1), 3), dtype=torch.float64, device=dev)
-    virial = torch.empty((max(nb.nstruct, 1), 3, 3), dtype=torch.float64, device=dev)
     L, st = lib(), _stream()
     check(L.so4_adjoint_y32(tab.handle, N, _ptr(utot), _ptr(beta), _ptr(y), st), "so4_adjoint_y32")
     if mark:
         mark(first + 1)
     check(L.so4_adjoint_deidrj32(tab.handle, C.byref(prm), N, _ptr(w_nb), _ptr(nb.img_ptr), _ptr(nb.img_j),
-                                 _ptr(nb.img_r), M, _ptr(y), _ptr(g), _ptr(vatom), st), "so4_adjoint_deidrj32")
+                                 _ptr(nb.img_r), M, _ptr(y), _ptr(g), st), "so4_adjoint_deidrj32")
     if mark:
         mark(first + 2)
-    check(L.so4_adjoint_gather(N, nb.nstruct, _ptr(nb.atom_ptr_dev), _ptr(nb.img_ptr), _ptr(nb.img_rev), _ptr(g),
-                               _ptr(vatom), _ptr(forces), _ptr(virial), st), "so4_adjoint_gather")
-    return forces[:N], virial[: nb.nstruct]
+    forces, virial, _ = gather(nb, g)
+    return forces, virial
 
 
 def jvp32(tab, prm, nb: Neighbors, w_nb, utot, v=None, G=None, workspace=None):
@@ -294,25 +315,27 @@ def jvp32(tab, prm, nb: Neighbors, w_nb, utot, v=None, G=None, workspace=None):
 
 
 def adjoint_linear32(tab, prm, nb: Neighbors, w_nb, w_site, beta, workspace=None):
-    """B (N,nB) f32, forces (N,3) f64 and virial (S,3,3) f64 for an energy linear in B
-    (beta = dE/dB fixed), in one fused pass (Z computed once)."""
+    """B (N,nB) f32, forces (N,3) f64, virial (S,3,3) f64 and energy (S,) f64 = sum beta.B for an
+    energy linear in B (beta = dE/dB fixed), in one fused pass (Z computed once)."""
     dev = w_nb.device
     beta = beta.to(torch.float32).contiguous()
     x = torch.empty((max(nb.natoms, 1), tab.nB), dtype=torch.float32, device=dev)
     forces = torch.empty((max(nb.natoms, 1), 3), dtype=torch.float64, device=dev)
     virial = torch.empty((max(nb.nstruct, 1), 3, 3), dtype=torch.float64, device=dev)
+    energy = torch.empty(max(nb.nstruct, 1), dtype=torch.float64, device=dev)
     need = lib().so4_linear_workspace_size(tab.handle, nb.natoms, nb.nimg)
     ws = workspace if (workspace is not None and workspace.numel() >= need) else torch.empty(need, dtype=torch.uint8, device=dev)
     check(lib().so4_adjoint_linear32(tab.handle, C.byref(prm), nb.nstruct, _ptr(nb.atom_struct), _ptr(nb.atom_ptr_dev),
                                      nb.natoms, _ptr(w_nb), _ptr(w_site), _ptr(nb.img_ptr), _ptr(nb.img_j),
                                      _ptr(nb.img_r), _ptr(nb.img_rev), nb.nimg, _ptr(beta), _ptr(x), _ptr(forces),
-                                     _ptr(virial), _ptr(ws), ws.numel(), _stream()), "so4_adjoint_linear32")
-    return x[: nb.natoms], forces[: nb.natoms], virial[: nb.nstruct]
+                                     _ptr(virial), _ptr(energy), _ptr(ws), ws.numel(), _stream()),
+          "so4_adjoint_linear32")
+    return x[: nb.natoms], forces[: nb.natoms], virial[: nb.nstruct], energy[: nb.nstruct]
 
 
 def linear_staged(tab, prm, nb: Neighbors, w_nb, w_site, beta, mark=None, first=0):
     """adjoint_linear32 as its C-ABI stages (U_tot; B and Y; per-image dE/dr; gather),
-    with mark(i) called between stages (for timing).  Returns (x, forces, virial)."""
+    with mark(i) called between stages (for timing).  Returns (x, forces, virial, energy)."""
     dev = w_nb.device
     beta = beta.to(torch.float32).contiguous()
     N, M = nb.natoms, nb.nimg
@@ -320,22 +343,20 @@ def linear_staged(tab, prm, nb: Neighbors, w_nb, w_site, beta, mark=None, first=
     x = torch.empty((max(N, 1), tab.nB), dtype=torch.float32, device=dev)
     y = torch.empty((max(N, 1), tab.n_half, 2), dtype=torch.float32, device=dev)
     bc = torch.empty((tab.n_bsec, max(N, 1)), dtype=torch.float32, device=dev)
+    eatom = torch.empty(max(N, 1), dtype=torch.float32, device=dev)
     g = torch.empty((max(M, 1), 3), dtype=torch.float32, device=dev)
-    vatom = torch.empty((max(N, 1), 9), dtype=torch.float64, device=dev)
-    forces = torch.empty((max(N, 1), 3), dtype=torch.float64, device=dev)
-    virial = torch.empty((max(nb.nstruct, 1), 3, 3), dtype=torch.float64, device=dev)
     L, st = lib(), _stream()
     check(L.so4_utot32(tab.handle, C.byref(prm), N, _ptr(w_nb), _ptr(w_site), _ptr(nb.img_ptr), _ptr(nb.img_j),
                        _ptr(nb.img_r), _ptr(utot), st), "so4_utot32")
     if mark:
         mark(first + 1)
-    check(L.so4_linear_by32(tab.handle, N, _ptr(utot), _ptr(beta), _ptr(x), _ptr(y), _ptr(bc), st), "so4_linear_by32")
+    check(L.so4_linear_by32(tab.handle, N, _ptr(utot), _ptr(beta), _ptr(x), _ptr(y), _ptr(bc), _ptr(eatom), st),
+          "so4_linear_by32")
     if mark:
         mark(first + 2)
     check(L.so4_adjoint_deidrj32(tab.handle, C.byref(prm), N, _ptr(w_nb), _ptr(nb.img_ptr), _ptr(nb.img_j),
-                                 _ptr(nb.img_r), M, _ptr(y), _ptr(g), _ptr(vatom), st), "so4_adjoint_deidrj32")
+                                 _ptr(nb.img_r), M, _ptr(y), _ptr(g), st), "so4_adjoint_deidrj32")
     if mark:
         mark(first + 3)
-    check(L.so4_adjoint_gather(N, nb.nstruct, _ptr(nb.atom_ptr_dev), _ptr(nb.img_ptr), _ptr(nb.img_rev), _ptr(g),
-                               _ptr(vatom), _ptr(forces), _ptr(virial), st), "so4_adjoint_gather")
-    return x[:N], forces[:N], virial[: nb.nstruct]
+    forces, virial, energy = gather(nb, g, eatom)
+    return x[:N], forces, virial, energy

@@ -178,12 +178,20 @@ def test_fused_linear_path_matches_unfused_and_oracle(cuda_device):
     beta = torch.from_numpy(np.random.default_rng(12).normal(0, 0.01, size=(len(pos), tab.nB))).float().cuda()
     x1, utot = engine.forward32(tab, prm, nb, w_nb, w_site)
     f1, v1 = engine.adjoint32(tab, prm, nb, w_nb, utot, beta)
-    x2, f2, v2 = engine.adjoint_linear32(tab, prm, nb, w_nb, w_site, beta)
-    x3, f3, v3 = engine.linear_staged(tab, prm, nb, w_nb, w_site, beta)
+    x2, f2, v2, e2 = engine.adjoint_linear32(tab, prm, nb, w_nb, w_site, beta)
+    x3, f3, v3, e3 = engine.linear_staged(tab, prm, nb, w_nb, w_site, beta)
     assert G.rel_err(x2.cpu().numpy(), x1.cpu().numpy()) < 1e-5
     assert G.rel_err(f2.cpu().numpy(), f1.cpu().numpy()) < 1e-5
     assert G.rel_err(v2.cpu().numpy(), v1.cpu().numpy()) < 1e-5
-    assert torch.equal(x2, x3) and torch.equal(f2, f3) and torch.equal(v2, v3)
+    assert torch.equal(x2, x3) and torch.equal(f2, f3) and torch.equal(v2, v3) and torch.equal(e2, e3)
+    # energy: per-atom beta . B (FP32) summed per structure in FP64
+    e_ref = [float((x2[a0:a1].double() * beta[a0:a1].double()).sum()) for a0, a1 in zip(ptr[:-1], ptr[1:])]
+    assert np.allclose(e2.cpu().numpy(), e_ref, rtol=1e-5, atol=0)
+    # the unfused path with the per-atom energy given gives the same forces / virial and its energy sum
+    f4, v4, e4 = engine.adjoint32(tab, prm, nb, w_nb, utot, beta, eatom=(x1 * beta).sum(-1))
+    assert torch.equal(f4, f1) and torch.equal(v4, v1)
+    e_ref1 = [float((x1[a0:a1] * beta[a0:a1]).sum(-1).double().sum()) for a0, a1 in zip(ptr[:-1], ptr[1:])]
+    assert np.allclose(e4.cpu().numpy(), e_ref1, rtol=1e-12, atol=0)
     for s, st in enumerate(structs):
         a0, a1 = ptr[s], ptr[s + 1]
         ref = O.forces_virial(st, beta[a0:a1].double().cpu().numpy(), kind="SNAP", lmax=4, rcut=5.0, weights=w,
