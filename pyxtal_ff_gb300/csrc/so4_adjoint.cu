@@ -16,7 +16,7 @@
 
 #include "so4_atom.cuh"
 #include "so4_rowchain.cuh"
-#include "so4_zlanes.cuh"
+#include "so4_zwin.cuh"
 
 namespace {
 
@@ -198,6 +198,8 @@ struct ZLArgs {
     float2 *Y;   // Y out  (k_zy32, k_zby32)
     float *bc;   // fused path: B-section contributions, entry-major [nbsec][natoms]
     float *eatom;  // fused path: sum_k beta_k B_k per atom (may be null)
+    const int4 *wsub;  // window sub-segments
+    const float *wca;  // window Ca rows
 };
 
 // B_k = 2 Re sum' conj(U_l) Z(l1,l2,l) for 32 atoms per CTA (compute_bi, SO4.py:1071-1111)
@@ -329,6 +331,114 @@ __global__ void __launch_bounds__(256) k_zby32(ZLArgs A) {
         eb[k * ZL_PITCH + l] = e;
     }
     if (A.eatom == nullptr) return;
+    __syncthreads();
+    if (threadIdx.x < 32 && a < A.natoms) {
+        float e = 0.f;
+        for (int k = 0; k < A.nB; ++k) e += eb[k * ZL_PITCH + threadIdx.x];
+        A.eatom[a] = e;
+    }
+}
+
+// Window form of k_zb32 / k_zy32 / k_zby32 (so4_zwin.cuh), 32 atoms per CTA.
+// MODE 0: B only (units of the B sections, B blocks only); 1: Y only; 2: Y and,
+// for the Z entries in a B section, w_e Re(conj(U_lam[e]) Z[e]) into the
+// entry-major scratch d_bc, then B_k = 2 sum over the section (compute_bi,
+// SO4.py:1071-1111) and, with d_eatom, beta . B per atom.
+template <int MODE>
+__global__ void __launch_bounds__(256) k_zw32(ZLArgs A) {
+    extern __shared__ __align__(16) float2 zw_smem[];
+    __shared__ int s_unit;
+    const int lane = threadIdx.x & 31;
+    const int a0 = blockIdx.x * 32, a = a0 + lane;
+    float2 *Ub = zw_smem;
+    float *coef = (float *)(Ub + (size_t)(A.nu + 2 * ZW_PAD) * ZL_PITCH);  // [nblk][33], MODE 1 and 2
+    if (threadIdx.x == 0) s_unit = 0;
+    zw_load_utot(A.utot, A.fmap, a0, A.natoms, A.nh, A.nu, Ub);
+    if (MODE != 0) {
+        for (int idx = threadIdx.x; idx < 32 * A.nblk; idx += blockDim.x) {
+            const int l = idx / A.nblk, b = idx - l * A.nblk;
+            const int aa = a0 + l;
+            float c = 0.f;
+            if (aa < A.natoms) {
+                const ZBlk &bk = A.blk[b];
+                for (int r = 0; r < bk.nrole; ++r)
+                    c += (float)bk.role_f[r] * __ldg(A.beta + (size_t)aa * A.nB + bk.role_k[r]);
+            }
+            coef[b * ZL_PITCH + l] = c;
+        }
+    }
+    __syncthreads();
+    const float2 *Ul = Ub + lane;
+    for (int u = zl_next(&s_unit); u < A.nunit; u = zl_next(&s_unit)) {
+        const int4 un = __ldg(A.unit + u);
+        const int lam = un.x & 0xff, mb = (un.x >> 8) & 0xff, ma0 = (un.x >> 16) & 0xff, nk = un.x >> 24;
+        const int off0 = mb * (lam + 1) + ma0;
+        const int cnt = section_count(lam);
+        float yr[ZW_K], yi[ZW_K];
+        float2 ul[ZW_K];
+#pragma unroll
+        for (int k = 0; k < ZW_K; ++k) {
+            yr[k] = yi[k] = 0.f;
+            // U_lam of the unit's entries (the pad rows keep a short last unit in bounds)
+            ul[k] = (MODE != 1) ? Ul[(ZW_PAD + A.st.u_block[lam] + off0 + k) * ZL_PITCH] : make_float2(0.f, 0.f);
+        }
+        for (int q = un.y; q < un.z; ++q) {
+            const int4 sg = __ldg(A.seg + q);
+            float zr[ZW_K], zi[ZW_K];
+#pragma unroll
+            for (int k = 0; k < ZW_K; ++k) zr[k] = zi[k] = 0.f;
+            for (int r = sg.x; r < sg.y; ++r) zw_rows(Ul, __ldg(A.wsub + r), A.wca, zr, zi);
+            if (MODE != 0) {
+                const float c = coef[sg.z * ZL_PITCH + lane];
+#pragma unroll
+                for (int k = 0; k < ZW_K; ++k) {
+                    yr[k] = fmaf(c, zr[k], yr[k]);
+                    yi[k] = fmaf(c, zi[k], yi[k]);
+                }
+            }
+            if (MODE != 1 && sg.w >= 0 && a < A.natoms) {
+#pragma unroll
+                for (int k = 0; k < ZW_K; ++k) {
+                    const int off = off0 + k;
+                    if (k < nk && off < cnt) {
+                        // scratch is entry-major, so the 32 lanes (atoms) store one contiguous line
+                        const float v = ul[k].x * zr[k] + ul[k].y * zi[k];
+                        A.bc[(size_t)(sg.w + k) * A.natoms + a] = ((lam & 1) == 0 && off == cnt - 1) ? 0.5f * v : v;
+                    }
+                }
+            }
+        }
+        if (MODE != 0 && a < A.natoms) {
+            const float un_l = __int_as_float(un.w);
+            float2 *Yo = A.Y + (size_t)a * A.nh + A.st.h_block[lam] + off0;
+#pragma unroll
+            for (int k = 0; k < ZW_K; ++k) {
+                if (k < nk) {
+                    const int ma = ma0 + k;
+                    const float wmid = (2 * mb < lam) ? 1.f : ((2 * ma < lam) ? 1.f : ((2 * ma == lam) ? 0.5f : 0.f));
+                    const float s = un_l * wmid;
+                    Yo[k] = make_float2(s * yr[k], s * yi[k]);
+                }
+            }
+        }
+    }
+    if (MODE == 1) return;
+    __syncthreads();
+    // B_k, and beta_k B_k kept in shared memory (over the U tiles, no longer read) for the energy
+    float *eb = (float *)zw_smem;  // [nB][33]
+    for (int idx = threadIdx.x; idx < 32 * A.nB; idx += blockDim.x) {
+        const int k = idx >> 5, l = idx & 31;
+        const int aa = a0 + l;
+        float acc = 0.f, e = 0.f;
+        if (aa < A.natoms) {
+            for (int q = __ldg(A.bpos + k); q < __ldg(A.bpos + k + 1); ++q) acc += A.bc[(size_t)q * A.natoms + aa];
+            acc *= 2.f;
+            A.x[(size_t)aa * A.nB + k] = acc;
+            if (MODE == 2) e = acc * __ldg(A.beta + (size_t)aa * A.nB + k);
+        }
+        if (MODE == 2) eb[k * ZL_PITCH + l] = e;
+    }
+    if (MODE != 2 || A.eatom == nullptr) return;
     __syncthreads();
     if (threadIdx.x < 32 && a < A.natoms) {
         float e = 0.f;
@@ -672,8 +782,18 @@ static ZLArgs zl_args(const so4_tables *t, int natoms) {
     Z.blk = t->d_blk;
     Z.yptr = t->d_yblk_ptr;
     Z.ylist = t->d_yblk;
+    Z.wsub = t->d_wsub;
+    Z.wca = t->d_wca;
     fill_small_tables(t, Z.st);
     return Z;
+}
+
+// shared memory of k_zw32: padded U tiles and the per-block coefficients; the B
+// epilogue (with_b) reuses the U tiles for nB x 33 floats
+static size_t zw_smem_bytes(const so4_tables *t, bool with_b) {
+    size_t u = sizeof(float2) * (size_t)(t->n_u + 2 * ZW_PAD) * ZL_PITCH;
+    if (with_b) u = std::max(u, sizeof(float) * (size_t)t->n_b * ZL_PITCH);
+    return u + sizeof(float) * (size_t)t->n_blk * ZL_PITCH;
 }
 
 extern "C" int so4_forward32(const so4_tables *t, const so4_params *p, int natoms, const double *d_w_nb,
@@ -751,15 +871,15 @@ extern "C" int so4_adjoint_y32(const so4_tables *t, int natoms, const float *d_u
     if (natoms == 0) return SO4_OK;
     ZLArgs Z = zl_args(t, natoms);
     Z.utot = (const float2 *)d_utot;
-    Z.unit = t->d_yunit;
-    Z.seg = t->d_yseg;
-    Z.nunit = t->n_half;
+    Z.unit = t->d_wunit_y;
+    Z.seg = t->d_wseg_y;
+    Z.nunit = t->n_wunit_y;
     Z.beta = d_beta;
     Z.Y = (float2 *)d_y;
-    const size_t smz = sizeof(float2) * (size_t)t->n_u * ZL_PITCH + sizeof(float) * (size_t)t->n_blk * ZL_PITCH;
-    int rc = set_smem(k_zy32, smz);
+    const size_t smz = zw_smem_bytes(t, false);
+    int rc = set_smem(k_zw32<1>, smz);
     if (rc) return rc;
-    k_zy32<<<(natoms + 31) / 32, 256, smz, (cudaStream_t)stream>>>(Z);
+    k_zw32<1><<<(natoms + 31) / 32, 256, smz, (cudaStream_t)stream>>>(Z);
     so4_count_launch();
     return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
 }
@@ -1004,9 +1124,9 @@ extern "C" int so4_linear_by32(const so4_tables *t, int natoms, const float *d_u
     if (natoms == 0) return SO4_OK;
     ZLArgs Z = zl_args(t, natoms);
     Z.utot = (const float2 *)d_utot;
-    Z.unit = t->d_yunit;
-    Z.seg = t->d_yseg;
-    Z.nunit = t->n_half;
+    Z.unit = t->d_wunit_y;
+    Z.seg = t->d_wseg_y;
+    Z.nunit = t->n_wunit_y;
     Z.beta = d_beta;
     Z.Y = (float2 *)d_y;
     Z.x = d_x;
@@ -1014,12 +1134,10 @@ extern "C" int so4_linear_by32(const so4_tables *t, int natoms, const float *d_u
     Z.nbsec = t->n_bsec;
     Z.bc = d_bc;
     Z.eatom = d_eatom;
-    // U tiles + per-block coefficients; the epilogue reuses the U tiles for nB x 33 floats
-    const size_t smz = std::max(sizeof(float2) * (size_t)t->n_u, sizeof(float) * (size_t)t->n_b) * ZL_PITCH +
-                       sizeof(float) * (size_t)t->n_blk * ZL_PITCH;
-    int rc = set_smem(k_zby32, smz);
+    const size_t smz = zw_smem_bytes(t, true);
+    int rc = set_smem(k_zw32<2>, smz);
     if (rc) return rc;
-    k_zby32<<<(natoms + 31) / 32, 256, smz, (cudaStream_t)stream>>>(Z);
+    k_zw32<2><<<(natoms + 31) / 32, 256, smz, (cudaStream_t)stream>>>(Z);
     so4_count_launch();
     return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
 }

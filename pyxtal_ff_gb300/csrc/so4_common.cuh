@@ -127,9 +127,25 @@ struct so4_tables {
     int n_bsec = 0;
     //   JVP unit {k, seg0, seg1, 0},     JVP segment {t0, t1, half index of dU_lam[e], bits of fac_s w_e}
     int4 *d_junit = nullptr, *d_jseg = nullptr;
+    // window work lists (so4_zwin.cuh), most expensive unit first:
+    //   unit {lam | mb << 8 | ma0 << 16 | nk << 24, seg0, seg1, bits of u_norm[lam]}
+    //   segment {sub0, sub1, block, B-section position of entry ma0 or -1}
+    //   sub-segment {f1 | f2 << 16 (shared-memory offsets), Ca offset, steps, bits of Cb}
+    // wunit_y/wseg_y cover every half entry and every block (Y, and B in the fused
+    // path); wunit_b/wseg_b only the B-section entries and the B blocks.
+    int4 *d_wunit_y = nullptr, *d_wseg_y = nullptr, *d_wunit_b = nullptr, *d_wseg_b = nullptr;
+    int4 *d_wsub = nullptr;
+    float *d_wca = nullptr;
+    int n_wunit_y = 0, n_wunit_b = 0;
     int n_terms = 0;
     std::vector<int> term_ptr;
 };
+
+// Window Z contractions: entries per unit and the zero rows kept before and
+// after the U tiles in shared memory (a window may reach ZW_K - 1 entries past
+// either end of the full layout, always with a zero coefficient).
+constexpr int ZW_K = 4;
+constexpr int ZW_PAD = ZW_K - 1;
 
 // Table data every kernel stages into shared memory at start.
 struct SmallTables {

@@ -10,6 +10,7 @@
 #include <cstring>
 #include <string>
 #include <algorithm>
+#include <map>
 #include <utility>
 
 #include "so4_common.cuh"
@@ -97,6 +98,12 @@ void free_device(so4_tables *t) {
     cudaFree(t->d_yseg);
     cudaFree(t->d_bpos);
     cudaFree(t->d_junit);
+    cudaFree(t->d_wunit_y);
+    cudaFree(t->d_wseg_y);
+    cudaFree(t->d_wunit_b);
+    cudaFree(t->d_wseg_b);
+    cudaFree(t->d_wsub);
+    cudaFree(t->d_wca);
     cudaFree(t->d_jseg);
 }
 
@@ -415,6 +422,106 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
         junit.push_back(make_int4(k, s0, (int)jseg.size(), 0));
     }
 
+    // Window work lists.  For block (a, b, lam) with d = (a + b - lam) / 2, the Z entry
+    // (ma, mb) is (SO4.py:1042-1063)
+    //   sum_{mb1} Cb(mb, mb1) sum_{ma1} Ca(ma, ma1) U_a[ma1, mb1] U_b[ma + d - ma1, mb + d - mb1].
+    // A unit holds ZW_K consecutive entries ma0.. of one half row; per block and per mb1
+    // a sub-segment walks ma1 = lo .. hi (the union of the entries' ranges) with the
+    // U_b values of the ZW_K entries in a register ring.  Ca[j][k] = cg(a, lo + j, b,
+    // ma0 + k + d - lo - j), 0 outside the ranges; the Ca table of a (block, ma0) is
+    // shared by every row.
+    std::vector<int4> wunit_y, wseg_y, wunit_b, wseg_b, wsub;
+    std::vector<float> wca;
+    std::map<std::pair<int, int>, int> ca_off;  // (block, ma0) -> offset
+    auto cga_of = [&](const ZBlk &bk, int m1, int m2) {
+        const int cgbase = t->idxcg_block[b3(ld, bk.l1, bk.l2, bk.l)];
+        return t->cglist[cgbase + m1 * (bk.l2 + 1) + m2];
+    };
+    std::vector<std::pair<long, int>> wcy, wcb;
+    struct WUnit {
+        int lam, mb, ma0, nk;
+        int sy0, sy1, sb0, sb1;  // segments in wseg_y / wseg_b
+    };
+    std::vector<WUnit> wun;
+    std::vector<int4> segy_all, segb_all;
+    for (int lam = 0; lam < ld; ++lam)
+        for (int mb = 0; 2 * mb <= lam; ++mb)
+            for (int ma0 = 0; ma0 <= lam; ma0 += ZW_K) {
+                WUnit u;
+                u.lam = lam;
+                u.mb = mb;
+                u.ma0 = ma0;
+                u.nk = std::min(ZW_K, lam + 1 - ma0);
+                const int off0 = mb * (lam + 1) + ma0;
+                const bool in_bsec = off0 < section_count(lam);  // the unit's first entry is in the B section
+                long costy = 0, costb = 0;
+                u.sy0 = (int)segy_all.size();
+                u.sb0 = (int)segb_all.size();
+                for (int qq = yptr[lam]; qq < yptr[lam + 1]; ++qq) {
+                    const int bi = ylist[qq];
+                    const ZBlk &bk = blks[bi];
+                    const int a = bk.l1, b = bk.l2, d = (a + b - lam) / 2;
+                    const int lo = std::max(0, ma0 + d - b), hi = std::min(a, ma0 + ZW_K - 1 + d);
+                    const int S = hi - lo + 1;
+                    if (S <= 0) continue;
+                    auto key = std::make_pair(bi, ma0);
+                    if (!ca_off.count(key)) {
+                        ca_off[key] = (int)wca.size();
+                        for (int j = 0; j < S; ++j)
+                            for (int k = 0; k < ZW_K; ++k) {
+                                const int ma = ma0 + k, ma1 = lo + j, ma2 = ma + d - ma1;
+                                const bool ok = ma <= lam && ma2 >= 0 && ma2 <= b;
+                                wca.push_back(ok ? (float)cga_of(bk, ma1, ma2) : 0.f);
+                            }
+                    }
+                    const int s0 = (int)wsub.size();
+                    for (int mb1 = std::max(0, mb + d - b); mb1 <= std::min(a, mb + d); ++mb1) {
+                        const int mb2 = mb + d - mb1;
+                        const int f1 = (ZW_PAD + t->idxu_block[a] + mb1 * (a + 1) + lo) * 33;
+                        const int f2 = (ZW_PAD + t->idxu_block[b] + mb2 * (b + 1) + ma0 + d - lo) * 33;
+                        const float cb = (float)cga_of(bk, mb1, mb2);
+                        int cbits;
+                        std::memcpy(&cbits, &cb, sizeof cbits);
+                        wsub.push_back(make_int4(f1 | (f2 << 16), ca_off[key], S, cbits));
+                    }
+                    const int s1 = (int)wsub.size();
+                    const long c = (long)(s1 - s0) * (S * ZW_K + 8) + 8;
+                    const int k = blk_k[bi];
+                    const int bcode = (k >= 0 && in_bsec) ? bpos[k] + off0 : -1;
+                    segy_all.push_back(make_int4(s0, s1, bi, bcode));
+                    costy += c;
+                    if (bcode >= 0) {
+                        segb_all.push_back(make_int4(s0, s1, bi, bcode));
+                        costb += c;
+                    }
+                }
+                u.sy1 = (int)segy_all.size();
+                u.sb1 = (int)segb_all.size();
+                wcy.push_back({-costy, (int)wun.size()});
+                if (u.sb1 > u.sb0) wcb.push_back({-costb, (int)wun.size()});
+                wun.push_back(u);
+            }
+    std::stable_sort(wcy.begin(), wcy.end());
+    std::stable_sort(wcb.begin(), wcb.end());
+    for (int pass = 0; pass < 2; ++pass) {
+        auto &order = pass ? wcb : wcy;
+        auto &units = pass ? wunit_b : wunit_y;
+        auto &segs = pass ? wseg_b : wseg_y;
+        const auto &src = pass ? segb_all : segy_all;
+        for (auto &v : order) {
+            const WUnit &u = wun[v.second];
+            const float un = (float)t->unorm_l[u.lam];
+            int ubits;
+            std::memcpy(&ubits, &un, sizeof ubits);
+            const int q0 = pass ? u.sb0 : u.sy0, q1 = pass ? u.sb1 : u.sy1;
+            const int s0 = (int)segs.size();
+            for (int q = q0; q < q1; ++q) segs.push_back(src[q]);
+            units.push_back(make_int4(u.lam | (u.mb << 8) | (u.ma0 << 16) | (u.nk << 24), s0, (int)segs.size(), ubits));
+        }
+    }
+    t->n_wunit_y = (int)wunit_y.size();
+    t->n_wunit_b = (int)wunit_b.size();
+
     std::vector<int> fmap(t->n_u);
     for (int l = 0; l < ld; ++l)
         for (int mb = 0; mb <= l; ++mb)
@@ -437,6 +544,12 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
     if (!rc) rc = upload(&t->d_yunit, yunit);
     if (!rc) rc = upload(&t->d_yseg, yseg);
     if (!rc) rc = upload(&t->d_bpos, bpos);
+    if (!rc) rc = upload(&t->d_wunit_y, wunit_y);
+    if (!rc) rc = upload(&t->d_wseg_y, wseg_y);
+    if (!rc && !wunit_b.empty()) rc = upload(&t->d_wunit_b, wunit_b);
+    if (!rc && !wseg_b.empty()) rc = upload(&t->d_wseg_b, wseg_b);
+    if (!rc) rc = upload(&t->d_wsub, wsub);
+    if (!rc) rc = upload(&t->d_wca, wca);
     if (!rc) rc = upload(&t->d_junit, junit);
     if (!rc) rc = upload(&t->d_jseg, jseg);
     if (!rc) rc = upload(&t->d_cg64, t->cglist);
