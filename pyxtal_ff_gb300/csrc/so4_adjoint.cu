@@ -344,8 +344,65 @@ __global__ void __launch_bounds__(256) k_zby32(ZLArgs A) {
 // for the Z entries in a B section, w_e Re(conj(U_lam[e]) Z[e]) into the
 // entry-major scratch d_bc, then B_k = 2 sum over the section (compute_bi,
 // SO4.py:1071-1111) and, with d_eatom, beta . B per atom.
+// One window unit of K entries: Z of every block feeding its level; Y (MODE 1, 2)
+// and the B-section scratch (MODE 0, 2).
+template <int MODE, int K>
+__device__ __forceinline__ void zw_unit(const ZLArgs &A, const int4 un, const float2 *Ul, const float *coef, int a,
+                                        int lane) {
+    const int lam = un.x & 0xff, mb = (un.x >> 8) & 0xff, ma0 = (un.x >> 16) & 0xff;
+    const int off0 = mb * (lam + 1) + ma0;
+    const int cnt = section_count(lam);
+    float yr[K], yi[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) yr[k] = yi[k] = 0.f;
+    for (int q = un.y; q < un.z; ++q) {
+        const int4 sg = __ldg(A.seg + q);
+        float zr[K], zi[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) zr[k] = zi[k] = 0.f;
+        for (int r = sg.x; r < sg.y; ++r) zw_rows<K>(Ul, __ldg(A.wsub + r), A.wca, zr, zi);
+        if (MODE != 0) {
+            const float c = coef[sg.z * ZL_PITCH + lane];
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                yr[k] = fmaf(c, zr[k], yr[k]);
+                yi[k] = fmaf(c, zi[k], yi[k]);
+            }
+        }
+        if (MODE != 1 && sg.w >= 0 && a < A.natoms) {
+            const float2 *ul = Ul + (ZW_PAD + A.st.u_block[lam] + off0) * ZL_PITCH;
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                const int off = off0 + k;
+                if (off < cnt) {
+                    // scratch is entry-major, so the 32 lanes (atoms) store one contiguous line
+                    const float2 uv = ul[k * ZL_PITCH];
+                    const float v = uv.x * zr[k] + uv.y * zi[k];
+                    A.bc[(size_t)(sg.w + k) * A.natoms + a] = ((lam & 1) == 0 && off == cnt - 1) ? 0.5f * v : v;
+                }
+            }
+        }
+    }
+    if (MODE != 0 && a < A.natoms) {
+        const float un_l = __int_as_float(un.w);
+        float2 *Yo = A.Y + (size_t)a * A.nh + A.st.h_block[lam] + off0;
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const int ma = ma0 + k;
+            const float wmid = (2 * mb < lam) ? 1.f : ((2 * ma < lam) ? 1.f : ((2 * ma == lam) ? 0.5f : 0.f));
+            const float s = un_l * wmid;
+            Yo[k] = make_float2(s * yr[k], s * yi[k]);
+        }
+    }
+}
+
+// Window form of k_zb32 / k_zy32 / k_zby32 (so4_zwin.cuh), 32 atoms per CTA.
+// MODE 0: B only (units of the B sections, B blocks only); 1: Y only; 2: Y and,
+// for the Z entries in a B section, w_e Re(conj(U_lam[e]) Z[e]) into the
+// entry-major scratch d_bc, then B_k = 2 sum over the section (compute_bi,
+// SO4.py:1071-1111) and, with d_eatom, beta . B per atom.
 template <int MODE>
-__global__ void __launch_bounds__(256) k_zw32(ZLArgs A) {
+__global__ void __launch_bounds__(256, 2) k_zw32(ZLArgs A) {
     extern __shared__ __align__(16) float2 zw_smem[];
     __shared__ int s_unit;
     const int lane = threadIdx.x & 31;
@@ -371,55 +428,15 @@ __global__ void __launch_bounds__(256) k_zw32(ZLArgs A) {
     const float2 *Ul = Ub + lane;
     for (int u = zl_next(&s_unit); u < A.nunit; u = zl_next(&s_unit)) {
         const int4 un = __ldg(A.unit + u);
-        const int lam = un.x & 0xff, mb = (un.x >> 8) & 0xff, ma0 = (un.x >> 16) & 0xff, nk = un.x >> 24;
-        const int off0 = mb * (lam + 1) + ma0;
-        const int cnt = section_count(lam);
-        float yr[ZW_K], yi[ZW_K];
-        float2 ul[ZW_K];
-#pragma unroll
-        for (int k = 0; k < ZW_K; ++k) {
-            yr[k] = yi[k] = 0.f;
-            // U_lam of the unit's entries (the pad rows keep a short last unit in bounds)
-            ul[k] = (MODE != 1) ? Ul[(ZW_PAD + A.st.u_block[lam] + off0 + k) * ZL_PITCH] : make_float2(0.f, 0.f);
-        }
-        for (int q = un.y; q < un.z; ++q) {
-            const int4 sg = __ldg(A.seg + q);
-            float zr[ZW_K], zi[ZW_K];
-#pragma unroll
-            for (int k = 0; k < ZW_K; ++k) zr[k] = zi[k] = 0.f;
-            for (int r = sg.x; r < sg.y; ++r) zw_rows(Ul, __ldg(A.wsub + r), A.wca, zr, zi);
-            if (MODE != 0) {
-                const float c = coef[sg.z * ZL_PITCH + lane];
-#pragma unroll
-                for (int k = 0; k < ZW_K; ++k) {
-                    yr[k] = fmaf(c, zr[k], yr[k]);
-                    yi[k] = fmaf(c, zi[k], yi[k]);
-                }
-            }
-            if (MODE != 1 && sg.w >= 0 && a < A.natoms) {
-#pragma unroll
-                for (int k = 0; k < ZW_K; ++k) {
-                    const int off = off0 + k;
-                    if (k < nk && off < cnt) {
-                        // scratch is entry-major, so the 32 lanes (atoms) store one contiguous line
-                        const float v = ul[k].x * zr[k] + ul[k].y * zi[k];
-                        A.bc[(size_t)(sg.w + k) * A.natoms + a] = ((lam & 1) == 0 && off == cnt - 1) ? 0.5f * v : v;
-                    }
-                }
-            }
-        }
-        if (MODE != 0 && a < A.natoms) {
-            const float un_l = __int_as_float(un.w);
-            float2 *Yo = A.Y + (size_t)a * A.nh + A.st.h_block[lam] + off0;
-#pragma unroll
-            for (int k = 0; k < ZW_K; ++k) {
-                if (k < nk) {
-                    const int ma = ma0 + k;
-                    const float wmid = (2 * mb < lam) ? 1.f : ((2 * ma < lam) ? 1.f : ((2 * ma == lam) ? 0.5f : 0.f));
-                    const float s = un_l * wmid;
-                    Yo[k] = make_float2(s * yr[k], s * yi[k]);
-                }
-            }
+        switch (un.x >> 24) {
+            case 1: zw_unit<MODE, 1>(A, un, Ul, coef, a, lane); break;
+            case 2: zw_unit<MODE, 2>(A, un, Ul, coef, a, lane); break;
+            case 3: zw_unit<MODE, 3>(A, un, Ul, coef, a, lane); break;
+            case 4: zw_unit<MODE, 4>(A, un, Ul, coef, a, lane); break;
+            case 5: zw_unit<MODE, 5>(A, un, Ul, coef, a, lane); break;
+            case 6: zw_unit<MODE, 6>(A, un, Ul, coef, a, lane); break;
+            case 7: zw_unit<MODE, 7>(A, un, Ul, coef, a, lane); break;
+            default: zw_unit<MODE, 8>(A, un, Ul, coef, a, lane); break;
         }
     }
     if (MODE == 1) return;

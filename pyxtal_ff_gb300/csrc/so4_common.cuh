@@ -128,7 +128,7 @@ struct so4_tables {
     //   JVP unit {k, seg0, seg1, 0},     JVP segment {t0, t1, half index of dU_lam[e], bits of fac_s w_e}
     int4 *d_junit = nullptr, *d_jseg = nullptr;
     // window work lists (so4_zwin.cuh), most expensive unit first:
-    //   unit {lam | mb << 8 | ma0 << 16 | nk << 24, seg0, seg1, bits of u_norm[lam]}
+    //   unit {lam | mb << 8 | ma0 << 16 | K << 24, seg0, seg1, bits of u_norm[lam]}
     //   segment {sub0, sub1, block, B-section position of entry ma0 or -1}
     //   sub-segment {f1 | f2 << 16 (shared-memory offsets), Ca offset, steps, bits of Cb}
     // wunit_y/wseg_y cover every half entry and every block (Y, and B in the fused
@@ -141,11 +141,11 @@ struct so4_tables {
     std::vector<int> term_ptr;
 };
 
-// Window Z contractions: entries per unit and the zero rows kept before and
-// after the U tiles in shared memory (a window may reach ZW_K - 1 entries past
-// either end of the full layout, always with a zero coefficient).
-constexpr int ZW_K = 4;
-constexpr int ZW_PAD = ZW_K - 1;
+// Window Z contractions: most entries per unit, and the zero rows kept before
+// and after the U tiles in shared memory (a window may reach ZW_KMAX - 1 entries
+// past either end of the full layout, always with a zero coefficient).
+constexpr int ZW_KMAX = 8;
+constexpr int ZW_PAD = ZW_KMAX - 1;
 
 // Table data every kernel stages into shared memory at start.
 struct SmallTables {

@@ -424,16 +424,18 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
 
     // Window work lists.  For block (a, b, lam) with d = (a + b - lam) / 2, the Z entry
     // (ma, mb) is (SO4.py:1042-1063)
-    //   sum_{mb1} Cb(mb, mb1) sum_{ma1} Ca(ma, ma1) U_a[ma1, mb1] U_b[ma + d - ma1, mb + d - mb1].
-    // A unit holds ZW_K consecutive entries ma0.. of one half row; per block and per mb1
-    // a sub-segment walks ma1 = lo .. hi (the union of the entries' ranges) with the
-    // U_b values of the ZW_K entries in a register ring.  Ca[j][k] = cg(a, lo + j, b,
-    // ma0 + k + d - lo - j), 0 outside the ranges; the Ca table of a (block, ma0) is
-    // shared by every row.
+    //   sum_{mb1} Cb(mb, mb1) sum_{ma2} Ca(ma, ma2) U_a[ma + d - ma2, mb1] U_b[ma2, mb + d - mb1].
+    // A unit holds K <= ZW_KMAX consecutive entries ma0.. of one half row (rows longer
+    // than ZW_KMAX are cut into near-equal parts).  Per block and per mb1 a sub-segment
+    // walks ma2 = lo .. hi (the union of the entries' ranges, at most b + 1 <= a + 1
+    // values, so the smaller U is the one stepped) with the K values of U_a in a
+    // register ring.  Ca[j][k] = cg(a, ma0 + k + d - lo - j, b, lo + j), 0 outside the
+    // ranges, in rows of KP = K rounded up to 4 floats; the Ca table of a
+    // (block, ma0, K) is shared by every row.
     std::vector<int4> wunit_y, wseg_y, wunit_b, wseg_b, wsub;
     std::vector<float> wca;
-    std::map<std::pair<int, int>, int> ca_off;  // (block, ma0) -> offset
-    auto cga_of = [&](const ZBlk &bk, int m1, int m2) {
+    std::map<std::pair<int, int>, int> ca_off;  // (block, ma0) -> offset (K is fixed by lam and ma0)
+    auto cg_of = [&](const ZBlk &bk, int m1, int m2) {
         const int cgbase = t->idxcg_block[b3(ld, bk.l1, bk.l2, bk.l)];
         return t->cglist[cgbase + m1 * (bk.l2 + 1) + m2];
     };
@@ -444,15 +446,18 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
     };
     std::vector<WUnit> wun;
     std::vector<int4> segy_all, segb_all;
-    for (int lam = 0; lam < ld; ++lam)
+    for (int lam = 0; lam < ld; ++lam) {
+        const int n = lam + 1, ng = (n + ZW_KMAX - 1) / ZW_KMAX;
         for (int mb = 0; 2 * mb <= lam; ++mb)
-            for (int ma0 = 0; ma0 <= lam; ma0 += ZW_K) {
+            for (int g = 0, ma0 = 0; g < ng; ++g) {
                 WUnit u;
                 u.lam = lam;
                 u.mb = mb;
                 u.ma0 = ma0;
-                u.nk = std::min(ZW_K, lam + 1 - ma0);
-                const int off0 = mb * (lam + 1) + ma0;
+                u.nk = n / ng + (g < n % ng ? 1 : 0);
+                const int K = u.nk, KP = (K + 3) / 4 * 4;
+                ma0 += K;
+                const int off0 = mb * (lam + 1) + u.ma0;
                 const bool in_bsec = off0 < section_count(lam);  // the unit's first entry is in the B section
                 long costy = 0, costb = 0;
                 u.sy0 = (int)segy_all.size();
@@ -461,31 +466,32 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
                     const int bi = ylist[qq];
                     const ZBlk &bk = blks[bi];
                     const int a = bk.l1, b = bk.l2, d = (a + b - lam) / 2;
-                    const int lo = std::max(0, ma0 + d - b), hi = std::min(a, ma0 + ZW_K - 1 + d);
+                    const int lo = std::max(0, u.ma0 + d - a), hi = std::min(b, u.ma0 + K - 1 + d);
                     const int S = hi - lo + 1;
                     if (S <= 0) continue;
-                    auto key = std::make_pair(bi, ma0);
+                    auto key = std::make_pair(bi, u.ma0);
                     if (!ca_off.count(key)) {
                         ca_off[key] = (int)wca.size();
                         for (int j = 0; j < S; ++j)
-                            for (int k = 0; k < ZW_K; ++k) {
-                                const int ma = ma0 + k, ma1 = lo + j, ma2 = ma + d - ma1;
-                                const bool ok = ma <= lam && ma2 >= 0 && ma2 <= b;
-                                wca.push_back(ok ? (float)cga_of(bk, ma1, ma2) : 0.f);
+                            for (int k = 0; k < KP; ++k) {
+                                const int ma = u.ma0 + k, ma2 = lo + j, ma1 = ma + d - ma2;
+                                const bool ok = k < K && ma <= lam && ma1 >= 0 && ma1 <= a;
+                                wca.push_back(ok ? (float)cg_of(bk, ma1, ma2) : 0.f);
                             }
                     }
                     const int s0 = (int)wsub.size();
                     for (int mb1 = std::max(0, mb + d - b); mb1 <= std::min(a, mb + d); ++mb1) {
                         const int mb2 = mb + d - mb1;
-                        const int f1 = (ZW_PAD + t->idxu_block[a] + mb1 * (a + 1) + lo) * 33;
-                        const int f2 = (ZW_PAD + t->idxu_block[b] + mb2 * (b + 1) + ma0 + d - lo) * 33;
-                        const float cb = (float)cga_of(bk, mb1, mb2);
+                        // stepped: U_b[lo + j, mb2]; ring base: U_a[ma0 + d - lo, mb1]
+                        const int f1 = (ZW_PAD + t->idxu_block[b] + mb2 * (b + 1) + lo) * 33;
+                        const int f2 = (ZW_PAD + t->idxu_block[a] + mb1 * (a + 1) + u.ma0 + d - lo) * 33;
+                        const float cb = (float)cg_of(bk, mb1, mb2);
                         int cbits;
                         std::memcpy(&cbits, &cb, sizeof cbits);
                         wsub.push_back(make_int4(f1 | (f2 << 16), ca_off[key], S, cbits));
                     }
                     const int s1 = (int)wsub.size();
-                    const long c = (long)(s1 - s0) * (S * ZW_K + 8) + 8;
+                    const long c = (long)(s1 - s0) * (S * (6 * K + 8) + 12) + 16;
                     const int k = blk_k[bi];
                     const int bcode = (k >= 0 && in_bsec) ? bpos[k] + off0 : -1;
                     segy_all.push_back(make_int4(s0, s1, bi, bcode));
@@ -501,6 +507,7 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
                 if (u.sb1 > u.sb0) wcb.push_back({-costb, (int)wun.size()});
                 wun.push_back(u);
             }
+    }
     std::stable_sort(wcy.begin(), wcy.end());
     std::stable_sort(wcb.begin(), wcb.end());
     for (int pass = 0; pass < 2; ++pass) {

@@ -1,13 +1,13 @@
 // so4_zwin.cuh -- Z contractions by sliding windows, atoms across lanes.
 //
 // Same CTA layout as so4_zlanes.cuh (32 atoms per CTA, lane = atom, U tiles in
-// shared memory as Uf[entry][lane]), but a work unit computes ZW_K neighbouring
-// entries (ma0 .. ma0 + ZW_K - 1) of one row of a Z block together.  For block
-// (a, b, lam), d = (a + b - lam) / 2, and one row pair (mb1, mb2):
-//   Z[ma0 + k] += Cb sum_j Ca[j][k] U_a[lo + j, mb1] U_b[ma0 + k + d - lo - j, mb2].
-// Step j reads one U_a value and one new U_b value; the ZW_K U_b values in use sit
+// shared memory as Uf[entry][lane]), but a work unit computes K <= ZW_KMAX
+// neighbouring entries (ma0 .. ma0 + K - 1) of one row of a Z block together.
+// For block (a, b, lam), d = (a + b - lam) / 2, and one row pair (mb1, mb2):
+//   Z[ma0 + k] += Cb sum_j Ca[j][k] U_a[ma0 + k + d - lo - j, mb1] U_b[lo + j, mb2].
+// Step j reads one U_b value and one new U_a value; the K U_a values in use sit
 // in a register ring (entry k at step j is the one entry k - 1 had at step j - 1),
-// so each shared-memory load feeds up to ZW_K products instead of one.
+// so each shared-memory load feeds up to K products instead of one.
 #pragma once
 
 #include "so4_zlanes.cuh"
@@ -24,34 +24,43 @@ __device__ __forceinline__ void zw_load_utot(const float2 *__restrict__ utot, co
 }
 
 // One sub-segment {f1 | f2 << 16, Ca offset, steps S, bits of Cb}: adds
-// Cb sum_j Ca[j][k] U_a[f1 + j] U_b[f2 - j + k] to z[k] for this lane's atom
-// (offsets in Ub rows, pre-scaled by the pitch; Ul = Ub + lane).
+// Cb sum_j Ca[j][k] U_a[f2 - j + k] U_b[f1 + j] to z[k], k < K, for this lane's
+// atom (offsets in Ub rows, pre-scaled by the pitch; Ul = Ub + lane).  Ca rows
+// hold KP = K rounded up to 4 floats.
+template <int K>
 __device__ __forceinline__ void zw_rows(const float2 *Ul, const int4 hd, const float *__restrict__ ca,
-                                        float (&zr)[ZW_K], float (&zi)[ZW_K]) {
-    static_assert(ZW_K == 4, "Ca rows are loaded as one float4");
+                                        float (&zr)[K], float (&zi)[K]) {
+    constexpr int KQ = (K + 3) / 4;  // float4 loads per Ca row
     const int f1 = hd.x & 0xffff, f2 = (int)((unsigned)hd.x >> 16);
     const int S = hd.z;
     const float cb = __int_as_float(hd.w);
     const float4 *cw = reinterpret_cast<const float4 *>(ca + hd.y);
-    float2 R[ZW_K];
+    float2 R[K];
 #pragma unroll
-    for (int k = 1; k < ZW_K; ++k) R[k] = Ul[f2 + k * ZL_PITCH];
+    for (int k = 1; k < K; ++k) R[k] = Ul[f2 + k * ZL_PITCH];
     R[0] = make_float2(0.f, 0.f);
-    for (int j0 = 0; j0 < S; j0 += ZW_K) {
+    for (int j0 = 0; j0 < S; j0 += K) {
 #pragma unroll
-        for (int t = 0; t < ZW_K; ++t) {
+        for (int t = 0; t < K; ++t) {
             const int j = j0 + t;
             if (j < S) {
-                // ring slot of entry k at step j is (k - j) mod ZW_K; entry 0 is new
-                R[(ZW_K - t) % ZW_K] = Ul[f2 - j * ZL_PITCH];
+                // ring slot of entry k at step j is (k - j) mod K; entry 0 is new
+                R[(K - t) % K] = Ul[f2 - j * ZL_PITCH];
                 float2 u = Ul[f1 + j * ZL_PITCH];
                 u.x *= cb;
                 u.y *= cb;
-                const float4 c4 = __ldg(cw + j);
-                const float cc[4] = {c4.x, c4.y, c4.z, c4.w};
+                float cc[4 * KQ];
 #pragma unroll
-                for (int k = 0; k < ZW_K; ++k) {
-                    const float2 w = R[(k - t + ZW_K) % ZW_K];
+                for (int q = 0; q < KQ; ++q) {
+                    const float4 c4 = __ldg(cw + j * KQ + q);
+                    cc[4 * q] = c4.x;
+                    cc[4 * q + 1] = c4.y;
+                    cc[4 * q + 2] = c4.z;
+                    cc[4 * q + 3] = c4.w;
+                }
+#pragma unroll
+                for (int k = 0; k < K; ++k) {
+                    const float2 w = R[(k - t + K) % K];
                     const float pr = u.x * w.x - u.y * w.y;
                     const float pi = u.x * w.y + u.y * w.x;
                     zr[k] = fmaf(cc[k], pr, zr[k]);
