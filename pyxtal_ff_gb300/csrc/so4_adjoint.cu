@@ -191,12 +191,12 @@ struct ZLArgs {
     const ZBlk *blk;
     const int *yptr, *ylist;
     const float *beta;
-    const int *bpos;  // fused path: start of each component's B-section entries
+    const int *bpos;  // nB + 1: first B partial slot of each component
     int nbsec;
     SmallTables st;
     float *x;    // B out  (k_zb32, k_zby32)
     float2 *Y;   // Y out  (k_zy32, k_zby32)
-    float *bc;   // fused path: B-section contributions, entry-major [nbsec][natoms]
+    float *bc;   // B partial sums, slot-major [nbsec][natoms]
     float *eatom;  // fused path: sum_k beta_k B_k per atom (may be null)
     const int4 *wsub;  // window sub-segments
     const float *wca;  // window Ca rows
@@ -228,122 +228,6 @@ __global__ void __launch_bounds__(256) k_zb32(ZLArgs A) {
     }
 }
 
-// Y for 32 atoms per CTA: Y_lam[e] = u_norm w_mid sum_{blocks (a,b,lam)} coef_block Z_block[e]
-__global__ void __launch_bounds__(256) k_zy32(ZLArgs A) {
-    extern __shared__ __align__(16) float2 zl_smem[];
-    __shared__ int s_unit;
-    const int lane = threadIdx.x & 31;
-    const int a0 = blockIdx.x * 32;
-    float2 *Uf = zl_smem;
-    float *coef = (float *)(Uf + (size_t)A.nu * ZL_PITCH);  // [nblk][33]
-    if (threadIdx.x == 0) s_unit = 0;
-    zl_load_utot(A.utot, A.fmap, a0, A.natoms, A.nh, A.nu, Uf);
-    for (int idx = threadIdx.x; idx < 32 * A.nblk; idx += blockDim.x) {
-        const int l = idx / A.nblk, b = idx - l * A.nblk;
-        const int a = a0 + l;
-        float c = 0.f;
-        if (a < A.natoms) {
-            const ZBlk &bk = A.blk[b];
-            for (int r = 0; r < bk.nrole; ++r) c += (float)bk.role_f[r] * __ldg(A.beta + (size_t)a * A.nB + bk.role_k[r]);
-        }
-        coef[b * ZL_PITCH + l] = c;
-    }
-    __syncthreads();
-    for (int u = zl_next(&s_unit); u < A.nunit; u = zl_next(&s_unit)) {
-        const int4 un = __ldg(A.unit + u);
-        float yr = 0.f, yi = 0.f;
-        int4 sg = (un.y < un.z) ? __ldg(A.seg + un.y) : make_int4(0, 0, 0, 0);
-        for (int q = un.y; q < un.z; ++q) {
-            const int4 cur = sg;
-            if (q + 1 < un.z) sg = __ldg(A.seg + q + 1);
-            const float2 z = zl_entry(A.terms, cur.x, cur.y, Uf + lane);
-            const float c = coef[cur.z * ZL_PITCH + lane];
-            yr += c * z.x;
-            yi += c * z.y;
-        }
-        const float s = __int_as_float(un.w);
-        if (a0 + lane < A.natoms) A.Y[(size_t)(a0 + lane) * A.nh + un.x] = make_float2(s * yr, s * yi);
-    }
-}
-
-// Fused forward + Y for an energy linear in B (beta known before B): every Z entry
-// is computed once; it feeds Y as in k_zy32 and, when it lies in a B section, its
-// contribution w_e Re(conj(U_l[e]) Z[e]) goes to the atom's scratch row, which is
-// then summed per component in a fixed order: B_k = 2 sum_e (compute_bi, SO4.py:1071-1111).
-// The scratch is [entry][atom] (d_bc holds nbsec * natoms floats).
-__global__ void __launch_bounds__(256) k_zby32(ZLArgs A) {
-    extern __shared__ __align__(16) float2 zl_smem[];
-    __shared__ int s_unit;
-    const int lane = threadIdx.x & 31;
-    const int a0 = blockIdx.x * 32;
-    const int a = a0 + lane;
-    float2 *Uf = zl_smem;
-    float *coef = (float *)(Uf + (size_t)A.nu * ZL_PITCH);  // [nblk][33]
-    if (threadIdx.x == 0) s_unit = 0;
-    zl_load_utot(A.utot, A.fmap, a0, A.natoms, A.nh, A.nu, Uf);
-    for (int idx = threadIdx.x; idx < 32 * A.nblk; idx += blockDim.x) {
-        const int l = idx / A.nblk, b = idx - l * A.nblk;
-        const int aa = a0 + l;
-        float c = 0.f;
-        if (aa < A.natoms) {
-            const ZBlk &bk = A.blk[b];
-            for (int r = 0; r < bk.nrole; ++r) c += (float)bk.role_f[r] * __ldg(A.beta + (size_t)aa * A.nB + bk.role_k[r]);
-        }
-        coef[b * ZL_PITCH + l] = c;
-    }
-    __syncthreads();
-    const int ldim = A.st.twol + 1;
-    for (int u = zl_next(&s_unit); u < A.nunit; u = zl_next(&s_unit)) {
-        const int4 un = __ldg(A.unit + u);
-        const int lam = level_of(A.st.h_block, ldim, un.x);
-        const float2 ul = Uf[(A.st.u_block[lam] + un.x - A.st.h_block[lam]) * ZL_PITCH + lane];
-        float yr = 0.f, yi = 0.f;
-        int4 sg = (un.y < un.z) ? __ldg(A.seg + un.y) : make_int4(0, 0, 0, -1);
-        for (int q = un.y; q < un.z; ++q) {
-            const int4 cur = sg;
-            if (q + 1 < un.z) sg = __ldg(A.seg + q + 1);
-            const float2 z = zl_entry(A.terms, cur.x, cur.y, Uf + lane);
-            const float c = coef[cur.z * ZL_PITCH + lane];
-            yr += c * z.x;
-            yi += c * z.y;
-            if (cur.w >= 0 && a < A.natoms) {
-                // scratch is entry-major, so the 32 lanes (atoms) store one contiguous line
-                const float v = ul.x * z.x + ul.y * z.y;
-                A.bc[(size_t)(cur.w >> 1) * A.natoms + a] = (cur.w & 1) ? 0.5f * v : v;
-            }
-        }
-        const float s = __int_as_float(un.w);
-        if (a < A.natoms) A.Y[(size_t)a * A.nh + un.x] = make_float2(s * yr, s * yi);
-    }
-    __syncthreads();
-    // B_k, and beta_k B_k kept in shared memory (over the U tiles, no longer read) for the energy
-    float *eb = (float *)zl_smem;  // [nB][33]
-    for (int idx = threadIdx.x; idx < 32 * A.nB; idx += blockDim.x) {
-        const int k = idx >> 5, l = idx & 31;
-        const int aa = a0 + l;
-        float acc = 0.f, e = 0.f;
-        if (aa < A.natoms) {
-            for (int q = __ldg(A.bpos + k); q < __ldg(A.bpos + k + 1); ++q) acc += A.bc[(size_t)q * A.natoms + aa];
-            acc *= 2.f;
-            A.x[(size_t)aa * A.nB + k] = acc;
-            e = acc * __ldg(A.beta + (size_t)aa * A.nB + k);
-        }
-        eb[k * ZL_PITCH + l] = e;
-    }
-    if (A.eatom == nullptr) return;
-    __syncthreads();
-    if (threadIdx.x < 32 && a < A.natoms) {
-        float e = 0.f;
-        for (int k = 0; k < A.nB; ++k) e += eb[k * ZL_PITCH + threadIdx.x];
-        A.eatom[a] = e;
-    }
-}
-
-// Window form of k_zb32 / k_zy32 / k_zby32 (so4_zwin.cuh), 32 atoms per CTA.
-// MODE 0: B only (units of the B sections, B blocks only); 1: Y only; 2: Y and,
-// for the Z entries in a B section, w_e Re(conj(U_lam[e]) Z[e]) into the
-// entry-major scratch d_bc, then B_k = 2 sum over the section (compute_bi,
-// SO4.py:1071-1111) and, with d_eatom, beta . B per atom.
 // One window unit of K entries: Z of every block feeding its level; Y (MODE 1, 2)
 // and the B-section scratch (MODE 0, 2).
 template <int MODE, int K>
@@ -355,12 +239,21 @@ __device__ __forceinline__ void zw_unit(const ZLArgs &A, const int4 un, const fl
     float yr[K], yi[K];
 #pragma unroll
     for (int k = 0; k < K; ++k) yr[k] = yi[k] = 0.f;
+    // headers are prefetched one ahead: the next segment's and the next sub-segment's
+    // loads are in flight while the current one computes
+    int4 sgn = (un.y < un.z) ? __ldg(A.seg + un.y) : make_int4(0, 0, 0, -1);
     for (int q = un.y; q < un.z; ++q) {
-        const int4 sg = __ldg(A.seg + q);
+        const int4 sg = sgn;
+        if (q + 1 < un.z) sgn = __ldg(A.seg + q + 1);
         float zr[K], zi[K];
 #pragma unroll
         for (int k = 0; k < K; ++k) zr[k] = zi[k] = 0.f;
-        for (int r = sg.x; r < sg.y; ++r) zw_rows<K>(Ul, __ldg(A.wsub + r), A.wca, zr, zi);
+        int4 hdn = (sg.x < sg.y) ? __ldg(A.wsub + sg.x) : make_int4(0, 0, 0, 0);
+        for (int r = sg.x; r < sg.y; ++r) {
+            const int4 hd = hdn;
+            if (r + 1 < sg.y) hdn = __ldg(A.wsub + r + 1);
+            zw_rows<K>(Ul, hd, A.wca, zr, zi);
+        }
         if (MODE != 0) {
             const float c = coef[sg.z * ZL_PITCH + lane];
 #pragma unroll
@@ -369,18 +262,22 @@ __device__ __forceinline__ void zw_unit(const ZLArgs &A, const int4 un, const fl
                 yi[k] = fmaf(c, zi[k], yi[k]);
             }
         }
-        if (MODE != 1 && sg.w >= 0 && a < A.natoms) {
+        if (MODE != 1 && sg.w >= 0) {
+            // this unit's part of the B component of the block: sum over its entries in the
+            // B section of w_e Re(conj(U_lam[e]) Z[e]), w_e = 1/2 at the middle-row centre
             const float2 *ul = Ul + (ZW_PAD + A.st.u_block[lam] + off0) * ZL_PITCH;
+            float v = 0.f;
 #pragma unroll
             for (int k = 0; k < K; ++k) {
                 const int off = off0 + k;
                 if (off < cnt) {
-                    // scratch is entry-major, so the 32 lanes (atoms) store one contiguous line
                     const float2 uv = ul[k * ZL_PITCH];
-                    const float v = uv.x * zr[k] + uv.y * zi[k];
-                    A.bc[(size_t)(sg.w + k) * A.natoms + a] = ((lam & 1) == 0 && off == cnt - 1) ? 0.5f * v : v;
+                    const float d = uv.x * zr[k] + uv.y * zi[k];
+                    v += ((lam & 1) == 0 && off == cnt - 1) ? 0.5f * d : d;
                 }
             }
+            // scratch is slot-major, so the 32 lanes (atoms) store one contiguous line
+            if (a < A.natoms) A.bc[(size_t)sg.w * A.natoms + a] = v;
         }
     }
     if (MODE != 0 && a < A.natoms) {
@@ -396,13 +293,15 @@ __device__ __forceinline__ void zw_unit(const ZLArgs &A, const int4 un, const fl
     }
 }
 
+constexpr int ZW_THREADS = 256;  // 8 warps share one CTA's 32 atoms
+
 // Window form of k_zb32 / k_zy32 / k_zby32 (so4_zwin.cuh), 32 atoms per CTA.
 // MODE 0: B only (units of the B sections, B blocks only); 1: Y only; 2: Y and,
-// for the Z entries in a B section, w_e Re(conj(U_lam[e]) Z[e]) into the
-// entry-major scratch d_bc, then B_k = 2 sum over the section (compute_bi,
-// SO4.py:1071-1111) and, with d_eatom, beta . B per atom.
+// per (unit, B block), the unit's part of the section sum sum_e w_e Re(conj(U_lam[e]) Z[e])
+// into the slot-major scratch d_bc, then B_k = 2 x the sum of component k's slots in
+// a fixed order (compute_bi, SO4.py:1071-1111) and, with d_eatom, beta . B per atom.
 template <int MODE>
-__global__ void __launch_bounds__(256, 2) k_zw32(ZLArgs A) {
+__global__ void __launch_bounds__(ZW_THREADS, 2) k_zw32(ZLArgs A) {
     extern __shared__ __align__(16) float2 zw_smem[];
     __shared__ int s_unit;
     const int lane = threadIdx.x & 31;
@@ -896,7 +795,7 @@ extern "C" int so4_adjoint_y32(const so4_tables *t, int natoms, const float *d_u
     const size_t smz = zw_smem_bytes(t, false);
     int rc = set_smem(k_zw32<1>, smz);
     if (rc) return rc;
-    k_zw32<1><<<(natoms + 31) / 32, 256, smz, (cudaStream_t)stream>>>(Z);
+    k_zw32<1><<<(natoms + 31) / 32, ZW_THREADS, smz, (cudaStream_t)stream>>>(Z);
     so4_count_launch();
     return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
 }
@@ -1154,7 +1053,7 @@ extern "C" int so4_linear_by32(const so4_tables *t, int natoms, const float *d_u
     const size_t smz = zw_smem_bytes(t, true);
     int rc = set_smem(k_zw32<2>, smz);
     if (rc) return rc;
-    k_zw32<2><<<(natoms + 31) / 32, 256, smz, (cudaStream_t)stream>>>(Z);
+    k_zw32<2><<<(natoms + 31) / 32, ZW_THREADS, smz, (cudaStream_t)stream>>>(Z);
     so4_count_launch();
     return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
 }

@@ -119,17 +119,16 @@ struct so4_tables {
     int *d_fmap = nullptr;      // n_u: full entry -> half source | conj << 15 | negate << 14
     // work units of the atoms-across-lanes kernels, most expensive first:
     //   B unit {k, seg0, seg1, 0},       B segment {t0, t1, full index of U_l[e], weight 1 or 2 (= 1/2)}
-    //   Y unit {half e, seg0, seg1, bits of u_norm w_mid},  Y segment {t0, t1, block, code}
-    //   (code = 2 pos + half for an entry of a B section, pos into the fused path's row, else -1)
     int4 *d_bunit = nullptr, *d_bseg = nullptr;
-    int4 *d_yunit = nullptr, *d_yseg = nullptr;
-    int *d_bpos = nullptr;  // nB + 1: start of each component's B-section entries (fused path)
+    // B partial slots of the window kernels: one per (window unit, B block), component k
+    // owning slots [bpos[k], bpos[k + 1]) in row order
+    int *d_bpos = nullptr;  // nB + 1
     int n_bsec = 0;
     //   JVP unit {k, seg0, seg1, 0},     JVP segment {t0, t1, half index of dU_lam[e], bits of fac_s w_e}
     int4 *d_junit = nullptr, *d_jseg = nullptr;
     // window work lists (so4_zwin.cuh), most expensive unit first:
     //   unit {lam | mb << 8 | ma0 << 16 | K << 24, seg0, seg1, bits of u_norm[lam]}
-    //   segment {sub0, sub1, block, B-section position of entry ma0 or -1}
+    //   segment {sub0, sub1, block, B partial slot or -1}
     //   sub-segment {f1 | f2 << 16 (shared-memory offsets), Ca offset, steps, bits of Cb}
     // wunit_y/wseg_y cover every half entry and every block (Y, and B in the fused
     // path); wunit_b/wseg_b only the B-section entries and the B blocks.

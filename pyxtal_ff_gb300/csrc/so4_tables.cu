@@ -94,8 +94,6 @@ void free_device(so4_tables *t) {
     cudaFree(t->d_term_ptr);
     cudaFree(t->d_bunit);
     cudaFree(t->d_bseg);
-    cudaFree(t->d_yunit);
-    cudaFree(t->d_yseg);
     cudaFree(t->d_bpos);
     cudaFree(t->d_junit);
     cudaFree(t->d_wunit_y);
@@ -332,7 +330,7 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
     t->n_terms = (int)terms.size();
     auto zcost = [&](int jz) { return t->term_ptr[jz + 1] - t->term_ptr[jz]; };
     // B units: one per component k, a segment per summed entry of its block
-    std::vector<std::pair<long, int>> bc, yc;
+    std::vector<std::pair<long, int>> bc;
     for (int k = 0; k < t->n_b; ++k) {
         long c = 0;
         for (int e = 0; e < bent[k].cnt[0]; ++e) c += zcost(bent[k].z[0] + e);
@@ -351,50 +349,11 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
         }
         bunit.push_back(make_int4(k, s0, (int)bseg.size(), 0));
     }
-    // B component of each block (blocks with l >= l1), and the start of each component's
-    // B-section entries in the fused path's per-atom scratch row
-    std::vector<int> blk_k(t->n_blk, -1), bpos(t->n_b + 1, 0);
-    for (int k = 0; k < t->n_b; ++k) {
+    // B component of each block (blocks with l >= l1)
+    std::vector<int> blk_k(t->n_blk, -1);
+    for (int k = 0; k < t->n_b; ++k)
         for (int bi = 0; bi < t->n_blk; ++bi)
             if (blks[bi].z0 == bent[k].z[0]) blk_k[bi] = k;
-        bpos[k + 1] = bpos[k] + bent[k].cnt[0];
-    }
-    t->n_bsec = bpos[t->n_b];
-    // Y units: one per half-layout entry (lam, off), a segment per block (a, b, lam)
-    for (int lam = 0; lam < ld; ++lam)
-        for (int off = 0; off < (lam / 2 + 1) * (lam + 1); ++off) {
-            long c = 0;
-            for (int qq = yptr[lam]; qq < yptr[lam + 1]; ++qq) c += zcost(blks[ylist[qq]].z0 + off);
-            yc.push_back({-c, t->h_block[lam] + off});
-        }
-    std::stable_sort(yc.begin(), yc.end());
-    std::vector<int4> yunit, yseg;
-    for (auto &v : yc) {
-        const int e = v.second;
-        int lam = 0;
-        while (lam + 1 < ld && t->h_block[lam + 1] <= e) ++lam;
-        const int off = e - t->h_block[lam];
-        const int mb = off / (lam + 1), ma = off - mb * (lam + 1);
-        double wmid = 1.0;
-        if (2 * mb == lam) wmid = (2 * ma < lam) ? 1.0 : ((2 * ma == lam) ? 0.5 : 0.0);
-        const float scale = (float)(t->unorm_l[lam] * wmid);
-        int bits;
-        std::memcpy(&bits, &scale, sizeof bits);
-        const int s0 = (int)yseg.size();
-        for (int qq = yptr[lam]; qq < yptr[lam + 1]; ++qq) {
-            const int b = ylist[qq];
-            const int jz = blks[b].z0 + off;
-            // code of the B-section entry this Z value also feeds (fused linear path), or -1
-            int code = -1;
-            const int k = blk_k[b];
-            if (k >= 0 && off < bent[k].cnt[0]) {
-                const int half = ((lam % 2) == 0 && off == bent[k].cnt[0] - 1) ? 1 : 0;
-                code = 2 * (bpos[k] + off) + half;
-            }
-            if (wmid != 0.0 || code >= 0) yseg.push_back(make_int4(t->term_ptr[jz], t->term_ptr[jz + 1], b, code));
-        }
-        yunit.push_back(make_int4(e, s0, (int)yseg.size(), bits));
-    }
 
     // JVP units: one per component k, a segment per summed entry of each of its three sections
     std::vector<std::pair<long, int>> jc;
@@ -446,7 +405,22 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
     };
     std::vector<WUnit> wun;
     std::vector<int4> segy_all, segb_all;
+    // B partial slots: component k owns nbu(lam_k) consecutive slots, one per window
+    // unit of level lam_k that starts inside the B section, in (mb, ma0) order
+    std::vector<int> nbu(ld, 0);
     for (int lam = 0; lam < ld; ++lam) {
+        const int n = lam + 1, ng = (n + ZW_KMAX - 1) / ZW_KMAX;
+        for (int mb = 0; 2 * mb <= lam; ++mb)
+            for (int g = 0, ma0 = 0; g < ng; ++g) {
+                if (mb * (lam + 1) + ma0 < section_count(lam)) nbu[lam]++;
+                ma0 += n / ng + (g < n % ng ? 1 : 0);
+            }
+    }
+    std::vector<int> bpos(t->n_b + 1, 0);
+    for (int k = 0; k < t->n_b; ++k) bpos[k + 1] = bpos[k] + nbu[bent[k].lam[0]];
+    t->n_bsec = bpos[t->n_b];
+    for (int lam = 0; lam < ld; ++lam) {
+        int bu = 0;  // index of the next B-section unit of this level
         const int n = lam + 1, ng = (n + ZW_KMAX - 1) / ZW_KMAX;
         for (int mb = 0; 2 * mb <= lam; ++mb)
             for (int g = 0, ma0 = 0; g < ng; ++g) {
@@ -459,6 +433,7 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
                 ma0 += K;
                 const int off0 = mb * (lam + 1) + u.ma0;
                 const bool in_bsec = off0 < section_count(lam);  // the unit's first entry is in the B section
+                const int bslot = in_bsec ? bu++ : -1;
                 long costy = 0, costb = 0;
                 u.sy0 = (int)segy_all.size();
                 u.sb0 = (int)segb_all.size();
@@ -493,7 +468,7 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
                     const int s1 = (int)wsub.size();
                     const long c = (long)(s1 - s0) * (S * (6 * K + 8) + 12) + 16;
                     const int k = blk_k[bi];
-                    const int bcode = (k >= 0 && in_bsec) ? bpos[k] + off0 : -1;
+                    const int bcode = (k >= 0 && in_bsec) ? bpos[k] + bslot : -1;
                     segy_all.push_back(make_int4(s0, s1, bi, bcode));
                     costy += c;
                     if (bcode >= 0) {
@@ -508,8 +483,16 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
                 wun.push_back(u);
             }
     }
-    std::stable_sort(wcy.begin(), wcy.end());
-    std::stable_sort(wcb.begin(), wcb.end());
+    // order: by K (largest first), so the warps of a CTA, which take units in list order,
+    // mostly run the same K specialisation at a time (fewer instruction-cache misses);
+    // within one K, most expensive first
+    auto by_k_cost = [&](const std::pair<long, int> &x, const std::pair<long, int> &y) {
+        const int kx = wun[x.second].nk, ky = wun[y.second].nk;
+        if (kx != ky) return kx > ky;
+        return x.first < y.first;
+    };
+    std::stable_sort(wcy.begin(), wcy.end(), by_k_cost);
+    std::stable_sort(wcb.begin(), wcb.end(), by_k_cost);
     for (int pass = 0; pass < 2; ++pass) {
         auto &order = pass ? wcb : wcy;
         auto &units = pass ? wunit_b : wunit_y;
@@ -548,8 +531,6 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
     if (!rc) rc = upload(&t->d_term_ptr, t->term_ptr);
     if (!rc) rc = upload(&t->d_bunit, bunit);
     if (!rc) rc = upload(&t->d_bseg, bseg);
-    if (!rc) rc = upload(&t->d_yunit, yunit);
-    if (!rc) rc = upload(&t->d_yseg, yseg);
     if (!rc) rc = upload(&t->d_bpos, bpos);
     if (!rc) rc = upload(&t->d_wunit_y, wunit_y);
     if (!rc) rc = upload(&t->d_wseg_y, wseg_y);
