@@ -237,46 +237,63 @@ def main():
         device_step()
     torch.cuda.synchronize()
 
-    # ---- device-resident timed region
+    # ---- the step as one CUDA graph (SO4Calculator.capture): the headline, positions in HBM
+    step = calc.capture(batch, model)
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
     clocks = Clocks(local)
-    nev = len(stage_names) + 1
-    stage_ms = np.zeros(len(stage_names))
+    natoms = len(atoms)
     step_ms = []
     barrier()
     torch.cuda.synchronize()
-    launches0 = L.so4_launch_count()
     clocks.start()
+    for _ in range(args.steps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        step()
+        e1.record()
+        e1.synchronize()
+        step_ms.append(e0.elapsed_time(e1))
+    torch.cuda.synchronize()
+    barrier()
+    if not step.check():
+        raise RuntimeError("neighbour list outgrew the captured capacity")
+    launches = step.launches
+    t_dev = max_over_ranks(float(np.sum(step_ms)))
+    value = ws * natoms * args.steps / (t_dev * 1e-3)
+
+    # ---- the same step eagerly, stage by stage (kernel table and roofline; not the headline)
+    nev = len(stage_names) + 1
+    stage_ms = np.zeros(len(stage_names))
+    eager_ms = []
     for _ in range(args.steps):
         flush.zero_()
         ev = [torch.cuda.Event(enable_timing=True) for _ in range(nev)]
         device_step(ev)
         ev[-1].synchronize()
-        step_ms.append(ev[0].elapsed_time(ev[-1]))
+        eager_ms.append(ev[0].elapsed_time(ev[-1]))
         stage_ms += np.array([ev[i].elapsed_time(ev[i + 1]) for i in range(nev - 1)])
-    torch.cuda.synchronize()
-    barrier()
-    launches = (L.so4_launch_count() - launches0) // args.steps
-    t_dev = max_over_ranks(float(np.sum(step_ms)))
-    natoms = len(atoms)
-    value = ws * natoms * args.steps / (t_dev * 1e-3)
     stage_ms /= args.steps
     if args.quick:
         clocks.stop()
         if rank == 0:
             print(json.dumps({"quick": True, "value": value, "unit": "atoms/s", "ms_per_step": t_dev / args.steps,
+                              "eager_ms_per_step": float(np.mean(eager_ms)),
                               "stages_ms": dict(zip(stage_names, stage_ms.tolist())),
                               "gpu_launches": int(launches)}), flush=True)
         if ws > 1:
             dist.destroy_process_group()
         return
 
-    # ---- e2e through the public API, host buffers
+    # ---- e2e through the public API (the captured step), host buffers
     pos_host = torch.from_numpy(batch.positions.copy()).pin_memory()
     out_e = torch.empty(1, dtype=torch.float64).pin_memory()
     out_f = torch.empty((natoms, 3), dtype=torch.float64).pin_memory()
     out_s = torch.empty((1, 6), dtype=torch.float64).pin_memory()
     for _ in range(2):
-        calc.compute(batch, model, positions=pos_host)
+        step(pos_host)
     torch.cuda.synchronize()
     barrier()
     t_e2e = 0.0
@@ -284,17 +301,30 @@ def main():
         flush.zero_()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        res = calc.compute(batch, model, positions=pos_host)
+        res = step(pos_host)
         out_e.copy_(res["energy"], non_blocking=True)
         out_f.copy_(res["forces"], non_blocking=True)
         out_s.copy_(res["stress"], non_blocking=True)
         torch.cuda.synchronize()
         t_e2e += time.perf_counter() - t0
     t_e2e = max_over_ranks(t_e2e)
+    if not step.check():
+        raise RuntimeError("neighbour list outgrew the captured capacity")
     e2e = {"value": ws * natoms * args.steps / t_e2e, "unit": "atoms/s",
            "h2d_bytes_per_step": int(pos_host.numel() * 8),
            "d2h_bytes_per_step": int(out_e.numel() * 8 + out_f.numel() * 8 + out_s.numel() * 8),
-           "ms_per_step": 1e3 * t_e2e / args.steps}
+           "ms_per_step": 1e3 * t_e2e / args.steps, "api": "SO4Calculator.capture(batch, model)(positions)"}
+    # the uncaptured public call on the same host buffers, for reference
+    t_eager = 0.0
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r2 = calc.compute(batch, model, positions=pos_host)
+        out_f.copy_(r2["forces"], non_blocking=True)
+        torch.cuda.synchronize()
+        t_eager += time.perf_counter() - t0
+    e2e["uncaptured_compute_ms_per_step"] = 1e3 * t_eager / args.steps
 
     # ---- plain FP64 dB/dr path on the same structure + errors of the FP32 path
     coef_t = torch.as_tensor(coef, dtype=torch.float64, device=dev)
@@ -320,13 +350,17 @@ def main():
     clk = clocks.stop()  # sampled over the device, e2e and FP64 timed legs
     clk["window"] = "device + e2e + fp64 timed legs"
     stress64 = c64["stress"]  # rdxdr already carries 1/vol
-    res = calc.compute(batch, model)
+    res = {k: v.clone() for k, v in step(pos_host).items()}  # the captured (headline) step
+    torch.cuda.synchronize()
+    res_eager = calc.compute(batch, model)
+    graph_equals_eager = all(torch.equal(res[k], res_eager[k]) for k in ("energy", "forces", "virial", "x"))
     e64 = float((d64["x"].double() @ coef_t).sum())
     err = {"force_max_abs_eV_per_A": float((res["forces"] - c64["forces"]).abs().max()),
            "force_max_rel": float((res["forces"] - c64["forces"]).abs().max() / c64["forces"].abs().max()),
            "stress_max_abs_GPa": float((res["stress"] - stress64).abs().max()),
            "energy_rel": abs(float(res["energy"].sum()) - e64) / abs(e64),
-           "B_max_rel": float((res["x"].double() - d64["x"]).abs().max() / d64["x"].abs().max())}
+           "B_max_rel": float((res["x"].double() - d64["x"]).abs().max() / d64["x"].abs().max()),
+           "graph_bitwise_equals_uncaptured": bool(graph_equals_eager)}
     del d64, c64
     fp64 = {"ms_per_step": ms64, "atoms_per_s": ws * natoms / (ms64 * 1e-3),
             "speedup_fp32_adjoint_over_fp64_plain": ms64 / (t_dev / args.steps)}

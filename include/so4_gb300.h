@@ -141,8 +141,13 @@ int so4_nl_pairs(const so4_geom *d_geom, int nstruct, const int *d_atom_struct, 
                  int64_t *d_seq, int32_t *d_pair_img, int32_t *d_nsite, int32_t *d_img_pair,
                  int32_t *d_img_rev, void *d_work, size_t work_bytes, void *stream);
 
-/* One synchronising read of {total images, total pairs, status bits} after the
- * three passes (d_pair_ptr may be NULL after pass 1 only). */
+/* {total images, total pairs, status bits} after the three passes (d_pair_ptr may
+ * be NULL after pass 1 only), written to ((int *)d_work)[4..6]; with h_summary
+ * non-NULL also copied there by one synchronising read.  With h_summary NULL the
+ * call does not synchronise (for stream capture); the caller reads the three
+ * ints later, e.g. with the step's results.  When a capacity was exceeded (status
+ * bit SO4_ERR_CAPACITY) the call also empties every range of d_img_ptr and
+ * d_pair_ptr, so that work enqueued behind it reads no image out of bounds. */
 int so4_nl_summary(const int32_t *d_img_ptr, const int32_t *d_pair_ptr, int natoms, const void *d_work,
                    size_t work_bytes, void *stream, int *h_summary);
 
@@ -190,7 +195,8 @@ int so4_adjoint32(const so4_tables *t, const so4_params *p, int nstruct, const i
 /* The three stages so4_adjoint32 runs, for callers that keep their own buffers:
  *   so4_adjoint_y32      Y[natoms*idxu_half*2] f32 from U_tot and beta (atoms across lanes);
  *   so4_adjoint_deidrj32 g[nimg*3] f32 = dE/dr of every image (U and dU by the
- *                        recursion, contracted with Y);
+ *                        recursion, contracted with Y); nimg may be the capacity of
+ *                        d_g, the images being [0, d_img_ptr[natoms]);
  *   so4_adjoint_gather   forces[natoms*3] f64 = sum_m (g_m - g_rev(m)), the
  *                        per-structure virial[nstruct*9] f64 = sum_m r_m (x) g_m and,
  *                        when d_eatom and d_energy are both non-NULL, energy[nstruct] f64 =

@@ -14,6 +14,8 @@ order-1 PolynomialRegression, pyxtal_ff/models/polynomialregression.py:374).
 """
 from __future__ import annotations
 
+import ctypes as C
+
 import numpy as np
 import torch
 
@@ -122,6 +124,11 @@ class SO4Calculator:
             self._batch_key = batch
         return self
 
+    def capture(self, batch: Batch, model, headroom=1.25):
+        """The whole energy / forces / stress step of this batch layout as one CUDA graph
+        (see CapturedStep); call the result with new positions."""
+        return CapturedStep(self, batch, model, headroom=headroom)
+
     def neighbors(self, batch: Batch, positions):
         return engine.build_neighbors(positions, batch.cells, batch.pbc, batch.atom_ptr, self.rcut, device=self.device)
 
@@ -189,3 +196,98 @@ def contract_plain(x, dxdr, rdxdr, seq, pair_ptr, atom_ptr, beta, volumes):
     energy = torch.zeros(len(atom_ptr) - 1, dtype=torch.float64, device=dev).index_add_(
         0, struct, (beta.double() * x.double()).sum(-1))
     return dict(forces=forces, stress=stress, energy=energy)
+
+
+class CapturedStep:
+    """Energy, forces and stress of one batch layout as a single CUDA graph replay.
+
+    For a LinearModel and fixed cells / pbc / atom ranges (an MD or relaxation loop
+    moves only the positions), the whole step -- the three neighbour-list passes,
+    U_tot, the fused B + Y pass, the per-image dE/dr and the gather, then the
+    per-structure constant and the stress -- is captured once into a CUDA graph on
+    static device buffers; a step copies the positions in and replays it, with no
+    host synchronisation and no per-kernel launch cost.
+
+    The image / pair buffers have a fixed capacity (the counts of the structure at
+    capture time plus `headroom`); the true counts are only known on the device.
+    `check()` reads them (one small synchronising copy) and returns False when the
+    neighbour list outgrew the buffers, after which the step must be captured again
+    (`SO4Calculator.capture`); it raises for non-finite positions like the eager path.
+    """
+
+    def __init__(self, calc: "SO4Calculator", batch: Batch, model: LinearModel, headroom=1.25):
+        if not isinstance(model, LinearModel):
+            raise TypeError("graph capture covers the linear model (beta = dE/dB fixed)")
+        calc.prepare(batch)
+        dev = calc.device
+        self.calc, self.batch = calc, batch
+        self.layout = engine.layout(batch.cells, batch.pbc, batch.atom_ptr, calc.rcut, dev)
+        lay = self.layout
+        N, S = lay.natoms, lay.nstruct
+        self.pos = torch.from_numpy(np.ascontiguousarray(batch.positions, dtype=np.float64)).to(dev)
+        # learn the counts at capture time, then size the buffers with headroom
+        nb0 = engine.build_neighbors(self.pos, batch.cells, batch.pbc, batch.atom_ptr, calc.rcut, device=dev)
+        self.cap_m = int(nb0.nimg * headroom) + 64
+        self.cap_p = int(nb0.npair * headroom) + 64 + N
+        del nb0
+        self.nl = engine.NeighborBuffers.allocate(lay, self.cap_m, self.cap_p, dev)
+        L = engine.lib()
+        tab = calc.tables
+        self.ws = torch.empty(L.so4_linear_workspace_size(tab.handle, N, self.cap_m), dtype=torch.uint8, device=dev)
+        self.beta = model.coef.detach()[calc._species].to(torch.float32).contiguous()
+        self.bias_s = (calc._counts @ model.bias.detach().double()).contiguous()
+        self.x = torch.empty((max(N, 1), tab.nB), dtype=torch.float32, device=dev)
+        self.forces = torch.empty((max(N, 1), 3), dtype=torch.float64, device=dev)
+        self.virial = torch.empty((max(S, 1), 3, 3), dtype=torch.float64, device=dev)
+        self.energy_sum = torch.empty(max(S, 1), dtype=torch.float64, device=dev)
+        self.energy = torch.empty(max(S, 1), dtype=torch.float64, device=dev)
+        self.stress = torch.empty((max(S, 1), 6), dtype=torch.float64, device=dev)
+        self._voigt = torch.tensor(VOIGT, device=dev)  # on the device before capture (no copies inside it)
+        self.launches = 0
+        # eager warm-up on a side stream (sets kernel attributes, lets torch's allocator settle)
+        side = torch.cuda.Stream(device=dev)
+        side.wait_stream(torch.cuda.current_stream(dev))
+        with torch.cuda.stream(side):
+            self._enqueue()
+        torch.cuda.current_stream(dev).wait_stream(side)
+        torch.cuda.synchronize(dev)
+        self.graph = torch.cuda.CUDAGraph()
+        c0 = L.so4_launch_count()
+        with torch.cuda.graph(self.graph):
+            self._enqueue()
+        self.launches = int(L.so4_launch_count() - c0)  # kernels of this library in one replay
+
+    def _enqueue(self):
+        lay, calc, tab, L = self.layout, self.calc, self.calc.tables, engine.lib()
+        engine.enqueue_neighbors(lay, self.pos, self.nl)
+        b = self.nl
+        _p = engine._ptr
+        check = engine.check
+        check(L.so4_adjoint_linear32(tab.handle, C.byref(calc.params), lay.nstruct, _p(lay.atom_struct),
+                                     _p(lay.atom_ptr_dev), lay.natoms, _p(calc._w_nb), _p(calc._w_site),
+                                     _p(b.img_ptr), _p(b.img_j), _p(b.img_r), _p(b.img_rev), self.cap_m,
+                                     _p(self.beta), _p(self.x), _p(self.forces), _p(self.virial),
+                                     _p(self.energy_sum), _p(self.ws), self.ws.numel(), engine._stream()),
+              "so4_adjoint_linear32")
+        S = lay.nstruct
+        torch.add(self.energy_sum[:S], self.bias_s, out=self.energy[:S])
+        # same operations as the uncaptured path, so the two agree bit for bit
+        self.stress[:S].copy_(-(self.virial[:S].reshape(S, 9)[:, self._voigt] / self.calc._vol[:, None]) * EV_A3_TO_GPA)
+
+    def __call__(self, positions=None):
+        """One step; positions (N,3) f64 from the host (pinned for an asynchronous copy)
+        or the device, or None to reuse the last ones.  Returns views of the static
+        outputs (valid until the next call)."""
+        if positions is not None:
+            if isinstance(positions, np.ndarray):
+                positions = torch.from_numpy(np.ascontiguousarray(positions, dtype=np.float64))
+            self.pos.copy_(positions, non_blocking=True)
+        self.graph.replay()
+        N, S = self.layout.natoms, self.layout.nstruct
+        return dict(energy=self.energy[:S], forces=self.forces[:N], virial=self.virial[:S], stress=self.stress[:S],
+                    x=self.x[:N])
+
+    def check(self):
+        """True if the last step's neighbour list fitted its buffers (raises on bad input)."""
+        M, P, bits = [int(v) for v in self.nl.summary_dev().cpu()]
+        return engine.check_summary(M, P, bits, self.cap_m, self.cap_p)

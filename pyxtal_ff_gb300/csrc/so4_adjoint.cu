@@ -54,10 +54,7 @@ size_t carve_adj(AdjWork &w, void *base, int natoms, int nh, int64_t nimg) {
 
 template <typename K>
 int set_smem(K kern, size_t smem) {
-    if (smem > 227 * 1024) return SO4_ERR_UNSUPPORTED;
-    if (smem > 48 * 1024)
-        SO4_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    return SO4_OK;
+    return so4_set_smem((const void *)kern, smem);
 }
 
 struct FwdArgs {
@@ -447,7 +444,8 @@ __global__ void __launch_bounds__(256) k_deidrj_rc(DArgs A, int64_t nimg) {
     const int64_t wg = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int grp = lane / RC::NCH, mb = lane - grp * RC::NCH;
     const int64_t m = wg * RC::IPW + grp;
-    const bool valid = (grp < RC::IPW) && (m < nimg);
+    // nimg may be a capacity: the images are [0, img_ptr[natoms])
+    const bool valid = (grp < RC::IPW) && (m < nimg) && (m < (int64_t)__ldg(A.img_ptr + A.natoms));
     float x = 1.f, y = 0.f, z = 0.f, wj = 0.f;
     int centre = 0;
     if (valid) {

@@ -404,3 +404,7 @@ __host__ __device__ __forceinline__ int section_count(int lam) {
 
 // number of kernels this library has launched (so4_launch_count)
 void so4_count_launch(int n = 1);
+// Raise a kernel's dynamic shared-memory limit to at least smem bytes on the current
+// device.  The attribute is set only when the limit grows, so launches after the
+// first make no runtime call besides the launch (safe inside stream capture).
+int so4_set_smem(const void *kern, size_t smem);

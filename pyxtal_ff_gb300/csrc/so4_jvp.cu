@@ -18,10 +18,7 @@ namespace {
 
 template <typename K>
 int set_smem_j(K kern, size_t smem) {
-    if (smem > 227 * 1024) return SO4_ERR_UNSUPPORTED;
-    if (smem > 48 * 1024)
-        SO4_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    return SO4_OK;
+    return so4_set_smem((const void *)kern, smem);
 }
 
 struct JArgs {

@@ -193,6 +193,16 @@ __global__ void k_summary(const int32_t *img_ptr, const int32_t *pair_ptr, int n
     out[2] = *status;
 }
 
+// After the summary has recorded the true totals: if a capacity was exceeded (or an
+// offset did not fit), empty every image and pair range, so that kernels enqueued
+// behind the list without a host check (a captured step) read nothing out of bounds.
+__global__ void k_clamp(int32_t *img_ptr, int32_t *pair_ptr, int natoms, const int *status) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i > natoms || !(*status & (1 << SO4_ERR_CAPACITY))) return;
+    img_ptr[i] = 0;
+    if (pair_ptr) pair_ptr[i] = 0;
+}
+
 // One warp per centre.  MODE 0: count images into w.cnt.  MODE 1: write the
 // packed (j, o) keys into w.keys[img_ptr[a] ...] (unsorted; slots are taken with
 // a shared-memory counter, the order is fixed later by k_sort).
@@ -386,6 +396,8 @@ __global__ void k_rev(const int *astruct, int natoms, const int32_t *img_ptr, co
                       const int32_t *img_off, const int32_t *img_pair, int64_t nimg, const int64_t *seq,
                       const so4_geom *geom, int32_t *img_rev, NLWork w) {
     const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    // after an overflow the pair arrays are incomplete: nothing here may be read
+    if (*(volatile int *)w.status & (1 << SO4_ERR_CAPACITY)) return;
     if (m >= nimg || m >= img_ptr[natoms]) return;
     const int j = img_j[m];
     const int p = img_pair[m];
@@ -587,11 +599,15 @@ extern "C" int so4_status_read(const void *d_work, size_t work_bytes, void *stre
 
 extern "C" int so4_nl_summary(const int32_t *d_img_ptr, const int32_t *d_pair_ptr, int natoms, const void *d_work,
                               size_t work_bytes, void *stream, int *h_summary) {
-    if (!d_work || !h_summary || work_bytes < SO4_WS_HEADER || natoms < 0) return SO4_ERR_ARG;
+    if (!d_work || work_bytes < SO4_WS_HEADER || natoms < 0) return SO4_ERR_ARG;
     cudaStream_t st = (cudaStream_t)stream;
     int *dev = (int *)d_work + 4;  // header scratch after the status word
     k_summary<<<1, 1, 0, st>>>(d_img_ptr, d_pair_ptr, natoms, (const int *)d_work, dev);
     so4_count_launch();
+    k_clamp<<<(natoms + 256) / 256, 256, 0, st>>>((int32_t *)d_img_ptr, (int32_t *)d_pair_ptr, natoms,
+                                                  (const int *)d_work);
+    so4_count_launch();
+    if (!h_summary) return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
     SO4_CUDA_TRY(cudaMemcpyAsync(h_summary, dev, 3 * sizeof(int), cudaMemcpyDeviceToHost, st));
     SO4_CUDA_TRY(cudaStreamSynchronize(st));
     return SO4_OK;

@@ -202,7 +202,8 @@ size_t plain_smem_bytes(const so4_tables *t, int NW) {
 template <typename T, int NW, int KS>
 int launch_plain(const PlainArgs<T> &A, size_t smem, cudaStream_t st) {
     auto kern = k_plain<T, NW, KS>;
-    if (smem > 48 * 1024) SO4_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int rc = so4_set_smem((const void *)kern, smem);
+    if (rc) return rc;
     kern<<<A.natoms, NW * 32, smem, st>>>(A);
     so4_count_launch();
     return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;

@@ -595,6 +595,37 @@ extern "C" int so4_tables_export(const so4_tables *t, double *cg, int *idxb, int
 extern "C" const char *so4_version(void) { return "so4_gb300 0.1.0 (sm_103a)"; }
 
 #include <atomic>
+#include <mutex>
 static std::atomic<long long> g_launches{0};
+
+namespace {
+struct SmemLimit {
+    const void *kern;
+    int dev;
+    size_t bytes;
+};
+std::mutex g_smem_mu;
+std::vector<SmemLimit> g_smem;
+}  // namespace
+
+int so4_set_smem(const void *kern, size_t smem) {
+    if (smem > 227 * 1024) return SO4_ERR_UNSUPPORTED;
+    if (smem <= 48 * 1024) return SO4_OK;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return SO4_ERR_CUDA;
+    std::lock_guard<std::mutex> lock(g_smem_mu);
+    for (auto &e : g_smem)
+        if (e.kern == kern && e.dev == dev) {
+            if (e.bytes >= smem) return SO4_OK;
+            if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+                return SO4_ERR_CUDA;
+            e.bytes = smem;
+            return SO4_OK;
+        }
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return SO4_ERR_CUDA;
+    g_smem.push_back({kern, dev, smem});
+    return SO4_OK;
+}
 void so4_count_launch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 extern "C" long long so4_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }

@@ -130,6 +130,128 @@ def geometry(cells, pbc, atom_ptr, rcut):
 
 
 _NL_CAPACITY = {}  # (natoms, nbins, rcut) -> (image capacity, pair capacity) seen last time
+_LAYOUTS = {}      # batch layout -> device copies of its geometry (read-only, shared)
+
+
+@dataclass
+class Layout:
+    """What the neighbour list needs of a batch besides the positions, on the device."""
+    natoms: int
+    nstruct: int
+    atom_ptr: np.ndarray
+    vol: np.ndarray
+    geom: torch.Tensor
+    nbins: int
+    atom_struct: torch.Tensor
+    atom_ptr_dev: torch.Tensor
+    rcut: float
+
+
+def layout(cells, pbc, atom_ptr, rcut, device="cuda"):
+    """Geometry of a batch (cells, pbc, atom ranges) uploaded once per distinct layout."""
+    dev = torch.device(device)
+    cells = np.ascontiguousarray(np.asarray(cells, dtype=np.float64).reshape(-1, 3, 3))
+    pbc = np.ascontiguousarray(np.asarray(pbc, dtype=np.int32).reshape(-1, 3))
+    atom_ptr = np.ascontiguousarray(np.asarray(atom_ptr, dtype=np.int64))
+    key = (str(dev), float(rcut), cells.tobytes(), pbc.tobytes(), atom_ptr.tobytes())
+    lay = _LAYOUTS.get(key)
+    if lay is not None:
+        return lay
+    N, S = int(atom_ptr[-1]), len(atom_ptr) - 1
+    raw, vol, nbins = geometry(cells, pbc, atom_ptr, rcut)
+    counts = np.diff(atom_ptr)
+    lay = Layout(N, S, atom_ptr, vol, torch.from_numpy(raw.copy()).to(dev), nbins,
+                 torch.from_numpy(np.repeat(np.arange(S, dtype=np.int32), counts)).to(dev),
+                 torch.from_numpy(atom_ptr.astype(np.int32)).to(dev), float(rcut))
+    if len(_LAYOUTS) >= 16:
+        _LAYOUTS.pop(next(iter(_LAYOUTS)))
+    _LAYOUTS[key] = lay
+    return lay
+
+
+@dataclass
+class NeighborBuffers:
+    """Device arrays of one neighbour list with room for cap_m images and cap_p pairs."""
+    cap_m: int
+    cap_p: int
+    ws: torch.Tensor
+    img_ptr: torch.Tensor
+    img_j: torch.Tensor
+    img_off: torch.Tensor
+    img_r: torch.Tensor
+    pair_ptr: torch.Tensor
+    seq: torch.Tensor
+    pair_img: torch.Tensor
+    nsite: torch.Tensor
+    img_pair: torch.Tensor
+    img_rev: torch.Tensor
+
+    @staticmethod
+    def allocate(lay: Layout, cap_m, cap_p, device, workspace=None):
+        dev, N = torch.device(device), lay.natoms
+        ws_bytes = lib().so4_nl_workspace_size(N, lay.nbins, cap_m)
+        ws = workspace if (workspace is not None and workspace.numel() >= ws_bytes) else \
+            torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
+        i32 = dict(dtype=torch.int32, device=dev)
+        return NeighborBuffers(cap_m, cap_p, ws, torch.empty(N + 1, **i32), torch.empty(cap_m, **i32),
+                               torch.empty((cap_m, 3), **i32), torch.empty((cap_m, 3), dtype=torch.float64, device=dev),
+                               torch.empty(N + 1, **i32), torch.empty((cap_p, 2), dtype=torch.int64, device=dev),
+                               torch.empty(cap_p + 1, **i32), torch.empty(max(N, 1), **i32),
+                               torch.empty(cap_m, **i32), torch.empty(cap_m, **i32))
+
+    def summary_dev(self):
+        """The device copy of {images, pairs, status bits} that enqueue_neighbors leaves."""
+        return self.ws[16:28].view(torch.int32)
+
+
+def enqueue_neighbors(lay: Layout, pos, bufs: NeighborBuffers, summary=None):
+    """Launch the three neighbour-list passes for positions pos (N,3) f64 on the device
+    into bufs, and the summary; with summary (a ctypes int[3]) the call waits and
+    fills it, else nothing synchronises (the summary stays on the device)."""
+    L, st, N, S = lib(), _stream(), lay.natoms, lay.nstruct
+    b = bufs
+    check(L.so4_nl_count(_ptr(lay.geom), S, lay.nbins, _ptr(pos), _ptr(lay.atom_struct), N, lay.rcut,
+                         _ptr(b.img_ptr), _ptr(b.ws), b.ws.numel(), st), "so4_nl_count")
+    check(L.so4_nl_fill(_ptr(lay.geom), S, lay.nbins, _ptr(pos), _ptr(lay.atom_struct), N, lay.rcut, _ptr(b.img_ptr),
+                        b.cap_m, _ptr(b.img_j), _ptr(b.img_off), _ptr(b.img_r), _ptr(b.pair_ptr), _ptr(b.ws),
+                        b.ws.numel(), st), "so4_nl_fill")
+    check(L.so4_nl_pairs(_ptr(lay.geom), S, _ptr(lay.atom_struct), N, _ptr(b.img_ptr), b.cap_m, _ptr(b.img_j),
+                         _ptr(b.img_off), _ptr(b.pair_ptr), b.cap_p, _ptr(b.seq), _ptr(b.pair_img), _ptr(b.nsite),
+                         _ptr(b.img_pair), _ptr(b.img_rev), _ptr(b.ws), b.ws.numel(), st), "so4_nl_pairs")
+    check(L.so4_nl_summary(_ptr(b.img_ptr), _ptr(b.pair_ptr), N, _ptr(b.ws), b.ws.numel(), st, summary),
+          "so4_nl_summary")
+
+
+def check_summary(M, P, bits, cap_m=None, cap_p=None):
+    """False if a neighbour list overflowed its buffers; else raise for its status bits
+    (non-finite positions, an offset beyond the encodable range, an asymmetric list)."""
+    if (cap_m is not None and M > cap_m) or (cap_p is not None and P > cap_p):
+        return False
+    if bits & (1 << _lib.SO4_ERR_NONFINITE):
+        raise ValueError("positions contain NaN or Inf")
+    for code in (_lib.SO4_ERR_CAPACITY, _lib.SO4_ERR_REVERSE):  # capacity here: an image offset beyond 511 cells
+        if bits & (1 << code):
+            raise _lib.SO4Error(code, "neighbour list")
+    return True
+
+
+def capacity_for(lay: Layout):
+    """Image / pair capacity for a layout: the last count seen with 10 % room, else 64 per atom."""
+    N = lay.natoms
+    return _NL_CAPACITY.get((N, lay.nbins, lay.rcut), (max(64 * N, 1), max(64 * N, 1) + N))
+
+
+def note_capacity(lay: Layout, M, P):
+    _NL_CAPACITY[(lay.natoms, lay.nbins, lay.rcut)] = (max(int(M * 1.1) + 16, 1), max(int(P * 1.1) + 16, 1))
+
+
+def neighbors_view(lay: Layout, b: NeighborBuffers, M, P, bits=0):
+    """A Neighbors record over buffers b holding M images and P pairs (M, P may be the
+    capacities when the true counts are still on the device)."""
+    return Neighbors(lay.natoms, lay.nstruct, M, P, lay.atom_ptr, lay.vol, lay.geom, lay.nbins, lay.atom_struct,
+                     lay.atom_ptr_dev, b.img_ptr, b.img_j[:M], b.img_off[:M], b.img_r[:M], b.pair_ptr, b.seq[:P],
+                     b.pair_img[: P + 1], b.nsite[: lay.natoms], b.img_pair[:M], b.img_rev[:M],
+                     bool(bits & (1 << _lib.SO4_ERR_NO_NEIGHBOR)))
 
 
 def build_neighbors(pos, cells, pbc, atom_ptr, rcut, device="cuda", workspace=None):
@@ -139,62 +261,26 @@ def build_neighbors(pos, cells, pbc, atom_ptr, rcut, device="cuda", workspace=No
     The image and pair arrays are sized from the counts of the previous call with
     the same shape (a first call uses an estimate); one synchronising read returns
     the true totals and the status, and an undersized call is repeated with room."""
-    L = lib()
     dev = torch.device(device)
     if not isinstance(pos, torch.Tensor):
         pos = torch.from_numpy(np.ascontiguousarray(pos, dtype=np.float64))
     pos = pos.to(dev, dtype=torch.float64).contiguous()
-    atom_ptr = np.asarray(atom_ptr, dtype=np.int64)
-    N, S = int(atom_ptr[-1]), len(atom_ptr) - 1
-    if pos.shape != (N, 3):
+    lay = layout(cells, pbc, atom_ptr, rcut, dev)
+    if pos.shape != (lay.natoms, 3):
         raise ValueError("positions must be (N,3) for N = atom_ptr[-1]")
-    raw, vol, nbins = geometry(cells, pbc, atom_ptr, rcut)
-    geom = torch.from_numpy(raw.copy()).to(dev)
-    counts = np.diff(atom_ptr)
-    atom_struct = torch.from_numpy(np.repeat(np.arange(S, dtype=np.int32), counts)).to(dev)
-    atom_ptr_dev = torch.from_numpy(atom_ptr.astype(np.int32)).to(dev)
-    st = _stream()
-    key = (N, nbins, float(rcut))
-    cap_m, cap_p = _NL_CAPACITY.get(key, (max(64 * N, 1), max(64 * N, 1) + N))
+    cap_m, cap_p = capacity_for(lay)
     summary = (C.c_int * 3)()
     for _attempt in range(3):
-        ws_bytes = L.so4_nl_workspace_size(N, nbins, cap_m)
-        ws = workspace if (workspace is not None and workspace.numel() >= ws_bytes) else \
-            torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
-        img_ptr = torch.empty(N + 1, dtype=torch.int32, device=dev)
-        check(L.so4_nl_count(_ptr(geom), S, nbins, _ptr(pos), _ptr(atom_struct), N, float(rcut), _ptr(img_ptr),
-                             _ptr(ws), ws.numel(), st), "so4_nl_count")
-        img_j = torch.empty(cap_m, dtype=torch.int32, device=dev)
-        img_off = torch.empty((cap_m, 3), dtype=torch.int32, device=dev)
-        img_r = torch.empty((cap_m, 3), dtype=torch.float64, device=dev)
-        pair_ptr = torch.empty(N + 1, dtype=torch.int32, device=dev)
-        check(L.so4_nl_fill(_ptr(geom), S, nbins, _ptr(pos), _ptr(atom_struct), N, float(rcut), _ptr(img_ptr), cap_m,
-                            _ptr(img_j), _ptr(img_off), _ptr(img_r), _ptr(pair_ptr), _ptr(ws), ws.numel(), st),
-              "so4_nl_fill")
-        seq = torch.empty((cap_p, 2), dtype=torch.int64, device=dev)
-        pair_img = torch.empty(cap_p + 1, dtype=torch.int32, device=dev)
-        nsite = torch.empty(max(N, 1), dtype=torch.int32, device=dev)
-        img_pair = torch.empty(cap_m, dtype=torch.int32, device=dev)
-        img_rev = torch.empty(cap_m, dtype=torch.int32, device=dev)
-        check(L.so4_nl_pairs(_ptr(geom), S, _ptr(atom_struct), N, _ptr(img_ptr), cap_m, _ptr(img_j), _ptr(img_off),
-                             _ptr(pair_ptr), cap_p, _ptr(seq), _ptr(pair_img), _ptr(nsite), _ptr(img_pair),
-                             _ptr(img_rev), _ptr(ws), ws.numel(), st), "so4_nl_pairs")
-        check(L.so4_nl_summary(_ptr(img_ptr), _ptr(pair_ptr), N, _ptr(ws), ws.numel(), st, summary), "so4_nl_summary")
+        bufs = NeighborBuffers.allocate(lay, cap_m, cap_p, dev, workspace)
+        enqueue_neighbors(lay, pos, bufs, summary)
         M, P, bits = int(summary[0]), int(summary[1]), int(summary[2])
-        if M <= cap_m and P <= cap_p:
+        if check_summary(M, P, bits, cap_m, cap_p):
             break
         cap_m, cap_p = max(cap_m, int(M * 1.25) + 16), max(cap_p, int(P * 1.25) + 16)
     else:
         raise _lib.SO4Error(_lib.SO4_ERR_CAPACITY, "neighbour list")
-    _NL_CAPACITY[key] = (max(int(M * 1.1) + 16, 1), max(int(P * 1.1) + 16, 1))
-    if bits & (1 << _lib.SO4_ERR_NONFINITE):
-        raise ValueError("positions contain NaN or Inf")
-    for code in (_lib.SO4_ERR_CAPACITY, _lib.SO4_ERR_REVERSE):  # capacity here: an image offset beyond 511 cells
-        if bits & (1 << code):
-            raise _lib.SO4Error(code, "neighbour list")
-    return Neighbors(N, S, M, P, atom_ptr, vol, geom, nbins, atom_struct, atom_ptr_dev, img_ptr, img_j[:M],
-                     img_off[:M], img_r[:M], pair_ptr, seq[:P], pair_img[: P + 1], nsite[:N], img_pair[:M],
-                     img_rev[:M], bool(bits & (1 << _lib.SO4_ERR_NO_NEIGHBOR)))
+    note_capacity(lay, M, P)
+    return neighbors_view(lay, bufs, M, P, bits)
 
 
 # ----------------------------------------------------------------- compute
