@@ -443,9 +443,12 @@ __global__ void __launch_bounds__(256) k_deidrj_rc(DArgs A, int64_t nimg) {
     const int lane = threadIdx.x & 31;
     const int64_t wg = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int grp = lane / RC::NCH, mb = lane - grp * RC::NCH;
+    // nimg may be a capacity: the images are [0, img_ptr[natoms]); warps past the end
+    // leave at once (the condition is uniform over the warp, which has no block barrier)
+    const int64_t mtot = min(nimg, (int64_t)__ldg(A.img_ptr + A.natoms));
+    if (wg * RC::IPW >= mtot) return;
     const int64_t m = wg * RC::IPW + grp;
-    // nimg may be a capacity: the images are [0, img_ptr[natoms])
-    const bool valid = (grp < RC::IPW) && (m < nimg) && (m < (int64_t)__ldg(A.img_ptr + A.natoms));
+    const bool valid = (grp < RC::IPW) && (m < mtot);
     float x = 1.f, y = 0.f, z = 0.f, wj = 0.f;
     int centre = 0;
     if (valid) {
