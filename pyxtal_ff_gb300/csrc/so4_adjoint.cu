@@ -433,18 +433,20 @@ __global__ void __launch_bounds__(NWD * 32) k_deidrj(DArgs A) {
     }
 }
 
-// Per-image dE/dr with the register-resident row-chain recursion.  Images are
-// flattened over all centres (load balance independent of the per-atom count):
-// warp w takes images [w*IPW, (w+1)*IPW), lane = image_in_warp * NCH + mb.
-template <int TWOL>
-__global__ void __launch_bounds__(256) k_deidrj_rc(DArgs A, int64_t nimg) {
+// Per-image dE/dr in reverse mode (RvFwd / RvBack, so4_rowchain.cuh): the same
+// lane layout as k_deidrj_rc, U rows kept in shared memory by the forward sweep,
+// one backward sweep of Y giving the gradients with respect to conj(a), conj(b).
+template <int TWOL, int NT>
+__global__ void __launch_bounds__(NT, (TWOL <= 8) ? 2 : 1) k_deidrj_rev(DArgs A, int64_t nimg) {
     using RC = RowChain<TWOL>;
     constexpr int W = TWOL + 1;
+    extern __shared__ __align__(16) float2 rv_smem[];  // [acc_block(TWOL + 1)][NT]
+    float2 *st = rv_smem + threadIdx.x;
     const int lane = threadIdx.x & 31;
     const int64_t wg = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int grp = lane / RC::NCH, mb = lane - grp * RC::NCH;
     // nimg may be a capacity: the images are [0, img_ptr[natoms]); warps past the end
-    // leave at once (the condition is uniform over the warp, which has no block barrier)
+    // leave at once (the condition is uniform over the warp; there is no block barrier)
     const int64_t mtot = min(nimg, (int64_t)__ldg(A.img_ptr + A.natoms));
     if (wg * RC::IPW >= mtot) return;
     const int64_t m = wg * RC::IPW + grp;
@@ -467,54 +469,65 @@ __global__ void __launch_bounds__(256) k_deidrj_rc(DArgs A, int64_t nimg) {
     }
     CK<float> ck;
     make_ck<float, true>(x, y, z, r, A.psi_fac * r, ck);
-    float ur[W], ui[W], dr[3][W], di[3][W];
+    float ur[W], ui[W];
 #pragma unroll
-    for (int q = 0; q < W; ++q) {
-        ur[q] = ui[q] = 0.f;
-#pragma unroll
-        for (int c = 0; c < 3; ++c) dr[c][q] = di[c][q] = 0.f;
-    }
+    for (int q = 0; q < W; ++q) ur[q] = ui[q] = 0.f;
     ur[0] = 1.f;
+    st[0] = make_float2(1.f, 0.f);  // level 0
+    RvFwd<TWOL, 1, NT>::run(mb, ck, ur, ui, st);
+    // backward sweep; ur/ui reused as the adjoint carry
+#pragma unroll
+    for (int q = 0; q < W; ++q) ur[q] = ui[q] = 0.f;
     const float2 *Y = A.Y + (size_t)centre * A.nh;
-    float su = (mb == 0) ? __ldg(Y).x : 0.f;  // level 0: U = 1, dU = 0
-    float sc[3] = {0.f, 0.f, 0.f};
-    RcDeidrj<TWOL, 1>::run(mb, ck, Y, ur, ui, dr, di, su, sc);
+    float su = 0.f, gar = 0.f, gai = 0.f, gbr = 0.f, gbi = 0.f;
+    RvBack<TWOL, TWOL, NT>::run(mb, ck, Y, st, ur, ui, su, gar, gai, gbr, gbi);
     // sum the chains of each image into its mb == 0 lane
-    float tu = su, t0 = sc[0], t1 = sc[1], t2 = sc[2];
+    float tu = su, t0 = gar, t1 = gai, t2 = gbr, t3 = gbi;
 #pragma unroll
     for (int k = 1; k < RC::NCH; ++k) {
         const float a0 = __shfl_down_sync(0xffffffffu, su, k);
-        const float a1 = __shfl_down_sync(0xffffffffu, sc[0], k);
-        const float a2 = __shfl_down_sync(0xffffffffu, sc[1], k);
-        const float a3 = __shfl_down_sync(0xffffffffu, sc[2], k);
+        const float a1 = __shfl_down_sync(0xffffffffu, gar, k);
+        const float a2 = __shfl_down_sync(0xffffffffu, gai, k);
+        const float a3 = __shfl_down_sync(0xffffffffu, gbr, k);
+        const float a4 = __shfl_down_sync(0xffffffffu, gbi, k);
         tu += a0;
         t0 += a1;
         t1 += a2;
         t2 += a3;
+        t3 += a4;
     }
     if (valid && mb == 0) {
         float sf, dsf;
         cutoff_fn<float>(A.prm.cutoff_id, r, A.rc32, sf, dsf);
-        float gx = wj * (sf * t0 + dsf * (x / r) * tu);
-        float gy = wj * (sf * t1 + dsf * (y / r) * tu);
-        float gz = wj * (sf * t2 + dsf * (z / r) * tu);
-        if (skip) gx = gy = gz = 0.f;
-        A.g[3 * m] = gx;
-        A.g[3 * m + 1] = gy;
-        A.g[3 * m + 2] = gz;
+        const float xr[3] = {x / r, y / r, z / r};
+        float gv[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            // d f / d r_c = Re(conj(G_ca) d conj(a)/dr_c) + Re(conj(G_cb) d conj(b)/dr_c)
+            const float sc = t0 * ck.cda[c].re + t1 * ck.cda[c].im + t2 * ck.cdb[c].re + t3 * ck.cdb[c].im;
+            gv[c] = skip ? 0.f : wj * (sf * sc + dsf * xr[c] * tu);
+        }
+        A.g[3 * m] = gv[0];
+        A.g[3 * m + 1] = gv[1];
+        A.g[3 * m + 2] = gv[2];
     }
 }
 
 template <int TWOL>
-int launch_deidrj_rc(const DArgs &D, int64_t nimg, cudaStream_t st) {
+int launch_deidrj_rev(const DArgs &D, int64_t nimg, cudaStream_t st) {
     using RC = RowChain<TWOL>;
+    constexpr int NT = (TWOL <= 8) ? 256 : 128;
     if (nimg <= 0) return SO4_OK;
+    const size_t smem = sizeof(float2) * (size_t)acc_block(TWOL + 1) * NT;
+    const int rc = so4_set_smem((const void *)k_deidrj_rev<TWOL, NT>, smem);
+    if (rc) return rc;
     const int64_t warps = (nimg + RC::IPW - 1) / RC::IPW;
-    const int64_t blocks = (warps + 7) / 8;
-    k_deidrj_rc<TWOL><<<(unsigned)blocks, 256, 0, st>>>(D, nimg);
+    const int64_t blocks = (warps + NT / 32 - 1) / (NT / 32);
+    k_deidrj_rev<TWOL, NT><<<(unsigned)blocks, NT, smem, st>>>(D, nimg);
     so4_count_launch();
     return SO4_OK;
 }
+
 
 // ---------------------------------------------------------------------------
 // Gather: forces, per-structure virial and energy in a fixed order.
@@ -825,12 +838,12 @@ extern "C" int so4_adjoint_deidrj32(const so4_tables *t, const so4_params *p, in
     cudaStream_t st = (cudaStream_t)stream;
     int rc = SO4_OK;
     switch (t->twol) {
-        case 2: rc = launch_deidrj_rc<2>(D, nimg, st); break;
-        case 4: rc = launch_deidrj_rc<4>(D, nimg, st); break;
-        case 6: rc = launch_deidrj_rc<6>(D, nimg, st); break;
-        case 8: rc = launch_deidrj_rc<8>(D, nimg, st); break;
-        case 10: rc = launch_deidrj_rc<10>(D, nimg, st); break;
-        case 12: rc = launch_deidrj_rc<12>(D, nimg, st); break;
+        case 2: rc = launch_deidrj_rev<2>(D, nimg, st); break;
+        case 4: rc = launch_deidrj_rev<4>(D, nimg, st); break;
+        case 6: rc = launch_deidrj_rev<6>(D, nimg, st); break;
+        case 8: rc = launch_deidrj_rev<8>(D, nimg, st); break;
+        case 10: rc = launch_deidrj_rev<10>(D, nimg, st); break;
+        case 12: rc = launch_deidrj_rev<12>(D, nimg, st); break;
         default: {
             const size_t smd = sizeof(float) * rootpq_floats(t->ldim) +
                                sizeof(cx<float>) * ((size_t)t->n_half + (size_t)NWD * 4 * t->n_half);

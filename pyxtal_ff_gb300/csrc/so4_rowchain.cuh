@@ -4,9 +4,9 @@
 // compute_uarray_recursive, pyxtal_ff/descriptors/SO4.py:888-906), except that
 // the middle row of an even level l = 2mb starts from row mb-1 of level l-1,
 // mirrored by the inversion symmetry (:908-925).  So each lane owns one chain
-// mb = 0..TWOL/2 of one image and keeps its row (U and the three dU/dr
-// components) in registers from level 2mb up to TWOL, updated in place; the
-// only exchange is one shuffle of the previous chain's row at the chain start.
+// mb = 0..TWOL/2 of one image and keeps its row (U, and for the JVP the three
+// dU/dr components) in registers from level 2mb up to TWOL, updated in place;
+// the only exchange is one shuffle of the previous chain's row at the chain start.
 // TWOL is a template parameter so every row index is a compile-time constant.
 #pragma once
 
@@ -158,37 +158,6 @@ __device__ __forceinline__ void rc_start(int mb, float (&ur)[TWOL + 1], float (&
 // offset of level L in the half layout: sum_{l<L} (l/2+1)(l+1)
 __host__ __device__ constexpr int half_block(int L) { return L == 0 ? 0 : half_block(L - 1) + ((L - 1) / 2 + 1) * L; }
 
-// Levels L..TWOL of the recursion with, after each level, the contraction of
-// the lane's row with the adjoint array Y (half layout of one centre):
-//   su += Re conj(U) Y,  sc += Re conj(dU_c) Y.
-template <int TWOL, int L>
-struct RcDeidrj {
-    __device__ __forceinline__ static void run(int mb, const CK<float> &ck, const float2 *__restrict__ Y,
-                                               float (&ur)[TWOL + 1], float (&ui)[TWOL + 1],
-                                               float (&dr)[3][TWOL + 1], float (&di)[3][TWOL + 1], float &su,
-                                               float (&sc)[3]) {
-        if ((L & 1) == 0) rc_start<TWOL, L, true>(mb, ur, ui, dr, di);
-        rc_level<TWOL, L, true>(mb, ck, ur, ui, dr, di);
-        if (2 * mb <= L) {
-            const float2 *Yl = Y + half_block(L) + mb * (L + 1);
-#pragma unroll
-            for (int ma = 0; ma <= L; ++ma) {
-                const float2 y = __ldg(Yl + ma);
-                su += ur[ma] * y.x + ui[ma] * y.y;
-#pragma unroll
-                for (int c = 0; c < 3; ++c) sc[c] += dr[c][ma] * y.x + di[c][ma] * y.y;
-            }
-        }
-        RcDeidrj<TWOL, L + 1>::run(mb, ck, Y, ur, ui, dr, di, su, sc);
-    }
-};
-template <int TWOL>
-struct RcDeidrj<TWOL, TWOL + 1> {
-    __device__ __forceinline__ static void run(int, const CK<float> &, const float2 *, float (&)[TWOL + 1],
-                                               float (&)[TWOL + 1], float (&)[3][TWOL + 1],
-                                               float (&)[3][TWOL + 1], float &, float (&)[3]) {}
-};
-
 // centre atom of image m: the largest i with img_ptr[i] <= m
 __device__ __forceinline__ int centre_of(const int32_t *img_ptr, int natoms, int m) {
     int lo = 0, hi = natoms - 1;
@@ -257,4 +226,119 @@ struct RcJvp<TWOL, TWOL + 1> {
     __device__ __forceinline__ static void run(int, const CK<float> &, float, float, float, float, float (&)[TWOL + 1],
                                                float (&)[TWOL + 1], float (&)[3][TWOL + 1], float (&)[3][TWOL + 1],
                                                float (&)[acc_block(TWOL + 1)], float (&)[acc_block(TWOL + 1)]) {}
+};
+
+// ---------------------------------------------------------------------------
+// Reverse mode.  The contraction the adjoint needs per image,
+//   f = sum_half Re(conj(U) Y)  and  df/dr_c = sum_half Re(conj(dU/dr_c) Y),
+// depends on r only through a and b, so one backward sweep of Y through the
+// recursion gives the gradients G_ca, G_cb of f with respect to conj(a) and
+// conj(b) (real-gradient convention G_z = df/dRe z + i df/dIm z), and then
+//   df/dr_c = Re(conj(G_ca) d conj(a)/dr_c) + Re(conj(G_cb) d conj(b)/dr_c)
+// -- about half the arithmetic of carrying dU/dx, dU/dy, dU/dz forward.
+// The forward sweep stores every row a lane computes (levels 2mb .. TWOL, and at
+// a chain start the mirrored row it started from, as level 2mb - 1) in shared
+// memory at st[(acc_block(L) + ma) * NT] (NT = threads per CTA, st = base + tid).
+template <int TWOL, int L, int NT>
+struct RvFwd {
+    __device__ __forceinline__ static void run(int mb, const CK<float> &ck, float (&ur)[TWOL + 1],
+                                               float (&ui)[TWOL + 1], float2 *st) {
+        float dr[3][TWOL + 1], di[3][TWOL + 1];  // unused (no derivatives)
+        if ((L & 1) == 0) {
+            rc_start<TWOL, L, false>(mb, ur, ui, dr, di);
+            if (mb == L / 2) {
+#pragma unroll
+                for (int c = 0; c < L; ++c) st[(acc_block(L - 1) + c) * NT] = make_float2(ur[c], ui[c]);
+            }
+        }
+        rc_level<TWOL, L, false>(mb, ck, ur, ui, dr, di);
+#pragma unroll
+        for (int ma = 0; ma <= L; ++ma) st[(acc_block(L) + ma) * NT] = make_float2(ur[ma], ui[ma]);
+        RvFwd<TWOL, L + 1, NT>::run(mb, ck, ur, ui, st);
+    }
+};
+template <int TWOL, int NT>
+struct RvFwd<TWOL, TWOL + 1, NT> {
+    __device__ __forceinline__ static void run(int, const CK<float> &, float (&)[TWOL + 1], float (&)[TWOL + 1],
+                                               float2 *) {}
+};
+
+// Backward sweep, level L down to 1.  (gr, gi): on entry the adjoint of this
+// lane's row of level L arriving from level L + 1; on exit that of its row of
+// level L - 1.  Adds Y's row, forms f, back-propagates through the middle-row
+// construction and the recursion, and accumulates G_ca (gar, gai), G_cb (gbr, gbi).
+template <int TWOL, int L, int NT>
+struct RvBack {
+    __device__ __forceinline__ static void run(int mb, const CK<float> &ck, const float2 *__restrict__ Y,
+                                               const float2 *st, float (&gr)[TWOL + 1], float (&gi)[TWOL + 1],
+                                               float &su, float &gar, float &gai, float &gbr, float &gbi) {
+        constexpr int H = L / 2;
+        if (2 * mb <= L) {
+            const float2 *Yr = Y + half_block(L) + mb * (L + 1);
+#pragma unroll
+            for (int ma = 0; ma <= L; ++ma) {
+                const float2 y = __ldg(Yr + ma);
+                const float2 w = st[(acc_block(L) + ma) * NT];
+                su = fmaf(w.x, y.x, fmaf(w.y, y.y, su));
+                gr[ma] += y.x;
+                gi[ma] += y.y;
+            }
+            if ((L & 1) == 0 && mb == H) {
+                // row = (V[0..H-1], conj V[H], (-1)^(H+ma) conj V[L-ma] for ma > H): adjoint onto V
+#pragma unroll
+                for (int ma = 0; ma < H; ++ma) {
+                    const float s = ((H + ma) & 1) ? -1.f : 1.f;
+                    gr[ma] += s * gr[L - ma];
+                    gi[ma] -= s * gi[L - ma];
+                }
+                gi[H] = -gi[H];
+#pragma unroll
+                for (int ma = H + 1; ma <= L; ++ma) gr[ma] = gi[ma] = 0.f;
+            }
+            // V[ma] = alpha_ma conj(a) P[ma] + beta_ma conj(b) P[ma-1],
+            // alpha_ma = sqrt(L-ma)/sqrt(L-mb), beta_ma = -sqrt(ma)/sqrt(L-mb)
+            const float inv_q = rsqrtf((float)max(L - mb, 1));
+            const float ar = ck.ca.re, ai = -ck.ca.im;  // a = conj(conj(a))
+            const float br = ck.cb.re, bi = -ck.cb.im;
+            // in place, ascending: the new G[ma] = alpha_ma a G[ma] + beta_{ma+1} b G[ma+1]
+            // reads G[ma + 1] before it is replaced
+#pragma unroll
+            for (int ma = 0; ma < L; ++ma) {
+                const float g0 = gr[ma], g1 = gi[ma], h0 = gr[ma + 1], h1 = gi[ma + 1];
+                const float al = c_sqrtk[L - ma] * inv_q, be = -c_sqrtk[ma + 1] * inv_q;
+                const float2 p = st[(acc_block(L - 1) + ma) * NT];
+                // G_ca += al conj(P) G[ma];  G_cb += be conj(P) G[ma+1]
+                gar = fmaf(al, p.x * g0 + p.y * g1, gar);
+                gai = fmaf(al, p.x * g1 - p.y * g0, gai);
+                gbr = fmaf(be, p.x * h0 + p.y * h1, gbr);
+                gbi = fmaf(be, p.x * h1 - p.y * h0, gbi);
+                gr[ma] = al * (ar * g0 - ai * g1) + be * (br * h0 - bi * h1);
+                gi[ma] = al * (ar * g1 + ai * g0) + be * (br * h1 + bi * h0);
+            }
+            gr[L] = gi[L] = 0.f;
+        }
+        if ((L & 1) == 0) {
+            // the chain mb = H started at this level from P[c] = (-1)^(H+c) conj(Q[L-1-c]),
+            // Q the row H-1 of level L-1 on lane - 1: hand it the adjoint of Q
+#pragma unroll
+            for (int k = 0; k < L; ++k) {
+                const float vr = __shfl_down_sync(0xffffffffu, gr[L - 1 - k], 1);
+                const float vi = __shfl_down_sync(0xffffffffu, gi[L - 1 - k], 1);
+                if (mb == H - 1) {
+                    const float s = ((H + L - 1 - k) & 1) ? -1.f : 1.f;
+                    gr[k] += s * vr;
+                    gi[k] -= s * vi;
+                }
+            }
+        }
+        RvBack<TWOL, L - 1, NT>::run(mb, ck, Y, st, gr, gi, su, gar, gai, gbr, gbi);
+    }
+};
+template <int TWOL, int NT>
+struct RvBack<TWOL, 0, NT> {
+    __device__ __forceinline__ static void run(int mb, const CK<float> &, const float2 *__restrict__ Y, const float2 *,
+                                               float (&)[TWOL + 1], float (&)[TWOL + 1], float &su, float &, float &,
+                                               float &, float &) {
+        if (mb == 0) su += __ldg(Y).x;  // level 0: U = 1
+    }
 };
