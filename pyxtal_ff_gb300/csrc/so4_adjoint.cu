@@ -433,9 +433,11 @@ __global__ void __launch_bounds__(NWD * 32) k_deidrj(DArgs A) {
     }
 }
 
-// Per-image dE/dr in reverse mode (RvFwd / RvBack, so4_rowchain.cuh): the same
-// lane layout as k_deidrj_rc, U rows kept in shared memory by the forward sweep,
-// one backward sweep of Y giving the gradients with respect to conj(a), conj(b).
+// Per-image dE/dr in reverse mode (RvFwd / RvBack, so4_rowchain.cuh).  Images are
+// flattened over all centres (load balance independent of the per-atom count):
+// warp w takes images [w*IPW, (w+1)*IPW), lane = image_in_warp * NCH + chain mb.
+// U rows are kept in shared memory by the forward sweep; one backward sweep of Y
+// gives the gradients with respect to conj(a), conj(b).
 template <int TWOL, int NT>
 __global__ void __launch_bounds__(NT, (TWOL <= 8) ? 2 : 1) k_deidrj_rev(DArgs A, int64_t nimg) {
     using RC = RowChain<TWOL>;
