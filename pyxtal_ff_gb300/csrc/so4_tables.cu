@@ -457,10 +457,15 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
                     const int s0 = (int)wsub.size();
                     for (int mb1 = std::max(0, mb + d - b); mb1 <= std::min(a, mb + d); ++mb1) {
                         const int mb2 = mb + d - mb1;
+                        // a == b: the row pairs (mb1, mb2) and (mb2, mb1) hold the same products with
+                        // the same coefficients (cg(j m1 j m2) = (-1)^d cg(j m2 j m1), once in Ca and
+                        // once in Cb), so only mb1 <= mb2 is walked, mb1 < mb2 with 2 Cb
+                        if (a == b && mb1 > mb2) continue;
+                        const double sym = (a == b && mb1 < mb2) ? 2.0 : 1.0;
                         // stepped: U_b[lo + j, mb2]; ring base: U_a[ma0 + d - lo, mb1]
                         const int f1 = (ZW_PAD + t->idxu_block[b] + mb2 * (b + 1) + lo) * 33;
                         const int f2 = (ZW_PAD + t->idxu_block[a] + mb1 * (a + 1) + u.ma0 + d - lo) * 33;
-                        const float cb = (float)cg_of(bk, mb1, mb2);
+                        const float cb = (float)(sym * cg_of(bk, mb1, mb2));
                         int cbits;
                         std::memcpy(&cbits, &cb, sizeof cbits);
                         wsub.push_back(make_int4(f1 | (f2 << 16), ca_off[key], S, cbits));
