@@ -98,7 +98,7 @@ __global__ void __launch_bounds__(NWF * 32) k_utot32(FwdArgs A) {
 // order, the self term f_c(0) w_site is put on the diagonal and u_norm applied
 // (SO4.py:1480-1505, 560-597).
 template <int TWOL, int NW>
-__global__ void __launch_bounds__(NW * 32) k_utot_rc(FwdArgs A) {
+__global__ void __launch_bounds__(NW * 32, (TWOL <= 8) ? 4 : 1) k_utot_rc(FwdArgs A) {
     using RC = RowChain<TWOL>;
     constexpr int W = TWOL + 1, NACC = acc_block(TWOL + 1);
     extern __shared__ __align__(16) float ut_smem[];  // [NW][32][2 * NACC]
