@@ -131,3 +131,28 @@ def kernel_flops(twol, natoms, nimg):
         "adjoint_deidrj32": nimg * (u + du + 16 * n["n_half"] + 24),
         "plain": natoms * (z + per_atom_b(twol)) + nimg * (utot_img + u + du + per_image_db(twol)),
     }
+
+
+# Per-unit algorithmic work of the reference's algorithm as tabulated for this path
+# (U, dU, dudr, dB/dr and virial per neighbour image; Z, B and the adjoint per atom),
+# for lmax 3 and 4: the figures a launch's roofline is quoted against.
+SURVEY_UNITS = {
+    6: dict(U=1240, dU=6696, dudr=4200, dB=24816, virial=1080, Z=98076, B=3824, adj_img=12600, adj_atom=200000),
+    8: dict(U=2600, dU=14040, dudr=8550, dB=72072, virial=1980, Z=455702, B=11304, adj_img=27000, adj_atom=900000),
+}
+
+
+def survey_flops(twol, natoms, nimg):
+    """Algorithmic flops of one launch of each stage from the tabulated per-unit work
+    (None where the table has no entry for this twol): U_tot per image; Z + Y (+ B) per
+    atom; the adjoint per image; the plain path's full per-image and per-atom work."""
+    t = SURVEY_UNITS.get(int(twol))
+    if t is None:
+        return None
+    return {
+        "utot32": nimg * t["U"],
+        "linear_by32": natoms * (t["adj_atom"] + t["B"]),
+        "adjoint_y32": natoms * t["adj_atom"],
+        "adjoint_deidrj32": nimg * t["adj_img"],
+        "plain": natoms * (t["Z"] + t["B"]) + nimg * (t["U"] + t["dU"] + t["dudr"] + t["dB"] + t["virial"]),
+    }
