@@ -36,8 +36,8 @@ CONFIG = {"workload": "diamond-Si 20x20x10 (32000 atoms), SO4 lmax=4, rcut=5.0 A
 
 
 # DRAM bytes (read + write) per launch of each stage's kernel, from the ncu capture
-# summarised in profiles/k_zw32_k_deidrj_rc_k_utot_rc_si32000_lmax4.md (same workload)
-NCU_TRAFFIC = {"utot32": 25.92e6, "linear_by32": 72.67e6, "adjoint_deidrj32": 66.81e6}
+# summarised in profiles/k_zw32_k_deidrj_rev_k_utot_rc_si32000_lmax4.md (same workload)
+NCU_TRAFFIC = {"utot32": 26.09e6, "linear_by32": 71.90e6, "adjoint_deidrj32": 67.30e6}
 
 
 def workload():
