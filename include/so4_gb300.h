@@ -171,6 +171,14 @@ int so4_plain(const so4_tables *t, const so4_params *p, int precision, const so4
               const int32_t *d_nsite, int want_deriv, int want_stress, void *d_x, void *d_dxdr,
               void *d_rdxdr, void *d_work, size_t work_bytes, void *stream);
 
+/* Per-atom stress rows from the plain path's per-pair rdxdr, as the reference's
+ * caller builds them after calculate() (pyxtal_ff/utilities/__init__.py:226-233):
+ * d_out[natoms*nB*6][m, k, v] = sum over the pairs p of centre m (d_pair_ptr) of
+ * rdxdr[p, k, a, b], v = 0..5 the Voigt order (0,0) (1,1) (2,2) (0,1) (0,2) (1,2).
+ * precision 0: double arrays, 1: float. */
+int so4_rdxdr_atom(int precision, const void *d_rdxdr, const int32_t *d_pair_ptr, int natoms, int nB, void *d_out,
+                   void *stream);
+
 /* ------------------------------------------------------------ adjoint path */
 /* Forward (FP32): U_tot per centre in the half layout (d_utot[natoms*idxu_half*2]
  * f32, kept for the adjoint) and B (d_x[natoms*nB] f32). */

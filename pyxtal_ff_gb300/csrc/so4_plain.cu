@@ -288,3 +288,45 @@ extern "C" int so4_plain(const so4_tables *t, const so4_params *p, int precision
                                 d_rdxdr, st);
     return SO4_ERR_ARG;
 }
+
+// ---------------------------------------------------------------------------
+// Per-atom stress rows.  The reference's caller turns the per-pair rdxdr of
+// calculate() into one row per centre (pyxtal_ff/utilities/__init__.py:226-233):
+//   out[m, k, :] = sum over the pairs (m, j) of rdxdr[p, k, a, b], (a, b) in the Voigt
+//   order (0,0) (1,1) (2,2) (0,1) (0,2) (1,2),
+// with a Python loop over atoms.  Pairs are grouped by centre here (pair_ptr), so
+// one thread per (m, k, component) sums its centre's pairs in pair order.
+namespace {
+template <typename T>
+__global__ void k_rdxdr_atom(const T *__restrict__ rdxdr, const int32_t *__restrict__ pair_ptr, int natoms, int nB,
+                             T *__restrict__ out) {
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t total = (int64_t)natoms * nB * 6;
+    if (idx >= total) return;
+    const int v = (int)(idx % 6);
+    const int64_t mk = idx / 6;
+    const int k = (int)(mk % nB);
+    const int m = (int)(mk / nB);
+    const int comp = (v < 3) ? 4 * v : ((v == 3) ? 1 : ((v == 4) ? 2 : 5));  // row-major a * 3 + b
+    T s = T(0);
+    const int p1 = __ldg(pair_ptr + m + 1);
+    for (int p = __ldg(pair_ptr + m); p < p1; ++p) s += __ldg(rdxdr + ((size_t)p * nB + k) * 9 + comp);
+    out[idx] = s;
+}
+}  // namespace
+
+extern "C" int so4_rdxdr_atom(int precision, const void *d_rdxdr, const int32_t *d_pair_ptr, int natoms, int nB,
+                              void *d_out, void *stream) {
+    if (natoms < 0 || nB <= 0 || (natoms > 0 && (!d_rdxdr || !d_pair_ptr || !d_out))) return SO4_ERR_ARG;
+    if (precision != 0 && precision != 1) return SO4_ERR_ARG;
+    if (natoms == 0) return SO4_OK;
+    const int64_t total = (int64_t)natoms * nB * 6;
+    const unsigned grid = (unsigned)((total + 255) / 256);
+    cudaStream_t st = (cudaStream_t)stream;
+    if (precision == 0)
+        k_rdxdr_atom<double><<<grid, 256, 0, st>>>((const double *)d_rdxdr, d_pair_ptr, natoms, nB, (double *)d_out);
+    else
+        k_rdxdr_atom<float><<<grid, 256, 0, st>>>((const float *)d_rdxdr, d_pair_ptr, natoms, nB, (float *)d_out);
+    so4_count_launch();
+    return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
+}

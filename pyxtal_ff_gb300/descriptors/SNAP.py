@@ -91,9 +91,9 @@ class SO4_Bispectrum(BispectrumBase):
         from ..engine import site_weights
         return site_weights("SNAP", numbers, symbols, self._weights_)
 
-    def calculate(self, atoms, atom_ids=None):
+    def calculate(self, atoms, atom_ids=None, *, stress_per_atom=False):
         if self._twol % 2:
             # the reference sizes its blist from lmax = twol // 2 (SNAP.py:329) and then
             # overruns it for an odd twol; no valid output exists to match
             raise NotImplementedError("half-integer lmax (odd 2*lmax) is not supported")
-        return super().calculate(atoms, atom_ids)
+        return super().calculate(atoms, atom_ids, stress_per_atom=stress_per_atom)

@@ -98,9 +98,14 @@ class BispectrumBase:
     def _rfac0(self):
         return 1.0
 
-    def calculate(self, atoms, atom_ids=None):
+    def calculate(self, atoms, atom_ids=None, *, stress_per_atom=False):
         """B, dB/dr and the per-pair virial of one structure, as the reference's
-        calculate() returns them (SO4.py:171-209), from the CUDA FP64 path."""
+        calculate() returns them (SO4.py:171-209), from the CUDA FP64 path.
+
+        stress_per_atom=True returns rdxdr already reduced the way the reference's
+        caller reduces it after calculate() (pyxtal_ff/utilities/__init__.py:226-233):
+        one (len(x), nB, 6) Voigt row block per centre, summed on the GPU, so the
+        per-pair array never leaves the device."""
         import torch
         from .. import engine
         from ..structures import as_arrays
@@ -142,11 +147,21 @@ class BispectrumBase:
         if self._derivative:
             res = {"x": out_x, "dxdr": dxdr[:pk].cpu().numpy(), "elements": elements,
                    "seq": nb.seq[:pk].cpu().numpy()}
-            res["rdxdr"] = rdxdr[:pk].cpu().numpy() if self._stress else None
+            if not self._stress:
+                res["rdxdr"] = None
+            elif stress_per_atom:
+                res["rdxdr"] = engine.rdxdr_atom(rdxdr, nb.pair_ptr, k).cpu().numpy()
+            else:
+                res["rdxdr"] = rdxdr[:pk].cpu().numpy()
         else:
             res = {"x": out_x, "dxdr": None, "elements": elements}
             # without derivatives the reference never fills bstress (SO4.py:1671-1728),
-            # so it returns -0/vol over every pair
-            res["rdxdr"] = (-np.zeros((pk, tab.nB, 3, 3)) / vol) if self._stress else None
+            # so it returns -0/vol over every pair (and its caller's per-atom sum, +0)
+            if not self._stress:
+                res["rdxdr"] = None
+            elif stress_per_atom:
+                res["rdxdr"] = np.zeros((k, tab.nB, 6))
+            else:
+                res["rdxdr"] = -np.zeros((pk, tab.nB, 3, 3)) / vol
         self.clear_memory()
         return res

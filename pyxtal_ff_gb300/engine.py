@@ -316,6 +316,18 @@ def plain(tab, prm, nb: Neighbors, pos, w_nb, w_site, precision=0, want_deriv=Tr
     return x, dxdr, rdxdr
 
 
+def rdxdr_atom(rdxdr, pair_ptr, natoms):
+    """Per-atom Voigt stress rows (natoms, nB, 6) from per-pair rdxdr (P, nB, 3, 3) whose
+    pairs are grouped by centre (pair_ptr), as the reference's caller forms them
+    (pyxtal_ff/utilities/__init__.py:226-233)."""
+    nB = rdxdr.shape[1]
+    out = torch.empty((max(natoms, 1), nB, 6), dtype=rdxdr.dtype, device=rdxdr.device)
+    prec = 0 if rdxdr.dtype == torch.float64 else 1
+    check(lib().so4_rdxdr_atom(prec, _ptr(rdxdr.contiguous()), _ptr(pair_ptr), natoms, nB, _ptr(out), _stream()),
+          "so4_rdxdr_atom")
+    return out[:natoms]
+
+
 def forward32(tab, prm, nb: Neighbors, w_nb, w_site):
     """FP32 B (N,nB) and U_tot (N, n_half, 2) for the adjoint."""
     dev = w_nb.device

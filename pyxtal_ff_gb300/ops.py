@@ -3,9 +3,11 @@
 Operators (``torch.ops.so4gb300.*``, registered with ``torch.library.custom_op``;
 they launch the CUDA kernels on torch's current stream):
 
-  forward32(...)  -> (B, U_tot)          so4_forward32
-  adjoint32(...)  -> (forces, virial)    so4_adjoint32
-  jvp32(...)      -> dB                  so4_jvp32
+  neighbors(...)      -> (img_ptr, img_j, img_off, img_r, pair_ptr, seq)   so4_nl_*
+  forward_deriv(...)  -> (B, dB/dr, rdxdr), FP64 or FP32                    so4_plain
+  forward32(...)      -> (B, U_tot)                                         so4_forward32
+  adjoint32(...)      -> (forces, virial)                                   so4_adjoint32
+  jvp32(...)          -> dB                                                 so4_jvp32
 
 Autograd:
 
@@ -46,7 +48,16 @@ class Context:
         nb = engine.build_neighbors(positions.detach(), cells, pbc, atom_ptr, rcut, device=positions.device)
         w_nb, w_site = engine.site_weights(kind, numbers, symbols, weights)
         dev = positions.device
-        return cls(tab, prm, nb, torch.from_numpy(w_nb).to(dev), torch.from_numpy(w_site).to(dev))
+        c = cls(tab, prm, nb, torch.from_numpy(w_nb).to(dev), torch.from_numpy(w_site).to(dev))
+        c.layout = (np.asarray(cells), np.asarray(pbc), np.asarray(atom_ptr), float(rcut))
+        return c
+
+    def rebuild_neighbors(self, positions):
+        """Neighbour list of new positions for the same cells and atom ranges."""
+        cells, pbc, atom_ptr, rcut = self.layout
+        self.nb = engine.build_neighbors(positions.detach(), cells, pbc, atom_ptr, rcut, device=positions.device)
+        self.utot = None
+        return self.nb
 
 
 _CTX = {}
@@ -56,6 +67,31 @@ def _register(ctx):
     key = id(ctx)
     _CTX[key] = ctx
     return key
+
+
+def key(ctx):
+    """The integer handle the operators take for a context (registers it)."""
+    return _register(ctx)
+
+
+@torch.library.custom_op(_NS + "::neighbors", mutates_args=())
+def neighbors_op(ctx_key: int, positions: torch.Tensor) -> tuple[torch.Tensor, torch.Tensor, torch.Tensor,
+                                                                 torch.Tensor, torch.Tensor, torch.Tensor]:
+    """Rebuild the context's neighbour list for positions (N,3) f64; CSR arrays by centre."""
+    nb = _CTX[ctx_key].rebuild_neighbors(positions)
+    return (nb.img_ptr.clone(), nb.img_j.clone(), nb.img_off.clone(), nb.img_r.clone(), nb.pair_ptr.clone(),
+            nb.seq.clone())
+
+
+@torch.library.custom_op(_NS + "::forward_deriv", mutates_args=())
+def forward_deriv_op(ctx_key: int, positions: torch.Tensor, precision: int) -> tuple[torch.Tensor, torch.Tensor,
+                                                                                     torch.Tensor]:
+    """The plain path: B (N,nB), dB/dr per (i, j) pair (P,nB,3) and rdxdr (P,nB,3,3),
+    FP64 (precision 0) or FP32 (1), on the context's neighbour list."""
+    c = _CTX[ctx_key]
+    x, dxdr, rdxdr = engine.plain(c.tab, c.prm, c.nb, positions.contiguous(), c.w_nb, c.w_site,
+                                  precision=int(precision))
+    return x.clone(), dxdr.clone(), rdxdr.clone()
 
 
 @torch.library.custom_op(_NS + "::forward32", mutates_args=())

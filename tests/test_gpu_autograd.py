@@ -104,3 +104,19 @@ def test_force_loss_gradient_in_beta_is_exact_difference(cuda_device):
         bm[i, k] -= eps
         fd = (loss(bp).item() - loss(bm).item()) / (2 * eps)
         assert abs(fd - g[i, k]) <= 2e-4 * max(1.0, np.abs(g).max()), (i, k, fd, g[i, k])
+
+
+def test_neighbor_and_plain_ops_match_engine(cuda_device):
+    _, _, p, ctx, _ = _ctx()
+    k = ops.key(ctx)
+    pos = p.detach().clone() + 0.01
+    img_ptr, img_j, img_off, img_r, pair_ptr, seq = torch.ops.so4gb300.neighbors(k, pos)
+    nb = engine.build_neighbors(pos, *ctx.layout[:3], ctx.layout[3])
+    for a, b in ((img_ptr, nb.img_ptr), (img_j, nb.img_j), (img_off, nb.img_off), (img_r, nb.img_r),
+                 (pair_ptr, nb.pair_ptr), (seq, nb.seq)):
+        assert torch.equal(a, b)
+    for prec in (0, 1):
+        x, dxdr, rdxdr = torch.ops.so4gb300.forward_deriv(k, pos, prec)
+        x2, dxdr2, rdxdr2 = engine.plain(ctx.tab, ctx.prm, nb, pos, ctx.w_nb, ctx.w_site, precision=prec)
+        assert torch.equal(x, x2) and torch.equal(dxdr, dxdr2) and torch.equal(rdxdr, rdxdr2)
+    ops.release(ctx)
