@@ -219,8 +219,12 @@ def test_dropin_per_atom_stress_matches_caller_reduction(cuda_device, name):
         pytest.skip("no stress in this case")
     desc, atom_ids = _dropin(meta)
     out = desc.calculate(atoms, atom_ids=atom_ids, stress_per_atom=True)
-    if meta["derivative"]:
+    if meta["derivative"] and "rdxdr" in d:
         ref = _caller_rdxdr(d)
+    elif meta["derivative"]:
+        # large cases keep the per-centre sums of rdxdr (N, nB, 3, 3) instead of every pair
+        N, L = d["x"].shape
+        ref = d["rdxdr_atom"].reshape(N, L, 9)[:, :, [0, 4, 8, 1, 2, 5]]
     else:
         ref = np.zeros((d["x"].shape[0], d["x"].shape[1], 6))
     assert out["rdxdr"].shape == ref.shape
