@@ -461,6 +461,11 @@ __global__ void __launch_bounds__(NT, (TWOL <= 8) ? 2 : 1) k_deidrj_rev(DArgs A,
         z = (float)A.img_r[3 * m + 2];
         wj = (float)A.w_nb[A.img_j[m]];
         centre = centre_of(A.img_ptr, A.natoms, (int)m);
+        // the backward sweep reads this centre's Y level by level, one 128-byte line per
+        // level: ask for all of its lines now, so the forward sweep hides their latency
+        const char *yb = reinterpret_cast<const char *>(A.Y + (size_t)centre * A.nh);
+        const int nlines = (A.nh * (int)sizeof(float2) + 127) / 128;
+        for (int l = mb; l < nlines; l += RC::NCH) asm volatile("prefetch.global.L1 [%0];" ::"l"(yb + 128 * l));
     }
     float r = sqrtf(x * x + y * y + z * z);
     const bool skip = !(r >= 1e-8f);  // SO4.py:1441 skips r < 1e-8
