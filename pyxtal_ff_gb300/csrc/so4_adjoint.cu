@@ -460,7 +460,7 @@ __global__ void __launch_bounds__(NT, (TWOL <= 8) ? 2 : 1) k_deidrj_rev(DArgs A,
         y = (float)A.img_r[3 * m + 1];
         z = (float)A.img_r[3 * m + 2];
         wj = (float)A.w_nb[A.img_j[m]];
-        centre = centre_of(A.img_ptr, A.natoms, (int)m);
+        centre = centre_of(A.img_ptr, A.natoms, (int)m, mtot);
         // the backward sweep reads this centre's Y level by level, one 128-byte line per
         // level: ask for all of its lines now, so the forward sweep hides their latency
         const char *yb = reinterpret_cast<const char *>(A.Y + (size_t)centre * A.nh);
