@@ -67,6 +67,7 @@ struct FwdArgs {
     const ZEnt *zent, *zentB;
     const BEnt *bent;
     SmallTables st;
+    const int2 *hmap;  // per half entry: accumulator slot, row, diagonal flag, u_norm
     float *utot, *x;
 };
 
@@ -151,18 +152,17 @@ __global__ void __launch_bounds__(NW * 32, (TWOL <= 8) ? 4 : 1) k_utot_rc(FwdArg
     const float selfw = f0 * (float)A.w_site[a];
     float2 *ug = (float2 *)A.utot + (size_t)a * A.nh;
     for (int e = lane; e < A.nh; e += 32) {
-        int L = 0;
-        while (L < TWOL && half_block(L + 1) <= e) ++L;
-        const int off = e - half_block(L);
-        const int row = off / (L + 1), ma = off - row * (L + 1);
+        const int2 h = __ldg(A.hmap + e);
+        const int slot = h.x & 0xff, row = (h.x >> 8) & 0x7f;
         float sr = 0.f, si = 0.f;
+#pragma unroll
         for (int g = 0; g < RC::IPW; ++g) {
-            const float *src = sw + (g * RC::NCH + row) * 2 * NACC + 2 * (acc_block(L) + ma);
+            const float *src = sw + (g * RC::NCH + row) * 2 * NACC + 2 * slot;
             sr += src[0];
             si += src[1];
         }
-        if (ma == row) sr += selfw;
-        const float un = (float)A.st.unorm[L];
+        if (h.x & (1 << 15)) sr += selfw;
+        const float un = __int_as_float(h.y);
         ug[e] = make_float2(sr * un, si * un);
     }
 }
@@ -760,6 +760,7 @@ extern "C" int so4_forward32(const so4_tables *t, const so4_params *p, int natom
     A.nzB = t->n_zB;
     A.bent = t->d_b;
     fill_small_tables(t, A.st);
+    A.hmap = t->d_hmap;
     A.utot = d_utot;
     A.x = d_x;
     A.psi_fac = (float)(p->rfac0 * SO4_PI / p->rcut);
@@ -1029,6 +1030,7 @@ extern "C" int so4_utot32(const so4_tables *t, const so4_params *p, int natoms, 
     A.nzB = t->n_zB;
     A.bent = t->d_b;
     fill_small_tables(t, A.st);
+    A.hmap = t->d_hmap;
     A.utot = d_utot;
     A.x = nullptr;
     A.psi_fac = (float)(p->rfac0 * SO4_PI / p->rcut);

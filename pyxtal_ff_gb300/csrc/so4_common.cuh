@@ -117,6 +117,9 @@ struct so4_tables {
     ZTerm *d_terms = nullptr;
     int *d_term_ptr = nullptr;  // n_z + 1
     int *d_fmap = nullptr;      // n_u: full entry -> half source | conj << 15 | negate << 14
+    // n_half: per half entry (level L, row, ma) {L(L+1)/2 + ma | row << 8 | (ma == row) << 15,
+    // bits of u_norm[L] as float}: where the row-chain kernels keep it and how it is finished
+    int2 *d_hmap = nullptr;
     // work units of the atoms-across-lanes kernels, most expensive first:
     //   B unit {k, seg0, seg1, 0},       B segment {t0, t1, full index of U_l[e], weight 1 or 2 (= 1/2)}
     int4 *d_bunit = nullptr, *d_bseg = nullptr;

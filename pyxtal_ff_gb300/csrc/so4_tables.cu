@@ -91,6 +91,7 @@ void free_device(so4_tables *t) {
     cudaFree(t->d_yblk);
     cudaFree(t->d_terms);
     cudaFree(t->d_fmap);
+    cudaFree(t->d_hmap);
     cudaFree(t->d_term_ptr);
     cudaFree(t->d_bunit);
     cudaFree(t->d_bseg);
@@ -531,7 +532,17 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
             }
 
     int rc = SO4_OK;
+    std::vector<int2> hmap;
+    for (int l = 0; l < ld; ++l) {
+        const float un = (float)t->unorm_l[l];
+        int ubits;
+        std::memcpy(&ubits, &un, sizeof ubits);
+        for (int mb = 0; 2 * mb <= l; ++mb)
+            for (int ma = 0; ma <= l; ++ma)
+                hmap.push_back(make_int2((l * (l + 1) / 2 + ma) | (mb << 8) | ((ma == mb ? 1 : 0) << 15), ubits));
+    }
     if (!rc) rc = upload(&t->d_fmap, fmap);
+    if (!rc) rc = upload(&t->d_hmap, hmap);
     if (!rc) rc = upload(&t->d_terms, terms);
     if (!rc) rc = upload(&t->d_term_ptr, t->term_ptr);
     if (!rc) rc = upload(&t->d_bunit, bunit);
