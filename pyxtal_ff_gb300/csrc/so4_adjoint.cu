@@ -13,7 +13,6 @@
 //   dE_i/dr_image = w_j Re sum_half conj(sfac dU + dsfac r^ U) Y_i.
 // Forces: F_i = sum_{images m of i} (g_m - g_rev(m)); virial: sum_m r_m (x) g_m.
 #include <algorithm>
-#include <cmath>
 
 #include "so4_atom.cuh"
 #include "so4_rowchain.cuh"
@@ -304,10 +303,6 @@ __global__ void __launch_bounds__(ZW_THREADS, 2) k_zw32(ZLArgs A) {
     __shared__ int s_unit;
     const int lane = threadIdx.x & 31;
     const int a0 = blockIdx.x * 32, a = a0 + lane;
-    // the units of one 32-atom group are split over gridDim.y CTAs, part p taking
-    // units p, p + S, p + 2S, ... of the cost-ordered list (so the grid fills the
-    // GPU in more, shorter waves)
-    const int S = gridDim.y, part = blockIdx.y;
     float2 *Ub = zw_smem;
     float *coef = (float *)(Ub + (size_t)(A.nu + 2 * ZW_PAD) * ZL_PITCH);  // [nblk][33], MODE 1 and 2
     if (threadIdx.x == 0) s_unit = 0;
@@ -327,7 +322,7 @@ __global__ void __launch_bounds__(ZW_THREADS, 2) k_zw32(ZLArgs A) {
     }
     __syncthreads();
     const float2 *Ul = Ub + lane;
-    for (int u = zl_next(&s_unit) * S + part; u < A.nunit; u = zl_next(&s_unit) * S + part) {
+    for (int u = zl_next(&s_unit); u < A.nunit; u = zl_next(&s_unit)) {
         const int4 un = __ldg(A.unit + u);
         switch (un.x >> 24) {
             case 1: zw_unit<MODE, 1>(A, un, Ul, coef, a, lane); break;
@@ -340,14 +335,10 @@ __global__ void __launch_bounds__(ZW_THREADS, 2) k_zw32(ZLArgs A) {
             default: zw_unit<MODE, 8>(A, un, Ul, coef, a, lane); break;
         }
     }
-}
-
-// After k_zw32 (MODE 0 or 2): B_k = 2 x the sum of component k's partial slots in a
-// fixed order, and with eatom (MODE 2) beta . B per atom; 32 atoms per CTA.
-template <int MODE>
-__global__ void __launch_bounds__(256) k_zw_bsum(ZLArgs A) {
-    extern __shared__ __align__(16) float eb[];  // [nB][33]
-    const int a0 = blockIdx.x * 32;
+    if (MODE == 1) return;
+    __syncthreads();
+    // B_k, and beta_k B_k kept in shared memory (over the U tiles, no longer read) for the energy
+    float *eb = (float *)zw_smem;  // [nB][33]
     for (int idx = threadIdx.x; idx < 32 * A.nB; idx += blockDim.x) {
         const int k = idx >> 5, l = idx & 31;
         const int aa = a0 + l;
@@ -362,7 +353,6 @@ __global__ void __launch_bounds__(256) k_zw_bsum(ZLArgs A) {
     }
     if (MODE != 2 || A.eatom == nullptr) return;
     __syncthreads();
-    const int a = a0 + threadIdx.x;
     if (threadIdx.x < 32 && a < A.natoms) {
         float e = 0.f;
         for (int k = 0; k < A.nB; ++k) e += eb[k * ZL_PITCH + threadIdx.x];
@@ -737,29 +727,6 @@ static ZLArgs zl_args(const so4_tables *t, int natoms) {
 
 // shared memory of k_zw32: padded U tiles and the per-block coefficients; the B
 // epilogue (with_b) reuses the U tiles for nB x 33 floats
-// Parts per 32-atom group for k_zw32: the split S in 1..4 that minimises the number of
-// waves times the time of one part (1/S of a group's units plus its U-tile load, taken
-// as 4 % of a whole group) for this GPU's resident CTA count.
-static int zw_split(const void *kern, size_t smem, int groups) {
-    int dev = 0, nsm = 0, occ = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) return 1;
-    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm <= 0) return 1;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, ZW_THREADS, smem) != cudaSuccess || occ <= 0)
-        return 1;
-    const double slots = (double)nsm * occ;
-    int best = 1;
-    double tbest = 1e300;
-    for (int S = 1; S <= 4; ++S) {
-        const double waves = std::ceil((double)groups * S / slots);
-        const double t = waves * (1.0 / S + 0.04);
-        if (t < tbest - 1e-12) {
-            tbest = t;
-            best = S;
-        }
-    }
-    return best;
-}
-
 static size_t zw_smem_bytes(const so4_tables *t, bool with_b) {
     size_t u = sizeof(float2) * (size_t)(t->n_u + 2 * ZW_PAD) * ZL_PITCH;
     if (with_b) u = std::max(u, sizeof(float) * (size_t)t->n_b * ZL_PITCH);
@@ -850,9 +817,7 @@ extern "C" int so4_adjoint_y32(const so4_tables *t, int natoms, const float *d_u
     const size_t smz = zw_smem_bytes(t, false);
     int rc = set_smem(k_zw32<1>, smz);
     if (rc) return rc;
-    const int groups = (natoms + 31) / 32;
-    const int S = zw_split((const void *)k_zw32<1>, smz, groups);
-    k_zw32<1><<<dim3(groups, S), ZW_THREADS, smz, (cudaStream_t)stream>>>(Z);
+    k_zw32<1><<<(natoms + 31) / 32, ZW_THREADS, smz, (cudaStream_t)stream>>>(Z);
     so4_count_launch();
     return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
 }
@@ -1111,14 +1076,7 @@ extern "C" int so4_linear_by32(const so4_tables *t, int natoms, const float *d_u
     const size_t smz = zw_smem_bytes(t, true);
     int rc = set_smem(k_zw32<2>, smz);
     if (rc) return rc;
-    const int groups = (natoms + 31) / 32;
-    const int S = zw_split((const void *)k_zw32<2>, smz, groups);
-    k_zw32<2><<<dim3(groups, S), ZW_THREADS, smz, (cudaStream_t)stream>>>(Z);
-    so4_count_launch();
-    const size_t smb = sizeof(float) * (size_t)t->n_b * ZL_PITCH;
-    rc = set_smem(k_zw_bsum<2>, smb);
-    if (rc) return rc;
-    k_zw_bsum<2><<<groups, 256, smb, (cudaStream_t)stream>>>(Z);
+    k_zw32<2><<<(natoms + 31) / 32, ZW_THREADS, smz, (cudaStream_t)stream>>>(Z);
     so4_count_launch();
     return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
 }
