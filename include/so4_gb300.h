@@ -181,10 +181,13 @@ int so4_rdxdr_atom(int precision, const void *d_rdxdr, const int32_t *d_pair_ptr
 
 /* ------------------------------------------------------------ adjoint path */
 /* Forward (FP32): U_tot per centre in the half layout (d_utot[natoms*idxu_half*2]
- * f32, kept for the adjoint) and B (d_x[natoms*nB] f32). */
+ * f32, kept for the adjoint) and B (d_x[natoms*nB] f32).  Scratch:
+ * so4_forward32_workspace_size() bytes (per-atom partial sums of B). */
+size_t so4_forward32_workspace_size(const so4_tables *t, int natoms);
 int so4_forward32(const so4_tables *t, const so4_params *p, int natoms, const double *d_w_nb,
                   const double *d_w_site, const int32_t *d_img_ptr, const int32_t *d_img_j,
-                  const double *d_img_r, float *d_utot, float *d_x, void *stream);
+                  const double *d_img_r, float *d_utot, float *d_x, void *d_work, size_t work_bytes,
+                  void *stream);
 
 /* Adjoint (FP32 arithmetic, FP64 accumulation of forces and virial): given
  * beta = dE/dB (d_beta[natoms*nB] f32) and the forward's d_utot, writes

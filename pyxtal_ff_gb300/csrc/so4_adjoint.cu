@@ -199,31 +199,6 @@ struct ZLArgs {
     const float *wca;  // window Ca rows
 };
 
-// B_k = 2 Re sum' conj(U_l) Z(l1,l2,l) for 32 atoms per CTA (compute_bi, SO4.py:1071-1111)
-__global__ void __launch_bounds__(256) k_zb32(ZLArgs A) {
-    extern __shared__ __align__(16) float2 zl_smem[];
-    __shared__ int s_unit;
-    const int lane = threadIdx.x & 31;
-    const int a0 = blockIdx.x * 32;
-    float2 *Uf = zl_smem;
-    if (threadIdx.x == 0) s_unit = 0;
-    zl_load_utot(A.utot, A.fmap, a0, A.natoms, A.nh, A.nu, Uf);
-    __syncthreads();
-    for (int u = zl_next(&s_unit); u < A.nunit; u = zl_next(&s_unit)) {
-        const int4 un = __ldg(A.unit + u);
-        float acc = 0.f;
-        int4 sg = (un.y < un.z) ? __ldg(A.seg + un.y) : make_int4(0, 0, 0, 1);
-        for (int q = un.y; q < un.z; ++q) {
-            const int4 cur = sg;
-            if (q + 1 < un.z) sg = __ldg(A.seg + q + 1);
-            const float2 z = zl_entry(A.terms, cur.x, cur.y, Uf + lane);
-            const float2 ul = Uf[cur.z * ZL_PITCH + lane];
-            const float v = ul.x * z.x + ul.y * z.y;
-            acc += (cur.w == 2) ? 0.5f * v : v;
-        }
-        if (a0 + lane < A.natoms) A.x[(size_t)(a0 + lane) * A.nB + un.x] = 2.f * acc;
-    }
-}
 
 // One window unit of K entries: Z of every block feeding its level; Y (MODE 1, 2)
 // and the B-section scratch (MODE 0, 2).
@@ -733,13 +708,20 @@ static size_t zw_smem_bytes(const so4_tables *t, bool with_b) {
     return u + sizeof(float) * (size_t)t->n_blk * ZL_PITCH;
 }
 
+extern "C" size_t so4_forward32_workspace_size(const so4_tables *t, int natoms) {
+    if (!t || natoms < 0) return 0;
+    return ((sizeof(float) * (size_t)(natoms + 1) * t->n_bsec) + 255) & ~(size_t)255;
+}
+
 extern "C" int so4_forward32(const so4_tables *t, const so4_params *p, int natoms, const double *d_w_nb,
                              const double *d_w_site, const int32_t *d_img_ptr, const int32_t *d_img_j,
-                             const double *d_img_r, float *d_utot, float *d_x, void *stream) {
+                             const double *d_img_r, float *d_utot, float *d_x, void *d_work, size_t work_bytes,
+                             void *stream) {
     if (!t || !p || natoms < 0 || !d_utot || !d_x) return SO4_ERR_ARG;
     if (p->twol != t->twol || !(p->rcut > 0.0) || !(p->rfac0 > 0.0)) return SO4_ERR_ARG;
     if (p->cutoff_id < 1 || p->cutoff_id > 7) return SO4_ERR_UNSUPPORTED;
     if (natoms == 0) return SO4_OK;
+    if (!d_work || work_bytes < so4_forward32_workspace_size(t, natoms)) return SO4_ERR_WORKSPACE;
     cudaStream_t st = (cudaStream_t)stream;
     FwdArgs A;
     A.prm = *p;
@@ -783,16 +765,20 @@ extern "C" int so4_forward32(const so4_tables *t, const so4_params *p, int natom
         }
     }
     if (rc) return rc;
+    // B by the window kernel (B blocks only), partial sums per (unit, B block) in d_work
     ZLArgs Z = zl_args(t, natoms);
     Z.utot = (const float2 *)d_utot;
-    Z.unit = t->d_bunit;
-    Z.seg = t->d_bseg;
-    Z.nunit = t->n_b;
+    Z.unit = t->d_wunit_b;
+    Z.seg = t->d_wseg_b;
+    Z.nunit = t->n_wunit_b;
     Z.x = d_x;
-    const size_t smz = sizeof(float2) * (size_t)t->n_u * ZL_PITCH;
-    rc = set_smem(k_zb32, smz);
+    Z.bpos = t->d_bpos;
+    Z.nbsec = t->n_bsec;
+    Z.bc = (float *)d_work;
+    const size_t smz = zw_smem_bytes(t, true);
+    rc = set_smem(k_zw32<0>, smz);
     if (rc) return rc;
-    k_zb32<<<(natoms + 31) / 32, 256, smz, st>>>(Z);
+    k_zw32<0><<<(natoms + 31) / 32, ZW_THREADS, smz, st>>>(Z);
     so4_count_launch();
     return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
 }

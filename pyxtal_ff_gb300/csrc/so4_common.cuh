@@ -120,9 +120,6 @@ struct so4_tables {
     // n_half: per half entry (level L, row, ma) {L(L+1)/2 + ma | row << 8 | (ma == row) << 15,
     // bits of u_norm[L] as float}: where the row-chain kernels keep it and how it is finished
     int2 *d_hmap = nullptr;
-    // work units of the atoms-across-lanes kernels, most expensive first:
-    //   B unit {k, seg0, seg1, 0},       B segment {t0, t1, full index of U_l[e], weight 1 or 2 (= 1/2)}
-    int4 *d_bunit = nullptr, *d_bseg = nullptr;
     // B partial slots of the window kernels: one per (window unit, B block), component k
     // owning slots [bpos[k], bpos[k + 1]) in row order
     int *d_bpos = nullptr;  // nB + 1

@@ -93,8 +93,6 @@ void free_device(so4_tables *t) {
     cudaFree(t->d_fmap);
     cudaFree(t->d_hmap);
     cudaFree(t->d_term_ptr);
-    cudaFree(t->d_bunit);
-    cudaFree(t->d_bseg);
     cudaFree(t->d_bpos);
     cudaFree(t->d_junit);
     cudaFree(t->d_wunit_y);
@@ -330,26 +328,6 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
     t->term_ptr[t->n_z] = (int)terms.size();
     t->n_terms = (int)terms.size();
     auto zcost = [&](int jz) { return t->term_ptr[jz + 1] - t->term_ptr[jz]; };
-    // B units: one per component k, a segment per summed entry of its block
-    std::vector<std::pair<long, int>> bc;
-    for (int k = 0; k < t->n_b; ++k) {
-        long c = 0;
-        for (int e = 0; e < bent[k].cnt[0]; ++e) c += zcost(bent[k].z[0] + e);
-        bc.push_back({-c, k});
-    }
-    std::stable_sort(bc.begin(), bc.end());
-    std::vector<int4> bunit, bseg;
-    for (auto &v : bc) {
-        const int k = v.second;
-        const BEnt &be = bent[k];
-        const int s0 = (int)bseg.size();
-        for (int e = 0; e < be.cnt[0]; ++e) {
-            const int jz = be.z[0] + e;
-            const int half = ((be.lam[0] % 2) == 0 && e == be.cnt[0] - 1) ? 2 : 1;
-            bseg.push_back(make_int4(t->term_ptr[jz], t->term_ptr[jz + 1], t->idxu_block[be.lam[0]] + e, half));
-        }
-        bunit.push_back(make_int4(k, s0, (int)bseg.size(), 0));
-    }
     // B component of each block (blocks with l >= l1)
     std::vector<int> blk_k(t->n_blk, -1);
     for (int k = 0; k < t->n_b; ++k)
@@ -545,8 +523,6 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
     if (!rc) rc = upload(&t->d_hmap, hmap);
     if (!rc) rc = upload(&t->d_terms, terms);
     if (!rc) rc = upload(&t->d_term_ptr, t->term_ptr);
-    if (!rc) rc = upload(&t->d_bunit, bunit);
-    if (!rc) rc = upload(&t->d_bseg, bseg);
     if (!rc) rc = upload(&t->d_bpos, bpos);
     if (!rc) rc = upload(&t->d_wunit_y, wunit_y);
     if (!rc) rc = upload(&t->d_wseg_y, wseg_y);

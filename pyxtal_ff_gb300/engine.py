@@ -333,8 +333,10 @@ def forward32(tab, prm, nb: Neighbors, w_nb, w_site):
     dev = w_nb.device
     x = torch.empty((max(nb.natoms, 1), tab.nB), dtype=torch.float32, device=dev)
     utot = torch.empty((max(nb.natoms, 1), tab.n_half, 2), dtype=torch.float32, device=dev)
+    ws = torch.empty(max(lib().so4_forward32_workspace_size(tab.handle, nb.natoms), 1), dtype=torch.uint8, device=dev)
     check(lib().so4_forward32(tab.handle, C.byref(prm), nb.natoms, _ptr(w_nb), _ptr(w_site), _ptr(nb.img_ptr),
-                              _ptr(nb.img_j), _ptr(nb.img_r), _ptr(utot), _ptr(x), _stream()), "so4_forward32")
+                              _ptr(nb.img_j), _ptr(nb.img_r), _ptr(utot), _ptr(x), _ptr(ws), ws.numel(), _stream()),
+          "so4_forward32")
     return x[: nb.natoms], utot[: nb.natoms]
 
 
