@@ -94,18 +94,24 @@ class SpeciesMLP(torch.nn.Module):
                     torch.nn.init.zeros_(m.bias)
             self.nets.append(net.to(dtype))
 
-    def forward(self, x, species):
+    def forward(self, x, species, index=None):
+        """Per-atom energies; index: optional list of per-species atom index tensors (given
+        once for a fixed batch, so that the forward needs no host synchronisation)."""
         if len(self.nets) == 1:
             return self.nets[0](x).squeeze(-1)
+        if index is None:
+            index = [(species == s).nonzero().squeeze(-1) for s in range(len(self.nets))]
         out = torch.zeros(x.shape[0], dtype=x.dtype, device=x.device)
-        for s, net in enumerate(self.nets):
-            m = species == s
-            out = out.index_put((m.nonzero().squeeze(-1),), net(x[m]).squeeze(-1))
+        for idx, net in zip(index, self.nets):
+            out = out.index_put((idx,), net(x.index_select(0, idx)).squeeze(-1))
         return out
 
 
 class ForceMatching:
-    """One-optimiser-step trainer: loss = MSE(E/atom) + w_f MSE(F), forces from the adjoint."""
+    """One-optimiser-step trainer: loss = MSE(E/atom) + w_f MSE(F), forces from the adjoint.
+
+    ``capture()`` records one whole step (model, adjoint forces, the JVP backward, Adam)
+    as a CUDA graph for the fixed batch; later ``step()`` calls replay it."""
 
     def __init__(self, structures, *, lmax=3, rcut=4.9, kind="SNAP", weights=None, rfac0=1.0, hidden=(30, 30),
                  seed=0, lr=1e-3, force_weight=0.1, targets=None, device="cuda"):
@@ -126,12 +132,16 @@ class ForceMatching:
             targets = stillinger_weber(b, device=self.device)
         self.e_ref, self.f_ref = targets
         self.model = SpeciesMLP(x.shape[1], len(b.species_order), hidden=hidden, seed=seed).to(self.device)
-        self.opt = torch.optim.Adam(self.model.parameters(), lr=lr)
+        # capturable: the optimiser's step counters live on the device, so a step can be graphed
+        self.opt = torch.optim.Adam(self.model.parameters(), lr=lr, capturable=True)
         self.force_weight = force_weight
+        self.sp_index = [torch.from_numpy(np.nonzero(b.species == s)[0]).to(self.device)
+                         for s in range(len(b.species_order))]
+        self.graph = None
 
     def loss(self):
         xg = self.x.detach().requires_grad_(True)
-        e_atom = self.model(xg, self.species)
+        e_atom = self.model(xg, self.species, self.sp_index)
         beta, = torch.autograd.grad(e_atom.sum(), xg, create_graph=True)
         forces, _ = ops.AdjointForces.apply(beta, self.ctx)
         energy = torch.zeros(self.batch.nstruct, dtype=torch.float64, device=self.device).index_add(
@@ -140,9 +150,35 @@ class ForceMatching:
         lf = torch.mean((forces - self.f_ref) ** 2)
         return le + self.force_weight * lf
 
-    def step(self):
-        self.opt.zero_grad(set_to_none=True)
+    def _step(self):
         L = self.loss()
         L.backward()
         self.opt.step()
         return L.detach()
+
+    def step(self):
+        """One optimiser step; the loss of this step (before the update) on the device."""
+        if self.graph is not None:
+            self.graph.replay()
+            return self._loss
+        self.opt.zero_grad(set_to_none=True)
+        return self._step()
+
+    def capture(self, warmup=3):
+        """Record one step as a CUDA graph (after `warmup` eager steps on a side stream, which
+        train the model like any other steps); later step() calls replay it."""
+        side = torch.cuda.Stream(device=self.device)
+        side.wait_stream(torch.cuda.current_stream(self.device))
+        with torch.cuda.stream(side):
+            for _ in range(warmup):
+                self.opt.zero_grad(set_to_none=True)
+                self._step()
+        torch.cuda.current_stream(self.device).wait_stream(side)
+        torch.cuda.synchronize(self.device)
+        # gradients are created inside the capture and overwritten by every replay
+        self.opt.zero_grad(set_to_none=True)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self._loss = self._step()
+        self.graph = g
+        return self

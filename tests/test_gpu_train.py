@@ -68,3 +68,20 @@ def test_config3_full_step_runs_and_loss_decreases(cuda_device):
     losses = [fm.step().item() for _ in range(5)]
     print("config3 atoms", fm.batch.natoms, "losses", ["%.4g" % v for v in losses])
     assert np.all(np.isfinite(losses)) and losses[-1] < losses[0]
+
+
+def test_captured_training_step_matches_eager(cuda_device):
+    # two species so the per-species model path is captured too
+    structs = _structs(24, 7) + [S.sio2_random(n_si=4, seed=8)]
+    targets = None
+    fa = ForceMatching(structs, lmax=3, rcut=4.9, seed=4, lr=3e-3, weights={"Si": 1.0, "O": 0.6})
+    targets = (fa.e_ref, fa.f_ref)
+    fb = ForceMatching(structs, lmax=3, rcut=4.9, seed=4, lr=3e-3, weights={"Si": 1.0, "O": 0.6}, targets=targets)
+    for _ in range(3):
+        fa.step()
+    fb.capture(warmup=3)  # the warm-up steps are real steps: both models have taken three
+    for _ in range(4):
+        la, lb = fa.step().item(), fb.step().item()
+        assert abs(la - lb) <= 1e-6 * abs(la), (la, lb)
+    for pa, pb in zip(fa.model.parameters(), fb.model.parameters()):
+        assert (pa - pb).abs().max().item() <= 1e-5 * max(pa.abs().max().item(), 1.0)
