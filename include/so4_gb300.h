@@ -205,9 +205,12 @@ int so4_adjoint32(const so4_tables *t, const so4_params *p, int nstruct, const i
 
 /* The three stages so4_adjoint32 runs, for callers that keep their own buffers:
  *   so4_adjoint_y32      Y[natoms*idxu_half*2] f32 from U_tot and beta (atoms across lanes);
- *   so4_adjoint_deidrj32 g[nimg*3] f32 = dE/dr of every image (U and dU by the
- *                        recursion, contracted with Y); nimg may be the capacity of
- *                        d_g, the images being [0, d_img_ptr[natoms]);
+ *   so4_adjoint_deidrj32 g[m*3] f32 = dE/dr of every image m of the natoms centres,
+ *                        m in [d_img_ptr[0], d_img_ptr[natoms]) (U and dU by the
+ *                        recursion, contracted with Y); nimg bounds the number of those
+ *                        images (a capacity will do).  d_img_ptr, d_y and the per-atom
+ *                        arrays may point at a range of centres of a longer list, d_g
+ *                        and the per-image arrays being that list's;
  *   so4_adjoint_gather   forces[natoms*3] f64 = sum_m (g_m - g_rev(m)), the
  *                        per-structure virial[nstruct*9] f64 = sum_m r_m (x) g_m and,
  *                        when d_eatom and d_energy are both non-NULL, energy[nstruct] f64 =

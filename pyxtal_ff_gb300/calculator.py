@@ -124,10 +124,10 @@ class SO4Calculator:
             self._batch_key = batch
         return self
 
-    def capture(self, batch: Batch, model, headroom=1.25):
+    def capture(self, batch: Batch, model, headroom=1.25, branches=2):
         """The whole energy / forces / stress step of this batch layout as one CUDA graph
         (see CapturedStep); call the result with new positions."""
-        return CapturedStep(self, batch, model, headroom=headroom)
+        return CapturedStep(self, batch, model, headroom=headroom, branches=branches)
 
     def neighbors(self, batch: Batch, positions):
         return engine.build_neighbors(positions, batch.cells, batch.pbc, batch.atom_ptr, self.rcut, device=self.device)
@@ -215,7 +215,7 @@ class CapturedStep:
     (`SO4Calculator.capture`); it raises for non-finite positions like the eager path.
     """
 
-    def __init__(self, calc: "SO4Calculator", batch: Batch, model: LinearModel, headroom=1.25):
+    def __init__(self, calc: "SO4Calculator", batch: Batch, model: LinearModel, headroom=1.25, branches=2):
         if not isinstance(model, LinearModel):
             raise TypeError("graph capture covers the linear model (beta = dE/dB fixed)")
         calc.prepare(batch)
@@ -240,6 +240,22 @@ class CapturedStep:
         self.forces = torch.empty((max(N, 1), 3), dtype=torch.float64, device=dev)
         self.virial = torch.empty((max(S, 1), 3, 3), dtype=torch.float64, device=dev)
         self.energy_sum = torch.empty(max(S, 1), dtype=torch.float64, device=dev)
+        # Two branches: after the neighbour list every stage up to the gather is independent
+        # per centre, so the two halves of the atoms run as parallel graph branches and the
+        # tail of one branch's kernels overlaps the other's work.
+        self.branches = 2 if (branches >= 2 and N >= 256) else 1
+        if self.branches == 2:
+            mid = (N // 2 + 31) // 32 * 32
+            self.chunks = [(0, mid), (mid, N)]
+            nh = tab.n_half
+            self.utot = torch.empty((N, nh, 2), dtype=torch.float32, device=dev)
+            self.ybuf = torch.empty((N, nh, 2), dtype=torch.float32, device=dev)
+            self.bc = [torch.empty((max(tab.n_bsec, 1), a1 - a0), dtype=torch.float32, device=dev)
+                       for a0, a1 in self.chunks]
+            self.eatom = torch.empty(N, dtype=torch.float32, device=dev)
+            self.g = torch.empty((self.cap_m, 3), dtype=torch.float32, device=dev)
+            self.part = torch.empty(L.so4_gather_workspace_size(N), dtype=torch.uint8, device=dev)
+            self.side = torch.cuda.Stream(device=dev)
         self.energy = torch.empty(max(S, 1), dtype=torch.float64, device=dev)
         self.stress = torch.empty((max(S, 1), 6), dtype=torch.float64, device=dev)
         self._voigt = torch.tensor(VOIGT, device=dev)  # on the device before capture (no copies inside it)
@@ -263,12 +279,33 @@ class CapturedStep:
         b = self.nl
         _p = engine._ptr
         check = engine.check
-        check(L.so4_adjoint_linear32(tab.handle, C.byref(calc.params), lay.nstruct, _p(lay.atom_struct),
-                                     _p(lay.atom_ptr_dev), lay.natoms, _p(calc._w_nb), _p(calc._w_site),
-                                     _p(b.img_ptr), _p(b.img_j), _p(b.img_r), _p(b.img_rev), self.cap_m,
-                                     _p(self.beta), _p(self.x), _p(self.forces), _p(self.virial),
-                                     _p(self.energy_sum), _p(self.ws), self.ws.numel(), engine._stream()),
-              "so4_adjoint_linear32")
+        if self.branches == 1:
+            check(L.so4_adjoint_linear32(tab.handle, C.byref(calc.params), lay.nstruct, _p(lay.atom_struct),
+                                         _p(lay.atom_ptr_dev), lay.natoms, _p(calc._w_nb), _p(calc._w_site),
+                                         _p(b.img_ptr), _p(b.img_j), _p(b.img_r), _p(b.img_rev), self.cap_m,
+                                         _p(self.beta), _p(self.x), _p(self.forces), _p(self.virial),
+                                         _p(self.energy_sum), _p(self.ws), self.ws.numel(), engine._stream()),
+                  "so4_adjoint_linear32")
+        else:
+            main = torch.cuda.current_stream()
+            self.side.wait_stream(main)
+            for (a0, a1), bc, st in zip(self.chunks, self.bc, (main, self.side)):
+                with torch.cuda.stream(st):
+                    s_ = engine._stream()
+                    n = a1 - a0
+                    check(L.so4_utot32(tab.handle, C.byref(calc.params), n, _p(calc._w_nb), _p(calc._w_site[a0:a1]),
+                                       _p(b.img_ptr[a0:a1 + 1]), _p(b.img_j), _p(b.img_r), _p(self.utot[a0:a1]),
+                                       s_), "so4_utot32")
+                    check(L.so4_linear_by32(tab.handle, n, _p(self.utot[a0:a1]), _p(self.beta[a0:a1]),
+                                            _p(self.x[a0:a1]), _p(self.ybuf[a0:a1]), _p(bc), _p(self.eatom[a0:a1]),
+                                            s_), "so4_linear_by32")
+                    check(L.so4_adjoint_deidrj32(tab.handle, C.byref(calc.params), n, _p(calc._w_nb),
+                                                 _p(b.img_ptr[a0:a1 + 1]), _p(b.img_j), _p(b.img_r), self.cap_m,
+                                                 _p(self.ybuf[a0:a1]), _p(self.g), s_), "so4_adjoint_deidrj32")
+            main.wait_stream(self.side)
+            check(L.so4_adjoint_gather(lay.natoms, lay.nstruct, _p(lay.atom_ptr_dev), _p(b.img_ptr), _p(b.img_rev),
+                                       _p(b.img_r), _p(self.g), _p(self.eatom), _p(self.part), _p(self.forces),
+                                       _p(self.virial), _p(self.energy_sum), engine._stream()), "so4_adjoint_gather")
         S = lay.nstruct
         torch.add(self.energy_sum[:S], self.bias_s, out=self.energy[:S])
         # same operations as the uncaptured path, so the two agree bit for bit

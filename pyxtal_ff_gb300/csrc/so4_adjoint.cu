@@ -422,12 +422,14 @@ __global__ void __launch_bounds__(NT, (TWOL <= 8) ? 2 : 1) k_deidrj_rev(DArgs A,
     const int lane = threadIdx.x & 31;
     const int64_t wg = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int grp = lane / RC::NCH, mb = lane - grp * RC::NCH;
-    // nimg may be a capacity: the images are [0, img_ptr[natoms]); warps past the end
-    // leave at once (the condition is uniform over the warp; there is no block barrier)
-    const int64_t mtot = min(nimg, (int64_t)__ldg(A.img_ptr + A.natoms));
+    // the images are [img_ptr[0], img_ptr[natoms]) (img_ptr may point into a longer list
+    // for a range of centres); nimg bounds their count (a capacity will do).  Warps past
+    // the end leave at once (uniform over the warp; there is no block barrier)
+    const int64_t mbase = __ldg(A.img_ptr);
+    const int64_t mtot = min(nimg, (int64_t)__ldg(A.img_ptr + A.natoms) - mbase);
     if (wg * RC::IPW >= mtot) return;
-    const int64_t m = wg * RC::IPW + grp;
-    const bool valid = (grp < RC::IPW) && (m < mtot);
+    const int64_t m = mbase + wg * RC::IPW + grp;
+    const bool valid = (grp < RC::IPW) && (m - mbase < mtot);
     float x = 1.f, y = 0.f, z = 0.f, wj = 0.f;
     int centre = 0;
     if (valid) {
@@ -435,7 +437,7 @@ __global__ void __launch_bounds__(NT, (TWOL <= 8) ? 2 : 1) k_deidrj_rev(DArgs A,
         y = (float)A.img_r[3 * m + 1];
         z = (float)A.img_r[3 * m + 2];
         wj = (float)A.w_nb[A.img_j[m]];
-        centre = centre_of(A.img_ptr, A.natoms, (int)m, mtot);
+        centre = centre_of(A.img_ptr, A.natoms, (int)m, (int)mbase, mtot);
         // the backward sweep reads this centre's Y level by level, one 128-byte line per
         // level: ask for all of its lines now, so the forward sweep hides their latency
         const char *yb = reinterpret_cast<const char *>(A.Y + (size_t)centre * A.nh);

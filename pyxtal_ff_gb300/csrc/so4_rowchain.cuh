@@ -158,12 +158,13 @@ __device__ __forceinline__ void rc_start(int mb, float (&ur)[TWOL + 1], float (&
 // offset of level L in the half layout: sum_{l<L} (l/2+1)(l+1)
 __host__ __device__ constexpr int half_block(int L) { return L == 0 ? 0 : half_block(L - 1) + ((L - 1) / 2 + 1) * L; }
 
-// centre atom of image m: the largest i with img_ptr[i] <= m (m < img_ptr[natoms]).
-// The search starts from the guess m * natoms / mtot (images per centre are close to
+// centre atom of image m: the largest i with img_ptr[i] <= m (img_ptr[0] = mbase <= m <
+// img_ptr[natoms], mtot images).  The search starts from the guess
+// (m - mbase) * natoms / mtot (images per centre are close to
 // uniform in practice) and gallops outwards before bisecting, so the chain of
 // dependent loads is a few steps instead of log2(natoms).
-__device__ __forceinline__ int centre_of(const int32_t *img_ptr, int natoms, int m, int64_t mtot) {
-    int g = (int)(((int64_t)m * natoms) / (mtot > 0 ? mtot : 1));
+__device__ __forceinline__ int centre_of(const int32_t *img_ptr, int natoms, int m, int mbase, int64_t mtot) {
+    int g = (int)(((int64_t)(m - mbase) * natoms) / (mtot > 0 ? mtot : 1));
     g = min(max(g, 0), natoms - 1);
     int lo, hi;  // img_ptr[lo] <= m < img_ptr[hi] (img_ptr[natoms] > m)
     if (__ldg(img_ptr + g) <= m) {

@@ -65,3 +65,22 @@ def test_graph_step_reports_overflow_and_bad_input(cuda_device):
     step(bad)
     with pytest.raises(ValueError):
         step.check()
+
+
+def test_two_branch_graph_matches_eager_bitwise(cuda_device):
+    # 280 atoms: the two halves split the first structure at atom 160
+    structs = [S.diamond_si(3, 3, 3, sigma=0.08, rng=np.random.default_rng(11)),
+               S.diamond_si(2, 2, 2, sigma=0.08, rng=np.random.default_rng(12))]
+    batch, calc, model = _setup(structs)
+    step = calc.capture(batch, model, branches=2)
+    assert step.branches == 2
+    one = calc.capture(batch, model, branches=1)
+    rng = np.random.default_rng(13)
+    for _ in range(2):
+        pos = batch.positions + rng.normal(0, 0.02, size=batch.positions.shape)
+        res = {k: v.clone() for k, v in step(pos).items()}
+        res1 = {k: v.clone() for k, v in one(pos).items()}
+        torch.cuda.synchronize()
+        assert step.check() and one.check()
+        _equal(res, calc.compute(batch, model, positions=pos))
+        _equal(res, res1)
