@@ -240,13 +240,14 @@ class CapturedStep:
         self.forces = torch.empty((max(N, 1), 3), dtype=torch.float64, device=dev)
         self.virial = torch.empty((max(S, 1), 3, 3), dtype=torch.float64, device=dev)
         self.energy_sum = torch.empty(max(S, 1), dtype=torch.float64, device=dev)
-        # Two branches: after the neighbour list every stage up to the gather is independent
-        # per centre, so the two halves of the atoms run as parallel graph branches and the
-        # tail of one branch's kernels overlaps the other's work.
-        self.branches = 2 if (branches >= 2 and N >= 256) else 1
-        if self.branches == 2:
-            mid = (N // 2 + 31) // 32 * 32
-            self.chunks = [(0, mid), (mid, N)]
+        # Branches: after the neighbour list every stage up to the gather is independent per
+        # centre, so consecutive ranges of atoms (cut at multiples of 32) run as parallel graph
+        # branches and the tail of one branch's kernels overlaps the others' work.
+        self.branches = max(1, min(int(branches), N // 128))
+        if self.branches > 1:
+            cuts = [0] + [min(N, (N * k // self.branches + 31) // 32 * 32) for k in range(1, self.branches)] + [N]
+            self.chunks = [(a0, a1) for a0, a1 in zip(cuts[:-1], cuts[1:]) if a1 > a0]
+            self.branches = len(self.chunks)
             nh = tab.n_half
             self.utot = torch.empty((N, nh, 2), dtype=torch.float32, device=dev)
             self.ybuf = torch.empty((N, nh, 2), dtype=torch.float32, device=dev)
@@ -255,7 +256,7 @@ class CapturedStep:
             self.eatom = torch.empty(N, dtype=torch.float32, device=dev)
             self.g = torch.empty((self.cap_m, 3), dtype=torch.float32, device=dev)
             self.part = torch.empty(L.so4_gather_workspace_size(N), dtype=torch.uint8, device=dev)
-            self.side = torch.cuda.Stream(device=dev)
+            self.sides = [torch.cuda.Stream(device=dev) for _ in range(self.branches - 1)]
         self.energy = torch.empty(max(S, 1), dtype=torch.float64, device=dev)
         self.stress = torch.empty((max(S, 1), 6), dtype=torch.float64, device=dev)
         self._voigt = torch.tensor(VOIGT, device=dev)  # on the device before capture (no copies inside it)
@@ -288,8 +289,9 @@ class CapturedStep:
                   "so4_adjoint_linear32")
         else:
             main = torch.cuda.current_stream()
-            self.side.wait_stream(main)
-            for (a0, a1), bc, st in zip(self.chunks, self.bc, (main, self.side)):
+            for sd in self.sides:
+                sd.wait_stream(main)
+            for (a0, a1), bc, st in zip(self.chunks, self.bc, [main] + self.sides):
                 with torch.cuda.stream(st):
                     s_ = engine._stream()
                     n = a1 - a0
@@ -302,7 +304,8 @@ class CapturedStep:
                     check(L.so4_adjoint_deidrj32(tab.handle, C.byref(calc.params), n, _p(calc._w_nb),
                                                  _p(b.img_ptr[a0:a1 + 1]), _p(b.img_j), _p(b.img_r), self.cap_m,
                                                  _p(self.ybuf[a0:a1]), _p(self.g), s_), "so4_adjoint_deidrj32")
-            main.wait_stream(self.side)
+            for sd in self.sides:
+                main.wait_stream(sd)
             check(L.so4_adjoint_gather(lay.natoms, lay.nstruct, _p(lay.atom_ptr_dev), _p(b.img_ptr), _p(b.img_rev),
                                        _p(b.img_r), _p(self.g), _p(self.eatom), _p(self.part), _p(self.forces),
                                        _p(self.virial), _p(self.energy_sum), engine._stream()), "so4_adjoint_gather")
