@@ -46,7 +46,8 @@ enum so4_status {
     SO4_ERR_WORKSPACE = 6,    /* workspace smaller than the size query returned     */
     SO4_ERR_NO_NEIGHBOR = 7,  /* an atom has no neighbour image (reference raises ValueError, SO4.py:275) */
     SO4_ERR_REVERSE = 8,      /* an image has no reverse image (asymmetric list)    */
-    SO4_ERR_TOO_LARGE = 9     /* problem needs more than the fixed scratch of so4_adjoint32_noalloc */
+    SO4_ERR_TOO_LARGE = 9,    /* problem needs more than the fixed scratch of so4_adjoint32_noalloc */
+    SO4_ERR_SLOTS = 10        /* an atom has more images than the per-atom key slots of so4_nl_count_keys */
 };
 
 /* Maximum 2*lmax the kernels are compiled for (lmax <= 6). */
@@ -140,6 +141,20 @@ int so4_nl_pairs(const so4_geom *d_geom, int nstruct, const int *d_atom_struct, 
                  const int32_t *d_img_off, const int32_t *d_pair_ptr, int64_t npair,
                  int64_t *d_seq, int32_t *d_pair_img, int32_t *d_nsite, int32_t *d_img_pair,
                  int32_t *d_img_rev, void *d_work, size_t work_bytes, void *stream);
+
+/* One pass instead of so4_nl_count + the key pass of so4_nl_fill: counts the images of
+ * every centre (d_img_ptr, as so4_nl_count) and writes their keys into slot_cap slots per
+ * atom of the workspace (so4_nl_workspace_size(natoms, nbins, natoms * slot_cap) bytes at
+ * least).  An atom with more than slot_cap images sets status bits SO4_ERR_SLOTS and
+ * SO4_ERR_CAPACITY; the largest per-atom count is left at ((int *)d_work)[8].
+ * so4_nl_sort then does the rest of so4_nl_fill from those slots (same outputs). */
+int so4_nl_count_keys(const so4_geom *d_geom, int nstruct, int nbins, const double *d_pos, const int *d_atom_struct,
+                      int natoms, double rcut, int slot_cap, int32_t *d_img_ptr, void *d_work, size_t work_bytes,
+                      void *stream);
+int so4_nl_sort(const so4_geom *d_geom, int nstruct, int nbins, const double *d_pos, const int *d_atom_struct,
+                int natoms, const int32_t *d_img_ptr, int64_t nimg, int slot_cap, int32_t *d_img_j,
+                int32_t *d_img_off, double *d_img_r, int32_t *d_pair_ptr, void *d_work, size_t work_bytes,
+                void *stream);
 
 /* {total images, total pairs, status bits} after the three passes (d_pair_ptr may
  * be NULL after pass 1 only), written to ((int *)d_work)[4..6]; with h_summary

@@ -20,6 +20,7 @@ SO4_ERR_WORKSPACE = 6
 SO4_ERR_NO_NEIGHBOR = 7
 SO4_ERR_REVERSE = 8
 SO4_ERR_TOO_LARGE = 9
+SO4_ERR_SLOTS = 10
 
 _MESSAGES = {
     SO4_ERR_ARG: "invalid argument",
@@ -31,6 +32,7 @@ _MESSAGES = {
     SO4_ERR_NO_NEIGHBOR: "an atom has no neighbour within rcut",
     SO4_ERR_REVERSE: "neighbour list is not symmetric",
     SO4_ERR_TOO_LARGE: "problem exceeds the fixed 64 MiB scratch of so4_adjoint32_noalloc",
+    SO4_ERR_SLOTS: "an atom has more images than the per-atom key slots",
 }
 
 
@@ -85,6 +87,8 @@ def lib():
         "so4_nl_pairs": (_i, [_vp, _i, _vp, _i, _vp, _i64, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp, _vp, _vp,
                               _sz, _vp]),
         "so4_status_read": (_i, [_vp, _sz, _vp, C.POINTER(_i)]),
+        "so4_nl_count_keys": (_i, [_vp, _i, _i, _vp, _vp, _i, _d, _i, _vp, _vp, _sz, _vp]),
+        "so4_nl_sort": (_i, [_vp, _i, _i, _vp, _vp, _i, _vp, _i64, _i, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
         "so4_nl_summary": (_i, [_vp, _vp, _i, _vp, _sz, _vp, C.POINTER(_i)]),
         "so4_plain_workspace_size": (_sz, [_vp, _i]),
         "so4_plain": (_i, [_vp, C.POINTER(Params), _i, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,

@@ -229,8 +229,11 @@ class CapturedStep:
         nb0 = engine.build_neighbors(self.pos, batch.cells, batch.pbc, batch.atom_ptr, calc.rcut, device=dev)
         self.cap_m = int(nb0.nimg * headroom) + 64
         self.cap_p = int(nb0.npair * headroom) + 64 + N
+        # one-pass neighbour list: per-atom key slots sized from the largest count seen now
+        counts = torch.diff(nb0.img_ptr[: N + 1]).max().item() if N else 0
+        self.slot_cap = (int(counts * headroom) + 8 + 7) // 8 * 8
         del nb0
-        self.nl = engine.NeighborBuffers.allocate(lay, self.cap_m, self.cap_p, dev)
+        self.nl = engine.NeighborBuffers.allocate(lay, self.cap_m, self.cap_p, dev, slot_cap=self.slot_cap)
         L = engine.lib()
         tab = calc.tables
         self.ws = torch.empty(L.so4_linear_workspace_size(tab.handle, N, self.cap_m), dtype=torch.uint8, device=dev)

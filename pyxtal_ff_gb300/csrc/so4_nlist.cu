@@ -32,9 +32,10 @@ struct NLWork {
     int *atom_shift; // 3 natoms
     int *cnt;        // natoms (image or pair counts)
     float4 *pos32;   // natoms: FP32 copy of the positions for the prefilter
-    unsigned long long *keys;  // nimg
+    unsigned long long *keys;  // nimg, or natoms * slot_cap in the slot mode
     int64_t cap_img;           // capacity of the image arrays (fill / sort / rev)
     int64_t cap_pair;          // capacity of the pair arrays (pairs)
+    int slot_cap;              // > 0: keys of atom a in [a slot_cap, (a + 1) slot_cap)
 };
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -218,7 +219,7 @@ __global__ void k_scan_images(const so4_geom *geom, const double *pos, const int
     __shared__ int s_cnt[8];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int a = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (MODE == 1 && lane == 0) s_cnt[wib] = 0;
+    if (MODE >= 1 && lane == 0) s_cnt[wib] = 0;
     __syncwarp();
     if (a >= natoms) return;
     const so4_geom &g = geom[astruct[a]];
@@ -237,7 +238,7 @@ __global__ void k_scan_images(const so4_geom *geom, const double *pos, const int
     const int si[3] = {w.atom_shift[3 * a], w.atom_shift[3 * a + 1], w.atom_shift[3 * a + 2]};
     const int n1 = 2 * g.mshift[1] + 1, n2 = 2 * g.mshift[2] + 1;
     const int nq = (2 * g.mshift[0] + 1) * n1 * n2;
-    const int base = (MODE == 1) ? img_ptr[a] : 0;
+    const int64_t base = (MODE == 1) ? (int64_t)img_ptr[a] : ((MODE == 2) ? (int64_t)a * w.slot_cap : 0);
     int mine = 0;
     for (int q = lane; q < nq; q += 32) {
         const int d[3] = {q / (n1 * n2) - g.mshift[0], (q / n2) % n1 - g.mshift[1], q % n2 - g.mshift[2]};
@@ -271,7 +272,7 @@ __global__ void k_scan_images(const so4_geom *geom, const double *pos, const int
             if (!(lo > 0.f && d2 < lo * lo)) {     // within the rounding band: decide in FP64
                 if (!exact_inside(g, pi, pos, j, o[0], o[1], o[2], rcut)) continue;
             }
-            if (MODE == 1) {
+            if (MODE >= 1) {
                 if (abs(o[0]) > OFF_MAX || abs(o[1]) > OFF_MAX || abs(o[2]) > OFF_MAX) {
                     flag(w.status, SO4_ERR_CAPACITY);
                     continue;
@@ -281,19 +282,27 @@ __global__ void k_scan_images(const so4_geom *geom, const double *pos, const int
                                                ((unsigned long long)(o[1] + OFF_BIAS) << 10) |
                                                (unsigned long long)(o[2] + OFF_BIAS);
                 const int slot = atomicAdd(&s_cnt[wib], 1);
-                if (base + slot < w.cap_img) w.keys[base + slot] = key;
-                else flag(w.status, SO4_ERR_CAPACITY);
+                if (MODE == 1) {
+                    if (base + slot < w.cap_img) w.keys[base + slot] = key;
+                    else flag(w.status, SO4_ERR_CAPACITY);
+                } else if (slot < w.slot_cap) {
+                    w.keys[base + slot] = key;
+                } else {
+                    flag(w.status, SO4_ERR_SLOTS);
+                    flag(w.status, SO4_ERR_CAPACITY);
+                }
             }
             ++mine;
         }
     }
-    if (MODE == 0) {
+    if (MODE == 0 || MODE == 2) {
         int tot = mine;
 #pragma unroll
         for (int d = 16; d > 0; d >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, d);
         if (lane == 0) {
             w.cnt[a] = tot;
             if (tot == 0) flag(w.status, SO4_ERR_NO_NEIGHBOR);
+            if (MODE == 2) atomicMax(w.status + 8, tot);
         }
     }
 }
@@ -306,7 +315,8 @@ __global__ void k_sort(const so4_geom *geom, const double *pos, const int *astru
     if (a >= natoms) return;
     const so4_geom &g = geom[astruct[a]];
     const int p0 = img_ptr[a], p1 = img_ptr[a + 1];
-    if (p1 > w.cap_img) {  // the arrays are too small for this call; the host grows them and retries
+    if (p1 > w.cap_img || (w.slot_cap > 0 && p1 - p0 > w.slot_cap)) {
+        // the arrays (or this atom's key slots) are too small for this call; the host grows them
         if (lane == 0) {
             w.cnt[a] = 1;
             flag(w.status, SO4_ERR_CAPACITY);
@@ -314,10 +324,12 @@ __global__ void k_sort(const so4_geom *geom, const double *pos, const int *astru
         return;
     }
     const double pi[3] = {pos[3 * a], pos[3 * a + 1], pos[3 * a + 2]};
+    // keys of this atom: compact at [p0, p1), or in its own slots
+    const unsigned long long *kk = w.keys + ((w.slot_cap > 0) ? (int64_t)a * w.slot_cap - p0 : 0);
     for (int q = p0 + lane; q < p1; q += 32) {
-        const unsigned long long kq = w.keys[q];
+        const unsigned long long kq = kk[q];
         int rank = 0;
-        for (int p = p0; p < p1; ++p) rank += (w.keys[p] < kq) ? 1 : 0;
+        for (int p = p0; p < p1; ++p) rank += (kk[p] < kq) ? 1 : 0;
         const int dst = p0 + rank;
         const int j = (int)(kq >> 30);
         const int o0 = (int)((kq >> 20) & 1023) - OFF_BIAS;
@@ -502,6 +514,7 @@ extern "C" int so4_nl_count(const so4_geom *d_geom, int nstruct, int nbins, cons
     carve(w, d_work, natoms, nbins, 0);
     w.cap_img = 0;
     w.cap_pair = 0;
+    w.slot_cap = 0;
     cudaStream_t st = (cudaStream_t)stream;
     SO4_CUDA_TRY(cudaMemsetAsync(w.status, 0, sizeof(int), st));
     if (natoms == 0) {
@@ -538,6 +551,7 @@ extern "C" int so4_nl_fill(const so4_geom *d_geom, int nstruct, int nbins, const
     carve(w, d_work, natoms, nbins, nimg);
     w.cap_img = nimg;
     w.cap_pair = 0;
+    w.slot_cap = 0;
     cudaStream_t st = (cudaStream_t)stream;
     if (natoms == 0) {
         k_set_int<<<1, 1, 0, st>>>(d_pair_ptr, 0);
@@ -548,6 +562,70 @@ extern "C" int so4_nl_fill(const so4_geom *d_geom, int nstruct, int nbins, const
     const int grid = (natoms + warps - 1) / warps;
     k_scan_images<1><<<grid, 32 * warps, 0, st>>>(d_geom, d_pos, d_astruct, natoms, rcut, d_img_ptr, w);
     so4_count_launch();
+    k_sort<<<grid, 32 * warps, 0, st>>>(d_geom, d_pos, d_astruct, natoms, d_img_ptr, d_img_j, d_img_off, d_img_r, w);
+    so4_count_launch();
+    k_scan<<<1, 1024, 0, st>>>(w.cnt, d_pair_ptr, natoms);
+    so4_count_launch();
+    return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
+}
+
+extern "C" int so4_nl_count_keys(const so4_geom *d_geom, int nstruct, int nbins, const double *d_pos,
+                                 const int *d_astruct, int natoms, double rcut, int slot_cap, int32_t *d_img_ptr,
+                                 void *d_work, size_t work_bytes, void *stream) {
+    if (natoms < 0 || nstruct < 0 || nbins < 0 || slot_cap <= 0 || !d_work) return SO4_ERR_ARG;
+    const int64_t nkeys = (int64_t)natoms * slot_cap;
+    NLWork w;
+    if (carve(w, nullptr, natoms, nbins, nkeys) > work_bytes) return SO4_ERR_WORKSPACE;
+    carve(w, d_work, natoms, nbins, nkeys);
+    w.cap_img = 0;
+    w.cap_pair = 0;
+    w.slot_cap = slot_cap;
+    cudaStream_t st = (cudaStream_t)stream;
+    SO4_CUDA_TRY(cudaMemsetAsync(w.status, 0, 9 * sizeof(int), st));  // status, summary, largest count
+    if (natoms == 0) {
+        k_set_int<<<1, 1, 0, st>>>(d_img_ptr, 0);
+        so4_count_launch();
+        return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
+    }
+    SO4_CUDA_TRY(cudaMemsetAsync(w.bin_cnt, 0, sizeof(int) * (nbins + 1), st));
+    SO4_CUDA_TRY(cudaMemsetAsync(w.bin_cur, 0, sizeof(int) * (nbins + 1), st));
+    const int tb = 256;
+    k_bin<<<(natoms + tb - 1) / tb, tb, 0, st>>>(d_geom, d_pos, d_astruct, natoms, w);
+    so4_count_launch();
+    k_scan<<<1, 1024, 0, st>>>(w.bin_cnt, w.bin_start, nbins);
+    so4_count_launch();
+    k_bin_fill<<<(natoms + tb - 1) / tb, tb, 0, st>>>(d_astruct, natoms, w);
+    so4_count_launch();
+    const int warps = 8;
+    k_scan_images<2><<<(natoms + warps - 1) / warps, 32 * warps, 0, st>>>(d_geom, d_pos, d_astruct, natoms, rcut,
+                                                                          nullptr, w);
+    so4_count_launch();
+    k_scan<<<1, 1024, 0, st>>>(w.cnt, d_img_ptr, natoms);
+    so4_count_launch();
+    return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
+}
+
+extern "C" int so4_nl_sort(const so4_geom *d_geom, int nstruct, int nbins, const double *d_pos,
+                           const int *d_astruct, int natoms, const int32_t *d_img_ptr, int64_t nimg, int slot_cap,
+                           int32_t *d_img_j, int32_t *d_img_off, double *d_img_r, int32_t *d_pair_ptr,
+                           void *d_work, size_t work_bytes, void *stream) {
+    if (natoms < 0 || nstruct < 0 || nimg < 0 || slot_cap <= 0 || !d_work) return SO4_ERR_ARG;
+    if (nimg > 0x7fffffff) return SO4_ERR_CAPACITY;
+    const int64_t nkeys = (int64_t)natoms * slot_cap;
+    NLWork w;
+    if (carve(w, nullptr, natoms, nbins, nkeys) > work_bytes) return SO4_ERR_WORKSPACE;
+    carve(w, d_work, natoms, nbins, nkeys);
+    w.cap_img = nimg;
+    w.cap_pair = 0;
+    w.slot_cap = slot_cap;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (natoms == 0) {
+        k_set_int<<<1, 1, 0, st>>>(d_pair_ptr, 0);
+        so4_count_launch();
+        return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
+    }
+    const int warps = 8;
+    const int grid = (natoms + warps - 1) / warps;
     k_sort<<<grid, 32 * warps, 0, st>>>(d_geom, d_pos, d_astruct, natoms, d_img_ptr, d_img_j, d_img_off, d_img_r, w);
     so4_count_launch();
     k_scan<<<1, 1024, 0, st>>>(w.cnt, d_pair_ptr, natoms);

@@ -186,10 +186,12 @@ class NeighborBuffers:
     img_pair: torch.Tensor
     img_rev: torch.Tensor
 
+    slot_cap: int = 0   # > 0: the one-pass count + keys mode (so4_nl_count_keys / so4_nl_sort)
+
     @staticmethod
-    def allocate(lay: Layout, cap_m, cap_p, device, workspace=None):
+    def allocate(lay: Layout, cap_m, cap_p, device, workspace=None, slot_cap=0):
         dev, N = torch.device(device), lay.natoms
-        ws_bytes = lib().so4_nl_workspace_size(N, lay.nbins, cap_m)
+        ws_bytes = lib().so4_nl_workspace_size(N, lay.nbins, max(cap_m, N * slot_cap))
         ws = workspace if (workspace is not None and workspace.numel() >= ws_bytes) else \
             torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
         i32 = dict(dtype=torch.int32, device=dev)
@@ -197,11 +199,15 @@ class NeighborBuffers:
                                torch.empty((cap_m, 3), **i32), torch.empty((cap_m, 3), dtype=torch.float64, device=dev),
                                torch.empty(N + 1, **i32), torch.empty((cap_p, 2), dtype=torch.int64, device=dev),
                                torch.empty(cap_p + 1, **i32), torch.empty(max(N, 1), **i32),
-                               torch.empty(cap_m, **i32), torch.empty(cap_m, **i32))
+                               torch.empty(cap_m, **i32), torch.empty(cap_m, **i32), int(slot_cap))
 
     def summary_dev(self):
         """The device copy of {images, pairs, status bits} that enqueue_neighbors leaves."""
         return self.ws[16:28].view(torch.int32)
+
+    def max_count_dev(self):
+        """Largest per-atom image count (slot mode only)."""
+        return self.ws[32:36].view(torch.int32)
 
 
 def enqueue_neighbors(lay: Layout, pos, bufs: NeighborBuffers, summary=None):
@@ -210,11 +216,18 @@ def enqueue_neighbors(lay: Layout, pos, bufs: NeighborBuffers, summary=None):
     fills it, else nothing synchronises (the summary stays on the device)."""
     L, st, N, S = lib(), _stream(), lay.natoms, lay.nstruct
     b = bufs
-    check(L.so4_nl_count(_ptr(lay.geom), S, lay.nbins, _ptr(pos), _ptr(lay.atom_struct), N, lay.rcut,
-                         _ptr(b.img_ptr), _ptr(b.ws), b.ws.numel(), st), "so4_nl_count")
-    check(L.so4_nl_fill(_ptr(lay.geom), S, lay.nbins, _ptr(pos), _ptr(lay.atom_struct), N, lay.rcut, _ptr(b.img_ptr),
-                        b.cap_m, _ptr(b.img_j), _ptr(b.img_off), _ptr(b.img_r), _ptr(b.pair_ptr), _ptr(b.ws),
-                        b.ws.numel(), st), "so4_nl_fill")
+    if b.slot_cap > 0:
+        check(L.so4_nl_count_keys(_ptr(lay.geom), S, lay.nbins, _ptr(pos), _ptr(lay.atom_struct), N, lay.rcut,
+                                  b.slot_cap, _ptr(b.img_ptr), _ptr(b.ws), b.ws.numel(), st), "so4_nl_count_keys")
+        check(L.so4_nl_sort(_ptr(lay.geom), S, lay.nbins, _ptr(pos), _ptr(lay.atom_struct), N, _ptr(b.img_ptr),
+                            b.cap_m, b.slot_cap, _ptr(b.img_j), _ptr(b.img_off), _ptr(b.img_r), _ptr(b.pair_ptr),
+                            _ptr(b.ws), b.ws.numel(), st), "so4_nl_sort")
+    else:
+        check(L.so4_nl_count(_ptr(lay.geom), S, lay.nbins, _ptr(pos), _ptr(lay.atom_struct), N, lay.rcut,
+                             _ptr(b.img_ptr), _ptr(b.ws), b.ws.numel(), st), "so4_nl_count")
+        check(L.so4_nl_fill(_ptr(lay.geom), S, lay.nbins, _ptr(pos), _ptr(lay.atom_struct), N, lay.rcut,
+                            _ptr(b.img_ptr), b.cap_m, _ptr(b.img_j), _ptr(b.img_off), _ptr(b.img_r),
+                            _ptr(b.pair_ptr), _ptr(b.ws), b.ws.numel(), st), "so4_nl_fill")
     check(L.so4_nl_pairs(_ptr(lay.geom), S, _ptr(lay.atom_struct), N, _ptr(b.img_ptr), b.cap_m, _ptr(b.img_j),
                          _ptr(b.img_off), _ptr(b.pair_ptr), b.cap_p, _ptr(b.seq), _ptr(b.pair_img), _ptr(b.nsite),
                          _ptr(b.img_pair), _ptr(b.img_rev), _ptr(b.ws), b.ws.numel(), st), "so4_nl_pairs")
@@ -225,7 +238,7 @@ def enqueue_neighbors(lay: Layout, pos, bufs: NeighborBuffers, summary=None):
 def check_summary(M, P, bits, cap_m=None, cap_p=None):
     """False if a neighbour list overflowed its buffers; else raise for its status bits
     (non-finite positions, an offset beyond the encodable range, an asymmetric list)."""
-    if (cap_m is not None and M > cap_m) or (cap_p is not None and P > cap_p):
+    if (cap_m is not None and M > cap_m) or (cap_p is not None and P > cap_p) or (bits & (1 << _lib.SO4_ERR_SLOTS)):
         return False
     if bits & (1 << _lib.SO4_ERR_NONFINITE):
         raise ValueError("positions contain NaN or Inf")
