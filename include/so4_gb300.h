@@ -135,7 +135,8 @@ int so4_nl_fill(const so4_geom *d_geom, int nstruct, int nbins_total, const doub
  * d_seq[2*npair] (i64, structure-local (i, j)), d_pair_img[npair+1]
  * (images of pair p are [pair_img[p], pair_img[p+1])), d_nsite[natoms] (the
  * (i, i) pair of each centre), d_img_pair[nimg] and d_img_rev[nimg] (index of
- * the image (i, -o) in the list of j). */
+ * the image (i, -o) in the list of j).  With d_seq, d_pair_img, d_nsite and
+ * d_img_pair all NULL only d_img_rev is written (what the adjoint needs). */
 int so4_nl_pairs(const so4_geom *d_geom, int nstruct, const int *d_atom_struct, int natoms,
                  const int32_t *d_img_ptr, int64_t nimg, const int32_t *d_img_j,
                  const int32_t *d_img_off, const int32_t *d_pair_ptr, int64_t npair,

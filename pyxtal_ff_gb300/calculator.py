@@ -279,7 +279,7 @@ class CapturedStep:
 
     def _enqueue(self):
         lay, calc, tab, L = self.layout, self.calc, self.calc.tables, engine.lib()
-        engine.enqueue_neighbors(lay, self.pos, self.nl)
+        engine.enqueue_neighbors(lay, self.pos, self.nl, lite=True)
         b = self.nl
         _p = engine._ptr
         check = engine.check

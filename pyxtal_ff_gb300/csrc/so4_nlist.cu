@@ -410,10 +410,44 @@ __global__ void k_rev(const int *astruct, int natoms, const int32_t *img_ptr, co
     const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     // after an overflow the pair arrays are incomplete: nothing here may be read
     if (*(volatile int *)w.status & (1 << SO4_ERR_CAPACITY)) return;
-    if (m >= nimg || m >= img_ptr[natoms]) return;
+    const int mt = img_ptr[natoms];
+    if (m >= nimg || m >= mt) return;
     const int j = img_j[m];
-    const int p = img_pair[m];
-    const int a = (int)seq[2 * p] + geom[astruct[j]].atom_base;
+    int a;
+    if (seq) {
+        const int p = img_pair[m];
+        a = (int)seq[2 * p] + geom[astruct[j]].atom_base;
+    } else {
+        // no pair arrays: the centre is the largest i with img_ptr[i] <= m (img_ptr[0] = 0),
+        // searched from the proportional guess outwards, then by bisection
+        const int g = min(max((int)((m * natoms) / (mt > 0 ? mt : 1)), 0), natoms - 1);
+        int lo, hi, step = 1;  // img_ptr[lo] <= m < img_ptr[hi], img_ptr[natoms] = mt > m
+        if (img_ptr[g] <= m) {
+            lo = g;
+            hi = g + 1;
+            while (hi < natoms && img_ptr[hi] <= m) {
+                lo = hi;
+                step <<= 1;
+                hi = min(lo + step, natoms);
+            }
+        } else {
+            hi = g;
+            lo = g - 1;  // g > 0 here
+            while (lo > 0 && img_ptr[lo] > m) {
+                hi = lo;
+                step <<= 1;
+                lo = max(hi - step, 0);
+            }
+        }
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (img_ptr[mid] <= m)
+                lo = mid;
+            else
+                hi = mid;
+        }
+        a = lo;
+    }
     const int t0 = -img_off[3 * m], t1 = -img_off[3 * m + 1], t2 = -img_off[3 * m + 2];
     int lo = img_ptr[j], hi = img_ptr[j + 1] - 1, found = -1;
     while (lo <= hi) {
@@ -647,19 +681,25 @@ extern "C" int so4_nl_pairs(const so4_geom *d_geom, int nstruct, const int *d_as
     w.cap_pair = npair;
     cudaStream_t st = (cudaStream_t)stream;
     if (natoms == 0) {
-        k_set_int<<<1, 1, 0, st>>>(d_pair_img, 0);
-        so4_count_launch();
+        if (d_pair_img) {
+            k_set_int<<<1, 1, 0, st>>>(d_pair_img, 0);
+            so4_count_launch();
+        }
         return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
     }
-    k_sentinel<<<1, 1, 0, st>>>(d_img_ptr, d_pair_ptr, natoms, d_pair_img, w);
-    so4_count_launch();
-    const int tb = 128;
-    k_pairs<<<(natoms + tb - 1) / tb, tb, 0, st>>>(d_geom, d_astruct, natoms, d_img_ptr, d_img_j, d_pair_ptr, d_seq,
-                                                   d_pair_img, d_nsite, d_img_pair, w);
-    so4_count_launch();
+    const bool pairs = d_seq && d_pair_img && d_nsite && d_img_pair;
+    if (pairs) {
+        k_sentinel<<<1, 1, 0, st>>>(d_img_ptr, d_pair_ptr, natoms, d_pair_img, w);
+        so4_count_launch();
+        const int tb = 128;
+        k_pairs<<<(natoms + tb - 1) / tb, tb, 0, st>>>(d_geom, d_astruct, natoms, d_img_ptr, d_img_j, d_pair_ptr,
+                                                       d_seq, d_pair_img, d_nsite, d_img_pair, w);
+        so4_count_launch();
+    }
     if (nimg > 0 && d_img_rev) {
         k_rev<<<(unsigned)((nimg + 255) / 256), 256, 0, st>>>(d_astruct, natoms, d_img_ptr, d_img_j, d_img_off,
-                                                              d_img_pair, nimg, d_seq, d_geom, d_img_rev, w);
+                                                              d_img_pair, nimg, pairs ? d_seq : nullptr, d_geom,
+                                                              d_img_rev, w);
         so4_count_launch();
     }
     return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;

@@ -210,10 +210,11 @@ class NeighborBuffers:
         return self.ws[32:36].view(torch.int32)
 
 
-def enqueue_neighbors(lay: Layout, pos, bufs: NeighborBuffers, summary=None):
+def enqueue_neighbors(lay: Layout, pos, bufs: NeighborBuffers, summary=None, lite=False):
     """Launch the three neighbour-list passes for positions pos (N,3) f64 on the device
     into bufs, and the summary; with summary (a ctypes int[3]) the call waits and
-    fills it, else nothing synchronises (the summary stays on the device)."""
+    fills it, else nothing synchronises (the summary stays on the device).  lite: skip
+    the pair arrays (seq, pair_img, nsite, img_pair), keeping what the adjoint reads."""
     L, st, N, S = lib(), _stream(), lay.natoms, lay.nstruct
     b = bufs
     if b.slot_cap > 0:
@@ -228,9 +229,12 @@ def enqueue_neighbors(lay: Layout, pos, bufs: NeighborBuffers, summary=None):
         check(L.so4_nl_fill(_ptr(lay.geom), S, lay.nbins, _ptr(pos), _ptr(lay.atom_struct), N, lay.rcut,
                             _ptr(b.img_ptr), b.cap_m, _ptr(b.img_j), _ptr(b.img_off), _ptr(b.img_r),
                             _ptr(b.pair_ptr), _ptr(b.ws), b.ws.numel(), st), "so4_nl_fill")
+    pairs = not lite
     check(L.so4_nl_pairs(_ptr(lay.geom), S, _ptr(lay.atom_struct), N, _ptr(b.img_ptr), b.cap_m, _ptr(b.img_j),
-                         _ptr(b.img_off), _ptr(b.pair_ptr), b.cap_p, _ptr(b.seq), _ptr(b.pair_img), _ptr(b.nsite),
-                         _ptr(b.img_pair), _ptr(b.img_rev), _ptr(b.ws), b.ws.numel(), st), "so4_nl_pairs")
+                         _ptr(b.img_off), _ptr(b.pair_ptr), b.cap_p, _ptr(b.seq if pairs else None),
+                         _ptr(b.pair_img if pairs else None), _ptr(b.nsite if pairs else None),
+                         _ptr(b.img_pair if pairs else None), _ptr(b.img_rev), _ptr(b.ws), b.ws.numel(), st),
+          "so4_nl_pairs")
     check(L.so4_nl_summary(_ptr(b.img_ptr), _ptr(b.pair_ptr), N, _ptr(b.ws), b.ws.numel(), st, summary),
           "so4_nl_summary")
 
