@@ -84,3 +84,21 @@ def test_two_branch_graph_matches_eager_bitwise(cuda_device):
         assert step.check() and one.check()
         _equal(res, calc.compute(batch, model, positions=pos))
         _equal(res, res1)
+
+
+def test_lite_and_one_pass_neighbor_lists_match_full(cuda_device):
+    from pyxtal_ff_gb300 import engine
+    structs = [S.diamond_si(2, 2, 2, sigma=0.1, rng=np.random.default_rng(21)), S.sio2_random(n_si=8, seed=22)]
+    batch = Batch(structs)
+    pos = torch.from_numpy(batch.positions).cuda()
+    full = engine.build_neighbors(pos, batch.cells, batch.pbc, batch.atom_ptr, 4.5)
+    lay = engine.layout(batch.cells, batch.pbc, batch.atom_ptr, 4.5)
+    counts = int(torch.diff(full.img_ptr).max())
+    bufs = engine.NeighborBuffers.allocate(lay, full.nimg + 64, full.npair + 64, "cuda", slot_cap=counts + 8)
+    engine.enqueue_neighbors(lay, pos, bufs, lite=True)
+    M, P, bits = [int(v) for v in bufs.summary_dev().cpu()]
+    assert M == full.nimg and P == full.npair and engine.check_summary(M, P, bits, bufs.cap_m, bufs.cap_p)
+    for a, b in ((bufs.img_ptr, full.img_ptr), (bufs.img_j[:M], full.img_j), (bufs.img_off[:M], full.img_off),
+                 (bufs.img_r[:M], full.img_r), (bufs.img_rev[:M], full.img_rev)):
+        assert torch.equal(a, b)
+    assert int(bufs.max_count_dev().cpu()[0]) == counts
