@@ -32,13 +32,14 @@ struct JArgs {
     const ZTerm *terms;
     const int4 *unit, *seg;
     SmallTables st;
+    const int2 *hmap;  // per half entry: accumulator slot, row, u_norm
     float2 *dU;
     float *dB;
 };
 
 // tangent of U_tot, one warp per centre (same layout as k_utot_rc)
 template <int TWOL, int NW>
-__global__ void __launch_bounds__(NW * 32) k_jvp_du_rc(JArgs A) {
+__global__ void __launch_bounds__(NW * 32, (TWOL <= 6) ? 4 : ((TWOL == 8) ? 3 : 1)) k_jvp_du_rc(JArgs A) {
     using RC = RowChain<TWOL>;
     constexpr int W = TWOL + 1, NACC = acc_block(TWOL + 1);
     extern __shared__ __align__(16) float jv_smem[];
@@ -61,7 +62,8 @@ __global__ void __launch_bounds__(NW * 32) k_jvp_du_rc(JArgs A) {
         }
         for (int base = m0; base < m1; base += RC::IPW) {
             const int m = base + grp;
-            float x = 1.f, y = 0.f, z = 0.f, a_du = 0.f, ax = 0.f, ay = 0.f, az = 0.f;
+            float x = 1.f, y = 0.f, z = 0.f, a_du = 0.f, a_d = 0.f;
+            float d[3] = {0.f, 0.f, 0.f};
             if (grp < RC::IPW && m < m1) {
                 x = (float)A.img_r[3 * m];
                 y = (float)A.img_r[3 * m + 1];
@@ -69,7 +71,6 @@ __global__ void __launch_bounds__(NW * 32) k_jvp_du_rc(JArgs A) {
                 const float rr = sqrtf(x * x + y * y + z * z);
                 if (rr >= 1e-8f) {
                     const int j = A.img_j[m];
-                    float d[3] = {0.f, 0.f, 0.f};
                     if (A.v)
                         for (int c = 0; c < 3; ++c) d[c] = (float)A.v[3 * j + c] - vi[c];
                     // dr_b += sum_a G_ab r_a
@@ -78,11 +79,9 @@ __global__ void __launch_bounds__(NW * 32) k_jvp_du_rc(JArgs A) {
                     d[2] += G[2] * x + G[5] * y + G[8] * z;
                     float sf, dsf;
                     cutoff_fn<float>(A.cutoff_id, rr, A.rc32, sf, dsf);
-                    const float w = (float)A.w_nb[A.img_j[m]];
+                    const float w = (float)A.w_nb[j];
                     a_du = w * dsf * (x * d[0] + y * d[1] + z * d[2]) / rr;
-                    ax = w * sf * d[0];
-                    ay = w * sf * d[1];
-                    az = w * sf * d[2];
+                    a_d = w * sf;
                 } else {
                     x = 1.f;
                     y = z = 0.f;
@@ -91,16 +90,25 @@ __global__ void __launch_bounds__(NW * 32) k_jvp_du_rc(JArgs A) {
             const float r = sqrtf(x * x + y * y + z * z);
             CK<float> ck;
             make_ck<float, true>(x, y, z, r, A.psi_fac * r, ck);
-            float ur[W], ui[W], dr[3][W], di[3][W];
+            // the derivative of conj(a), conj(b) along dr_m, in slot 0
+            {
+                cx<float> da = mk<float>(0.f, 0.f), db = mk<float>(0.f, 0.f);
 #pragma unroll
-            for (int q = 0; q < W; ++q) {
-                ur[q] = ui[q] = 0.f;
-#pragma unroll
-                for (int c = 0; c < 3; ++c) dr[c][q] = di[c][q] = 0.f;
+                for (int c = 0; c < 3; ++c) {
+                    da.re += d[c] * ck.cda[c].re;
+                    da.im += d[c] * ck.cda[c].im;
+                    db.re += d[c] * ck.cdb[c].re;
+                    db.im += d[c] * ck.cdb[c].im;
+                }
+                ck.cda[0] = da;
+                ck.cdb[0] = db;
             }
+            float ur[W], ui[W], dr[1][W], di[1][W];
+#pragma unroll
+            for (int q = 0; q < W; ++q) ur[q] = ui[q] = dr[0][q] = di[0][q] = 0.f;
             ur[0] = 1.f;
             if (mb == 0) accr[0] += a_du;  // level 0: U = 1, dU = 0
-            RcJvp<TWOL, 1>::run(mb, ck, a_du, ax, ay, az, ur, ui, dr, di, accr, acci);
+            RcJvp<TWOL, 1>::run(mb, ck, a_du, a_d, ur, ui, dr, di, accr, acci);
         }
     }
     float *sw = jv_smem + (size_t)wid * 32 * 2 * NACC;
@@ -113,17 +121,16 @@ __global__ void __launch_bounds__(NW * 32) k_jvp_du_rc(JArgs A) {
     if (a >= A.natoms) return;
     float2 *out = A.dU + (size_t)a * A.nh;
     for (int e = lane; e < A.nh; e += 32) {
-        int L = 0;
-        while (L < TWOL && half_block(L + 1) <= e) ++L;
-        const int off = e - half_block(L);
-        const int row = off / (L + 1), ma = off - row * (L + 1);
+        const int2 h = __ldg(A.hmap + e);
+        const int slot = h.x & 0xff, row = (h.x >> 8) & 0x7f;
         float sr = 0.f, si = 0.f;
+#pragma unroll
         for (int g = 0; g < RC::IPW; ++g) {
-            const float *src = sw + (g * RC::NCH + row) * 2 * NACC + 2 * (acc_block(L) + ma);
+            const float *src = sw + (g * RC::NCH + row) * 2 * NACC + 2 * slot;
             sr += src[0];
             si += src[1];
         }
-        const float un = (float)A.st.unorm[L];
+        const float un = __int_as_float(h.y);
         out[e] = make_float2(sr * un, si * un);
     }
 }
@@ -207,6 +214,7 @@ extern "C" int so4_jvp32(const so4_tables *t, const so4_params *p, const int *d_
     A.unit = t->d_junit;
     A.seg = t->d_jseg;
     fill_small_tables(t, A.st);
+    A.hmap = t->d_hmap;
     A.dU = (float2 *)((char *)d_work + a256j(SO4_WS_HEADER));
     A.dB = d_dB;
     int rc;

@@ -40,16 +40,18 @@ struct RowChain {
 
 // Advance one image's chain `mb` from level L-1 to level L (in place).
 // u, d0, d1, d2: the row (re, im) of U and of dU/dx, dU/dy, dU/dz.
-template <int TWOL, int L, bool DERIV>
+template <int TWOL, int L, bool DERIV, int NDER = 3>
 __device__ __forceinline__ void rc_level(int mb, const CK<float> &ck, float (&ur)[TWOL + 1], float (&ui)[TWOL + 1],
-                                         float (&dr)[3][TWOL + 1], float (&di)[3][TWOL + 1]) {
+                                         float (&dr)[NDER][TWOL + 1], float (&di)[NDER][TWOL + 1]) {
     // 1 / sqrt(l - mb); lanes whose chain has not started (mb > L/2) compute values nobody reads
     const float inv_q = rsqrtf((float)max(L - mb, 1));
     // descending in place: new[ma] uses old[ma] (a-term) and old[ma-1] (b-term)
 #pragma unroll
     for (int ma = L; ma >= 0; --ma) {
         float vr = 0.f, vi = 0.f;
-        float er[3] = {0.f, 0.f, 0.f}, ei[3] = {0.f, 0.f, 0.f};
+        float er[NDER], ei[NDER];
+#pragma unroll
+        for (int c = 0; c < NDER; ++c) er[c] = ei[c] = 0.f;
         if (ma > 0) {
             const float rp = -c_sqrtk[ma] * inv_q;
             const float pr = ur[ma - 1], pi = ui[ma - 1];
@@ -60,7 +62,7 @@ __device__ __forceinline__ void rc_level(int mb, const CK<float> &ck, float (&ur
             vi = rp * bi;
             if (DERIV) {
 #pragma unroll
-                for (int c = 0; c < 3; ++c) {
+                for (int c = 0; c < NDER; ++c) {
                     const float qr = dr[c][ma - 1], qi = di[c][ma - 1];
                     const float tr = ck.cdb[c].re * pr - ck.cdb[c].im * pi + ck.cb.re * qr - ck.cb.im * qi;
                     const float ti = ck.cdb[c].re * pi + ck.cdb[c].im * pr + ck.cb.re * qi + ck.cb.im * qr;
@@ -78,7 +80,7 @@ __device__ __forceinline__ void rc_level(int mb, const CK<float> &ck, float (&ur
             vi += rp * ai;
             if (DERIV) {
 #pragma unroll
-                for (int c = 0; c < 3; ++c) {
+                for (int c = 0; c < NDER; ++c) {
                     const float qr = dr[c][ma], qi = di[c][ma];
                     const float tr = ck.cda[c].re * pr - ck.cda[c].im * pi + ck.ca.re * qr - ck.ca.im * qi;
                     const float ti = ck.cda[c].re * pi + ck.cda[c].im * pr + ck.ca.re * qi + ck.ca.im * qr;
@@ -91,7 +93,7 @@ __device__ __forceinline__ void rc_level(int mb, const CK<float> &ck, float (&ur
         ui[ma] = vi;
         if (DERIV) {
 #pragma unroll
-            for (int c = 0; c < 3; ++c) {
+            for (int c = 0; c < NDER; ++c) {
                 dr[c][ma] = er[c];
                 di[c][ma] = ei[c];
             }
@@ -103,7 +105,7 @@ __device__ __forceinline__ void rc_level(int mb, const CK<float> &ck, float (&ur
         ui[H] = -ui[H];
         if (DERIV) {
 #pragma unroll
-            for (int c = 0; c < 3; ++c) di[c][H] = -di[c][H];
+            for (int c = 0; c < NDER; ++c) di[c][H] = -di[c][H];
         }
 #pragma unroll
         for (int ma = H + 1; ma <= L; ++ma) {
@@ -112,7 +114,7 @@ __device__ __forceinline__ void rc_level(int mb, const CK<float> &ck, float (&ur
             ui[ma] = -s * ui[L - ma];
             if (DERIV) {
 #pragma unroll
-                for (int c = 0; c < 3; ++c) {
+                for (int c = 0; c < NDER; ++c) {
                     dr[c][ma] = s * dr[c][L - ma];
                     di[c][ma] = -s * di[c][L - ma];
                 }
@@ -127,9 +129,9 @@ __device__ __forceinline__ void rc_level(int mb, const CK<float> &ck, float (&ur
 // Every lane shuffles (the warp stays converged); only mb == L/2 keeps the
 // values.  The source lane is never the taking lane, so writing slot c while
 // later shuffles read slots L-1-c of lane-1 is safe.
-template <int TWOL, int L, bool DERIV>
+template <int TWOL, int L, bool DERIV, int NDER = 3>
 __device__ __forceinline__ void rc_start(int mb, float (&ur)[TWOL + 1], float (&ui)[TWOL + 1],
-                                         float (&dr)[3][TWOL + 1], float (&di)[3][TWOL + 1]) {
+                                         float (&dr)[NDER][TWOL + 1], float (&di)[NDER][TWOL + 1]) {
     constexpr int H = L / 2;
     const bool take = (mb == H);
 #pragma unroll
@@ -143,7 +145,7 @@ __device__ __forceinline__ void rc_start(int mb, float (&ur)[TWOL + 1], float (&
         }
         if (DERIV) {
 #pragma unroll
-            for (int k = 0; k < 3; ++k) {
+            for (int k = 0; k < NDER; ++k) {
                 const float wr = __shfl_up_sync(0xffffffffu, dr[k][L - 1 - c], 1);
                 const float wi = __shfl_up_sync(0xffffffffu, di[k][L - 1 - c], 1);
                 if (take) {
@@ -226,32 +228,32 @@ struct RcUtot<TWOL, TWOL + 1> {
                                                float (&)[acc_block(TWOL + 1)], float (&)[acc_block(TWOL + 1)]) {}
 };
 
-// Levels L..TWOL with derivatives; after each level the lane adds the
-// directional derivative of its row along the image displacement dr_m,
-//   w (sfac sum_c dU_c dr_c + dsfac (r^ . dr) U),
-// into its accumulator (the tangent of U_tot used by the JVP).
+// Levels L..TWOL with the derivative along one direction per image (ck.cda[0],
+// ck.cdb[0] hold d conj(a), d conj(b) along it); after each level the lane adds
+//   a_du U + a_d dU   (a_du = w dsfac (r^ . dr_m), a_d = w sfac)
+// of its row into its accumulator (the tangent of U_tot used by the JVP).
 template <int TWOL, int L>
 struct RcJvp {
-    __device__ __forceinline__ static void run(int mb, const CK<float> &ck, float a_du, float a_dx, float a_dy,
-                                               float a_dz, float (&ur)[TWOL + 1], float (&ui)[TWOL + 1],
-                                               float (&dr)[3][TWOL + 1], float (&di)[3][TWOL + 1],
+    __device__ __forceinline__ static void run(int mb, const CK<float> &ck, float a_du, float a_d,
+                                               float (&ur)[TWOL + 1], float (&ui)[TWOL + 1],
+                                               float (&dr)[1][TWOL + 1], float (&di)[1][TWOL + 1],
                                                float (&accr)[acc_block(TWOL + 1)], float (&acci)[acc_block(TWOL + 1)]) {
-        if ((L & 1) == 0) rc_start<TWOL, L, true>(mb, ur, ui, dr, di);
-        rc_level<TWOL, L, true>(mb, ck, ur, ui, dr, di);
+        if ((L & 1) == 0) rc_start<TWOL, L, true, 1>(mb, ur, ui, dr, di);
+        rc_level<TWOL, L, true, 1>(mb, ck, ur, ui, dr, di);
         if (2 * mb <= L) {
 #pragma unroll
             for (int ma = 0; ma <= L; ++ma) {
-                accr[acc_block(L) + ma] += a_du * ur[ma] + a_dx * dr[0][ma] + a_dy * dr[1][ma] + a_dz * dr[2][ma];
-                acci[acc_block(L) + ma] += a_du * ui[ma] + a_dx * di[0][ma] + a_dy * di[1][ma] + a_dz * di[2][ma];
+                accr[acc_block(L) + ma] += a_du * ur[ma] + a_d * dr[0][ma];
+                acci[acc_block(L) + ma] += a_du * ui[ma] + a_d * di[0][ma];
             }
         }
-        RcJvp<TWOL, L + 1>::run(mb, ck, a_du, a_dx, a_dy, a_dz, ur, ui, dr, di, accr, acci);
+        RcJvp<TWOL, L + 1>::run(mb, ck, a_du, a_d, ur, ui, dr, di, accr, acci);
     }
 };
 template <int TWOL>
 struct RcJvp<TWOL, TWOL + 1> {
-    __device__ __forceinline__ static void run(int, const CK<float> &, float, float, float, float, float (&)[TWOL + 1],
-                                               float (&)[TWOL + 1], float (&)[3][TWOL + 1], float (&)[3][TWOL + 1],
+    __device__ __forceinline__ static void run(int, const CK<float> &, float, float, float (&)[TWOL + 1],
+                                               float (&)[TWOL + 1], float (&)[1][TWOL + 1], float (&)[1][TWOL + 1],
                                                float (&)[acc_block(TWOL + 1)], float (&)[acc_block(TWOL + 1)]) {}
 };
 
