@@ -197,13 +197,15 @@ struct ZLArgs {
     float *eatom;  // fused path: sum_k beta_k B_k per atom (may be null)
     const int4 *wsub;  // window sub-segments
     const float *wca;  // window Ca rows
+    int nwca;          // their floats (a multiple of 4)
 };
 
 
 // One window unit of K entries: Z of every block feeding its level; Y (MODE 1, 2)
 // and the B-section scratch (MODE 0, 2).
 template <int MODE, int K>
-__device__ __forceinline__ void zw_unit(const ZLArgs &A, const int4 un, const float2 *Ul, const float *coef, int a,
+__device__ __forceinline__ void zw_unit(const ZLArgs &A, const int4 un, const float2 *Ul, const float *coef,
+                                        const float *__restrict__ ca, int a,
                                         int lane) {
     const int lam = un.x & 0xff, mb = (un.x >> 8) & 0xff, ma0 = (un.x >> 16) & 0xff;
     const int off0 = mb * (lam + 1) + ma0;
@@ -224,7 +226,7 @@ __device__ __forceinline__ void zw_unit(const ZLArgs &A, const int4 un, const fl
         for (int r = sg.x; r < sg.y; ++r) {
             const int4 hd = hdn;
             if (r + 1 < sg.y) hdn = __ldg(A.wsub + r + 1);
-            zw_rows<K>(Ul, hd, A.wca, zr, zi);
+            zw_rows<K>(Ul, hd, ca, zr, zi);
         }
         if (MODE != 0) {
             const float c = coef[sg.z * ZL_PITCH + lane];
@@ -272,7 +274,7 @@ constexpr int ZW_THREADS = 256;  // 8 warps share one CTA's 32 atoms
 // per (unit, B block), the unit's part of the section sum sum_e w_e Re(conj(U_lam[e]) Z[e])
 // into the slot-major scratch d_bc, then B_k = 2 x the sum of component k's slots in
 // a fixed order (compute_bi, SO4.py:1071-1111) and, with d_eatom, beta . B per atom.
-template <int MODE>
+template <int MODE, bool CA_SMEM>
 __global__ void __launch_bounds__(ZW_THREADS, 2) k_zw32(ZLArgs A) {
     extern __shared__ __align__(16) float2 zw_smem[];
     __shared__ int s_unit;
@@ -295,19 +297,29 @@ __global__ void __launch_bounds__(ZW_THREADS, 2) k_zw32(ZLArgs A) {
             coef[b * ZL_PITCH + l] = c;
         }
     }
+    // the window coefficients (read at every step) in shared memory when they fit
+    // (16-byte aligned for the float4 reads; the launch adds 16 bytes of slack)
+    float *ca_s = reinterpret_cast<float *>((reinterpret_cast<uintptr_t>(coef + (size_t)A.nblk * ZL_PITCH) + 15) &
+                                            ~(uintptr_t)15);
+    if (CA_SMEM) {
+        const float4 *src = reinterpret_cast<const float4 *>(A.wca);
+        float4 *dst = reinterpret_cast<float4 *>(ca_s);
+        for (int i = threadIdx.x; i < A.nwca / 4; i += blockDim.x) dst[i] = __ldg(src + i);
+    }
+    const float *ca = CA_SMEM ? ca_s : A.wca;
     __syncthreads();
     const float2 *Ul = Ub + lane;
     for (int u = zl_next(&s_unit); u < A.nunit; u = zl_next(&s_unit)) {
         const int4 un = __ldg(A.unit + u);
         switch (un.x >> 24) {
-            case 1: zw_unit<MODE, 1>(A, un, Ul, coef, a, lane); break;
-            case 2: zw_unit<MODE, 2>(A, un, Ul, coef, a, lane); break;
-            case 3: zw_unit<MODE, 3>(A, un, Ul, coef, a, lane); break;
-            case 4: zw_unit<MODE, 4>(A, un, Ul, coef, a, lane); break;
-            case 5: zw_unit<MODE, 5>(A, un, Ul, coef, a, lane); break;
-            case 6: zw_unit<MODE, 6>(A, un, Ul, coef, a, lane); break;
-            case 7: zw_unit<MODE, 7>(A, un, Ul, coef, a, lane); break;
-            default: zw_unit<MODE, 8>(A, un, Ul, coef, a, lane); break;
+            case 1: zw_unit<MODE, 1>(A, un, Ul, coef, ca, a, lane); break;
+            case 2: zw_unit<MODE, 2>(A, un, Ul, coef, ca, a, lane); break;
+            case 3: zw_unit<MODE, 3>(A, un, Ul, coef, ca, a, lane); break;
+            case 4: zw_unit<MODE, 4>(A, un, Ul, coef, ca, a, lane); break;
+            case 5: zw_unit<MODE, 5>(A, un, Ul, coef, ca, a, lane); break;
+            case 6: zw_unit<MODE, 6>(A, un, Ul, coef, ca, a, lane); break;
+            case 7: zw_unit<MODE, 7>(A, un, Ul, coef, ca, a, lane); break;
+            default: zw_unit<MODE, 8>(A, un, Ul, coef, ca, a, lane); break;
         }
     }
     if (MODE == 1) return;
@@ -698,12 +710,32 @@ static ZLArgs zl_args(const so4_tables *t, int natoms) {
     Z.ylist = t->d_yblk;
     Z.wsub = t->d_wsub;
     Z.wca = t->d_wca;
+    Z.nwca = t->n_wca;
     fill_small_tables(t, Z.st);
     return Z;
 }
 
 // shared memory of k_zw32: padded U tiles and the per-block coefficients; the B
 // epilogue (with_b) reuses the U tiles for nB x 33 floats
+// Launch k_zw32<MODE> with the Ca table in shared memory when two CTAs per SM still fit.
+template <int MODE>
+static int launch_zw(const so4_tables *t, const ZLArgs &Z, int natoms, size_t smz, cudaStream_t st) {
+    const size_t with_ca = smz + 16 + sizeof(float) * (size_t)t->n_wca;
+    const int groups = (natoms + 31) / 32;
+    int rc;
+    if (2 * (with_ca + 1024) <= 228 * 1024) {
+        rc = set_smem(k_zw32<MODE, true>, with_ca);
+        if (rc) return rc;
+        k_zw32<MODE, true><<<groups, ZW_THREADS, with_ca, st>>>(Z);
+    } else {
+        rc = set_smem(k_zw32<MODE, false>, smz);
+        if (rc) return rc;
+        k_zw32<MODE, false><<<groups, ZW_THREADS, smz, st>>>(Z);
+    }
+    so4_count_launch();
+    return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
+}
+
 static size_t zw_smem_bytes(const so4_tables *t, bool with_b) {
     size_t u = sizeof(float2) * (size_t)(t->n_u + 2 * ZW_PAD) * ZL_PITCH;
     if (with_b) u = std::max(u, sizeof(float) * (size_t)t->n_b * ZL_PITCH);
@@ -778,11 +810,7 @@ extern "C" int so4_forward32(const so4_tables *t, const so4_params *p, int natom
     Z.nbsec = t->n_bsec;
     Z.bc = (float *)d_work;
     const size_t smz = zw_smem_bytes(t, true);
-    rc = set_smem(k_zw32<0>, smz);
-    if (rc) return rc;
-    k_zw32<0><<<(natoms + 31) / 32, ZW_THREADS, smz, st>>>(Z);
-    so4_count_launch();
-    return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
+    return launch_zw<0>(t, Z, natoms, smz, st);
 }
 
 extern "C" size_t so4_adjoint_workspace_size(const so4_tables *t, int natoms, int64_t nimg) {
@@ -803,11 +831,7 @@ extern "C" int so4_adjoint_y32(const so4_tables *t, int natoms, const float *d_u
     Z.beta = d_beta;
     Z.Y = (float2 *)d_y;
     const size_t smz = zw_smem_bytes(t, false);
-    int rc = set_smem(k_zw32<1>, smz);
-    if (rc) return rc;
-    k_zw32<1><<<(natoms + 31) / 32, ZW_THREADS, smz, (cudaStream_t)stream>>>(Z);
-    so4_count_launch();
-    return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
+    return launch_zw<1>(t, Z, natoms, smz, (cudaStream_t)stream);
 }
 
 extern "C" int so4_adjoint_deidrj32(const so4_tables *t, const so4_params *p, int natoms, const double *d_w_nb,
@@ -1062,11 +1086,7 @@ extern "C" int so4_linear_by32(const so4_tables *t, int natoms, const float *d_u
     Z.bc = d_bc;
     Z.eatom = d_eatom;
     const size_t smz = zw_smem_bytes(t, true);
-    int rc = set_smem(k_zw32<2>, smz);
-    if (rc) return rc;
-    k_zw32<2><<<(natoms + 31) / 32, ZW_THREADS, smz, (cudaStream_t)stream>>>(Z);
-    so4_count_launch();
-    return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
+    return launch_zw<2>(t, Z, natoms, smz, (cudaStream_t)stream);
 }
 
 extern "C" int so4_adjoint_linear32(const so4_tables *t, const so4_params *p, int nstruct, const int *d_atom_struct,

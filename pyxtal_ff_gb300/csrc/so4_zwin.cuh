@@ -52,7 +52,7 @@ __device__ __forceinline__ void zw_rows(const float2 *Ul, const int4 hd, const f
                 float cc[4 * KQ];
 #pragma unroll
                 for (int q = 0; q < KQ; ++q) {
-                    const float4 c4 = __ldg(cw + j * KQ + q);
+                    const float4 c4 = cw[j * KQ + q];  // shared memory or the read-only global table
                     cc[4 * q] = c4.x;
                     cc[4 * q + 1] = c4.y;
                     cc[4 * q + 2] = c4.z;
