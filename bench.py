@@ -35,9 +35,10 @@ CONFIG = {"workload": "diamond-Si 20x20x10 (32000 atoms), SO4 lmax=4, rcut=5.0 A
                   "dE/dr, gather (compensated FP32 per atom, FP64 across atoms)"}
 
 
-# DRAM bytes (read + write) per launch of each stage's kernel, from the ncu capture
-# summarised in profiles/k_zw32_k_deidrj_rev_k_utot_rc_si32000_lmax4.md (same workload)
-NCU_TRAFFIC = {"utot32": 26.09e6, "linear_by32": 71.90e6, "adjoint_deidrj32": 67.30e6}
+# DRAM bytes (read + write) per full launch of each stage's kernel: twice the figures of
+# the half-size launches (one graph branch each) captured with ncu and summarised in
+# profiles/k_zw32_k_deidrj_rev_k_utot_rc_si32000_lmax4.md (same workload)
+NCU_TRAFFIC = {"utot32": 25.8e6, "linear_by32": 47.2e6, "adjoint_deidrj32": 65.5e6}
 
 
 def workload():
