@@ -198,7 +198,6 @@ struct ZLArgs {
     const int4 *wsub;  // window sub-segments
     const float *wca;  // window Ca rows
     int nwca;          // their floats (a multiple of 4)
-    int nwsub;         // sub-segment headers
 };
 
 
@@ -214,33 +213,19 @@ __device__ __forceinline__ void zw_unit(const ZLArgs &A, const int4 un, const fl
     float yr[K], yi[K];
 #pragma unroll
     for (int k = 0; k < K; ++k) yr[k] = yi[k] = 0.f;
-    // The unit's segment and sub-segment headers are read 32 at a time, one per lane
-    // (one coalesced load), and handed to the whole warp by shuffles: a header costs a
-    // few shuffles instead of a dependent global load.  The chunk index is uniform over
-    // the warp, so every lane takes the same branch.
-    int4 sreg = make_int4(0, 0, 0, -1), hreg = make_int4(0, 0, 0, 0);
-    int schunk = -1, hbase = -64;  // sub-segment indices only grow within a unit
+    // headers are prefetched one ahead: the next segment's and the next sub-segment's
+    // loads are in flight while the current one computes
+    int4 sgn = (un.y < un.z) ? __ldg(A.seg + un.y) : make_int4(0, 0, 0, -1);
     for (int q = un.y; q < un.z; ++q) {
-        const int qc = (q - un.y) >> 5;
-        if (qc != schunk) {
-            schunk = qc;
-            const int i = un.y + 32 * qc + lane;
-            sreg = (i < un.z) ? __ldg(A.seg + i) : make_int4(0, 0, 0, -1);
-        }
-        const int qs = (q - un.y) & 31;
-        const int4 sg = make_int4(__shfl_sync(0xffffffffu, sreg.x, qs), __shfl_sync(0xffffffffu, sreg.y, qs),
-                                  __shfl_sync(0xffffffffu, sreg.z, qs), __shfl_sync(0xffffffffu, sreg.w, qs));
+        const int4 sg = sgn;
+        if (q + 1 < un.z) sgn = __ldg(A.seg + q + 1);
         float zr[K], zi[K];
 #pragma unroll
         for (int k = 0; k < K; ++k) zr[k] = zi[k] = 0.f;
+        int4 hdn = (sg.x < sg.y) ? __ldg(A.wsub + sg.x) : make_int4(0, 0, 0, 0);
         for (int r = sg.x; r < sg.y; ++r) {
-            if (r - hbase >= 32) {
-                hbase = r;
-                hreg = __ldg(A.wsub + min(r + lane, A.nwsub - 1));
-            }
-            const int rs = r - hbase;
-            const int4 hd = make_int4(__shfl_sync(0xffffffffu, hreg.x, rs), __shfl_sync(0xffffffffu, hreg.y, rs),
-                                      __shfl_sync(0xffffffffu, hreg.z, rs), __shfl_sync(0xffffffffu, hreg.w, rs));
+            const int4 hd = hdn;
+            if (r + 1 < sg.y) hdn = __ldg(A.wsub + r + 1);
             zw_rows<K>(Ul, hd, ca, zr, zi);
         }
         if (MODE != 0) {
@@ -726,7 +711,6 @@ static ZLArgs zl_args(const so4_tables *t, int natoms) {
     Z.wsub = t->d_wsub;
     Z.wca = t->d_wca;
     Z.nwca = t->n_wca;
-    Z.nwsub = t->n_wsub;
     fill_small_tables(t, Z.st);
     return Z;
 }

@@ -135,7 +135,7 @@ struct so4_tables {
     int4 *d_wunit_y = nullptr, *d_wseg_y = nullptr, *d_wunit_b = nullptr, *d_wseg_b = nullptr;
     int4 *d_wsub = nullptr;
     float *d_wca = nullptr;
-    int n_wunit_y = 0, n_wunit_b = 0, n_wca = 0, n_wsub = 0;
+    int n_wunit_y = 0, n_wunit_b = 0, n_wca = 0;
     int n_terms = 0;
     std::vector<int> term_ptr;
 };

@@ -496,7 +496,6 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
     t->n_wunit_y = (int)wunit_y.size();
     t->n_wunit_b = (int)wunit_b.size();
     t->n_wca = (int)wca.size();
-    t->n_wsub = (int)wsub.size();
 
     std::vector<int> fmap(t->n_u);
     for (int l = 0; l < ld; ++l)
