@@ -199,12 +199,10 @@ def main():
         if ws > 1:
             dist.barrier()
 
+    from pyxtal_ff_gb300 import replicas
+
     def max_over_ranks(v):
-        if ws == 1:
-            return v
-        t = torch.tensor([v], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return replicas.max_over_ranks(v, device=dev)
 
     from pyxtal_ff_gb300 import _lib, engine, flops
     from pyxtal_ff_gb300.calculator import Batch, LinearModel, SO4Calculator, contract_plain
