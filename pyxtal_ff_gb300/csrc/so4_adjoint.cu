@@ -198,11 +198,16 @@ struct ZLArgs {
     const int4 *wsub;  // window sub-segments
     const float *wca;  // window Ca rows
     int nwca;          // their floats (a multiple of 4)
+    // JVP (MODE 3): tangent dU [natoms][nh], per (block, role) slot base / factor, slot range
+    // of each component; the slots go to bc and dB to x
+    const float2 *dU;
+    const int *jbase, *jpos;
+    const float *jfac;
 };
 
 
-// One window unit of K entries: Z of every block feeding its level; Y (MODE 1, 2)
-// and the B-section scratch (MODE 0, 2).
+// One window unit of K entries: Z of every block feeding its level; Y (MODE 1, 2),
+// the B-section scratch (MODE 0, 2) or the JVP section scratch (MODE 3).
 template <int MODE, int K>
 __device__ __forceinline__ void zw_unit(const ZLArgs &A, const int4 un, const float2 *Ul, const float *coef,
                                         const float *__restrict__ ca, int a,
@@ -213,6 +218,20 @@ __device__ __forceinline__ void zw_unit(const ZLArgs &A, const int4 un, const fl
     float yr[K], yi[K];
 #pragma unroll
     for (int k = 0; k < K; ++k) yr[k] = yi[k] = 0.f;
+    // MODE 3: w_e dU[e] of the unit's entries in the section (0 past its end), reused by every block
+    float dur[K], dui[K];
+    if (MODE == 3) {
+        const float2 *dp = A.dU + (size_t)min(a, A.natoms - 1) * A.nh + A.st.h_block[lam] + off0;
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const int off = off0 + k;
+            float2 d = make_float2(0.f, 0.f);
+            if (off < cnt) d = __ldg(dp + k);
+            const float w = ((lam & 1) == 0 && off == cnt - 1) ? 0.5f : 1.f;
+            dur[k] = w * d.x;
+            dui[k] = w * d.y;
+        }
+    }
     // headers are prefetched one ahead: the next segment's and the next sub-segment's
     // loads are in flight while the current one computes
     int4 sgn = (un.y < un.z) ? __ldg(A.seg + un.y) : make_int4(0, 0, 0, -1);
@@ -228,7 +247,22 @@ __device__ __forceinline__ void zw_unit(const ZLArgs &A, const int4 un, const fl
             if (r + 1 < sg.y) hdn = __ldg(A.wsub + r + 1);
             zw_rows<K>(Ul, hd, ca, zr, zi);
         }
-        if (MODE != 0) {
+        if (MODE == 3) {
+            // sum_e w_e Re(conj(dU[e]) Z[e]) over the unit's section entries, once per role of
+            // the block: slot (jbase + unit index) of the role's component, scaled by fac_s
+            float v = 0.f;
+#pragma unroll
+            for (int k = 0; k < K; ++k) v = fmaf(dur[k], zr[k], fmaf(dui[k], zi[k], v));
+            if (a < A.natoms) {
+#pragma unroll
+                for (int r = 0; r < 3; ++r) {
+                    const int jb = __ldg(A.jbase + 3 * sg.z + r);
+                    if (jb < 0) break;
+                    A.bc[(size_t)(jb + sg.w) * A.natoms + a] = __ldg(A.jfac + 3 * sg.z + r) * v;
+                }
+            }
+        }
+        if (MODE == 1 || MODE == 2) {
             const float c = coef[sg.z * ZL_PITCH + lane];
 #pragma unroll
             for (int k = 0; k < K; ++k) {
@@ -236,7 +270,7 @@ __device__ __forceinline__ void zw_unit(const ZLArgs &A, const int4 un, const fl
                 yi[k] = fmaf(c, zi[k], yi[k]);
             }
         }
-        if (MODE != 1 && sg.w >= 0) {
+        if ((MODE == 0 || MODE == 2) && sg.w >= 0) {
             // this unit's part of the B component of the block: sum over its entries in the
             // B section of w_e Re(conj(U_lam[e]) Z[e]), w_e = 1/2 at the middle-row centre
             const float2 *ul = Ul + (ZW_PAD + A.st.u_block[lam] + off0) * ZL_PITCH;
@@ -254,7 +288,7 @@ __device__ __forceinline__ void zw_unit(const ZLArgs &A, const int4 un, const fl
             if (a < A.natoms) A.bc[(size_t)sg.w * A.natoms + a] = v;
         }
     }
-    if (MODE != 0 && a < A.natoms) {
+    if ((MODE == 1 || MODE == 2) && a < A.natoms) {
         const float un_l = __int_as_float(un.w);
         float2 *Yo = A.Y + (size_t)a * A.nh + A.st.h_block[lam] + off0;
 #pragma unroll
@@ -274,6 +308,8 @@ constexpr int ZW_THREADS = 256;  // 8 warps share one CTA's 32 atoms
 // per (unit, B block), the unit's part of the section sum sum_e w_e Re(conj(U_lam[e]) Z[e])
 // into the slot-major scratch d_bc, then B_k = 2 x the sum of component k's slots in
 // a fixed order (compute_bi, SO4.py:1071-1111) and, with d_eatom, beta . B per atom.
+// MODE 3: the JVP dB_k = sum_s fac_s sum_e w_e Re(conj(dU[e]) Z_s[e]) (compute_dbidrj,
+// SO4.py:1113-1227, along one tangent dU): per (unit, block, role) slots, summed per k.
 template <int MODE, bool CA_SMEM>
 __global__ void __launch_bounds__(ZW_THREADS, 2) k_zw32(ZLArgs A) {
     extern __shared__ __align__(16) float2 zw_smem[];
@@ -284,7 +320,7 @@ __global__ void __launch_bounds__(ZW_THREADS, 2) k_zw32(ZLArgs A) {
     float *coef = (float *)(Ub + (size_t)(A.nu + 2 * ZW_PAD) * ZL_PITCH);  // [nblk][33], MODE 1 and 2
     if (threadIdx.x == 0) s_unit = 0;
     zw_load_utot(A.utot, A.fmap, a0, A.natoms, A.nh, A.nu, Ub);
-    if (MODE != 0) {
+    if (MODE == 1 || MODE == 2) {
         for (int idx = threadIdx.x; idx < 32 * A.nblk; idx += blockDim.x) {
             const int l = idx / A.nblk, b = idx - l * A.nblk;
             const int aa = a0 + l;
@@ -324,6 +360,17 @@ __global__ void __launch_bounds__(ZW_THREADS, 2) k_zw32(ZLArgs A) {
     }
     if (MODE == 1) return;
     __syncthreads();
+    if (MODE == 3) {
+        // dB_k: the sum of component k's slots (sections 0, 1, 2, each in unit order)
+        for (int idx = threadIdx.x; idx < 32 * A.nB; idx += blockDim.x) {
+            const int k = idx >> 5, aa = a0 + (idx & 31);
+            if (aa >= A.natoms) continue;
+            float acc = 0.f;
+            for (int q = __ldg(A.jpos + k); q < __ldg(A.jpos + k + 1); ++q) acc += A.bc[(size_t)q * A.natoms + aa];
+            A.x[(size_t)aa * A.nB + k] = acc;
+        }
+        return;
+    }
     // B_k, and beta_k B_k kept in shared memory (over the U tiles, no longer read) for the energy
     float *eb = (float *)zw_smem;  // [nB][33]
     for (int idx = threadIdx.x; idx < 32 * A.nB; idx += blockDim.x) {
@@ -832,6 +879,22 @@ extern "C" int so4_adjoint_y32(const so4_tables *t, int natoms, const float *d_u
     Z.Y = (float2 *)d_y;
     const size_t smz = zw_smem_bytes(t, false);
     return launch_zw<1>(t, Z, natoms, smz, (cudaStream_t)stream);
+}
+
+int so4_zw_jvp32(const so4_tables *t, int natoms, const float *d_utot, const float *d_du, float *d_slots, float *d_dB,
+                 cudaStream_t stream) {
+    ZLArgs Z = zl_args(t, natoms);
+    Z.utot = (const float2 *)d_utot;
+    Z.unit = t->d_wunit_j;
+    Z.seg = t->d_wseg_j;
+    Z.nunit = t->n_wunit_j;
+    Z.dU = (const float2 *)d_du;
+    Z.jbase = t->d_jbase;
+    Z.jpos = t->d_jpos;
+    Z.jfac = t->d_jfac;
+    Z.bc = d_slots;
+    Z.x = d_dB;
+    return launch_zw<3>(t, Z, natoms, zw_smem_bytes(t, false), stream);
 }
 
 extern "C" int so4_adjoint_deidrj32(const so4_tables *t, const so4_params *p, int natoms, const double *d_w_nb,

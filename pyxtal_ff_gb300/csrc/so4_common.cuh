@@ -124,8 +124,6 @@ struct so4_tables {
     // owning slots [bpos[k], bpos[k + 1]) in row order
     int *d_bpos = nullptr;  // nB + 1
     int n_bsec = 0;
-    //   JVP unit {k, seg0, seg1, 0},     JVP segment {t0, t1, half index of dU_lam[e], bits of fac_s w_e}
-    int4 *d_junit = nullptr, *d_jseg = nullptr;
     // window work lists (so4_zwin.cuh), most expensive unit first:
     //   unit {lam | mb << 8 | ma0 << 16 | K << 24, seg0, seg1, bits of u_norm[lam]}
     //   segment {sub0, sub1, block, B partial slot or -1}
@@ -136,6 +134,12 @@ struct so4_tables {
     int4 *d_wsub = nullptr;
     float *d_wca = nullptr;
     int n_wunit_y = 0, n_wunit_b = 0, n_wca = 0;
+    // window JVP lists (units of the B sections, blocks with a role; segment .w = the unit's
+    // section index), the slot range of each component, and per (block, role) slot base / factor
+    int4 *d_wunit_j = nullptr, *d_wseg_j = nullptr;
+    int *d_jpos = nullptr, *d_jbase = nullptr;
+    float *d_jfac = nullptr;
+    int n_wunit_j = 0, n_jslot = 0;
     int n_terms = 0;
     std::vector<int> term_ptr;
 };
@@ -408,3 +412,8 @@ void so4_count_launch(int n = 1);
 // device.  The attribute is set only when the limit grows, so launches after the
 // first make no runtime call besides the launch (safe inside stream capture).
 int so4_set_smem(const void *kern, size_t smem);
+// The JVP's Z contraction by the window kernel (so4_adjoint.cu): dB [natoms][nB] from
+// U_tot and its tangent dU (both [natoms][nh] float2), with n_jslot x natoms floats of
+// slot scratch.
+int so4_zw_jvp32(const so4_tables *t, int natoms, const float *d_utot, const float *d_du, float *d_slots, float *d_dB,
+                 cudaStream_t stream);

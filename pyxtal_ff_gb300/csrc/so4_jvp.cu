@@ -12,7 +12,6 @@
 
 #include "so4_atom.cuh"
 #include "so4_rowchain.cuh"
-#include "so4_zlanes.cuh"
 
 namespace {
 
@@ -27,10 +26,6 @@ struct JArgs {
     const int *astruct;
     const double *w_nb, *img_r, *v, *G;
     const int32_t *img_ptr, *img_j;
-    const float2 *utot;
-    const int *fmap;
-    const ZTerm *terms;
-    const int4 *unit, *seg;
     SmallTables st;
     const int2 *hmap;  // per half entry: accumulator slot, row, u_norm
     float2 *dU;
@@ -135,33 +130,6 @@ __global__ void __launch_bounds__(NW * 32, (TWOL <= 6) ? 4 : ((TWOL == 8) ? 3 : 
     }
 }
 
-// dB_k = sum_{sections s, entries e} fac_s w_e Re(conj(dU[e]) Z_s[e]) for 32 atoms per CTA
-__global__ void __launch_bounds__(256) k_zjvp32(JArgs A) {
-    extern __shared__ __align__(16) float2 zl_smem[];
-    __shared__ int s_unit;
-    const int lane = threadIdx.x & 31;
-    const int a0 = blockIdx.x * 32;
-    float2 *Uf = zl_smem;
-    if (threadIdx.x == 0) s_unit = 0;
-    zl_load_utot(A.utot, A.fmap, a0, A.natoms, A.nh, A.nu, Uf);
-    __syncthreads();
-    const int a = a0 + lane;
-    const float2 *dU = A.dU + (size_t)min(a, A.natoms - 1) * A.nh;
-    for (int u = zl_next(&s_unit); u < A.nB; u = zl_next(&s_unit)) {
-        const int4 un = __ldg(A.unit + u);
-        float acc = 0.f;
-        int4 sg = (un.y < un.z) ? __ldg(A.seg + un.y) : make_int4(0, 0, 0, 0);
-        for (int q = un.y; q < un.z; ++q) {
-            const int4 cur = sg;
-            if (q + 1 < un.z) sg = __ldg(A.seg + q + 1);
-            const float2 z = zl_entry(A.terms, cur.x, cur.y, Uf + lane);
-            const float2 d = __ldg(dU + cur.z);
-            acc += __int_as_float(cur.w) * (d.x * z.x + d.y * z.y);
-        }
-        if (a < A.natoms) A.dB[(size_t)a * A.nB + un.x] = acc;
-    }
-}
-
 template <int TWOL>
 int launch_jvp_du(const JArgs &A, cudaStream_t st) {
     constexpr int NW = 4;
@@ -179,7 +147,8 @@ size_t a256j(size_t x) { return (x + 255) & ~(size_t)255; }
 
 extern "C" size_t so4_jvp_workspace_size(const so4_tables *t, int natoms) {
     if (!t) return 0;
-    return a256j(SO4_WS_HEADER) + a256j(sizeof(float2) * (size_t)t->n_half * (natoms + 1));
+    return a256j(SO4_WS_HEADER) + a256j(sizeof(float2) * (size_t)t->n_half * (natoms + 1)) +
+           a256j(sizeof(float) * (size_t)t->n_jslot * (natoms + 1));
 }
 
 extern "C" int so4_jvp32(const so4_tables *t, const so4_params *p, const int *d_atom_struct, int natoms,
@@ -208,11 +177,6 @@ extern "C" int so4_jvp32(const so4_tables *t, const so4_params *p, const int *d_
     A.G = d_G;
     A.img_ptr = d_img_ptr;
     A.img_j = d_img_j;
-    A.utot = (const float2 *)d_utot;
-    A.fmap = t->d_fmap;
-    A.terms = t->d_terms;
-    A.unit = t->d_junit;
-    A.seg = t->d_jseg;
     fill_small_tables(t, A.st);
     A.hmap = t->d_hmap;
     A.dU = (float2 *)((char *)d_work + a256j(SO4_WS_HEADER));
@@ -228,10 +192,6 @@ extern "C" int so4_jvp32(const so4_tables *t, const so4_params *p, const int *d_
         default: return SO4_ERR_UNSUPPORTED;
     }
     if (rc) return rc;
-    const size_t smz = sizeof(float2) * (size_t)t->n_u * ZL_PITCH;
-    rc = set_smem_j(k_zjvp32, smz);
-    if (rc) return rc;
-    k_zjvp32<<<(natoms + 31) / 32, 256, smz, st>>>(A);
-    so4_count_launch();
-    return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
+    float *slots = (float *)((char *)d_work + a256j(SO4_WS_HEADER) + a256j(sizeof(float2) * (size_t)t->n_half * (natoms + 1)));
+    return so4_zw_jvp32(t, natoms, d_utot, (const float *)A.dU, slots, d_dB, st);
 }

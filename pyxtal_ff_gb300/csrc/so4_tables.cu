@@ -94,14 +94,17 @@ void free_device(so4_tables *t) {
     cudaFree(t->d_hmap);
     cudaFree(t->d_term_ptr);
     cudaFree(t->d_bpos);
-    cudaFree(t->d_junit);
     cudaFree(t->d_wunit_y);
     cudaFree(t->d_wseg_y);
     cudaFree(t->d_wunit_b);
     cudaFree(t->d_wseg_b);
     cudaFree(t->d_wsub);
+    cudaFree(t->d_wunit_j);
+    cudaFree(t->d_wseg_j);
+    cudaFree(t->d_jpos);
+    cudaFree(t->d_jbase);
+    cudaFree(t->d_jfac);
     cudaFree(t->d_wca);
-    cudaFree(t->d_jseg);
 }
 
 }  // namespace
@@ -327,38 +330,11 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
     }
     t->term_ptr[t->n_z] = (int)terms.size();
     t->n_terms = (int)terms.size();
-    auto zcost = [&](int jz) { return t->term_ptr[jz + 1] - t->term_ptr[jz]; };
     // B component of each block (blocks with l >= l1)
     std::vector<int> blk_k(t->n_blk, -1);
     for (int k = 0; k < t->n_b; ++k)
         for (int bi = 0; bi < t->n_blk; ++bi)
             if (blks[bi].z0 == bent[k].z[0]) blk_k[bi] = k;
-
-    // JVP units: one per component k, a segment per summed entry of each of its three sections
-    std::vector<std::pair<long, int>> jc;
-    for (int k = 0; k < t->n_b; ++k) {
-        long c = 0;
-        for (int sct = 0; sct < 3; ++sct)
-            for (int e = 0; e < bent[k].cnt[sct]; ++e) c += zcost(bent[k].z[sct] + e);
-        jc.push_back({-c, k});
-    }
-    std::stable_sort(jc.begin(), jc.end());
-    std::vector<int4> junit, jseg;
-    for (auto &v : jc) {
-        const int k = v.second;
-        const BEnt &be = bent[k];
-        const int s0 = (int)jseg.size();
-        for (int sct = 0; sct < 3; ++sct)
-            for (int e = 0; e < be.cnt[sct]; ++e) {
-                const int jz = be.z[sct] + e;
-                const double w = (((be.lam[sct] % 2) == 0) && e == be.cnt[sct] - 1) ? 0.5 : 1.0;
-                const float f = (float)(be.fac[sct] * w);
-                int bits;
-                std::memcpy(&bits, &f, sizeof bits);
-                jseg.push_back(make_int4(t->term_ptr[jz], t->term_ptr[jz + 1], be.h[sct] + e, bits));
-            }
-        junit.push_back(make_int4(k, s0, (int)jseg.size(), 0));
-    }
 
     // Window work lists.  For block (a, b, lam) with d = (a + b - lam) / 2, the Z entry
     // (ma, mb) is (SO4.py:1042-1063)
@@ -381,9 +357,11 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
     struct WUnit {
         int lam, mb, ma0, nk;
         int sy0, sy1, sb0, sb1;  // segments in wseg_y / wseg_b
+        int bslot;               // index among the level's units that start in the B section, or -1
     };
     std::vector<WUnit> wun;
     std::vector<int4> segy_all, segb_all;
+    std::vector<long> segy_cost;  // the work of each segment of segy_all
     // B partial slots: component k owns nbu(lam_k) consecutive slots, one per window
     // unit of level lam_k that starts inside the B section, in (mb, ma0) order
     std::vector<int> nbu(ld, 0);
@@ -413,6 +391,7 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
                 const int off0 = mb * (lam + 1) + u.ma0;
                 const bool in_bsec = off0 < section_count(lam);  // the unit's first entry is in the B section
                 const int bslot = in_bsec ? bu++ : -1;
+                u.bslot = bslot;
                 long costy = 0, costb = 0;
                 u.sy0 = (int)segy_all.size();
                 u.sb0 = (int)segb_all.size();
@@ -454,6 +433,7 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
                     const int k = blk_k[bi];
                     const int bcode = (k >= 0 && in_bsec) ? bpos[k] + bslot : -1;
                     segy_all.push_back(make_int4(s0, s1, bi, bcode));
+                    segy_cost.push_back(c);
                     costy += c;
                     if (bcode >= 0) {
                         segb_all.push_back(make_int4(s0, s1, bi, bcode));
@@ -495,6 +475,64 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
     }
     t->n_wunit_y = (int)wunit_y.size();
     t->n_wunit_b = (int)wunit_b.size();
+
+    // JVP lists: the section entries of every level (units starting in the B section) and
+    // every block with a role; a segment's .w is the unit's section-unit index.  Component
+    // k owns the slots [jpos[k], jpos[k+1]): for each section s, nbu(lam_s) of them.  The
+    // r-th role of block b (component k, section s) writes slot jbase[3b + r] + index,
+    // scaled by jfac[3b + r] = fac_s.
+    std::vector<int> jpos(t->n_b + 1, 0), jbase(3 * t->n_blk, 0), rdone(t->n_blk, 0);
+    std::vector<float> jfac(3 * t->n_blk, 0.f);
+    std::vector<int> zb_of(t->n_z + 1, -1);
+    for (int bi = 0; bi < t->n_blk; ++bi) zb_of[blks[bi].z0] = bi;
+    for (int k = 0; k < t->n_b; ++k) {
+        int base = jpos[k];
+        for (int sct = 0; sct < 3; ++sct) {
+            const int bi = zb_of[bent[k].z[sct]];
+            const int r = rdone[bi]++;  // roles were appended to each block in this (k, s) order
+            jbase[3 * bi + r] = base;
+            jfac[3 * bi + r] = (float)bent[k].fac[sct];
+            base += nbu[bent[k].lam[sct]];
+        }
+        jpos[k + 1] = base;
+    }
+    t->n_jslot = jpos[t->n_b];
+    for (int bi = 0; bi < t->n_blk; ++bi)
+        for (int r = blks[bi].nrole; r < 3; ++r) jbase[3 * bi + r] = -1;  // no role r
+    std::vector<std::pair<long, int>> wcj;
+    for (int ui = 0; ui < (int)wun.size(); ++ui) {
+        const WUnit &u = wun[ui];
+        if (u.bslot < 0) continue;
+        long c = 0;
+        for (int q = u.sy0; q < u.sy1; ++q)
+            if (blks[segy_all[q].z].nrole > 0) c += segy_cost[q];
+        wcj.push_back({-c, ui});
+    }
+    std::stable_sort(wcj.begin(), wcj.end(), by_k_cost);
+    std::vector<int4> wunit_j, wseg_j;
+    std::vector<int> jwrites(jpos[t->n_b], 0);
+    for (auto &v : wcj) {
+        const WUnit &u = wun[v.second];
+        const int s0 = (int)wseg_j.size();
+        for (int q = u.sy0; q < u.sy1; ++q) {
+            const int4 sg = segy_all[q];
+            if (blks[sg.z].nrole == 0) continue;
+            wseg_j.push_back(make_int4(sg.x, sg.y, sg.z, u.bslot));
+            for (int r = 0; r < blks[sg.z].nrole; ++r) jwrites[jbase[3 * sg.z + r] + u.bslot]++;
+        }
+        if ((int)wseg_j.size() > s0) {
+            const float un = (float)t->unorm_l[u.lam];
+            int ubits;
+            std::memcpy(&ubits, &un, sizeof ubits);
+            wunit_j.push_back(make_int4(u.lam | (u.mb << 8) | (u.ma0 << 16) | (u.nk << 24), s0, (int)wseg_j.size(),
+                                        ubits));
+        }
+    }
+    t->n_wunit_j = (int)wunit_j.size();
+    // every slot is written by exactly one (unit, block, role): the sums read no stale scratch
+    int jrc = SO4_OK;
+    for (int q = 0; q < t->n_jslot; ++q)
+        if (jwrites[q] != 1) jrc = SO4_ERR_UNSUPPORTED;
     t->n_wca = (int)wca.size();
 
     std::vector<int> fmap(t->n_u);
@@ -510,7 +548,7 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
                 }
             }
 
-    int rc = SO4_OK;
+    int rc = jrc;
     std::vector<int2> hmap;
     for (int l = 0; l < ld; ++l) {
         const float un = (float)t->unorm_l[l];
@@ -530,9 +568,12 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
     if (!rc && !wunit_b.empty()) rc = upload(&t->d_wunit_b, wunit_b);
     if (!rc && !wseg_b.empty()) rc = upload(&t->d_wseg_b, wseg_b);
     if (!rc) rc = upload(&t->d_wsub, wsub);
+    if (!rc) rc = upload(&t->d_wunit_j, wunit_j);
+    if (!rc) rc = upload(&t->d_wseg_j, wseg_j);
+    if (!rc) rc = upload(&t->d_jpos, jpos);
+    if (!rc) rc = upload(&t->d_jbase, jbase);
+    if (!rc) rc = upload(&t->d_jfac, jfac);
     if (!rc) rc = upload(&t->d_wca, wca);
-    if (!rc) rc = upload(&t->d_junit, junit);
-    if (!rc) rc = upload(&t->d_jseg, jseg);
     if (!rc) rc = upload(&t->d_cg64, t->cglist);
     if (!rc) rc = upload(&t->d_cg32, cg32);
     if (!rc) rc = upload(&t->d_rootpq64, rp64);
