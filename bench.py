@@ -205,7 +205,7 @@ def main():
         return replicas.max_over_ranks(v, device=dev)
 
     from pyxtal_ff_gb300 import _lib, engine, flops
-    from pyxtal_ff_gb300.calculator import Batch, LinearModel, SO4Calculator, contract_plain
+    from pyxtal_ff_gb300.calculator import EV_A3_TO_GPA, Batch, LinearModel, SO4Calculator
 
     atoms, coef = workload()
     batch = Batch([atoms])
@@ -334,12 +334,19 @@ def main():
     # ---- plain FP64 dB/dr path on the same structure + errors of the FP32 path
     coef_t = torch.as_tensor(coef, dtype=torch.float64, device=dev)
 
+    beta64 = coef_t.expand(natoms, -1).contiguous()
+
+    def contract(d):
+        # the reference NN consumer's contraction of dxdr / rdxdr with dE/dB (so4_contract_dxdr)
+        nb = d["neighbors"]
+        rda = engine.rdxdr_atom(d["rdxdr"], nb.pair_ptr, nb.natoms)
+        f, s = engine.contract_dxdr(beta64, nb.pair_ptr, nb.seq, nb.atom_struct, nb.atom_ptr_dev, dxdr=d["dxdr"],
+                                    rdxdr_atom=rda)
+        return {"forces": f, "stress": s * EV_A3_TO_GPA, "rdxdr_atom": rda}
+
     def plain_step():
         d = calc.descriptors(batch, pos_dev, precision="fp64")
-        beta64 = coef_t.expand(natoms, -1)
-        c = contract_plain(d["x"], d["dxdr"], d["rdxdr"], d["seq"], d["pair_ptr"], batch.atom_ptr, beta64,
-                           batch.volumes)
-        return d, c
+        return d, contract(d)
     plain_step()
     torch.cuda.synchronize()
     t64 = []
@@ -352,6 +359,24 @@ def main():
         e1.synchronize()
         t64.append(e0.elapsed_time(e1))
     ms64 = max_over_ranks(float(np.mean(t64)))
+    # the contraction alone on the FP64 dxdr (HBM-bound: each dxdr row is read once)
+    nbp = d64["neighbors"]
+    tc = []
+    cstat = torch.zeros(1, dtype=torch.int32, device=dev)
+    for _ in range(3):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        engine.contract_dxdr(beta64, nbp.pair_ptr, nbp.seq, nbp.atom_struct, nbp.atom_ptr_dev, dxdr=d64["dxdr"],
+                             rdxdr_atom=c64["rdxdr_atom"], status=cstat)
+        e1.record()
+        e1.synchronize()
+        tc.append(e0.elapsed_time(e1))
+    if int(cstat.item()):
+        raise RuntimeError("so4_contract_dxdr: asymmetric pair list")
+    nB = calc.nB
+    cbytes = 8 * (nbp.npair * nB * 3 + natoms * nB * 6 + natoms * nB + 2 * nbp.npair + 3 * natoms + 6 * natoms)
+    ms_c = float(np.min(tc))
     clk = clocks.stop()  # sampled over the device, e2e and FP64 timed legs
     clk["window"] = "device + e2e + fp64 timed legs"
     stress64 = c64["stress"]  # rdxdr already carries 1/vol
@@ -400,6 +425,11 @@ def main():
             k["frac_fp32"] = k["tflops"] / peaks["fp32_tflops"]
             k["tflops_executed"] = kf[nme] / sec / 1e12
         kernels[nme] = k
+    kernels["contract_dxdr_fp64"] = {
+        "ms": ms_c, "gbs": cbytes / (ms_c * 1e-3) / 1e9, "frac_hbm": cbytes / (ms_c * 1e-3) / 1e9 / peaks["hbm_gbs"],
+        "bytes": cbytes, "what": "forces and stress of the reference NN consumer from the FP64 dxdr (%.2f GB) and "
+                                 "per-atom rdxdr; bytes = dxdr + rdxdr_atom + beta + seq + outputs" %
+                                 (8e-9 * nbp.npair * nB * 3)}
     kernels["plain_fp64"] = {"ms": ms64, "tflops_fp64_incl_nl_contraction": ks["plain"] / (ms64 * 1e-3) / 1e12,
                              "frac_fp64": ks["plain"] / (ms64 * 1e-3) / 1e12 / peaks["fp64_tflops"]}
 

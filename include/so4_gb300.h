@@ -195,6 +195,23 @@ int so4_plain(const so4_tables *t, const so4_params *p, int precision, const so4
 int so4_rdxdr_atom(int precision, const void *d_rdxdr, const int32_t *d_pair_ptr, int natoms, int nB, void *d_out,
                    void *stream);
 
+/* The NN potential's contraction of the plain path's outputs with dE/dx
+ * (replaces the dense (N, N, nB, 3) array / per-atom np.where loop of
+ * pyxtal_ff/models/neuralnetwork.py:579-678, calculate_properties):
+ *   d_forces[m, c]    = -sum over pairs p with seq[p, 1] == m of beta[seq[p, 0]] . dxdr[p, :, c]
+ *   d_stress_atom[m, v] = -sum_k beta[m, k] rdxdr_atom[m, k, v]
+ *   d_stress[s, v]    = sum of d_stress_atom over the atoms of structure s
+ * d_beta[natoms*nB] = dE/dx (normalisation already folded in), d_seq / d_pair_ptr
+ * as so4_nl_pairs writes them (pairs grouped by centre, j ascending), the
+ * pair list symmetric (every (i, j) has its (j, i)); a pair without its reverse
+ * sets bit SO4_ERR_REVERSE in *d_status (device int, zeroed by the caller).  Pass
+ * d_dxdr NULL to skip the forces, d_rdxdr_atom NULL to skip the stress.  Fixed
+ * summation order (deterministic).  precision 0: double arrays, 1: float. */
+int so4_contract_dxdr(int precision, int natoms, int nB, int nstruct, const int32_t *d_atom_struct,
+                      const int32_t *d_atom_ptr, const int32_t *d_pair_ptr, const int64_t *d_seq,
+                      const void *d_dxdr, const void *d_beta, const void *d_rdxdr_atom, void *d_forces,
+                      void *d_stress_atom, void *d_stress, int *d_status, void *stream);
+
 /* ------------------------------------------------------------ adjoint path */
 /* Forward (FP32): U_tot per centre in the half layout (d_utot[natoms*idxu_half*2]
  * f32, kept for the adjoint) and B (d_x[natoms*nB] f32).  Scratch:

@@ -173,7 +173,8 @@ class SO4Calculator:
         forces, virial, energy = engine.adjoint32(self.tables, self.params, nb, self._w_nb, utot, beta,
                                                   eatom=e_atom.detach())
         stress = -(virial.reshape(-1, 9)[:, VOIGT] / self._vol[:, None]) * EV_A3_TO_GPA
-        return dict(energy=energy, forces=forces, virial=virial, stress=stress, x=x, neighbors=nb)
+        return dict(energy=energy, forces=forces, virial=virial, stress=stress, x=x, neighbors=nb,
+                    energies=e_atom.detach())
 
 
 def contract_plain(x, dxdr, rdxdr, seq, pair_ptr, atom_ptr, beta, volumes):

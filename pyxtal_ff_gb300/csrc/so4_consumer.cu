@@ -1,0 +1,180 @@
+// so4_consumer.cu -- what the reference's NN potential does with the plain path's
+// outputs (pyxtal_ff/models/neuralnetwork.py:579-678, calculate_properties):
+//   forces[m] -= sum over pairs p with seq[p, 1] == m of dedx[seq[p, 0]] . dxdr[p]
+//   stress    -= sum_i dedx[i] . rdxdr_atom[i]            (per structure, Voigt order)
+// The reference forms the first with an (N, N, nB, 3) dense array (N <= 400) or one
+// np.where over all pairs per atom (N > 400).  Here one warp per target atom m walks
+// the pairs whose centre is m: the pair list is symmetric (j is within rcut of an
+// image of i exactly when i is within rcut of an image of j), so the pairs that point
+// at m are the reverse pairs (j, m) of m's own pairs (m, j), found by a binary search
+// of m in j's sorted neighbour list.  No transpose, no atomics, a fixed summation
+// order: sources in ascending j, components in a fixed lane pattern, then a fixed
+// shuffle tree.
+#include "so4_common.cuh"
+
+namespace {
+
+template <typename T>
+struct CArgs {
+    int natoms, nB;
+    const int32_t *astruct, *atom_ptr, *pair_ptr;
+    const int64_t *seq;  // (P, 2), structure-local (i, j), pairs grouped by centre, j ascending
+    const T *dxdr;       // (P, nB, 3) or null
+    const T *beta;       // (N, nB) dE/dx per atom
+    const T *rdxdr;      // (N, nB, 6) per-atom Voigt rows or null
+    T *forces;           // (N, 3)
+    T *stress_atom;      // (N, 6)
+    int *status;
+};
+
+template <typename T, int NV>
+__device__ __forceinline__ void add_sel(T (&acc)[NV], int c, T v) {
+#pragma unroll
+    for (int u = 0; u < NV; ++u)
+        if (u == c) acc[u] += v;
+}
+
+template <typename T, int NV>
+__device__ __forceinline__ void warp_sum(T (&acc)[NV]) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int u = 0; u < NV; ++u) acc[u] += __shfl_xor_sync(0xffffffffu, acc[u], o);
+}
+
+// acc[i] for a run-time i < NV without dynamic register indexing
+template <typename T, int NV>
+__device__ __forceinline__ T pick(const T (&acc)[NV], int i) {
+    T v = acc[0];
+#pragma unroll
+    for (int u = 1; u < NV; ++u)
+        if (u == i) v = acc[u];
+    return v;
+}
+
+constexpr int CW = 8;  // warps (target atoms) per CTA
+
+template <typename T>
+__global__ void __launch_bounds__(CW * 32) k_contract_dxdr(CArgs<T> A) {
+    const int lane = threadIdx.x & 31;
+    const int m = blockIdx.x * CW + (threadIdx.x >> 5);
+    if (m >= A.natoms) return;
+    const int nB = A.nB, n3 = 3 * nB;
+    if (A.dxdr) {
+        const int base = A.atom_ptr[A.astruct[m]];
+        const int64_t ml = m - base;
+        const int q0 = A.pair_ptr[m], q1 = A.pair_ptr[m + 1];
+        T f[3] = {T(0), T(0), T(0)};
+        for (int qb = q0; qb < q1; qb += 32) {
+            // lane t finds the reverse of pair qb + t: the pair (j, m) in centre j's list
+            int p = -1, j = 0;
+            const int q = qb + lane;
+            if (q < q1) {
+                j = base + (int)A.seq[2 * (size_t)q + 1];
+                int lo = A.pair_ptr[j], hi = A.pair_ptr[j + 1] - 1;
+                while (lo <= hi) {
+                    const int mid = (lo + hi) >> 1;
+                    const int64_t v = A.seq[2 * (size_t)mid + 1];
+                    if (v < ml) {
+                        lo = mid + 1;
+                    } else if (v > ml) {
+                        hi = mid - 1;
+                    } else {
+                        p = mid;
+                        break;
+                    }
+                }
+                if (p < 0) atomicOr(A.status, 1 << SO4_ERR_REVERSE);
+            }
+            const int nq = min(32, q1 - qb);
+            for (int t = 0; t < nq; ++t) {
+                const int pp = __shfl_sync(0xffffffffu, p, t), jj = __shfl_sync(0xffffffffu, j, t);
+                if (pp < 0) continue;  // warp-uniform
+                const T *d = A.dxdr + (size_t)pp * n3;
+                const T *b = A.beta + (size_t)jj * nB;
+                // lane holds components idx = lane + 32 s; idx % 3 advances by 2 per stride
+                int c = lane % 3;
+                for (int idx = lane; idx < n3; idx += 32) {
+                    add_sel<T, 3>(f, c, __ldg(b + idx / 3) * __ldg(d + idx));
+                    c = (c + 2) % 3;
+                }
+            }
+        }
+        warp_sum<T, 3>(f);
+        if (lane < 3) A.forces[3 * (size_t)m + lane] = -pick<T, 3>(f, lane);
+    }
+    if (A.rdxdr) {
+        T s[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
+        const T *r = A.rdxdr + (size_t)m * 6 * nB;
+        const T *b = A.beta + (size_t)m * nB;
+        int c = lane % 6;
+        for (int idx = lane; idx < 6 * nB; idx += 32) {
+            add_sel<T, 6>(s, c, __ldg(b + idx / 6) * __ldg(r + idx));
+            c = (c + 2) % 6;
+        }
+        warp_sum<T, 6>(s);
+        if (lane < 6) A.stress_atom[6 * (size_t)m + lane] = -pick<T, 6>(s, lane);
+    }
+}
+
+// per-structure sums of the per-atom stress rows, one warp per structure, fixed order
+template <typename T>
+__global__ void __launch_bounds__(CW * 32) k_struct_stress(int nstruct, const int32_t *atom_ptr, const T *sa,
+                                                           T *out) {
+    const int lane = threadIdx.x & 31;
+    const int s = blockIdx.x * CW + (threadIdx.x >> 5);
+    if (s >= nstruct) return;
+    T acc[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
+    for (int a = atom_ptr[s] + lane; a < atom_ptr[s + 1]; a += 32)
+#pragma unroll
+        for (int u = 0; u < 6; ++u) acc[u] += sa[6 * (size_t)a + u];
+    warp_sum<T, 6>(acc);
+    if (lane < 6) out[6 * (size_t)s + lane] = pick<T, 6>(acc, lane);
+}
+
+template <typename T>
+int run(int natoms, int nB, int nstruct, const int32_t *astruct, const int32_t *atom_ptr, const int32_t *pair_ptr,
+        const int64_t *seq, const void *dxdr, const void *beta, const void *rdxdr, void *forces, void *stress_atom,
+        void *stress, int *status, cudaStream_t st) {
+    CArgs<T> A;
+    A.natoms = natoms;
+    A.nB = nB;
+    A.astruct = astruct;
+    A.atom_ptr = atom_ptr;
+    A.pair_ptr = pair_ptr;
+    A.seq = seq;
+    A.dxdr = (const T *)dxdr;
+    A.beta = (const T *)beta;
+    A.rdxdr = (const T *)rdxdr;
+    A.forces = (T *)forces;
+    A.stress_atom = (T *)stress_atom;
+    A.status = status;
+    k_contract_dxdr<T><<<(natoms + CW - 1) / CW, CW * 32, 0, st>>>(A);
+    so4_count_launch();
+    if (rdxdr) {
+        k_struct_stress<T><<<(nstruct + CW - 1) / CW, CW * 32, 0, st>>>(nstruct, atom_ptr, (const T *)stress_atom,
+                                                                        (T *)stress);
+        so4_count_launch();
+    }
+    return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
+}
+
+}  // namespace
+
+extern "C" int so4_contract_dxdr(int precision, int natoms, int nB, int nstruct, const int32_t *d_atom_struct,
+                                 const int32_t *d_atom_ptr, const int32_t *d_pair_ptr, const int64_t *d_seq,
+                                 const void *d_dxdr, const void *d_beta, const void *d_rdxdr_atom, void *d_forces,
+                                 void *d_stress_atom, void *d_stress, int *d_status, void *stream) {
+    if (precision != 0 && precision != 1) return SO4_ERR_ARG;
+    if (natoms < 0 || nB <= 0 || nstruct < 0) return SO4_ERR_ARG;
+    if (natoms == 0) return SO4_OK;
+    if (!d_beta || !d_atom_ptr || !d_status || (!d_dxdr && !d_rdxdr_atom)) return SO4_ERR_ARG;
+    if (d_dxdr && (!d_atom_struct || !d_pair_ptr || !d_seq || !d_forces)) return SO4_ERR_ARG;
+    if (d_rdxdr_atom && (!d_stress_atom || !d_stress || nstruct < 1)) return SO4_ERR_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (precision == 0)
+        return run<double>(natoms, nB, nstruct, d_atom_struct, d_atom_ptr, d_pair_ptr, d_seq, d_dxdr, d_beta,
+                           d_rdxdr_atom, d_forces, d_stress_atom, d_stress, d_status, st);
+    return run<float>(natoms, nB, nstruct, d_atom_struct, d_atom_ptr, d_pair_ptr, d_seq, d_dxdr, d_beta,
+                      d_rdxdr_atom, d_forces, d_stress_atom, d_stress, d_status, st);
+}

@@ -345,6 +345,36 @@ def rdxdr_atom(rdxdr, pair_ptr, natoms):
     return out[:natoms]
 
 
+def contract_dxdr(beta, pair_ptr, seq, atom_struct, atom_ptr, dxdr=None, rdxdr_atom=None, status=None):
+    """Forces (N, 3) and per-structure stress sums (S, 6) from the plain path's dxdr /
+    per-atom rdxdr and beta = dE/dx (so4_contract_dxdr):
+      forces[m] = -sum over pairs p with seq[p, 1] == m of beta[i(p)] . dxdr[p]
+      stress[s] = -sum over the atoms i of s of beta[i] . rdxdr_atom[i]   (no unit factor)
+    Either output is None when its input is.  All arrays on one device, one dtype.
+    Without `status` the call reads the status word back and raises ValueError for a
+    pair without its reverse; with a zeroed device int32 `status` it does not
+    synchronise and leaves the bits there."""
+    natoms, nB = beta.shape
+    nstruct = int(atom_ptr.numel()) - 1
+    dev, dt = beta.device, beta.dtype
+    prec = 0 if dt == torch.float64 else 1
+    forces = torch.empty((max(natoms, 1), 3), dtype=dt, device=dev) if dxdr is not None else None
+    sa = torch.empty((max(natoms, 1), 6), dtype=dt, device=dev) if rdxdr_atom is not None else None
+    stress = torch.empty((max(nstruct, 1), 6), dtype=dt, device=dev) if rdxdr_atom is not None else None
+    own = status is None
+    if own:
+        status = torch.zeros(1, dtype=torch.int32, device=dev)
+    keep = [t.contiguous() if t is not None else None for t in (beta, pair_ptr, seq, atom_struct, atom_ptr, dxdr,
+                                                                  rdxdr_atom)]
+    check(lib().so4_contract_dxdr(prec, natoms, nB, nstruct, _ptr(keep[3]), _ptr(keep[4]), _ptr(keep[1]),
+                                  _ptr(keep[2]), _ptr(keep[5]), _ptr(keep[0]), _ptr(keep[6]), _ptr(forces), _ptr(sa),
+                                  _ptr(stress), _ptr(status), _stream()), "so4_contract_dxdr")
+    bits = int(status.item()) if own else 0
+    if bits & (1 << _lib.SO4_ERR_REVERSE):
+        raise ValueError("so4_contract_dxdr: a pair has no reverse pair (the pair list is not symmetric)")
+    return (forces[:natoms] if forces is not None else None), (stress[:nstruct] if stress is not None else None)
+
+
 def forward32(tab, prm, nb: Neighbors, w_nb, w_site):
     """FP32 B (N,nB) and U_tot (N, n_half, 2) for the adjoint."""
     dev = w_nb.device

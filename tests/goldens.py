@@ -12,8 +12,37 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
 def names():
+    """Descriptor cases (tests/golden/make_golden.py)."""
     return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
-                  if not os.path.basename(p).startswith("reference_tables"))
+                  if not os.path.basename(p).startswith(("reference_tables", "nn_")))
+
+
+def nn_names():
+    """NN-potential cases (tests/golden/make_golden_nn.py)."""
+    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "nn_*.npz")))
+
+
+def load_nn(name):
+    """atoms, descriptor parameters, the fixture dict, and per element its network
+    (torch, FP64, the reference's layer layout) and drange."""
+    import torch
+    d = dict(np.load(os.path.join(GOLDEN, name + ".npz")))
+    meta = json.loads(str(d.pop("descriptor_meta")))
+    arch = json.loads(str(d.pop("arch")))
+    atoms = Atoms(d["numbers"], d["positions"], d["cell"], pbc=d["pbc"].astype(bool))
+    nets, drange = {}, {}
+    for e, a in arch.items():
+        layers = []
+        for i, act in enumerate(a["acts"]):
+            layers.append(torch.nn.Linear(a["sizes"][i], a["sizes"][i + 1]))
+            if act != "Linear":
+                layers.append(getattr(torch.nn, act)())
+        net = torch.nn.Sequential(*layers).double()
+        pre = "w_%s_" % e
+        net.load_state_dict({k[len(pre):]: torch.from_numpy(v) for k, v in d.items() if k.startswith(pre)})
+        nets[e] = net
+        drange[e] = d["drange_" + e]
+    return atoms, meta, d, nets, drange
 
 
 def load(name):
