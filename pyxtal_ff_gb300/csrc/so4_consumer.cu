@@ -8,8 +8,8 @@
 // image of i exactly when i is within rcut of an image of j), so the pairs that point
 // at m are the reverse pairs (j, m) of m's own pairs (m, j), found by a binary search
 // of m in j's sorted neighbour list.  No transpose, no atomics, a fixed summation
-// order: sources in ascending j, components in a fixed lane pattern, then a fixed
-// shuffle tree.
+// order: sources in ascending j (four at a time), components in a fixed lane pattern,
+// then a fixed shuffle tree.
 #include "so4_common.cuh"
 
 namespace {
@@ -53,6 +53,7 @@ __device__ __forceinline__ T pick(const T (&acc)[NV], int i) {
 }
 
 constexpr int CW = 8;  // warps (target atoms) per CTA
+constexpr int CP = 4;  // incoming pairs read together
 
 template <typename T>
 __global__ void __launch_bounds__(CW * 32) k_contract_dxdr(CArgs<T> A) {
@@ -87,15 +88,29 @@ __global__ void __launch_bounds__(CW * 32) k_contract_dxdr(CArgs<T> A) {
                 if (p < 0) atomicOr(A.status, 1 << SO4_ERR_REVERSE);
             }
             const int nq = min(32, q1 - qb);
-            for (int t = 0; t < nq; ++t) {
-                const int pp = __shfl_sync(0xffffffffu, p, t), jj = __shfl_sync(0xffffffffu, j, t);
-                if (pp < 0) continue;  // warp-uniform
-                const T *d = A.dxdr + (size_t)pp * n3;
-                const T *b = A.beta + (size_t)jj * nB;
+            // CP incoming pairs per pass, so each lane has 2 CP independent loads in flight
+            for (int t0 = 0; t0 < nq; t0 += CP) {
+                const T *d[CP];
+                const T *b[CP];
+                bool ok[CP];
+#pragma unroll
+                for (int u = 0; u < CP; ++u) {
+                    const int pp = __shfl_sync(0xffffffffu, p, (t0 + u) & 31);
+                    const int jj = __shfl_sync(0xffffffffu, j, (t0 + u) & 31);
+                    ok[u] = t0 + u < nq && pp >= 0;  // warp-uniform
+                    d[u] = A.dxdr + (size_t)(ok[u] ? pp : 0) * n3;
+                    b[u] = A.beta + (size_t)(ok[u] ? jj : 0) * nB;
+                }
                 // lane holds components idx = lane + 32 s; idx % 3 advances by 2 per stride
                 int c = lane % 3;
+#pragma unroll 2
                 for (int idx = lane; idx < n3; idx += 32) {
-                    add_sel<T, 3>(f, c, __ldg(b + idx / 3) * __ldg(d + idx));
+                    const int k = idx / 3;
+                    T v = T(0);
+#pragma unroll
+                    for (int u = 0; u < CP; ++u)
+                        if (ok[u]) v += __ldg(b[u] + k) * __ldg(d[u] + idx);
+                    add_sel<T, 3>(f, c, v);
                     c = (c + 2) % 3;
                 }
             }
@@ -108,6 +123,7 @@ __global__ void __launch_bounds__(CW * 32) k_contract_dxdr(CArgs<T> A) {
         const T *r = A.rdxdr + (size_t)m * 6 * nB;
         const T *b = A.beta + (size_t)m * nB;
         int c = lane % 6;
+#pragma unroll 4
         for (int idx = lane; idx < 6 * nB; idx += 32) {
             add_sel<T, 6>(s, c, __ldg(b + idx / 6) * __ldg(r + idx));
             c = (c + 2) % 6;
