@@ -35,11 +35,12 @@ BOHR = 0.529177
 
 
 class NeuralNetworkPotential:
-    def __init__(self, models, drange, elements=None, unit="eV", device="cuda"):
+    def __init__(self, models, drange, elements=None, unit="eV", device="cuda", path=""):
         if unit not in ("eV", "Ha"):
             raise NotImplementedError(f"{unit} is not implemented. Please choose from ['eV', 'Ha'].")
         self.elements = sorted(elements if elements is not None else models.keys())
         self.unit = unit
+        self.path = path
         self.device = torch.device(device)
         self.models = {e: models[e].to(self.device) for e in self.elements}
         self.drange = {e: np.asarray(drange[e], dtype=np.float64) for e in self.elements}
@@ -114,6 +115,17 @@ class NeuralNetworkPotential:
             if s is not None:
                 stress = s[0].cpu().numpy() * EV2GPA
         return energies.cpu().numpy(), forces, stress
+
+    @property
+    def no_of_descriptors(self):
+        first = next(m for m in self.models[self.elements[0]].modules() if isinstance(m, torch.nn.Linear))
+        return first.in_features
+
+    def save_weights_to_txt(self, des_info):
+        """NN_weights.txt and DescriptorParam.txt for LAMMPS ML-IAP under the prefix self.path
+        (neuralnetwork.py:719-836; the format is in lammps_export)."""
+        from .lammps_export import write_nn
+        write_nn(self.path, self.elements, self.models, self.drange, self.no_of_descriptors, des_info)
 
     def energy_model(self, species_order):
         """The networks as a module (x (N, nB), species (N,) indices into species_order)
