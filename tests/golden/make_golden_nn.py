@@ -16,13 +16,17 @@ reads -- elements, models, drange, unit -- as a loaded checkpoint gives them
 Per case: the descriptor inputs as the reference's caller passes them (x, dxdr,
 seq, elements, and rdxdr reduced per atom to Voigt order, utilities/__init__.py:226-233),
 the per-element networks (layer sizes, activation names, weights), drange, and the
-reference's outputs (energies, forces, stress).
+reference's outputs (energies, forces, stress); and the LAMMPS ML-IAP text files the
+reference writes for that potential (NeuralNetwork.save_weights_to_txt, :719-836)
+and for a linear potential with random coefficients
+(PR.save_weights_to_txt, polynomialregression.py:286-345).
 
     python tests/golden/make_golden_nn.py
 """
 import json
 import os
 import sys
+import tempfile
 import types
 
 import numpy as np
@@ -121,6 +125,7 @@ def main():
     import importlib
     import torch
     nnmod = importlib.import_module("pyxtal_ff.models.neuralnetwork")
+    prmod = importlib.import_module("pyxtal_ff.models.polynomialregression")
     torch.set_default_dtype(torch.float64)
     for name, fix, run, spec, seed in _cases():
         if fix is None:
@@ -147,6 +152,26 @@ def main():
             d["drange_" + e] = drange[e]
             for k, v in nets[e].state_dict().items():
                 d["w_%s_%s" % (e, k)] = v.detach().numpy()
+        # the LAMMPS export of the same potential, and of a linear one
+        meta = json.loads(str(fix["meta"]))
+        des_info = {"type": meta["kind"], "Rc": meta["rcut"], "weights": meta.get("weights"),
+                    "parameters": {"lmax": meta["lmax"], "rfac": meta.get("rfac0", 0.99363)}}
+        with tempfile.TemporaryDirectory() as tmp:
+            pot.path = tmp + "/"
+            pot.hiddenlayers = {e: arch[e]["sizes"][1:] for e in elements}
+            pot.activation = {e: arch[e]["acts"] for e in elements}
+            pot.no_of_descriptors = nB
+            pot.save_weights_to_txt(des_info)
+            d["nn_weights_txt"] = open(tmp + "/NN_weights.txt").read()
+            d["descriptor_param_txt"] = open(tmp + "/DescriptorParam.txt").read()
+            pr = prmod.PR.__new__(prmod.PR)
+            pr.path, pr.elements, pr.d_max = tmp + "/", elements, nB
+            pr.coef_ = np.random.default_rng(seed).normal(size=len(elements) * (nB + 1))
+            pr.save_weights_to_txt(des_info)
+            d["pr_coef"] = pr.coef_
+            d["pr_weights_txt"] = open(tmp + "/PR_weights.txt").read()
+            d["pr_descriptor_param_txt"] = open(tmp + "/DescriptorParam.txt").read()
+        d["des_info"] = json.dumps(des_info, sort_keys=True)
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **d)
         print("%-16s atoms %4d  nB %3d  E %.6f  |F|max %.3e  S %s" % (name, n, nB, energies.sum(), np.abs(forces).max(),
                                                                     np.array2string(stress, precision=4)), flush=True)
