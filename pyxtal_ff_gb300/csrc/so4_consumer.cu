@@ -8,8 +8,9 @@
 // image of i exactly when i is within rcut of an image of j), so the pairs that point
 // at m are the reverse pairs (j, m) of m's own pairs (m, j), found by a binary search
 // of m in j's sorted neighbour list.  No transpose, no atomics, a fixed summation
-// order: sources in ascending j (four at a time), components in a fixed lane pattern,
-// then a fixed shuffle tree.
+// order: sources in ascending j (four at a time), each lane one component over a fixed
+// set of descriptor indices, then the lanes of a component in lane order.  With FP64
+// arrays the FP64 pipe (one FMA per dxdr element) and HBM bound it about equally.
 #include "so4_common.cuh"
 
 namespace {
@@ -26,13 +27,6 @@ struct CArgs {
     T *stress_atom;      // (N, 6)
     int *status;
 };
-
-template <typename T, int NV>
-__device__ __forceinline__ void add_sel(T (&acc)[NV], int c, T v) {
-#pragma unroll
-    for (int u = 0; u < NV; ++u)
-        if (u == c) acc[u] += v;
-}
 
 template <typename T, int NV>
 __device__ __forceinline__ void warp_sum(T (&acc)[NV]) {
@@ -65,7 +59,7 @@ __global__ void __launch_bounds__(CW * 32) k_contract_dxdr(CArgs<T> A) {
         const int base = A.atom_ptr[A.astruct[m]];
         const int64_t ml = m - base;
         const int q0 = A.pair_ptr[m], q1 = A.pair_ptr[m + 1];
-        T f[3] = {T(0), T(0), T(0)};
+        T fc = T(0);  // this lane's part of component lane % 3
         for (int qb = q0; qb < q1; qb += 32) {
             // lane t finds the reverse of pair qb + t: the pair (j, m) in centre j's list
             int p = -1, j = 0;
@@ -101,51 +95,69 @@ __global__ void __launch_bounds__(CW * 32) k_contract_dxdr(CArgs<T> A) {
                     d[u] = A.dxdr + (size_t)(ok[u] ? pp : 0) * n3;
                     b[u] = A.beta + (size_t)(ok[u] ? jj : 0) * nB;
                 }
-                // lane holds components idx = lane + 32 s; idx % 3 advances by 2 per stride
-                int c = lane % 3;
+                // lanes 0..29 take idx = lane + 30 s: the component c = idx % 3 = lane % 3 is
+                // fixed per lane, so each element costs one FMA (k = idx / 3 = lane / 3 + 10 s)
+                if (lane < 30) {
 #pragma unroll 2
-                for (int idx = lane; idx < n3; idx += 32) {
-                    const int k = idx / 3;
-                    T v = T(0);
+                    for (int idx = lane, k = lane / 3; idx < n3; idx += 30, k += 10) {
 #pragma unroll
-                    for (int u = 0; u < CP; ++u)
-                        if (ok[u]) v += __ldg(b[u] + k) * __ldg(d[u] + idx);
-                    add_sel<T, 3>(f, c, v);
-                    c = (c + 2) % 3;
+                        for (int u = 0; u < CP; ++u)
+                            if (ok[u]) fc = fma(__ldg(b[u] + k), __ldg(d[u] + idx), fc);
+                    }
                 }
             }
         }
-        warp_sum<T, 3>(f);
+        // component sums in a fixed order: lanes c, c + 3, ..., c + 27 (lane % 3 == c)
+        T f[3] = {T(0), T(0), T(0)};
+#pragma unroll
+        for (int l = 0; l < 30; ++l) {
+            const T v = __shfl_sync(0xffffffffu, fc, l);
+            f[l % 3] += v;
+        }
         if (lane < 3) A.forces[3 * (size_t)m + lane] = -pick<T, 3>(f, lane);
     }
     if (A.rdxdr) {
-        T s[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
+        // lanes 0..29, idx = lane + 30 s: Voigt entry lane % 6 fixed per lane, k = lane / 6 + 5 s
         const T *r = A.rdxdr + (size_t)m * 6 * nB;
         const T *b = A.beta + (size_t)m * nB;
-        int c = lane % 6;
+        T sv = T(0);
+        if (lane < 30) {
 #pragma unroll 4
-        for (int idx = lane; idx < 6 * nB; idx += 32) {
-            add_sel<T, 6>(s, c, __ldg(b + idx / 6) * __ldg(r + idx));
-            c = (c + 2) % 6;
+            for (int idx = lane, k = lane / 6; idx < 6 * nB; idx += 30, k += 5) sv = fma(__ldg(b + k), __ldg(r + idx), sv);
         }
-        warp_sum<T, 6>(s);
+        T s[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
+#pragma unroll
+        for (int l = 0; l < 30; ++l) {
+            const T v = __shfl_sync(0xffffffffu, sv, l);
+            s[l % 6] += v;
+        }
         if (lane < 6) A.stress_atom[6 * (size_t)m + lane] = -pick<T, 6>(s, lane);
     }
 }
 
-// per-structure sums of the per-atom stress rows, one warp per structure, fixed order
+// per-structure sums of the per-atom stress rows, one CTA per structure: thread t adds
+// atoms t, t + ST, ... in order, then the warps' shuffle trees and the warps in order
+constexpr int ST = 256;
 template <typename T>
-__global__ void __launch_bounds__(CW * 32) k_struct_stress(int nstruct, const int32_t *atom_ptr, const T *sa,
-                                                           T *out) {
-    const int lane = threadIdx.x & 31;
-    const int s = blockIdx.x * CW + (threadIdx.x >> 5);
-    if (s >= nstruct) return;
+__global__ void __launch_bounds__(ST) k_struct_stress(const int32_t *atom_ptr, const T *sa, T *out) {
+    __shared__ T part[ST / 32][6];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int s = blockIdx.x;
     T acc[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
-    for (int a = atom_ptr[s] + lane; a < atom_ptr[s + 1]; a += 32)
+#pragma unroll 4
+    for (int a = atom_ptr[s] + threadIdx.x; a < atom_ptr[s + 1]; a += ST)
 #pragma unroll
         for (int u = 0; u < 6; ++u) acc[u] += sa[6 * (size_t)a + u];
     warp_sum<T, 6>(acc);
-    if (lane < 6) out[6 * (size_t)s + lane] = pick<T, 6>(acc, lane);
+    if (lane == 0)
+#pragma unroll
+        for (int u = 0; u < 6; ++u) part[wid][u] = acc[u];
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        T v = T(0);
+        for (int w = 0; w < ST / 32; ++w) v += part[w][threadIdx.x];
+        out[6 * (size_t)s + threadIdx.x] = v;
+    }
 }
 
 template <typename T>
@@ -168,8 +180,7 @@ int run(int natoms, int nB, int nstruct, const int32_t *astruct, const int32_t *
     k_contract_dxdr<T><<<(natoms + CW - 1) / CW, CW * 32, 0, st>>>(A);
     so4_count_launch();
     if (rdxdr) {
-        k_struct_stress<T><<<(nstruct + CW - 1) / CW, CW * 32, 0, st>>>(nstruct, atom_ptr, (const T *)stress_atom,
-                                                                        (T *)stress);
+        k_struct_stress<T><<<nstruct, ST, 0, st>>>(atom_ptr, (const T *)stress_atom, (T *)stress);
         so4_count_launch();
     }
     return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
