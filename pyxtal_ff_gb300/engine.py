@@ -345,7 +345,7 @@ def rdxdr_atom(rdxdr, pair_ptr, natoms):
     return out[:natoms]
 
 
-def contract_dxdr(beta, pair_ptr, seq, atom_struct, atom_ptr, dxdr=None, rdxdr_atom=None, status=None):
+def contract_dxdr(beta, pair_ptr, seq, atom_struct, atom_ptr, dxdr=None, rdxdr_atom=None, status=None, out=None):
     """Forces (N, 3) and per-structure stress sums (S, 6) from the plain path's dxdr /
     per-atom rdxdr and beta = dE/dx (so4_contract_dxdr):
       forces[m] = -sum over pairs p with seq[p, 1] == m of beta[i(p)] . dxdr[p]
@@ -353,14 +353,20 @@ def contract_dxdr(beta, pair_ptr, seq, atom_struct, atom_ptr, dxdr=None, rdxdr_a
     Either output is None when its input is.  All arrays on one device, one dtype.
     Without `status` the call reads the status word back and raises ValueError for a
     pair without its reverse; with a zeroed device int32 `status` it does not
-    synchronise and leaves the bits there."""
+    synchronise and leaves the bits there.  `out` = (forces, stress_atom, stress) reuses
+    caller buffers of shapes (N, 3), (N, 6), (S, 6)."""
     natoms, nB = beta.shape
     nstruct = int(atom_ptr.numel()) - 1
     dev, dt = beta.device, beta.dtype
     prec = 0 if dt == torch.float64 else 1
-    forces = torch.empty((max(natoms, 1), 3), dtype=dt, device=dev) if dxdr is not None else None
-    sa = torch.empty((max(natoms, 1), 6), dtype=dt, device=dev) if rdxdr_atom is not None else None
-    stress = torch.empty((max(nstruct, 1), 6), dtype=dt, device=dev) if rdxdr_atom is not None else None
+    if out is not None:
+        forces, sa, stress = out
+        forces = forces if dxdr is not None else None
+        sa, stress = (sa, stress) if rdxdr_atom is not None else (None, None)
+    else:
+        forces = torch.empty((max(natoms, 1), 3), dtype=dt, device=dev) if dxdr is not None else None
+        sa = torch.empty((max(natoms, 1), 6), dtype=dt, device=dev) if rdxdr_atom is not None else None
+        stress = torch.empty((max(nstruct, 1), 6), dtype=dt, device=dev) if rdxdr_atom is not None else None
     own = status is None
     if own:
         status = torch.zeros(1, dtype=torch.int32, device=dev)
