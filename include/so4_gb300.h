@@ -212,6 +212,27 @@ int so4_contract_dxdr(int precision, int natoms, int nB, int nstruct, const int3
                       const void *d_dxdr, const void *d_beta, const void *d_rdxdr_atom, void *d_forces,
                       void *d_stress_atom, void *d_stress, int *d_status, void *stream);
 
+/* Rows of the linear (order 1) potential's design matrix d_X (row-major, ncols
+ * columns, FP64), replacing the per-atom np.where loops of
+ * pyxtal_ff/models/polynomialregression.py:438-682 (parse_descriptors).  Column
+ * block e (element index d_species[i] in 0..nelem-1) spans [e (1 + nB), (e + 1)(1 + nB)):
+ * the bias column, then the nB descriptors.
+ * so4_design_forces: for every atom m of structure s, rows d_force_row[s] + 3 (m - atom_ptr[s]) + c
+ *   get in block e columns 1 + k: -sum over the pairs p with seq[p, 1] == m whose centre
+ *   has element e of dxdr[p, k, c] (bias columns untouched).  Pair list and status as
+ *   so4_contract_dxdr; an element index outside [0, nelem) sets bit SO4_ERR_ARG.
+ * so4_design_struct: for structure s with d_energy_row[s] >= 0 that row gets, per block
+ *   e, the count of atoms of element e and the sums of their x; with d_stress_row[s] >= 0
+ *   (d_stress_row may be NULL) rows d_stress_row[s] + v get -sum rdxdr_atom[i, k, v] in
+ *   columns 1 + k. */
+int so4_design_forces(int natoms, int nB, int nelem, const int32_t *d_atom_struct, const int32_t *d_atom_ptr,
+                      const int32_t *d_pair_ptr, const int64_t *d_seq, const int32_t *d_species,
+                      const double *d_dxdr, const int64_t *d_force_row, int64_t ncols, double *d_X,
+                      int *d_status, void *stream);
+int so4_design_struct(int nstruct, int nB, int nelem, const int32_t *d_atom_ptr, const int32_t *d_species,
+                      const double *d_x, const double *d_rdxdr_atom, const int64_t *d_energy_row,
+                      const int64_t *d_stress_row, int64_t ncols, double *d_X, void *stream);
+
 /* ------------------------------------------------------------ adjoint path */
 /* Forward (FP32): U_tot per centre in the half layout (d_utot[natoms*idxu_half*2]
  * f32, kept for the adjoint) and B (d_x[natoms*nB] f32).  Scratch:

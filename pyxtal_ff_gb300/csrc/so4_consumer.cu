@@ -186,7 +186,142 @@ int run(int natoms, int nB, int nstruct, const int32_t *astruct, const int32_t *
     return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
 }
 
+// ---------------------------------------------------------------- linear design matrix
+// Rows of the linear potential's design matrix (pyxtal_ff/models/polynomialregression.py:
+// 438-682, parse_descriptors, order 1).  Columns: per element e (sorted) a block of 1 + nB,
+// the bias column then the descriptors.
+
+// Force rows, one warp per target atom m: row force_row[s] + 3 (m - atom_ptr[s]) + c holds
+// in block e the columns 1 + k = -sum over the pairs p with seq[p, 1] == m whose centre has
+// element e of dxdr[p, k, c].  The incoming pairs are the reverse pairs of m's own, as in
+// k_contract_dxdr; each lane owns the entries idx = lane + 32 s of a per-warp shared
+// accumulator [nelem][3 nB], so no two lanes touch one entry.
+constexpr int DW = 4;  // warps per CTA
+__global__ void __launch_bounds__(DW * 32) k_design_forces(int natoms, int nB, int nelem, const int32_t *astruct,
+                                                          const int32_t *atom_ptr, const int32_t *pair_ptr,
+                                                          const int64_t *seq, const int32_t *species,
+                                                          const double *dxdr, const int64_t *force_row,
+                                                          int64_t ncols, double *X, int *status) {
+    extern __shared__ double dacc[];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int m = blockIdx.x * DW + wid;
+    const int n3 = 3 * nB;
+    double *acc = dacc + (size_t)wid * nelem * n3;
+    if (m >= natoms) return;
+    for (int i = lane; i < nelem * n3; i += 32) acc[i] = 0.0;
+    __syncwarp();  // entries are zeroed and accumulated by different lanes
+    const int s = astruct[m], base = atom_ptr[s];
+    const int64_t ml = m - base;
+    const int q0 = pair_ptr[m], q1 = pair_ptr[m + 1];
+    for (int qb = q0; qb < q1; qb += 32) {
+        int p = -1, e = 0;
+        const int q = qb + lane;
+        if (q < q1) {
+            const int j = base + (int)seq[2 * (size_t)q + 1];
+            e = species[j];
+            int lo = pair_ptr[j], hi = pair_ptr[j + 1] - 1;
+            while (lo <= hi) {
+                const int mid = (lo + hi) >> 1;
+                const int64_t v = seq[2 * (size_t)mid + 1];
+                if (v < ml) {
+                    lo = mid + 1;
+                } else if (v > ml) {
+                    hi = mid - 1;
+                } else {
+                    p = mid;
+                    break;
+                }
+            }
+            if (p < 0) atomicOr(status, 1 << SO4_ERR_REVERSE);
+            if (e < 0 || e >= nelem) {
+                atomicOr(status, 1 << SO4_ERR_ARG);
+                p = -1;
+            }
+        }
+        const int nq = min(32, q1 - qb);
+        for (int t = 0; t < nq; ++t) {
+            const int pp = __shfl_sync(0xffffffffu, p, t), ee = __shfl_sync(0xffffffffu, e, t);
+            if (pp < 0) continue;  // warp-uniform
+            const double *d = dxdr + (size_t)pp * n3;
+            double *a = acc + (size_t)ee * n3;
+#pragma unroll 4
+            for (int idx = lane; idx < n3; idx += 32) a[idx] -= __ldg(d + idx);
+        }
+    }
+    __syncwarp();
+    const int64_t row0 = force_row[s] + 3 * ml;
+    for (int i = lane; i < nelem * n3; i += 32) {
+        const int ee = i / n3, r = i - ee * n3, k = r / 3, c = r - 3 * k;
+        X[(row0 + c) * ncols + (int64_t)ee * (1 + nB) + 1 + k] = acc[i];
+    }
+}
+
+// Energy and stress rows of each structure, one CTA per (structure, element): the energy
+// row (energy_row[s] >= 0) gets in block e the atom count and the sums of x over the
+// structure's atoms of element e; the six stress rows (stress_row[s] >= 0) get
+// -sum rdxdr_atom[i, k, v] in columns 1 + k.  Each thread owns columns and adds the
+// atoms in order.
+constexpr int DS = 128;
+__global__ void __launch_bounds__(DS) k_design_struct(int nB, const int32_t *atom_ptr, const int32_t *species,
+                                                      const double *x, const double *rdxdr,
+                                                      const int64_t *energy_row, const int64_t *stress_row,
+                                                      int64_t ncols, double *X) {
+    const int s = blockIdx.x, e = blockIdx.y;
+    const int a0 = atom_ptr[s], a1 = atom_ptr[s + 1];
+    const int64_t col0 = (int64_t)e * (1 + nB);
+    const int64_t er = energy_row[s], sr = stress_row ? stress_row[s] : -1;
+    if (er >= 0)
+        for (int col = threadIdx.x; col <= nB; col += DS) {
+            double v = 0.0;
+            for (int i = a0; i < a1; ++i)
+                if (species[i] == e) v += (col == 0) ? 1.0 : x[(size_t)i * nB + col - 1];
+            X[er * ncols + col0 + col] = v;
+        }
+    if (sr >= 0 && rdxdr)
+        for (int t = threadIdx.x; t < 6 * nB; t += DS) {
+            const int k = t / 6, v = t - 6 * k;
+            double acc = 0.0;
+            for (int i = a0; i < a1; ++i)
+                if (species[i] == e) acc -= rdxdr[(size_t)i * 6 * nB + t];
+            X[(sr + v) * ncols + col0 + 1 + k] = acc;
+        }
+}
+
 }  // namespace
+
+extern "C" int so4_design_forces(int natoms, int nB, int nelem, const int32_t *d_atom_struct,
+                                 const int32_t *d_atom_ptr, const int32_t *d_pair_ptr, const int64_t *d_seq,
+                                 const int32_t *d_species, const double *d_dxdr, const int64_t *d_force_row,
+                                 int64_t ncols, double *d_X, int *d_status, void *stream) {
+    if (natoms < 0 || nB <= 0 || nelem <= 0 || ncols < (int64_t)nelem * (1 + nB)) return SO4_ERR_ARG;
+    if (natoms == 0) return SO4_OK;
+    if (!d_atom_struct || !d_atom_ptr || !d_pair_ptr || !d_seq || !d_species || !d_dxdr || !d_force_row || !d_X ||
+        !d_status)
+        return SO4_ERR_ARG;
+    const size_t smem = sizeof(double) * DW * (size_t)nelem * 3 * nB;
+    if (smem > 227 * 1024) return SO4_ERR_UNSUPPORTED;
+    int rc = so4_set_smem((const void *)k_design_forces, smem);
+    if (rc) return rc;
+    k_design_forces<<<(natoms + DW - 1) / DW, DW * 32, smem, (cudaStream_t)stream>>>(
+        natoms, nB, nelem, d_atom_struct, d_atom_ptr, d_pair_ptr, d_seq, d_species, d_dxdr, d_force_row, ncols, d_X,
+        d_status);
+    so4_count_launch();
+    return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
+}
+
+extern "C" int so4_design_struct(int nstruct, int nB, int nelem, const int32_t *d_atom_ptr, const int32_t *d_species,
+                                 const double *d_x, const double *d_rdxdr_atom, const int64_t *d_energy_row,
+                                 const int64_t *d_stress_row, int64_t ncols, double *d_X, void *stream) {
+    if (nstruct < 0 || nB <= 0 || nelem <= 0 || ncols < (int64_t)nelem * (1 + nB)) return SO4_ERR_ARG;
+    if (nstruct == 0) return SO4_OK;
+    if (!d_atom_ptr || !d_species || !d_x || !d_energy_row || !d_X || (d_stress_row && !d_rdxdr_atom))
+        return SO4_ERR_ARG;
+    k_design_struct<<<dim3(nstruct, nelem), DS, 0, (cudaStream_t)stream>>>(nB, d_atom_ptr, d_species, d_x,
+                                                                           d_rdxdr_atom, d_energy_row, d_stress_row,
+                                                                           ncols, d_X);
+    so4_count_launch();
+    return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
+}
 
 extern "C" int so4_contract_dxdr(int precision, int natoms, int nB, int nstruct, const int32_t *d_atom_struct,
                                  const int32_t *d_atom_ptr, const int32_t *d_pair_ptr, const int64_t *d_seq,

@@ -381,6 +381,28 @@ def contract_dxdr(beta, pair_ptr, seq, atom_struct, atom_ptr, dxdr=None, rdxdr_a
     return (forces[:natoms] if forces is not None else None), (stress[:nstruct] if stress is not None else None)
 
 
+def design_forces(X, ncols, nB, nelem, species, pair_ptr, seq, atom_struct, atom_ptr, dxdr, force_row):
+    """Force rows of the linear design matrix X (so4_design_forces), in place."""
+    natoms = int(species.numel())
+    status = torch.zeros(1, dtype=torch.int32, device=X.device)
+    check(lib().so4_design_forces(natoms, nB, nelem, _ptr(atom_struct), _ptr(atom_ptr), _ptr(pair_ptr), _ptr(seq),
+                                  _ptr(species), _ptr(dxdr), _ptr(force_row), int(ncols), _ptr(X), _ptr(status),
+                                  _stream()), "so4_design_forces")
+    bits = int(status.item())
+    if bits & (1 << _lib.SO4_ERR_REVERSE):
+        raise ValueError("so4_design_forces: a pair has no reverse pair (the pair list is not symmetric)")
+    if bits & (1 << _lib.SO4_ERR_ARG):
+        raise ValueError("so4_design_forces: an element index is out of range")
+
+
+def design_struct(X, ncols, nB, nelem, species, atom_ptr, x, rdxdr_atom, energy_row, stress_row):
+    """Energy (count, sum x) and stress (-sum rdxdr_atom) rows per structure (so4_design_struct)."""
+    nstruct = int(atom_ptr.numel()) - 1
+    check(lib().so4_design_struct(nstruct, nB, nelem, _ptr(atom_ptr), _ptr(species), _ptr(x), _ptr(rdxdr_atom),
+                                  _ptr(energy_row), _ptr(stress_row), int(ncols), _ptr(X), _stream()),
+          "so4_design_struct")
+
+
 def forward32(tab, prm, nb: Neighbors, w_nb, w_site):
     """FP32 B (N,nB) and U_tot (N, n_half, 2) for the adjoint."""
     dev = w_nb.device
