@@ -14,7 +14,7 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 def names():
     """Descriptor cases (tests/golden/make_golden.py)."""
     return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
-                  if not os.path.basename(p).startswith(("reference_tables", "nn_")))
+                  if not os.path.basename(p).startswith(("reference_tables", "nn_", "pr_")))
 
 
 def nn_names():
