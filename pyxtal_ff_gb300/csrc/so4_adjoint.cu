@@ -215,9 +215,9 @@ __device__ __forceinline__ void zw_unit(const ZLArgs &A, const int4 un, const fl
     const int lam = un.x & 0xff, mb = (un.x >> 8) & 0xff, ma0 = (un.x >> 16) & 0xff;
     const int off0 = mb * (lam + 1) + ma0;
     const int cnt = section_count(lam);
-    float yr[K], yi[K];
+    float2 y[K];
 #pragma unroll
-    for (int k = 0; k < K; ++k) yr[k] = yi[k] = 0.f;
+    for (int k = 0; k < K; ++k) y[k] = make_float2(0.f, 0.f);
     // MODE 3: w_e dU[e] of the unit's entries in the section (0 past its end), reused by every block
     float dur[K], dui[K];
     if (MODE == 3) {
@@ -238,21 +238,21 @@ __device__ __forceinline__ void zw_unit(const ZLArgs &A, const int4 un, const fl
     for (int q = un.y; q < un.z; ++q) {
         const int4 sg = sgn;
         if (q + 1 < un.z) sgn = __ldg(A.seg + q + 1);
-        float zr[K], zi[K];
+        float2 z[K];
 #pragma unroll
-        for (int k = 0; k < K; ++k) zr[k] = zi[k] = 0.f;
+        for (int k = 0; k < K; ++k) z[k] = make_float2(0.f, 0.f);
         int4 hdn = (sg.x < sg.y) ? __ldg(A.wsub + sg.x) : make_int4(0, 0, 0, 0);
         for (int r = sg.x; r < sg.y; ++r) {
             const int4 hd = hdn;
             if (r + 1 < sg.y) hdn = __ldg(A.wsub + r + 1);
-            zw_rows<K>(Ul, hd, ca, zr, zi);
+            zw_rows<K>(Ul, hd, ca, z);
         }
         if (MODE == 3) {
             // sum_e w_e Re(conj(dU[e]) Z[e]) over the unit's section entries, once per role of
             // the block: slot (jbase + unit index) of the role's component, scaled by fac_s
             float v = 0.f;
 #pragma unroll
-            for (int k = 0; k < K; ++k) v = fmaf(dur[k], zr[k], fmaf(dui[k], zi[k], v));
+            for (int k = 0; k < K; ++k) v = fmaf(dur[k], z[k].x, fmaf(dui[k], z[k].y, v));
             if (a < A.natoms) {
 #pragma unroll
                 for (int r = 0; r < 3; ++r) {
@@ -266,8 +266,7 @@ __device__ __forceinline__ void zw_unit(const ZLArgs &A, const int4 un, const fl
             const float c = coef[sg.z * ZL_PITCH + lane];
 #pragma unroll
             for (int k = 0; k < K; ++k) {
-                yr[k] = fmaf(c, zr[k], yr[k]);
-                yi[k] = fmaf(c, zi[k], yi[k]);
+                y[k] = __ffma2_rn(make_float2(c, c), z[k], y[k]);
             }
         }
         if ((MODE == 0 || MODE == 2) && sg.w >= 0) {
@@ -280,7 +279,7 @@ __device__ __forceinline__ void zw_unit(const ZLArgs &A, const int4 un, const fl
                 const int off = off0 + k;
                 if (off < cnt) {
                     const float2 uv = ul[k * ZL_PITCH];
-                    const float d = uv.x * zr[k] + uv.y * zi[k];
+                    const float d = uv.x * z[k].x + uv.y * z[k].y;
                     v += ((lam & 1) == 0 && off == cnt - 1) ? 0.5f * d : d;
                 }
             }
@@ -296,7 +295,7 @@ __device__ __forceinline__ void zw_unit(const ZLArgs &A, const int4 un, const fl
             const int ma = ma0 + k;
             const float wmid = (2 * mb < lam) ? 1.f : ((2 * ma < lam) ? 1.f : ((2 * ma == lam) ? 0.5f : 0.f));
             const float s = un_l * wmid;
-            Yo[k] = make_float2(s * yr[k], s * yi[k]);
+            Yo[k] = make_float2(s * y[k].x, s * y[k].y);
         }
     }
 }

@@ -24,31 +24,40 @@ __device__ __forceinline__ void zw_load_utot(const float2 *__restrict__ utot, co
 }
 
 // One sub-segment {f1 | f2 << 16, Ca offset, steps S, bits of Cb}: adds
-// Cb sum_j Ca[j][k] U_a[f2 - j + k] U_b[f1 + j] to z[k], k < K, for this lane's
-// atom (offsets in Ub rows, pre-scaled by the pitch; Ul = Ub + lane).  Ca rows
-// hold KP = K rounded up to 4 floats.
+// Cb sum_j Ca[j][k] U_a[f2 - j + k] U_b[f1 + j] to z[k] = (re, im), k < K, for this
+// lane's atom (offsets in Ub rows, pre-scaled by the pitch; Ul = Ub + lane).  Ca rows
+// hold KP = K rounded up to 4 floats.  Packed FP32 pairs (sm_100+): the ring keeps each
+// U_a value w as (w.x, w.x) and (-w.y, w.y), so with a = Cb U_b and as = (a.y, a.x) the
+// complex product is (w.x, w.x) * a + (-w.y, w.y) * as, and one more packed FMA adds
+// Ca[j][k] times it: three packed instructions per (step, entry).
 template <int K>
 __device__ __forceinline__ void zw_rows(const float2 *Ul, const int4 hd, const float *__restrict__ ca,
-                                        float (&zr)[K], float (&zi)[K]) {
+                                        float2 (&z)[K]) {
     constexpr int KQ = (K + 3) / 4;  // float4 loads per Ca row
     const int f1 = hd.x & 0xffff, f2 = (int)((unsigned)hd.x >> 16);
     const int S = hd.z;
     const float cb = __int_as_float(hd.w);
+    const float2 cb2 = make_float2(cb, cb);
     const float4 *cw = reinterpret_cast<const float4 *>(ca + hd.y);
-    float2 R[K];
+    float2 WX[K], WY[K];
 #pragma unroll
-    for (int k = 1; k < K; ++k) R[k] = Ul[f2 + k * ZL_PITCH];
-    R[0] = make_float2(0.f, 0.f);
+    for (int k = 1; k < K; ++k) {
+        const float2 w = Ul[f2 + k * ZL_PITCH];
+        WX[k] = make_float2(w.x, w.x);
+        WY[k] = make_float2(-w.y, w.y);
+    }
+    WX[0] = WY[0] = make_float2(0.f, 0.f);
     for (int j0 = 0; j0 < S; j0 += K) {
 #pragma unroll
         for (int t = 0; t < K; ++t) {
             const int j = j0 + t;
             if (j < S) {
                 // ring slot of entry k at step j is (k - j) mod K; entry 0 is new
-                R[(K - t) % K] = Ul[f2 - j * ZL_PITCH];
-                float2 u = Ul[f1 + j * ZL_PITCH];
-                u.x *= cb;
-                u.y *= cb;
+                const float2 w = Ul[f2 - j * ZL_PITCH];
+                WX[(K - t) % K] = make_float2(w.x, w.x);
+                WY[(K - t) % K] = make_float2(-w.y, w.y);
+                const float2 a = __fmul2_rn(Ul[f1 + j * ZL_PITCH], cb2);
+                const float2 as = make_float2(a.y, a.x);
                 float cc[4 * KQ];
 #pragma unroll
                 for (int q = 0; q < KQ; ++q) {
@@ -60,11 +69,9 @@ __device__ __forceinline__ void zw_rows(const float2 *Ul, const int4 hd, const f
                 }
 #pragma unroll
                 for (int k = 0; k < K; ++k) {
-                    const float2 w = R[(k - t + K) % K];
-                    const float pr = u.x * w.x - u.y * w.y;
-                    const float pi = u.x * w.y + u.y * w.x;
-                    zr[k] = fmaf(cc[k], pr, zr[k]);
-                    zi[k] = fmaf(cc[k], pi, zi[k]);
+                    const int r = (k - t + K) % K;
+                    const float2 p = __ffma2_rn(WY[r], as, __fmul2_rn(WX[r], a));
+                    z[k] = __ffma2_rn(make_float2(cc[k], cc[k]), p, z[k]);
                 }
             }
         }
