@@ -327,7 +327,7 @@ __global__ void __launch_bounds__(ZW_THREADS, 2) k_zw32(ZLArgs A) {
             if (aa < A.natoms) {
                 const ZBlk &bk = A.blk[b];
                 for (int r = 0; r < bk.nrole; ++r)
-                    c += (float)bk.role_f[r] * __ldg(A.beta + (size_t)aa * A.nB + bk.role_k[r]);
+                    c += bk.role_f32[r] * __ldg(A.beta + (size_t)aa * A.nB + bk.role_k[r]);
             }
             coef[b * ZL_PITCH + l] = c;
         }
@@ -365,7 +365,9 @@ __global__ void __launch_bounds__(ZW_THREADS, 2) k_zw32(ZLArgs A) {
             const int k = idx >> 5, aa = a0 + (idx & 31);
             if (aa >= A.natoms) continue;
             float acc = 0.f;
-            for (int q = __ldg(A.jpos + k); q < __ldg(A.jpos + k + 1); ++q) acc += A.bc[(size_t)q * A.natoms + aa];
+            const int q1 = __ldg(A.jpos + k + 1);
+#pragma unroll 4
+            for (int q = __ldg(A.jpos + k); q < q1; ++q) acc += A.bc[(size_t)q * A.natoms + aa];
             A.x[(size_t)aa * A.nB + k] = acc;
         }
         return;
@@ -377,7 +379,10 @@ __global__ void __launch_bounds__(ZW_THREADS, 2) k_zw32(ZLArgs A) {
         const int aa = a0 + l;
         float acc = 0.f, e = 0.f;
         if (aa < A.natoms) {
-            for (int q = __ldg(A.bpos + k); q < __ldg(A.bpos + k + 1); ++q) acc += A.bc[(size_t)q * A.natoms + aa];
+            // the slots are independent loads: unrolled so they are in flight together
+            const int q1 = __ldg(A.bpos + k + 1);
+#pragma unroll 4
+            for (int q = __ldg(A.bpos + k); q < q1; ++q) acc += A.bc[(size_t)q * A.natoms + aa];
             acc *= 2.f;
             A.x[(size_t)aa * A.nB + k] = acc;
             if (MODE == 2) e = acc * __ldg(A.beta + (size_t)aa * A.nB + k);

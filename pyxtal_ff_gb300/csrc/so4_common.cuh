@@ -83,6 +83,7 @@ struct ZBlk {
     int nrole;
     int role_k[3];
     double role_f[3];
+    float role_f32[3];  // role_f in FP32 for the FP32 kernels (no FP64 conversion on the device)
 };
 
 // One product term of a Z entry: Z += c * U[i1] * U[i2] with c = cg_a * cg_b

@@ -271,6 +271,7 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
                 if (bk.z0 == blk_of[s]) {
                     bk.role_k[bk.nrole] = k;
                     bk.role_f[bk.nrole] = b.fac[s];
+                    bk.role_f32[bk.nrole] = (float)b.fac[s];
                     bk.nrole++;
                 }
         }

@@ -16,6 +16,9 @@ constexpr int ZL_PITCH = 33;
 // Uf[f][lane] for the 32 atoms a0.. (zeros past natoms)
 __device__ __forceinline__ void zl_load_utot(const float2 *__restrict__ utot, const int *__restrict__ fmap, int a0,
                                              int natoms, int nh, int nu, float2 *Uf) {
+    // unrolled: each iteration is a dependent pair of loads (map, then U), so several
+    // iterations are kept in flight
+#pragma unroll 4
     for (int idx = threadIdx.x; idx < 32 * nu; idx += blockDim.x) {
         const int lane = idx / nu, f = idx - lane * nu;
         const int a = a0 + lane;
