@@ -113,6 +113,13 @@ __global__ void __launch_bounds__(NW * 32, (TWOL <= 8) ? 4 : 1) k_utot_rc(FwdArg
         const int m0 = A.img_ptr[a], m1 = A.img_ptr[a + 1];
         for (int base = m0; base < m1; base += RC::IPW) {
             const int m = base + grp;
+            // the next iteration's image vector and neighbour index into L1 while this
+            // iteration's recursion runs (no registers held)
+            const int mn = m + RC::IPW;
+            if (grp < RC::IPW && mn < m1) {
+                asm volatile("prefetch.global.L1 [%0];" ::"l"(A.img_r + 3 * mn));
+                asm volatile("prefetch.global.L1 [%0];" ::"l"(A.img_j + mn));
+            }
             float x = 1.f, y = 0.f, z = 0.f, wsf = 0.f;
             if (grp < RC::IPW && m < m1) {
                 x = (float)A.img_r[3 * m];

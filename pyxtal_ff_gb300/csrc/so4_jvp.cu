@@ -57,6 +57,12 @@ __global__ void __launch_bounds__(NW * 32, (TWOL <= 6) ? 4 : ((TWOL == 8) ? 3 : 
         }
         for (int base = m0; base < m1; base += RC::IPW) {
             const int m = base + grp;
+            // the next iteration's image vector and neighbour index into L1 (no registers held)
+            const int mn = m + RC::IPW;
+            if (grp < RC::IPW && mn < m1) {
+                asm volatile("prefetch.global.L1 [%0];" ::"l"(A.img_r + 3 * mn));
+                asm volatile("prefetch.global.L1 [%0];" ::"l"(A.img_j + mn));
+            }
             float x = 1.f, y = 0.f, z = 0.f, a_du = 0.f, a_d = 0.f;
             float d[3] = {0.f, 0.f, 0.f};
             if (grp < RC::IPW && m < m1) {
