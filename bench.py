@@ -172,6 +172,47 @@ def run_reference(args, ws, rank):
 
 
 # ----------------------------------------------------------------- GPU side
+def run_contract(args):
+    """The contraction alone: plain FP64 descriptors of an N x N x 10 cell, then
+    args.steps back-to-back so4_contract_dxdr calls (forces and stress) timed with events."""
+    import torch
+    from pyxtal_ff_gb300 import engine
+    from pyxtal_ff_gb300 import structures as S
+    from pyxtal_ff_gb300.calculator import Batch, SO4Calculator
+    n = args.contract_cells
+    atoms = S.diamond_si(n, n, 10, sigma=0.1, rng=np.random.default_rng(5))
+    batch = Batch([atoms])
+    calc = SO4Calculator(lmax=LMAX, rcut=RCUT, kind="SNAP", weights={"Si": 1.0}, rfac0=1.0)
+    d = calc.descriptors(batch, precision="fp64")
+    nb = d["neighbors"]
+    rda = engine.rdxdr_atom(d["rdxdr"], nb.pair_ptr, nb.natoms)
+    del d["rdxdr"]
+    beta = torch.from_numpy(np.random.default_rng(6).normal(0, 0.01, (nb.natoms, calc.nB))).cuda()
+    st = torch.zeros(1, dtype=torch.int32, device="cuda")
+    out = (torch.empty((nb.natoms, 3), dtype=torch.float64, device="cuda"),
+           torch.empty((nb.natoms, 6), dtype=torch.float64, device="cuda"),
+           torch.empty((1, 6), dtype=torch.float64, device="cuda"))
+
+    def once():
+        engine.contract_dxdr(beta, nb.pair_ptr, nb.seq, nb.atom_struct, nb.atom_ptr_dev, dxdr=d["dxdr"],
+                             rdxdr_atom=rda, status=st, out=out)
+    for _ in range(max(args.warmup, 1)):
+        once()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        once()
+    e1.record()
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    if int(st.item()):
+        raise RuntimeError("asymmetric pair list")
+    byt = 8 * (nb.npair * calc.nB * 3 + nb.natoms * calc.nB * 7 + 2 * nb.npair)
+    print(json.dumps({"contract_only": True, "atoms": nb.natoms, "pairs": nb.npair, "ms": ms,
+                      "gbs": byt / (ms * 1e-3) / 1e9}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -182,10 +223,16 @@ def main():
     ap.add_argument("--no-train", action="store_true", help="skip the training-step leg")
     ap.add_argument("--quick", action="store_true",
                     help="device-resident steps only (no e2e, FP64, CPU or peak legs); for profiler runs")
+    ap.add_argument("--contract-cells", type=int, default=0,
+                    help="only the NN consumer's dxdr contraction (so4_contract_dxdr) on an N x N x 10 diamond-Si "
+                         "cell at lmax 4 (a small case for profiler runs)")
     args = ap.parse_args()
     ws, rank, local = dist_env()
     if args.impl == "reference":
         run_reference(args, ws, rank)
+        return
+    if args.contract_cells:
+        run_contract(args)
         return
 
     import torch
