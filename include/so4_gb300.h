@@ -258,7 +258,10 @@ int so4_adjoint32(const so4_tables *t, const so4_params *p, int nstruct, const i
                   double *d_virial, void *d_work, size_t work_bytes, void *stream);
 
 /* The three stages so4_adjoint32 runs, for callers that keep their own buffers:
- *   so4_adjoint_y32      Y[natoms*idxu_half*2] f32 from U_tot and beta (atoms across lanes);
+ *   so4_adjoint_y32      Y[natoms*idxu_half*2] f32 from U_tot and beta (atoms across lanes),
+ *                        each half entry (l, mb, ma) stored times sqrt(C(l, mb) / C(l, ma))
+ *                        (C binomial), the row scale of the recursion so4_adjoint_deidrj32
+ *                        runs; a buffer for that call, not a result to read;
  *   so4_adjoint_deidrj32 g[m*3] f32 = dE/dr of every image m of the natoms centres,
  *                        m in [d_img_ptr[0], d_img_ptr[natoms]) (U and dU by the
  *                        recursion, contracted with Y); nimg bounds the number of those

@@ -67,7 +67,7 @@ struct FwdArgs {
     const ZEnt *zent, *zentB;
     const BEnt *bent;
     SmallTables st;
-    const int2 *hmap;  // per half entry: accumulator slot, row, diagonal flag, u_norm
+    const int4 *hmap;  // per half entry: accumulator slot, row, diagonal flag, u_norm F, u_norm
     float *utot, *x;
 };
 
@@ -159,7 +159,7 @@ __global__ void __launch_bounds__(NW * 32, (TWOL <= 8) ? 4 : 1) k_utot_rc(FwdArg
     const float selfw = f0 * (float)A.w_site[a];
     float2 *ug = (float2 *)A.utot + (size_t)a * A.nh;
     for (int e = lane; e < A.nh; e += 32) {
-        const int2 h = __ldg(A.hmap + e);
+        const int4 h = __ldg(A.hmap + e);
         const int slot = h.x & 0xff, row = (h.x >> 8) & 0x7f;
         float sr = 0.f, si = 0.f;
 #pragma unroll
@@ -168,9 +168,11 @@ __global__ void __launch_bounds__(NW * 32, (TWOL <= 8) ? 4 : 1) k_utot_rc(FwdArg
             sr += src[0];
             si += src[1];
         }
-        if (h.x & (1 << 15)) sr += selfw;
-        const float un = __int_as_float(h.y);
-        ug[e] = make_float2(sr * un, si * un);
+        // sums of scaled rows: times u_norm F; the self term (diagonal) times u_norm
+        const float unf = __int_as_float(h.y), un = __int_as_float(h.z);
+        sr *= unf;
+        if (h.x & (1 << 15)) sr = fmaf(selfw, un, sr);
+        ug[e] = make_float2(sr, si * unf);
     }
 }
 
@@ -210,6 +212,7 @@ struct ZLArgs {
     const float2 *dU;
     const int *jbase, *jpos;
     const float *jfac;
+    const float *yscale;  // n_half: Y is stored times the row scale F of its entry
 };
 
 
@@ -297,11 +300,13 @@ __device__ __forceinline__ void zw_unit(const ZLArgs &A, const int4 un, const fl
     if ((MODE == 1 || MODE == 2) && a < A.natoms) {
         const float un_l = __int_as_float(un.w);
         float2 *Yo = A.Y + (size_t)a * A.nh + A.st.h_block[lam] + off0;
+        const float *ys = A.yscale + A.st.h_block[lam] + off0;
 #pragma unroll
         for (int k = 0; k < K; ++k) {
             const int ma = ma0 + k;
             const float wmid = (2 * mb < lam) ? 1.f : ((2 * ma < lam) ? 1.f : ((2 * ma == lam) ? 0.5f : 0.f));
-            const float s = un_l * wmid;
+            // times the row scale F: the reverse sweep contracts the scaled rows with it
+            const float s = un_l * wmid * __ldg(ys + k);
             Yo[k] = make_float2(s * y[k].x, s * y[k].y);
         }
     }
@@ -769,6 +774,7 @@ static ZLArgs zl_args(const so4_tables *t, int natoms) {
     Z.wsub = t->d_wsub;
     Z.wca = t->d_wca;
     Z.nwca = t->n_wca;
+    Z.yscale = t->d_yscale;
     fill_small_tables(t, Z.st);
     return Z;
 }

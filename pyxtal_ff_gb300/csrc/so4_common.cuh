@@ -119,8 +119,10 @@ struct so4_tables {
     int *d_term_ptr = nullptr;  // n_z + 1
     int *d_fmap = nullptr;      // n_u: full entry -> half source | conj << 15 | negate << 14
     // n_half: per half entry (level L, row, ma) {L(L+1)/2 + ma | row << 8 | (ma == row) << 15,
-    // bits of u_norm[L] as float}: where the row-chain kernels keep it and how it is finished
-    int2 *d_hmap = nullptr;
+    // bits of u_norm[L] F, bits of u_norm[L], 0}: where the row-chain kernels keep it and how
+    // it is finished (F the row scale of the scaled recursion, so4_tables.cu)
+    int4 *d_hmap = nullptr;
+    float *d_yscale = nullptr;  // n_half: the row-scale F of each half entry (so4_tables.cu)
     // B partial slots of the window kernels: one per (window unit, B block), component k
     // owning slots [bpos[k], bpos[k + 1]) in row order
     int *d_bpos = nullptr;  // nB + 1

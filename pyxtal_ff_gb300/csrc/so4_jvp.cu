@@ -27,7 +27,7 @@ struct JArgs {
     const double *w_nb, *img_r, *v, *G;
     const int32_t *img_ptr, *img_j;
     SmallTables st;
-    const int2 *hmap;  // per half entry: accumulator slot, row, u_norm
+    const int4 *hmap;  // per half entry: accumulator slot, row, diagonal flag, u_norm F, u_norm
     float2 *dU;
     float *dB;
 };
@@ -122,7 +122,7 @@ __global__ void __launch_bounds__(NW * 32, (TWOL <= 6) ? 4 : ((TWOL == 8) ? 3 : 
     if (a >= A.natoms) return;
     float2 *out = A.dU + (size_t)a * A.nh;
     for (int e = lane; e < A.nh; e += 32) {
-        const int2 h = __ldg(A.hmap + e);
+        const int4 h = __ldg(A.hmap + e);
         const int slot = h.x & 0xff, row = (h.x >> 8) & 0x7f;
         float sr = 0.f, si = 0.f;
 #pragma unroll
@@ -131,8 +131,8 @@ __global__ void __launch_bounds__(NW * 32, (TWOL <= 6) ? 4 : ((TWOL == 8) ? 3 : 
             sr += src[0];
             si += src[1];
         }
-        const float un = __int_as_float(h.y);
-        out[e] = make_float2(sr * un, si * un);
+        const float unf = __int_as_float(h.y);  // u_norm times the row scale
+        out[e] = make_float2(sr * unf, si * unf);
     }
 }
 

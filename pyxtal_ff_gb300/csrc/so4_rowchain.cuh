@@ -8,28 +8,18 @@
 // dU/dr components) in registers from level 2mb up to TWOL, updated in place;
 // the only exchange is one shuffle of the previous chain's row at the chain start.
 // TWOL is a template parameter so every row index is a compile-time constant.
+//
+// Rows are carried scaled: V_l[ma] = U_l[ma][mb] sqrt(C(l, ma) / C(l, mb)) (C the
+// binomial coefficient).  The reference's step
+//   U_l[ma] = sqrt(l-ma)/sqrt(l-mb) conj(a) U_{l-1}[ma] - sqrt(ma)/sqrt(l-mb) conj(b) U_{l-1}[ma-1]
+// then reads V_l[ma] = conj(a) V_{l-1}[ma] - conj(b) V_{l-1}[ma-1] (the square roots
+// cancel against the scale), while the chain-start mirror and the middle-row
+// symmetry hold unchanged because C(l, ma) = C(l, l - ma).  Consumers undo the scale
+// per half entry: the U_tot epilogue through its table, the reverse sweep by reading
+// a Y that the window kernel scaled by the same factor.
 #pragma once
 
 #include "so4_common.cuh"
-
-// sqrt(k) for k = 0..16, the numerators of rootpq[p][q] = sqrt(p / q)
-__constant__ float c_sqrtk[17] = {0.0f,
-                                  1.0f,
-                                  1.41421356237309515f,
-                                  1.73205080756887719f,
-                                  2.0f,
-                                  2.23606797749978981f,
-                                  2.44948974278317788f,
-                                  2.64575131106459072f,
-                                  2.82842712474619029f,
-                                  3.0f,
-                                  3.16227766016837952f,
-                                  3.31662479035539981f,
-                                  3.46410161513775439f,
-                                  3.60555127546398912f,
-                                  3.74165738677394133f,
-                                  3.87298334620741702f,
-                                  4.0f};
 
 template <int TWOL>
 struct RowChain {
@@ -38,13 +28,13 @@ struct RowChain {
     static constexpr int W = TWOL + 1;         // longest row
 };
 
-// Advance one image's chain `mb` from level L-1 to level L (in place).
-// u, d0, d1, d2: the row (re, im) of U and of dU/dx, dU/dy, dU/dz.
+// Advance one image's chain `mb` from level L-1 to level L (in place), scaled rows:
+// V_L[ma] = conj(a) V_{L-1}[ma] - conj(b) V_{L-1}[ma-1].
+// u, d0, d1, d2: the row (re, im) of V and of dV/dx, dV/dy, dV/dz.  Lanes whose chain
+// has not started (mb > L/2) compute values nobody reads.
 template <int TWOL, int L, bool DERIV, int NDER = 3>
 __device__ __forceinline__ void rc_level(int mb, const CK<float> &ck, float (&ur)[TWOL + 1], float (&ui)[TWOL + 1],
                                          float (&dr)[NDER][TWOL + 1], float (&di)[NDER][TWOL + 1]) {
-    // 1 / sqrt(l - mb); lanes whose chain has not started (mb > L/2) compute values nobody reads
-    const float inv_q = rsqrtf((float)max(L - mb, 1));
     // descending in place: new[ma] uses old[ma] (a-term) and old[ma-1] (b-term)
 #pragma unroll
     for (int ma = L; ma >= 0; --ma) {
@@ -53,39 +43,30 @@ __device__ __forceinline__ void rc_level(int mb, const CK<float> &ck, float (&ur
 #pragma unroll
         for (int c = 0; c < NDER; ++c) er[c] = ei[c] = 0.f;
         if (ma > 0) {
-            const float rp = -c_sqrtk[ma] * inv_q;
+            // - conj(b) * P[ma-1]
             const float pr = ur[ma - 1], pi = ui[ma - 1];
-            // conj(b) * P
-            const float br = ck.cb.re * pr - ck.cb.im * pi;
-            const float bi = ck.cb.re * pi + ck.cb.im * pr;
-            vr = rp * br;
-            vi = rp * bi;
+            vr = fmaf(ck.cb.im, pi, -ck.cb.re * pr);
+            vi = fmaf(-ck.cb.im, pr, -ck.cb.re * pi);
             if (DERIV) {
 #pragma unroll
                 for (int c = 0; c < NDER; ++c) {
                     const float qr = dr[c][ma - 1], qi = di[c][ma - 1];
-                    const float tr = ck.cdb[c].re * pr - ck.cdb[c].im * pi + ck.cb.re * qr - ck.cb.im * qi;
-                    const float ti = ck.cdb[c].re * pi + ck.cdb[c].im * pr + ck.cb.re * qi + ck.cb.im * qr;
-                    er[c] = rp * tr;
-                    ei[c] = rp * ti;
+                    er[c] = -(ck.cdb[c].re * pr - ck.cdb[c].im * pi + ck.cb.re * qr - ck.cb.im * qi);
+                    ei[c] = -(ck.cdb[c].re * pi + ck.cdb[c].im * pr + ck.cb.re * qi + ck.cb.im * qr);
                 }
             }
         }
         if (ma < L) {
-            const float rp = c_sqrtk[L - ma] * inv_q;
+            // + conj(a) * P[ma]
             const float pr = ur[ma], pi = ui[ma];
-            const float ar = ck.ca.re * pr - ck.ca.im * pi;
-            const float ai = ck.ca.re * pi + ck.ca.im * pr;
-            vr += rp * ar;
-            vi += rp * ai;
+            vr = fmaf(ck.ca.re, pr, fmaf(-ck.ca.im, pi, vr));
+            vi = fmaf(ck.ca.re, pi, fmaf(ck.ca.im, pr, vi));
             if (DERIV) {
 #pragma unroll
                 for (int c = 0; c < NDER; ++c) {
                     const float qr = dr[c][ma], qi = di[c][ma];
-                    const float tr = ck.cda[c].re * pr - ck.cda[c].im * pi + ck.ca.re * qr - ck.ca.im * qi;
-                    const float ti = ck.cda[c].re * pi + ck.cda[c].im * pr + ck.ca.re * qi + ck.ca.im * qr;
-                    er[c] += rp * tr;
-                    ei[c] += rp * ti;
+                    er[c] += ck.cda[c].re * pr - ck.cda[c].im * pi + ck.ca.re * qr - ck.ca.im * qi;
+                    ei[c] += ck.cda[c].re * pi + ck.cda[c].im * pr + ck.ca.re * qi + ck.ca.im * qr;
                 }
             }
         }
@@ -324,25 +305,22 @@ struct RvBack {
 #pragma unroll
                 for (int ma = H + 1; ma <= L; ++ma) gr[ma] = gi[ma] = 0.f;
             }
-            // V[ma] = alpha_ma conj(a) P[ma] + beta_ma conj(b) P[ma-1],
-            // alpha_ma = sqrt(L-ma)/sqrt(L-mb), beta_ma = -sqrt(ma)/sqrt(L-mb)
-            const float inv_q = rsqrtf((float)max(L - mb, 1));
+            // scaled rows: V[ma] = conj(a) P[ma] - conj(b) P[ma-1]
             const float ar = ck.ca.re, ai = -ck.ca.im;  // a = conj(conj(a))
             const float br = ck.cb.re, bi = -ck.cb.im;
-            // in place, ascending: the new G[ma] = alpha_ma a G[ma] + beta_{ma+1} b G[ma+1]
-            // reads G[ma + 1] before it is replaced
+            // in place, ascending: the new G[ma] = a G[ma] - b G[ma+1] reads G[ma + 1]
+            // before it is replaced
 #pragma unroll
             for (int ma = 0; ma < L; ++ma) {
                 const float g0 = gr[ma], g1 = gi[ma], h0 = gr[ma + 1], h1 = gi[ma + 1];
-                const float al = c_sqrtk[L - ma] * inv_q, be = -c_sqrtk[ma + 1] * inv_q;
                 const float2 p = st[(acc_block(L - 1) + ma) * NT];
-                // G_ca += al conj(P) G[ma];  G_cb += be conj(P) G[ma+1]
-                gar = fmaf(al, p.x * g0 + p.y * g1, gar);
-                gai = fmaf(al, p.x * g1 - p.y * g0, gai);
-                gbr = fmaf(be, p.x * h0 + p.y * h1, gbr);
-                gbi = fmaf(be, p.x * h1 - p.y * h0, gbi);
-                gr[ma] = al * (ar * g0 - ai * g1) + be * (br * h0 - bi * h1);
-                gi[ma] = al * (ar * g1 + ai * g0) + be * (br * h1 + bi * h0);
+                // G_ca += conj(P) G[ma];  G_cb -= conj(P) G[ma+1]
+                gar = fmaf(p.x, g0, fmaf(p.y, g1, gar));
+                gai = fmaf(p.x, g1, fmaf(-p.y, g0, gai));
+                gbr = fmaf(-p.x, h0, fmaf(-p.y, h1, gbr));
+                gbi = fmaf(-p.x, h1, fmaf(p.y, h0, gbi));
+                gr[ma] = fmaf(ar, g0, fmaf(-ai, g1, fmaf(-br, h0, bi * h1)));
+                gi[ma] = fmaf(ar, g1, fmaf(ai, g0, fmaf(-br, h1, -bi * h0)));
             }
             gr[L] = gi[L] = 0.f;
         }

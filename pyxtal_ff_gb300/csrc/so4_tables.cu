@@ -92,6 +92,7 @@ void free_device(so4_tables *t) {
     cudaFree(t->d_terms);
     cudaFree(t->d_fmap);
     cudaFree(t->d_hmap);
+    cudaFree(t->d_yscale);
     cudaFree(t->d_term_ptr);
     cudaFree(t->d_bpos);
     cudaFree(t->d_wunit_y);
@@ -550,17 +551,36 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
             }
 
     int rc = jrc;
-    std::vector<int2> hmap;
+    // The FP32 row-chain kernels carry each row in the scaled form V with
+    //   U_l[ma][mb] = sqrt(C(l, mb) / C(l, ma)) V_l[ma][mb],
+    // in which the recursion's coefficients sqrt(l - ma) / sqrt(l - mb) and
+    // -sqrt(ma) / sqrt(l - mb) become 1 and -1; the chain-start mirror and the middle-row
+    // symmetry keep their form.  hmap: per half entry {slot | row << 8 | diagonal << 15,
+    // bits of u_norm F, bits of u_norm, 0}; yscale: F, by which the window kernels scale Y so
+    // that the reverse sweep contracts V with it.
+    auto binom = [](int n, int k) {
+        double c = 1.0;
+        for (int i = 1; i <= k; ++i) c = c * (double)(n - k + i) / (double)i;
+        return c;
+    };
+    std::vector<int4> hmap;
+    std::vector<float> yscale;
     for (int l = 0; l < ld; ++l) {
         const float un = (float)t->unorm_l[l];
-        int ubits;
-        std::memcpy(&ubits, &un, sizeof ubits);
         for (int mb = 0; 2 * mb <= l; ++mb)
-            for (int ma = 0; ma <= l; ++ma)
-                hmap.push_back(make_int2((l * (l + 1) / 2 + ma) | (mb << 8) | ((ma == mb ? 1 : 0) << 15), ubits));
+            for (int ma = 0; ma <= l; ++ma) {
+                const double F = std::sqrt(binom(l, mb) / binom(l, ma));
+                const float unf = (float)(t->unorm_l[l] * F);
+                int b_unf, b_un;
+                std::memcpy(&b_unf, &unf, sizeof b_unf);
+                std::memcpy(&b_un, &un, sizeof b_un);
+                hmap.push_back(make_int4((l * (l + 1) / 2 + ma) | (mb << 8) | ((ma == mb ? 1 : 0) << 15), b_unf, b_un, 0));
+                yscale.push_back((float)F);
+            }
     }
     if (!rc) rc = upload(&t->d_fmap, fmap);
     if (!rc) rc = upload(&t->d_hmap, hmap);
+    if (!rc) rc = upload(&t->d_yscale, yscale);
     if (!rc) rc = upload(&t->d_terms, terms);
     if (!rc) rc = upload(&t->d_term_ptr, t->term_ptr);
     if (!rc) rc = upload(&t->d_bpos, bpos);
