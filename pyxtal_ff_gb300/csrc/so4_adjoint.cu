@@ -111,17 +111,13 @@ __global__ void __launch_bounds__(NW * 32, (TWOL <= 8) ? 4 : 1) k_utot_rc(FwdArg
     for (int q = 0; q < NACC; ++q) accr[q] = acci[q] = 0.f;
     if (a < A.natoms) {
         const int m0 = A.img_ptr[a], m1 = A.img_ptr[a + 1];
-        for (int base = m0; base < m1; base += RC::IPW) {
-            const int m = base + grp;
-            // the next iteration's image vector and neighbour index into L1 while this
-            // iteration's recursion runs (no registers held)
-            const int mn = m + RC::IPW;
-            if (grp < RC::IPW && mn < m1) {
-                asm volatile("prefetch.global.L1 [%0];" ::"l"(A.img_r + 3 * mn));
-                asm volatile("prefetch.global.L1 [%0];" ::"l"(A.img_j + mn));
-            }
-            float x = 1.f, y = 0.f, z = 0.f, wsf = 0.f;
-            if (grp < RC::IPW && m < m1) {
+        // Cayley-Klein parameters and weights of up to 32 images at once, one per lane;
+        // each recursion iteration then takes its IPW images' values by shuffles (one
+        // setup pass per 32 images instead of one per IPW)
+        for (int base = m0; base < m1; base += 32) {
+            float x = 1.f, y = 0.f, z = 0.f, wsf0 = 0.f;
+            const int m = base + lane;
+            if (m < m1) {
                 x = (float)A.img_r[3 * m];
                 y = (float)A.img_r[3 * m + 1];
                 z = (float)A.img_r[3 * m + 2];
@@ -129,21 +125,37 @@ __global__ void __launch_bounds__(NW * 32, (TWOL <= 8) ? 4 : 1) k_utot_rc(FwdArg
                 if (rr >= 1e-8f) {
                     float sf, dsf;
                     cutoff_fn<float>(A.prm.cutoff_id, rr, A.rc32, sf, dsf);
-                    wsf = (float)A.w_nb[A.img_j[m]] * sf;
+                    wsf0 = (float)A.w_nb[A.img_j[m]] * sf;
                 } else {
                     x = 1.f;
                     y = z = 0.f;
                 }
             }
-            const float r = sqrtf(x * x + y * y + z * z);
-            CK<float> ck;
-            make_ck<float, false>(x, y, z, r, A.psi_fac * r, ck);
-            float ur[W], ui[W], dr[3][W], di[3][W];
+            CK<float> ck0;
+            {
+                const float r = sqrtf(x * x + y * y + z * z);
+                make_ck<float, false>(x, y, z, r, A.psi_fac * r, ck0);
+            }
+            const int nimg = min(32, m1 - base);
+            for (int sub = 0; sub < nimg; sub += RC::IPW) {
+                // lane (grp, mb) takes image sub + grp; lanes past the images take a zero weight
+                const int src = sub + grp;
+                const bool ok = grp < RC::IPW && src < nimg;
+                const int sl = ok ? src : 0;
+                CK<float> ck;
+                ck.ca.re = __shfl_sync(0xffffffffu, ck0.ca.re, sl);
+                ck.ca.im = __shfl_sync(0xffffffffu, ck0.ca.im, sl);
+                ck.cb.re = __shfl_sync(0xffffffffu, ck0.cb.re, sl);
+                ck.cb.im = __shfl_sync(0xffffffffu, ck0.cb.im, sl);
+                float wsf = __shfl_sync(0xffffffffu, wsf0, sl);
+                if (!ok) wsf = 0.f;
+                float ur[W], ui[W], dr[3][W], di[3][W];
 #pragma unroll
-            for (int q = 0; q < W; ++q) ur[q] = ui[q] = 0.f;
-            ur[0] = 1.f;
-            if (mb == 0) accr[0] += wsf;
-            RcUtot<TWOL, 1>::run(mb, ck, wsf, ur, ui, dr, di, accr, acci);
+                for (int q = 0; q < W; ++q) ur[q] = ui[q] = 0.f;
+                ur[0] = 1.f;
+                if (mb == 0) accr[0] += wsf;
+                RcUtot<TWOL, 1>::run(mb, ck, wsf, ur, ui, dr, di, accr, acci);
+            }
         }
     }
     float *sw = ut_smem + (size_t)wid * 32 * 2 * NACC;
