@@ -504,6 +504,7 @@ template <int TWOL, int NT>
 __global__ void __launch_bounds__(NT, (TWOL <= 8) ? 2 : 1) k_deidrj_rev(DArgs A, int64_t nimg) {
     using RC = RowChain<TWOL>;
     constexpr int W = TWOL + 1;
+    constexpr int NIT = 32 / RC::IPW, PASS = NIT * RC::IPW;  // images per warp: one per lane
     extern __shared__ __align__(16) float2 rv_smem[];  // [acc_block(TWOL + 1)][NT]
     float2 *st = rv_smem + threadIdx.x;
     const int lane = threadIdx.x & 31;
@@ -514,22 +515,21 @@ __global__ void __launch_bounds__(NT, (TWOL <= 8) ? 2 : 1) k_deidrj_rev(DArgs A,
     // the end leave at once (uniform over the warp; there is no block barrier)
     const int64_t mbase = __ldg(A.img_ptr);
     const int64_t mtot = min(nimg, (int64_t)__ldg(A.img_ptr + A.natoms) - mbase);
-    if (wg * RC::IPW >= mtot) return;
-    const int64_t m = mbase + wg * RC::IPW + grp;
-    const bool valid = (grp < RC::IPW) && (m - mbase < mtot);
+    const int64_t p0 = wg * PASS;  // this warp's first image, relative to mbase
+    if (p0 >= mtot) return;
+    // one pass over the warp's images, one per lane: vector, weight, centre, the Cayley-Klein
+    // parameters with their derivatives and the cutoff; the recursion iterations below take
+    // their images' parameters by shuffles and hand the sums back to the owning lane
+    const int64_t mo = mbase + p0 + lane;
+    const bool own = lane < PASS && (p0 + lane < mtot);
     float x = 1.f, y = 0.f, z = 0.f, wj = 0.f;
     int centre = 0;
-    if (valid) {
-        x = (float)A.img_r[3 * m];
-        y = (float)A.img_r[3 * m + 1];
-        z = (float)A.img_r[3 * m + 2];
-        wj = (float)A.w_nb[A.img_j[m]];
-        centre = centre_of(A.img_ptr, A.natoms, (int)m, (int)mbase, mtot);
-        // the backward sweep reads this centre's Y level by level, one 128-byte line per
-        // level: ask for all of its lines now, so the forward sweep hides their latency
-        const char *yb = reinterpret_cast<const char *>(A.Y + (size_t)centre * A.nh);
-        const int nlines = (A.nh * (int)sizeof(float2) + 127) / 128;
-        for (int l = mb; l < nlines; l += RC::NCH) asm volatile("prefetch.global.L1 [%0];" ::"l"(yb + 128 * l));
+    if (own) {
+        x = (float)A.img_r[3 * mo];
+        y = (float)A.img_r[3 * mo + 1];
+        z = (float)A.img_r[3 * mo + 2];
+        wj = (float)A.w_nb[A.img_j[mo]];
+        centre = centre_of(A.img_ptr, A.natoms, (int)mo, (int)mbase, mtot);
     }
     float r = sqrtf(x * x + y * y + z * z);
     const bool skip = !(r >= 1e-8f);  // SO4.py:1441 skips r < 1e-8
@@ -538,49 +538,72 @@ __global__ void __launch_bounds__(NT, (TWOL <= 8) ? 2 : 1) k_deidrj_rev(DArgs A,
         y = z = 0.f;
         r = 1.f;
     }
-    CK<float> ck;
-    make_ck<float, true>(x, y, z, r, A.psi_fac * r, ck);
-    float ur[W], ui[W];
-#pragma unroll
-    for (int q = 0; q < W; ++q) ur[q] = ui[q] = 0.f;
-    ur[0] = 1.f;
-    st[0] = make_float2(1.f, 0.f);  // level 0
-    RvFwd<TWOL, 1, NT>::run(mb, ck, ur, ui, st);
-    // backward sweep; ur/ui reused as the adjoint carry
-#pragma unroll
-    for (int q = 0; q < W; ++q) ur[q] = ui[q] = 0.f;
-    const float2 *Y = A.Y + (size_t)centre * A.nh;
-    float su = 0.f, gar = 0.f, gai = 0.f, gbr = 0.f, gbi = 0.f;
-    RvBack<TWOL, TWOL, NT>::run(mb, ck, Y, st, ur, ui, su, gar, gai, gbr, gbi);
-    // sum the chains of each image into its mb == 0 lane
-    float tu = su, t0 = gar, t1 = gai, t2 = gbr, t3 = gbi;
-#pragma unroll
-    for (int k = 1; k < RC::NCH; ++k) {
-        const float a0 = __shfl_down_sync(0xffffffffu, su, k);
-        const float a1 = __shfl_down_sync(0xffffffffu, gar, k);
-        const float a2 = __shfl_down_sync(0xffffffffu, gai, k);
-        const float a3 = __shfl_down_sync(0xffffffffu, gbr, k);
-        const float a4 = __shfl_down_sync(0xffffffffu, gbi, k);
-        tu += a0;
-        t0 += a1;
-        t1 += a2;
-        t2 += a3;
-        t3 += a4;
-    }
-    if (valid && mb == 0) {
-        float sf, dsf;
-        cutoff_fn<float>(A.prm.cutoff_id, r, A.rc32, sf, dsf);
-        const float xr[3] = {x / r, y / r, z / r};
-        float gv[3];
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            // d f / d r_c = Re(conj(G_ca) d conj(a)/dr_c) + Re(conj(G_cb) d conj(b)/dr_c)
-            const float sc = t0 * ck.cda[c].re + t1 * ck.cda[c].im + t2 * ck.cdb[c].re + t3 * ck.cdb[c].im;
-            gv[c] = skip ? 0.f : wj * (sf * sc + dsf * xr[c] * tu);
+    CK<float> ck0;
+    make_ck<float, true>(x, y, z, r, A.psi_fac * r, ck0);
+    const int nit = (int)min((int64_t)NIT, (mtot - p0 + RC::IPW - 1) / RC::IPW);
+    for (int it = 0; it < nit; ++it) {
+        const int src = it * RC::IPW + grp;  // owning lane of this lane's image
+        const bool valid = grp < RC::IPW && p0 + src < mtot;
+        const int sl = valid ? src : 0;
+        CK<float> ck;
+        ck.ca.re = __shfl_sync(0xffffffffu, ck0.ca.re, sl);
+        ck.ca.im = __shfl_sync(0xffffffffu, ck0.ca.im, sl);
+        ck.cb.re = __shfl_sync(0xffffffffu, ck0.cb.re, sl);
+        ck.cb.im = __shfl_sync(0xffffffffu, ck0.cb.im, sl);
+        const int c_it = __shfl_sync(0xffffffffu, centre, sl);
+        if (valid) {
+            // the backward sweep reads this centre's Y level by level, one 128-byte line per
+            // level: ask for all of its lines now, so the forward sweep hides their latency
+            const char *yb = reinterpret_cast<const char *>(A.Y + (size_t)c_it * A.nh);
+            const int nlines = (A.nh * (int)sizeof(float2) + 127) / 128;
+            for (int l = mb; l < nlines; l += RC::NCH) asm volatile("prefetch.global.L1 [%0];" ::"l"(yb + 128 * l));
         }
-        A.g[3 * m] = gv[0];
-        A.g[3 * m + 1] = gv[1];
-        A.g[3 * m + 2] = gv[2];
+        float ur[W], ui[W];
+#pragma unroll
+        for (int q = 0; q < W; ++q) ur[q] = ui[q] = 0.f;
+        ur[0] = 1.f;
+        st[0] = make_float2(1.f, 0.f);  // level 0
+        RvFwd<TWOL, 1, NT>::run(mb, ck, ur, ui, st);
+        // backward sweep; ur/ui reused as the adjoint carry
+#pragma unroll
+        for (int q = 0; q < W; ++q) ur[q] = ui[q] = 0.f;
+        const float2 *Y = A.Y + (size_t)c_it * A.nh;
+        float su = 0.f, gar = 0.f, gai = 0.f, gbr = 0.f, gbi = 0.f;
+        RvBack<TWOL, TWOL, NT>::run(mb, ck, Y, st, ur, ui, su, gar, gai, gbr, gbi);
+        // sum the chains of each image into its mb == 0 lane
+        float tu = su, t0 = gar, t1 = gai, t2 = gbr, t3 = gbi;
+#pragma unroll
+        for (int k = 1; k < RC::NCH; ++k) {
+            tu += __shfl_down_sync(0xffffffffu, su, k);
+            t0 += __shfl_down_sync(0xffffffffu, gar, k);
+            t1 += __shfl_down_sync(0xffffffffu, gai, k);
+            t2 += __shfl_down_sync(0xffffffffu, gbr, k);
+            t3 += __shfl_down_sync(0xffffffffu, gbi, k);
+        }
+        // the owning lanes of this iteration's images take the sums of their mb == 0 lane
+        const int ol = lane - it * RC::IPW;
+        const bool mine = own && ol >= 0 && ol < RC::IPW;
+        const int from = mine ? ol * RC::NCH : 0;
+        tu = __shfl_sync(0xffffffffu, tu, from);
+        t0 = __shfl_sync(0xffffffffu, t0, from);
+        t1 = __shfl_sync(0xffffffffu, t1, from);
+        t2 = __shfl_sync(0xffffffffu, t2, from);
+        t3 = __shfl_sync(0xffffffffu, t3, from);
+        if (mine) {
+            float sf, dsf;
+            cutoff_fn<float>(A.prm.cutoff_id, r, A.rc32, sf, dsf);
+            const float xr[3] = {x / r, y / r, z / r};
+            float gv[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                // d f / d r_c = Re(conj(G_ca) d conj(a)/dr_c) + Re(conj(G_cb) d conj(b)/dr_c)
+                const float sc = t0 * ck0.cda[c].re + t1 * ck0.cda[c].im + t2 * ck0.cdb[c].re + t3 * ck0.cdb[c].im;
+                gv[c] = skip ? 0.f : wj * (sf * sc + dsf * xr[c] * tu);
+            }
+            A.g[3 * mo] = gv[0];
+            A.g[3 * mo + 1] = gv[1];
+            A.g[3 * mo + 2] = gv[2];
+        }
     }
 }
 
@@ -592,7 +615,8 @@ int launch_deidrj_rev(const DArgs &D, int64_t nimg, cudaStream_t st) {
     const size_t smem = sizeof(float2) * (size_t)acc_block(TWOL + 1) * NT;
     const int rc = so4_set_smem((const void *)k_deidrj_rev<TWOL, NT>, smem);
     if (rc) return rc;
-    const int64_t warps = (nimg + RC::IPW - 1) / RC::IPW;
+    constexpr int PASS = (32 / RC::IPW) * RC::IPW;  // images per warp (k_deidrj_rev)
+    const int64_t warps = (nimg + PASS - 1) / PASS;
     const int64_t blocks = (warps + NT / 32 - 1) / (NT / 32);
     k_deidrj_rev<TWOL, NT><<<(unsigned)blocks, NT, smem, st>>>(D, nimg);
     so4_count_launch();
