@@ -55,17 +55,14 @@ __global__ void __launch_bounds__(NW * 32, (TWOL <= 6) ? 4 : ((TWOL == 8) ? 3 : 
             const int s = A.astruct[a];
             for (int q = 0; q < 9; ++q) G[q] = (float)A.G[9 * s + q];
         }
-        for (int base = m0; base < m1; base += RC::IPW) {
-            const int m = base + grp;
-            // the next iteration's image vector and neighbour index into L1 (no registers held)
-            const int mn = m + RC::IPW;
-            if (grp < RC::IPW && mn < m1) {
-                asm volatile("prefetch.global.L1 [%0];" ::"l"(A.img_r + 3 * mn));
-                asm volatile("prefetch.global.L1 [%0];" ::"l"(A.img_j + mn));
-            }
-            float x = 1.f, y = 0.f, z = 0.f, a_du = 0.f, a_d = 0.f;
+        // per-image setup (vector, weight, tangent, Cayley-Klein parameters and their
+        // derivative along the tangent) for up to 32 images at once, one per lane; each
+        // recursion iteration takes its IPW images' values by shuffles
+        for (int base = m0; base < m1; base += 32) {
+            const int m = base + lane;
+            float x = 1.f, y = 0.f, z = 0.f, a_du0 = 0.f, a_d0 = 0.f;
             float d[3] = {0.f, 0.f, 0.f};
-            if (grp < RC::IPW && m < m1) {
+            if (m < m1) {
                 x = (float)A.img_r[3 * m];
                 y = (float)A.img_r[3 * m + 1];
                 z = (float)A.img_r[3 * m + 2];
@@ -81,35 +78,51 @@ __global__ void __launch_bounds__(NW * 32, (TWOL <= 6) ? 4 : ((TWOL == 8) ? 3 : 
                     float sf, dsf;
                     cutoff_fn<float>(A.cutoff_id, rr, A.rc32, sf, dsf);
                     const float w = (float)A.w_nb[j];
-                    a_du = w * dsf * (x * d[0] + y * d[1] + z * d[2]) / rr;
-                    a_d = w * sf;
+                    a_du0 = w * dsf * (x * d[0] + y * d[1] + z * d[2]) / rr;
+                    a_d0 = w * sf;
                 } else {
                     x = 1.f;
                     y = z = 0.f;
                 }
             }
-            const float r = sqrtf(x * x + y * y + z * z);
-            CK<float> ck;
-            make_ck<float, true>(x, y, z, r, A.psi_fac * r, ck);
-            // the derivative of conj(a), conj(b) along dr_m, in slot 0
+            CK<float> ck0;
             {
-                cx<float> da = mk<float>(0.f, 0.f), db = mk<float>(0.f, 0.f);
-#pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    da.re += d[c] * ck.cda[c].re;
-                    da.im += d[c] * ck.cda[c].im;
-                    db.re += d[c] * ck.cdb[c].re;
-                    db.im += d[c] * ck.cdb[c].im;
-                }
-                ck.cda[0] = da;
-                ck.cdb[0] = db;
+                const float r = sqrtf(x * x + y * y + z * z);
+                make_ck<float, true>(x, y, z, r, A.psi_fac * r, ck0);
             }
-            float ur[W], ui[W], dr[1][W], di[1][W];
+            // the derivative of conj(a), conj(b) along dr_m
+            cx<float> da0 = mk<float>(0.f, 0.f), db0 = mk<float>(0.f, 0.f);
 #pragma unroll
-            for (int q = 0; q < W; ++q) ur[q] = ui[q] = dr[0][q] = di[0][q] = 0.f;
-            ur[0] = 1.f;
-            if (mb == 0) accr[0] += a_du;  // level 0: U = 1, dU = 0
-            RcJvp<TWOL, 1>::run(mb, ck, a_du, a_d, ur, ui, dr, di, accr, acci);
+            for (int c = 0; c < 3; ++c) {
+                da0.re += d[c] * ck0.cda[c].re;
+                da0.im += d[c] * ck0.cda[c].im;
+                db0.re += d[c] * ck0.cdb[c].re;
+                db0.im += d[c] * ck0.cdb[c].im;
+            }
+            const int nimg = min(32, m1 - base);
+            for (int sub = 0; sub < nimg; sub += RC::IPW) {
+                const int src = sub + grp;
+                const bool ok = grp < RC::IPW && src < nimg;
+                const int sl = ok ? src : 0;
+                CK<float> ck;  // slot 0 of the derivatives holds the one direction
+                ck.ca.re = __shfl_sync(0xffffffffu, ck0.ca.re, sl);
+                ck.ca.im = __shfl_sync(0xffffffffu, ck0.ca.im, sl);
+                ck.cb.re = __shfl_sync(0xffffffffu, ck0.cb.re, sl);
+                ck.cb.im = __shfl_sync(0xffffffffu, ck0.cb.im, sl);
+                ck.cda[0].re = __shfl_sync(0xffffffffu, da0.re, sl);
+                ck.cda[0].im = __shfl_sync(0xffffffffu, da0.im, sl);
+                ck.cdb[0].re = __shfl_sync(0xffffffffu, db0.re, sl);
+                ck.cdb[0].im = __shfl_sync(0xffffffffu, db0.im, sl);
+                float a_du = __shfl_sync(0xffffffffu, a_du0, sl);
+                float a_d = __shfl_sync(0xffffffffu, a_d0, sl);
+                if (!ok) a_du = a_d = 0.f;
+                float ur[W], ui[W], dr[1][W], di[1][W];
+#pragma unroll
+                for (int q = 0; q < W; ++q) ur[q] = ui[q] = dr[0][q] = di[0][q] = 0.f;
+                ur[0] = 1.f;
+                if (mb == 0) accr[0] += a_du;  // level 0: U = 1, dU = 0
+                RcJvp<TWOL, 1>::run(mb, ck, a_du, a_d, ur, ui, dr, di, accr, acci);
+            }
         }
     }
     float *sw = jv_smem + (size_t)wid * 32 * 2 * NACC;
