@@ -157,6 +157,31 @@ int so4_nl_sort(const so4_geom *d_geom, int nstruct, int nbins, const double *d_
                 int32_t *d_img_off, double *d_img_r, int32_t *d_pair_ptr, void *d_work, size_t work_bytes,
                 void *stream);
 
+/* The same one-pass list in parts, so that a graph can run the list of one range of
+ * centres while another range already computes (so4_nl_count_keys = bins, then the key
+ * pass and the scan of [0, natoms)):
+ *   so4_nl_bins              bins every atom and clears the status;
+ *   so4_nl_count_keys_range  counts and keys of the centres [a0, a1) into their slots;
+ *   so4_nl_scan_range        d_img_ptr[a0 .. a1] = d_img_ptr[a0] (0 when a0 = 0) + the exclusive
+ *                            scan of those counts: ranges are scanned in order, each after the
+ *                            previous one's scan;
+ *   so4_nl_sort_range        so4_nl_sort for the centres [a0, a1) without the pair counts, and,
+ *                            if any capacity was exceeded so far, empties d_img_ptr[a0 .. a1]
+ *                            so that work enqueued behind it on the range reads nothing out of
+ *                            bounds.
+ * The lite reverse pass (so4_nl_pairs with NULL pair arrays) and so4_nl_summary run after
+ * every range is sorted. */
+int so4_nl_bins(const so4_geom *d_geom, int nstruct, int nbins, const double *d_pos, const int *d_atom_struct,
+                int natoms, int slot_cap, void *d_work, size_t work_bytes, void *stream);
+int so4_nl_count_keys_range(const so4_geom *d_geom, int nstruct, int nbins, const double *d_pos,
+                            const int *d_atom_struct, int natoms, double rcut, int slot_cap, int a0, int a1,
+                            void *d_work, size_t work_bytes, void *stream);
+int so4_nl_scan_range(int natoms, int nbins, int slot_cap, int a0, int a1, int32_t *d_img_ptr, void *d_work,
+                      size_t work_bytes, void *stream);
+int so4_nl_sort_range(const so4_geom *d_geom, int nstruct, int nbins, const double *d_pos, const int *d_atom_struct,
+                      int natoms, int a0, int a1, int32_t *d_img_ptr, int64_t nimg, int slot_cap, int32_t *d_img_j,
+                      int32_t *d_img_off, double *d_img_r, void *d_work, size_t work_bytes, void *stream);
+
 /* {total images, total pairs, status bits} after the three passes (d_pair_ptr may
  * be NULL after pass 1 only), written to ((int *)d_work)[4..6]; with h_summary
  * non-NULL also copied there by one synchronising read.  With h_summary NULL the

@@ -89,6 +89,10 @@ def lib():
         "so4_status_read": (_i, [_vp, _sz, _vp, C.POINTER(_i)]),
         "so4_nl_count_keys": (_i, [_vp, _i, _i, _vp, _vp, _i, _d, _i, _vp, _vp, _sz, _vp]),
         "so4_nl_sort": (_i, [_vp, _i, _i, _vp, _vp, _i, _vp, _i64, _i, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
+        "so4_nl_bins": (_i, [_vp, _i, _i, _vp, _vp, _i, _i, _vp, _sz, _vp]),
+        "so4_nl_count_keys_range": (_i, [_vp, _i, _i, _vp, _vp, _i, _d, _i, _i, _i, _vp, _sz, _vp]),
+        "so4_nl_scan_range": (_i, [_i, _i, _i, _i, _i, _vp, _vp, _sz, _vp]),
+        "so4_nl_sort_range": (_i, [_vp, _i, _i, _vp, _vp, _i, _i, _i, _vp, _i64, _i, _vp, _vp, _vp, _vp, _sz, _vp]),
         "so4_nl_summary": (_i, [_vp, _vp, _i, _vp, _sz, _vp, C.POINTER(_i)]),
         "so4_plain_workspace_size": (_sz, [_vp, _i]),
         "so4_plain": (_i, [_vp, C.POINTER(Params), _i, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,

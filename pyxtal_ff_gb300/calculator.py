@@ -280,11 +280,11 @@ class CapturedStep:
 
     def _enqueue(self):
         lay, calc, tab, L = self.layout, self.calc, self.calc.tables, engine.lib()
-        engine.enqueue_neighbors(lay, self.pos, self.nl, lite=True)
         b = self.nl
         _p = engine._ptr
         check = engine.check
         if self.branches == 1:
+            engine.enqueue_neighbors(lay, self.pos, b, lite=True)
             check(L.so4_adjoint_linear32(tab.handle, C.byref(calc.params), lay.nstruct, _p(lay.atom_struct),
                                          _p(lay.atom_ptr_dev), lay.natoms, _p(calc._w_nb), _p(calc._w_site),
                                          _p(b.img_ptr), _p(b.img_j), _p(b.img_r), _p(b.img_rev), self.cap_m,
@@ -292,13 +292,33 @@ class CapturedStep:
                                          _p(self.energy_sum), _p(self.ws), self.ws.numel(), engine._stream()),
                   "so4_adjoint_linear32")
         else:
+            # the list itself runs per branch: bins for all atoms, then each branch counts and
+            # sorts its own centres (their scans chained in branch order) and goes on to its
+            # compute while the other branches' lists are still being built; the reverse images
+            # (read only by the gather) and the summary follow the join
+            N, S_, G = lay.natoms, lay.nstruct, lay.nbins
+            check(L.so4_nl_bins(_p(lay.geom), S_, G, _p(self.pos), _p(lay.atom_struct), N, b.slot_cap, _p(b.ws),
+                                b.ws.numel(), engine._stream()), "so4_nl_bins")
             main = torch.cuda.current_stream()
             for sd in self.sides:
                 sd.wait_stream(main)
+            scanned = None
             for (a0, a1), bc, st in zip(self.chunks, self.bc, [main] + self.sides):
                 with torch.cuda.stream(st):
                     s_ = engine._stream()
                     n = a1 - a0
+                    check(L.so4_nl_count_keys_range(_p(lay.geom), S_, G, _p(self.pos), _p(lay.atom_struct), N,
+                                                    lay.rcut, b.slot_cap, a0, a1, _p(b.ws), b.ws.numel(), s_),
+                          "so4_nl_count_keys_range")
+                    if scanned is not None:
+                        st.wait_event(scanned)
+                    check(L.so4_nl_scan_range(N, G, b.slot_cap, a0, a1, _p(b.img_ptr), _p(b.ws), b.ws.numel(), s_),
+                          "so4_nl_scan_range")
+                    scanned = torch.cuda.Event()
+                    scanned.record(st)
+                    check(L.so4_nl_sort_range(_p(lay.geom), S_, G, _p(self.pos), _p(lay.atom_struct), N, a0, a1,
+                                              _p(b.img_ptr), b.cap_m, b.slot_cap, _p(b.img_j), _p(b.img_off),
+                                              _p(b.img_r), _p(b.ws), b.ws.numel(), s_), "so4_nl_sort_range")
                     check(L.so4_utot32(tab.handle, C.byref(calc.params), n, _p(calc._w_nb), _p(calc._w_site[a0:a1]),
                                        _p(b.img_ptr[a0:a1 + 1]), _p(b.img_j), _p(b.img_r), _p(self.utot[a0:a1]),
                                        s_), "so4_utot32")
@@ -310,6 +330,11 @@ class CapturedStep:
                                                  _p(self.ybuf[a0:a1]), _p(self.g), s_), "so4_adjoint_deidrj32")
             for sd in self.sides:
                 main.wait_stream(sd)
+            check(L.so4_nl_pairs(_p(lay.geom), S_, _p(lay.atom_struct), N, _p(b.img_ptr), b.cap_m, _p(b.img_j),
+                                 _p(b.img_off), _p(None), b.cap_p, _p(None), _p(None), _p(None), _p(None),
+                                 _p(b.img_rev), _p(b.ws), b.ws.numel(), engine._stream()), "so4_nl_pairs")
+            check(L.so4_nl_summary(_p(b.img_ptr), _p(None), N, _p(b.ws), b.ws.numel(), engine._stream(), None),
+                  "so4_nl_summary")
             check(L.so4_adjoint_gather(lay.natoms, lay.nstruct, _p(lay.atom_ptr_dev), _p(b.img_ptr), _p(b.img_rev),
                                        _p(b.img_r), _p(self.g), _p(self.eatom), _p(self.part), _p(self.forces),
                                        _p(self.virial), _p(self.energy_sum), engine._stream()), "so4_adjoint_gather")

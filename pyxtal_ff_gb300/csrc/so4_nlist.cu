@@ -131,22 +131,27 @@ __global__ void k_bin_fill(const int *astruct, int natoms, NLWork w) {
     w.bin_atoms[w.bin_start[bin] + slot] = a;
 }
 
-// single-CTA exclusive scan: out[0..n] from in[0..n-1].  Chunks of 4096 values
-// (four per thread, coalesced), warp-shuffle scans inside, a running carry across chunks.
-__global__ void __launch_bounds__(1024) k_scan(const int *in, int *out, int n) {
+// single-CTA exclusive scan: out[0..n] from in[0..n-1].  Each pass covers SCAN_PER x 1024
+// values, thread t a contiguous run of SCAN_PER of them, all loaded before any is used (one
+// memory latency per pass); warp-shuffle scans of the run totals, a running carry across
+// passes.
+// With chained != 0 the scan continues a previous one: out[0] already holds the running
+// total before in[0], and it is kept (ranges of centres scanned one after another).
+constexpr int SCAN_PER = 32;
+__global__ void __launch_bounds__(1024) k_scan(const int *in, int *out, int n, int chained = 0) {
     __shared__ int wsum[32];
     __shared__ int carry_s;
     const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
-    if (t == 0) carry_s = 0;
+    if (t == 0) carry_s = chained ? out[0] : 0;
     __syncthreads();
-    for (int base = 0; base < n; base += 4096) {
-        int v[4];
+    for (int base = 0; base < n; base += SCAN_PER * 1024) {
+        const int i0 = base + SCAN_PER * t;
+        int v[SCAN_PER];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const int i = base + 4 * t + q;
-            v[q] = (i < n) ? in[i] : 0;
-        }
-        const int tot = v[0] + v[1] + v[2] + v[3];
+        for (int q = 0; q < SCAN_PER; ++q) v[q] = (i0 + q < n) ? __ldg(in + i0 + q) : 0;
+        int tot = 0;
+#pragma unroll
+        for (int q = 0; q < SCAN_PER; ++q) tot += v[q];
         int inc = tot;
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
@@ -168,9 +173,8 @@ __global__ void __launch_bounds__(1024) k_scan(const int *in, int *out, int n) {
         __syncthreads();
         int run = carry_s + wsum[wid] + inc - tot;
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const int i = base + 4 * t + q;
-            if (i < n) out[i] = run;
+        for (int q = 0; q < SCAN_PER; ++q) {
+            if (i0 + q < n) out[i0 + q] = run;
             run += v[q];
         }
         __syncthreads();
@@ -204,6 +208,14 @@ __global__ void k_clamp(int32_t *img_ptr, int32_t *pair_ptr, int natoms, const i
     if (pair_ptr) pair_ptr[i] = 0;
 }
 
+// The range form of k_clamp: after a range's sort, if any capacity was exceeded so far,
+// empty the range's image ranges (img_ptr[a0 .. a1]) before work on them is enqueued.
+__global__ void k_clamp_range(int32_t *img_ptr, int a0, int a1, const int *status) {
+    const int i = a0 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (i > a1 || !(*(volatile const int *)status & (1 << SO4_ERR_CAPACITY))) return;
+    img_ptr[i] = 0;
+}
+
 // One warp per centre.  MODE 0: count images into w.cnt.  MODE 1: write the
 // packed (j, o) keys into w.keys[img_ptr[a] ...] (unsorted; slots are taken with
 // a shared-memory counter, the order is fixed later by k_sort).
@@ -215,10 +227,11 @@ __global__ void k_clamp(int32_t *img_ptr, int32_t *pair_ptr, int natoms, const i
 // (1/64 of the FP32 rate on this GPU) is almost never issued.
 template <int MODE>
 __global__ void k_scan_images(const so4_geom *geom, const double *pos, const int *astruct, int natoms,
-                              double rcut, const int32_t *img_ptr, NLWork w) {
+                              double rcut, const int32_t *img_ptr, NLWork w, int a0 = 0) {
+    // centres a0 .. natoms - 1 (a range of the list when a0 > 0)
     __shared__ int s_cnt[8];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const int a = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int a = a0 + (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     if (MODE >= 1 && lane == 0) s_cnt[wib] = 0;
     __syncwarp();
     if (a >= natoms) return;
@@ -309,9 +322,11 @@ __global__ void k_scan_images(const so4_geom *geom, const double *pos, const int
 
 // One warp per centre: rank-sort the keys, write the sorted images and count pairs.
 __global__ void k_sort(const so4_geom *geom, const double *pos, const int *astruct, int natoms,
-                       const int32_t *img_ptr, int32_t *img_j, int32_t *img_off, double *img_r, NLWork w) {
+                       const int32_t *img_ptr, int32_t *img_j, int32_t *img_off, double *img_r, NLWork w,
+                       int a0 = 0) {
+    // centres a0 .. natoms - 1
     const int lane = threadIdx.x & 31;
-    const int a = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int a = a0 + (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     if (a >= natoms) return;
     const so4_geom &g = geom[astruct[a]];
     const int p0 = img_ptr[a], p1 = img_ptr[a + 1];
@@ -603,24 +618,25 @@ extern "C" int so4_nl_fill(const so4_geom *d_geom, int nstruct, int nbins, const
     return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
 }
 
-extern "C" int so4_nl_count_keys(const so4_geom *d_geom, int nstruct, int nbins, const double *d_pos,
-                                 const int *d_astruct, int natoms, double rcut, int slot_cap, int32_t *d_img_ptr,
-                                 void *d_work, size_t work_bytes, void *stream) {
-    if (natoms < 0 || nstruct < 0 || nbins < 0 || slot_cap <= 0 || !d_work) return SO4_ERR_ARG;
+static int one_pass_work(NLWork &w, int natoms, int nbins, int slot_cap, void *d_work, size_t work_bytes) {
     const int64_t nkeys = (int64_t)natoms * slot_cap;
-    NLWork w;
     if (carve(w, nullptr, natoms, nbins, nkeys) > work_bytes) return SO4_ERR_WORKSPACE;
     carve(w, d_work, natoms, nbins, nkeys);
     w.cap_img = 0;
     w.cap_pair = 0;
     w.slot_cap = slot_cap;
+    return SO4_OK;
+}
+
+extern "C" int so4_nl_bins(const so4_geom *d_geom, int nstruct, int nbins, const double *d_pos, const int *d_astruct,
+                           int natoms, int slot_cap, void *d_work, size_t work_bytes, void *stream) {
+    if (natoms < 0 || nstruct < 0 || nbins < 0 || slot_cap <= 0 || !d_work) return SO4_ERR_ARG;
+    NLWork w;
+    int rc = one_pass_work(w, natoms, nbins, slot_cap, d_work, work_bytes);
+    if (rc) return rc;
     cudaStream_t st = (cudaStream_t)stream;
     SO4_CUDA_TRY(cudaMemsetAsync(w.status, 0, 9 * sizeof(int), st));  // status, summary, largest count
-    if (natoms == 0) {
-        k_set_int<<<1, 1, 0, st>>>(d_img_ptr, 0);
-        so4_count_launch();
-        return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
-    }
+    if (natoms == 0) return SO4_OK;
     SO4_CUDA_TRY(cudaMemsetAsync(w.bin_cnt, 0, sizeof(int) * (nbins + 1), st));
     SO4_CUDA_TRY(cudaMemsetAsync(w.bin_cur, 0, sizeof(int) * (nbins + 1), st));
     const int tb = 256;
@@ -630,11 +646,74 @@ extern "C" int so4_nl_count_keys(const so4_geom *d_geom, int nstruct, int nbins,
     so4_count_launch();
     k_bin_fill<<<(natoms + tb - 1) / tb, tb, 0, st>>>(d_astruct, natoms, w);
     so4_count_launch();
+    return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
+}
+
+extern "C" int so4_nl_count_keys_range(const so4_geom *d_geom, int nstruct, int nbins, const double *d_pos,
+                                       const int *d_astruct, int natoms, double rcut, int slot_cap, int a0, int a1,
+                                       void *d_work, size_t work_bytes, void *stream) {
+    if (natoms < 0 || nstruct < 0 || nbins < 0 || slot_cap <= 0 || !d_work) return SO4_ERR_ARG;
+    if (a0 < 0 || a1 < a0 || a1 > natoms) return SO4_ERR_ARG;
+    NLWork w;
+    int rc = one_pass_work(w, natoms, nbins, slot_cap, d_work, work_bytes);
+    if (rc) return rc;
+    if (a1 == a0) return SO4_OK;
     const int warps = 8;
-    k_scan_images<2><<<(natoms + warps - 1) / warps, 32 * warps, 0, st>>>(d_geom, d_pos, d_astruct, natoms, rcut,
-                                                                          nullptr, w);
+    k_scan_images<2><<<(a1 - a0 + warps - 1) / warps, 32 * warps, 0, (cudaStream_t)stream>>>(
+        d_geom, d_pos, d_astruct, a1, rcut, nullptr, w, a0);
     so4_count_launch();
-    k_scan<<<1, 1024, 0, st>>>(w.cnt, d_img_ptr, natoms);
+    return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
+}
+
+extern "C" int so4_nl_scan_range(int natoms, int nbins, int slot_cap, int a0, int a1, int32_t *d_img_ptr,
+                                 void *d_work, size_t work_bytes, void *stream) {
+    if (natoms < 0 || nbins < 0 || slot_cap <= 0 || !d_work || !d_img_ptr) return SO4_ERR_ARG;
+    if (a0 < 0 || a1 < a0 || a1 > natoms) return SO4_ERR_ARG;
+    NLWork w;
+    int rc = one_pass_work(w, natoms, nbins, slot_cap, d_work, work_bytes);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (a1 == a0) {
+        if (a0 == 0) {
+            k_set_int<<<1, 1, 0, st>>>(d_img_ptr, 0);
+            so4_count_launch();
+        }
+        return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
+    }
+    k_scan<<<1, 1024, 0, st>>>(w.cnt + a0, d_img_ptr + a0, a1 - a0, a0 > 0 ? 1 : 0);
+    so4_count_launch();
+    return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
+}
+
+extern "C" int so4_nl_count_keys(const so4_geom *d_geom, int nstruct, int nbins, const double *d_pos,
+                                 const int *d_astruct, int natoms, double rcut, int slot_cap, int32_t *d_img_ptr,
+                                 void *d_work, size_t work_bytes, void *stream) {
+    int rc = so4_nl_bins(d_geom, nstruct, nbins, d_pos, d_astruct, natoms, slot_cap, d_work, work_bytes, stream);
+    if (!rc) rc = so4_nl_count_keys_range(d_geom, nstruct, nbins, d_pos, d_astruct, natoms, rcut, slot_cap, 0, natoms,
+                                          d_work, work_bytes, stream);
+    if (!rc && d_img_ptr) rc = so4_nl_scan_range(natoms, nbins, slot_cap, 0, natoms, d_img_ptr, d_work, work_bytes, stream);
+    else if (!rc) rc = SO4_ERR_ARG;
+    return rc;
+}
+
+extern "C" int so4_nl_sort_range(const so4_geom *d_geom, int nstruct, int nbins, const double *d_pos,
+                                 const int *d_astruct, int natoms, int a0, int a1, int32_t *d_img_ptr, int64_t nimg,
+                                 int slot_cap, int32_t *d_img_j, int32_t *d_img_off, double *d_img_r, void *d_work,
+                                 size_t work_bytes, void *stream) {
+    if (natoms < 0 || nstruct < 0 || nimg < 0 || slot_cap <= 0 || !d_work || !d_img_ptr) return SO4_ERR_ARG;
+    if (a0 < 0 || a1 < a0 || a1 > natoms) return SO4_ERR_ARG;
+    if (nimg > 0x7fffffff) return SO4_ERR_CAPACITY;
+    NLWork w;
+    int rc = one_pass_work(w, natoms, nbins, slot_cap, d_work, work_bytes);
+    if (rc) return rc;
+    w.cap_img = nimg;
+    if (a1 == a0) return SO4_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int warps = 8;
+    k_sort<<<(a1 - a0 + warps - 1) / warps, 32 * warps, 0, st>>>(d_geom, d_pos, d_astruct, a1, d_img_ptr, d_img_j,
+                                                                 d_img_off, d_img_r, w, a0);
+    so4_count_launch();
+    k_clamp_range<<<(a1 - a0 + 1 + 255) / 256, 256, 0, st>>>(d_img_ptr, a0, a1, w.status);
     so4_count_launch();
     return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
 }

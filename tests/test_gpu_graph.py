@@ -86,6 +86,30 @@ def test_two_branch_graph_matches_eager_bitwise(cuda_device):
         _equal(res, res1)
 
 
+def test_two_branch_graph_reports_overflow(cuda_device):
+    # per-branch neighbour lists: an overflow in either range empties the ranges on the
+    # device, so the step reads nothing out of bounds and check() reports it
+    structs = [S.diamond_si(4, 4, 2, sigma=0.05, rng=np.random.default_rng(31))]  # 256 atoms: two branches
+    batch, calc, model = _setup(structs)
+    step = calc.capture(batch, model, headroom=1.0, branches=2)
+    assert step.branches == 2
+    step()
+    assert step.check()
+    ref = {k: v.clone() for k, v in step().items()}
+    pos = batch.positions.copy()
+    pos[:100] *= 0.6  # the first range gets far more neighbours than captured
+    step(pos)
+    assert not step.check()
+    pos = batch.positions.copy()
+    pos[150:] *= 0.6  # now the second
+    step(pos)
+    assert not step.check()
+    res = {k: v.clone() for k, v in step(batch.positions).items()}  # and back
+    torch.cuda.synchronize()
+    assert step.check()
+    _equal(res, ref)
+
+
 def test_lite_and_one_pass_neighbor_lists_match_full(cuda_device):
     from pyxtal_ff_gb300 import engine
     structs = [S.diamond_si(2, 2, 2, sigma=0.1, rng=np.random.default_rng(21)), S.sio2_random(n_si=8, seed=22)]
