@@ -131,27 +131,29 @@ __global__ void k_bin_fill(const int *astruct, int natoms, NLWork w) {
     w.bin_atoms[w.bin_start[bin] + slot] = a;
 }
 
-// single-CTA exclusive scan: out[0..n] from in[0..n-1].  Each pass covers SCAN_PER x 1024
-// values, thread t a contiguous run of SCAN_PER of them, all loaded before any is used (one
-// memory latency per pass); warp-shuffle scans of the run totals, a running carry across
-// passes.
-// With chained != 0 the scan continues a previous one: out[0] already holds the running
-// total before in[0], and it is kept (ranges of centres scanned one after another).
-constexpr int SCAN_PER = 32;
+// single-CTA exclusive scan: out[0..n] from in[0..n-1].  Chunks of 4096 values (four per
+// thread, coalesced), warp-shuffle scans inside, a running carry across chunks; the next
+// chunk's values are loaded before the current one is scanned.  With chained != 0 the scan
+// continues a previous one: out[0] already holds the running total before in[0] (ranges of
+// centres scanned one after another).
 __global__ void __launch_bounds__(1024) k_scan(const int *in, int *out, int n, int chained = 0) {
     __shared__ int wsum[32];
     __shared__ int carry_s;
     const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
     if (t == 0) carry_s = chained ? out[0] : 0;
+    int nv[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) nv[q] = (4 * t + q < n) ? __ldg(in + 4 * t + q) : 0;
     __syncthreads();
-    for (int base = 0; base < n; base += SCAN_PER * 1024) {
-        const int i0 = base + SCAN_PER * t;
-        int v[SCAN_PER];
+    for (int base = 0; base < n; base += 4096) {
+        int v[4];
 #pragma unroll
-        for (int q = 0; q < SCAN_PER; ++q) v[q] = (i0 + q < n) ? __ldg(in + i0 + q) : 0;
-        int tot = 0;
-#pragma unroll
-        for (int q = 0; q < SCAN_PER; ++q) tot += v[q];
+        for (int q = 0; q < 4; ++q) {
+            v[q] = nv[q];
+            const int i = base + 4096 + 4 * t + q;
+            nv[q] = (i < n) ? __ldg(in + i) : 0;
+        }
+        const int tot = v[0] + v[1] + v[2] + v[3];
         int inc = tot;
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
@@ -173,8 +175,9 @@ __global__ void __launch_bounds__(1024) k_scan(const int *in, int *out, int n, i
         __syncthreads();
         int run = carry_s + wsum[wid] + inc - tot;
 #pragma unroll
-        for (int q = 0; q < SCAN_PER; ++q) {
-            if (i0 + q < n) out[i0 + q] = run;
+        for (int q = 0; q < 4; ++q) {
+            const int i = base + 4 * t + q;
+            if (i < n) out[i] = run;
             run += v[q];
         }
         __syncthreads();
