@@ -406,17 +406,12 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
                     if (S <= 0) continue;
                     auto key = std::make_pair(bi, u.ma0);
                     if (!ca_off.count(key)) {
-                        // each coefficient stored twice, (c, c), the operand of a packed FP32
-                        // multiply; a row holds KH = ceil(K / 2) float4 (two pairs each)
                         ca_off[key] = (int)wca.size();
-                        const int KH = (K + 1) / 2;
                         for (int j = 0; j < S; ++j)
-                            for (int k = 0; k < 2 * KH; ++k) {
+                            for (int k = 0; k < KP; ++k) {
                                 const int ma = u.ma0 + k, ma2 = lo + j, ma1 = ma + d - ma2;
                                 const bool ok = k < K && ma <= lam && ma1 >= 0 && ma1 <= a;
-                                const float c = ok ? (float)cg_of(bk, ma1, ma2) : 0.f;
-                                wca.push_back(c);
-                                wca.push_back(c);
+                                wca.push_back(ok ? (float)cg_of(bk, ma1, ma2) : 0.f);
                             }
                     }
                     const int s0 = (int)wsub.size();

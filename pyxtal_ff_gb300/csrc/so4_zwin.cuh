@@ -25,15 +25,15 @@ __device__ __forceinline__ void zw_load_utot(const float2 *__restrict__ utot, co
 
 // One sub-segment {f1 | f2 << 16, Ca offset, steps S, bits of Cb}: adds
 // Cb sum_j Ca[j][k] U_a[f2 - j + k] U_b[f1 + j] to z[k] = (re, im), k < K, for this
-// lane's atom (offsets in Ub rows, pre-scaled by the pitch; Ul = Ub + lane).  Packed FP32
-// pairs (sm_100+): the ring keeps each U_a value w as (w.x, w.x) and (-w.y, w.y), so with
-// a = Cb U_b and as = (a.y, a.x) the complex product is (w.x, w.x) * a + (-w.y, w.y) * as,
-// and one more packed FMA adds Ca[j][k] times it: three packed instructions per
-// (step, entry).  Ca rows hold each coefficient as a pair (c, c), KH = ceil(K / 2) float4.
+// lane's atom (offsets in Ub rows, pre-scaled by the pitch; Ul = Ub + lane).  Ca rows
+// hold KP = K rounded up to 4 floats.  Packed FP32 pairs (sm_100+): the ring keeps each
+// U_a value w as (w.x, w.x) and (-w.y, w.y), so with a = Cb U_b and as = (a.y, a.x) the
+// complex product is (w.x, w.x) * a + (-w.y, w.y) * as, and one more packed FMA adds
+// Ca[j][k] times it: three packed instructions per (step, entry).
 template <int K>
 __device__ __forceinline__ void zw_rows(const float2 *Ul, const int4 hd, const float *__restrict__ ca,
                                         float2 (&z)[K]) {
-    constexpr int KH = (K + 1) / 2;  // float4 loads per Ca row (two coefficient pairs each)
+    constexpr int KQ = (K + 3) / 4;  // float4 loads per Ca row
     const int f1 = hd.x & 0xffff, f2 = (int)((unsigned)hd.x >> 16);
     const int S = hd.z;
     const float cb = __int_as_float(hd.w);
@@ -58,18 +58,20 @@ __device__ __forceinline__ void zw_rows(const float2 *Ul, const int4 hd, const f
                 WY[(K - t) % K] = make_float2(-w.y, w.y);
                 const float2 a = __fmul2_rn(Ul[f1 + j * ZL_PITCH], cb2);
                 const float2 as = make_float2(a.y, a.x);
-                float2 cp[2 * KH];
+                float cc[4 * KQ];
 #pragma unroll
-                for (int q = 0; q < KH; ++q) {
-                    const float4 c4 = cw[j * KH + q];  // shared memory or the read-only global table
-                    cp[2 * q] = make_float2(c4.x, c4.y);
-                    cp[2 * q + 1] = make_float2(c4.z, c4.w);
+                for (int q = 0; q < KQ; ++q) {
+                    const float4 c4 = cw[j * KQ + q];  // shared memory or the read-only global table
+                    cc[4 * q] = c4.x;
+                    cc[4 * q + 1] = c4.y;
+                    cc[4 * q + 2] = c4.z;
+                    cc[4 * q + 3] = c4.w;
                 }
 #pragma unroll
                 for (int k = 0; k < K; ++k) {
                     const int r = (k - t + K) % K;
                     const float2 p = __ffma2_rn(WY[r], as, __fmul2_rn(WX[r], a));
-                    z[k] = __ffma2_rn(cp[k], p, z[k]);
+                    z[k] = __ffma2_rn(make_float2(cc[k], cc[k]), p, z[k]);
                 }
             }
         }
