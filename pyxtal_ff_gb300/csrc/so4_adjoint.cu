@@ -378,8 +378,7 @@ __global__ void __launch_bounds__(ZW_THREADS, 2) k_zw32(ZLArgs A) {
             case 5: zw_unit<MODE, 5>(A, un, Ul, coef, ca, a, lane); break;
             case 6: zw_unit<MODE, 6>(A, un, Ul, coef, ca, a, lane); break;
             case 7: zw_unit<MODE, 7>(A, un, Ul, coef, ca, a, lane); break;
-            case 8: zw_unit<MODE, 8>(A, un, Ul, coef, ca, a, lane); break;
-            default: zw_unit<MODE, 9>(A, un, Ul, coef, ca, a, lane); break;
+            default: zw_unit<MODE, 8>(A, un, Ul, coef, ca, a, lane); break;
         }
     }
     if (MODE == 1) return;
