@@ -564,12 +564,16 @@ __global__ void __launch_bounds__(NT, (TWOL <= 8) ? 2 : 1) k_deidrj_rev(DArgs A,
         ur[0] = 1.f;
         st[0] = make_float2(1.f, 0.f);  // level 0
         RvFwd<TWOL, 1, NT>::run(mb, ck, ur, ui, st);
-        // backward sweep; ur/ui reused as the adjoint carry
+        // backward sweep (packed pairs), the adjoint carry in g
+        float2 g[W];
 #pragma unroll
-        for (int q = 0; q < W; ++q) ur[q] = ui[q] = 0.f;
+        for (int q = 0; q < W; ++q) g[q] = make_float2(0.f, 0.f);
         const float2 *Y = A.Y + (size_t)c_it * A.nh;
-        float su = 0.f, gar = 0.f, gai = 0.f, gbr = 0.f, gbi = 0.f;
-        RvBack<TWOL, TWOL, NT>::run(mb, ck, Y, st, ur, ui, su, gar, gai, gbr, gbi);
+        const float2 z2 = make_float2(0.f, 0.f);
+        float2 su2 = z2, sa1 = z2, sa2 = z2, sb1 = z2, sb2 = z2;
+        RvBack<TWOL, TWOL, NT>::run(mb, rv_pairs(ck), Y, st, g, su2, sa1, sa2, sb1, sb2);
+        const float su = su2.x + su2.y, gar = sa1.x + sa1.y, gai = sa2.x - sa2.y;
+        const float gbr = -(sb1.x + sb1.y), gbi = -(sb2.x - sb2.y);
         // sum the chains of each image into its mb == 0 lane
         float tu = su, t0 = gar, t1 = gai, t2 = gbr, t3 = gbi;
 #pragma unroll

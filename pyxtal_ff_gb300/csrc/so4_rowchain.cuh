@@ -273,79 +273,91 @@ struct RvFwd<TWOL, TWOL + 1, NT> {
                                                float2 *) {}
 };
 
-// Backward sweep, level L down to 1.  (gr, gi): on entry the adjoint of this
-// lane's row of level L arriving from level L + 1; on exit that of its row of
-// level L - 1.  Adds Y's row, forms f, back-propagates through the middle-row
-// construction and the recursion, and accumulates G_ca (gar, gai), G_cb (gbr, gbi).
+// Backward sweep, level L down to 1, in packed FP32 pairs.  g: on entry the adjoint of
+// this lane's row of level L arriving from level L + 1; on exit that of its row of level
+// L - 1.  Adds Y's row, forms f, back-propagates through the middle-row construction and
+// the recursion.  Sums are kept as elementwise pairs and folded by the caller:
+//   f = su.x + su.y,  G_ca = (sa1.x + sa1.y, sa2.x - sa2.y),
+//   G_cb = -(sb1.x + sb1.y, sb2.x - sb2.y).
+// With a = conj(conj a) = (ar, ai), b = (br, bi): AX = (ar, ar), AYn = (-ai, ai),
+// BXn = (-br, -br), BY = (bi, -bi), so that a g = AX g + AYn swap(g) and
+// -b h = BXn h + BY swap(h) (elementwise products, swap(v) = (v.y, v.x)).
+struct RvPairs {
+    float2 ax, ayn, bxn, by;
+};
+__device__ __forceinline__ RvPairs rv_pairs(const CK<float> &ck) {
+    const float ar = ck.ca.re, ai = -ck.ca.im, br = ck.cb.re, bi = -ck.cb.im;
+    RvPairs q;
+    q.ax = make_float2(ar, ar);
+    q.ayn = make_float2(-ai, ai);
+    q.bxn = make_float2(-br, -br);
+    q.by = make_float2(bi, -bi);
+    return q;
+}
 template <int TWOL, int L, int NT>
 struct RvBack {
-    __device__ __forceinline__ static void run(int mb, const CK<float> &ck, const float2 *__restrict__ Y,
-                                               const float2 *st, float (&gr)[TWOL + 1], float (&gi)[TWOL + 1],
-                                               float &su, float &gar, float &gai, float &gbr, float &gbi) {
+    __device__ __forceinline__ static void run(int mb, const RvPairs &q, const float2 *__restrict__ Y,
+                                               const float2 *st, float2 (&g)[TWOL + 1], float2 &su, float2 &sa1,
+                                               float2 &sa2, float2 &sb1, float2 &sb2) {
         constexpr int H = L / 2;
         if (2 * mb <= L) {
             const float2 *Yr = Y + half_block(L) + mb * (L + 1);
 #pragma unroll
             for (int ma = 0; ma <= L; ++ma) {
                 const float2 y = __ldg(Yr + ma);
-                const float2 w = st[(acc_block(L) + ma) * NT];
-                su = fmaf(w.x, y.x, fmaf(w.y, y.y, su));
-                gr[ma] += y.x;
-                gi[ma] += y.y;
+                su = __ffma2_rn(st[(acc_block(L) + ma) * NT], y, su);
+                g[ma] = __fadd2_rn(g[ma], y);
             }
             if ((L & 1) == 0 && mb == H) {
                 // row = (V[0..H-1], conj V[H], (-1)^(H+ma) conj V[L-ma] for ma > H): adjoint onto V
 #pragma unroll
                 for (int ma = 0; ma < H; ++ma) {
                     const float s = ((H + ma) & 1) ? -1.f : 1.f;
-                    gr[ma] += s * gr[L - ma];
-                    gi[ma] -= s * gi[L - ma];
+                    g[ma].x += s * g[L - ma].x;
+                    g[ma].y -= s * g[L - ma].y;
                 }
-                gi[H] = -gi[H];
+                g[H].y = -g[H].y;
 #pragma unroll
-                for (int ma = H + 1; ma <= L; ++ma) gr[ma] = gi[ma] = 0.f;
+                for (int ma = H + 1; ma <= L; ++ma) g[ma] = make_float2(0.f, 0.f);
             }
-            // scaled rows: V[ma] = conj(a) P[ma] - conj(b) P[ma-1]
-            const float ar = ck.ca.re, ai = -ck.ca.im;  // a = conj(conj(a))
-            const float br = ck.cb.re, bi = -ck.cb.im;
-            // in place, ascending: the new G[ma] = a G[ma] - b G[ma+1] reads G[ma + 1]
-            // before it is replaced
+            // scaled rows: V[ma] = conj(a) P[ma] - conj(b) P[ma-1]; in place, ascending: the
+            // new G[ma] = a G[ma] - b G[ma+1] reads G[ma + 1] before it is replaced
 #pragma unroll
             for (int ma = 0; ma < L; ++ma) {
-                const float g0 = gr[ma], g1 = gi[ma], h0 = gr[ma + 1], h1 = gi[ma + 1];
+                const float2 gv = g[ma], hv = g[ma + 1];
+                const float2 gs = make_float2(gv.y, gv.x), hs = make_float2(hv.y, hv.x);
                 const float2 p = st[(acc_block(L - 1) + ma) * NT];
-                // G_ca += conj(P) G[ma];  G_cb -= conj(P) G[ma+1]
-                gar = fmaf(p.x, g0, fmaf(p.y, g1, gar));
-                gai = fmaf(p.x, g1, fmaf(-p.y, g0, gai));
-                gbr = fmaf(-p.x, h0, fmaf(-p.y, h1, gbr));
-                gbi = fmaf(-p.x, h1, fmaf(p.y, h0, gbi));
-                gr[ma] = fmaf(ar, g0, fmaf(-ai, g1, fmaf(-br, h0, bi * h1)));
-                gi[ma] = fmaf(ar, g1, fmaf(ai, g0, fmaf(-br, h1, -bi * h0)));
+                // G_ca += conj(P) G[ma];  G_cb -= conj(P) G[ma+1]  (as elementwise pairs)
+                sa1 = __ffma2_rn(p, gv, sa1);
+                sa2 = __ffma2_rn(p, gs, sa2);
+                sb1 = __ffma2_rn(p, hv, sb1);
+                sb2 = __ffma2_rn(p, hs, sb2);
+                g[ma] = __ffma2_rn(q.ax, gv, __ffma2_rn(q.ayn, gs, __ffma2_rn(q.bxn, hv, __fmul2_rn(q.by, hs))));
             }
-            gr[L] = gi[L] = 0.f;
+            g[L] = make_float2(0.f, 0.f);
         }
         if ((L & 1) == 0) {
             // the chain mb = H started at this level from P[c] = (-1)^(H+c) conj(Q[L-1-c]),
             // Q the row H-1 of level L-1 on lane - 1: hand it the adjoint of Q
 #pragma unroll
             for (int k = 0; k < L; ++k) {
-                const float vr = __shfl_down_sync(0xffffffffu, gr[L - 1 - k], 1);
-                const float vi = __shfl_down_sync(0xffffffffu, gi[L - 1 - k], 1);
+                const float vr = __shfl_down_sync(0xffffffffu, g[L - 1 - k].x, 1);
+                const float vi = __shfl_down_sync(0xffffffffu, g[L - 1 - k].y, 1);
                 if (mb == H - 1) {
                     const float s = ((H + L - 1 - k) & 1) ? -1.f : 1.f;
-                    gr[k] += s * vr;
-                    gi[k] -= s * vi;
+                    g[k].x += s * vr;
+                    g[k].y -= s * vi;
                 }
             }
         }
-        RvBack<TWOL, L - 1, NT>::run(mb, ck, Y, st, gr, gi, su, gar, gai, gbr, gbi);
+        RvBack<TWOL, L - 1, NT>::run(mb, q, Y, st, g, su, sa1, sa2, sb1, sb2);
     }
 };
 template <int TWOL, int NT>
 struct RvBack<TWOL, 0, NT> {
-    __device__ __forceinline__ static void run(int mb, const CK<float> &, const float2 *__restrict__ Y, const float2 *,
-                                               float (&)[TWOL + 1], float (&)[TWOL + 1], float &su, float &, float &,
-                                               float &, float &) {
-        if (mb == 0) su += __ldg(Y).x;  // level 0: U = 1
+    __device__ __forceinline__ static void run(int mb, const RvPairs &, const float2 *__restrict__ Y, const float2 *,
+                                               float2 (&)[TWOL + 1], float2 &su, float2 &, float2 &, float2 &,
+                                               float2 &) {
+        if (mb == 0) su.x += __ldg(Y).x;  // level 0: U = 1
     }
 };
