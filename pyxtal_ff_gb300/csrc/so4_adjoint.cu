@@ -106,9 +106,9 @@ __global__ void __launch_bounds__(NW * 32, (TWOL <= 8) ? 4 : 1) k_utot_rc(FwdArg
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int a = blockIdx.x * NW + wid;
     const int grp = lane / RC::NCH, mb = lane - grp * RC::NCH;
-    float2 acc[NACC];
+    float accr[NACC], acci[NACC];
 #pragma unroll
-    for (int q = 0; q < NACC; ++q) acc[q] = make_float2(0.f, 0.f);
+    for (int q = 0; q < NACC; ++q) accr[q] = acci[q] = 0.f;
     if (a < A.natoms) {
         const int m0 = A.img_ptr[a], m1 = A.img_ptr[a + 1];
         // Cayley-Klein parameters and weights of up to 32 images at once, one per lane;
@@ -149,20 +149,20 @@ __global__ void __launch_bounds__(NW * 32, (TWOL <= 8) ? 4 : 1) k_utot_rc(FwdArg
                 ck.cb.im = __shfl_sync(0xffffffffu, ck0.cb.im, sl);
                 float wsf = __shfl_sync(0xffffffffu, wsf0, sl);
                 if (!ok) wsf = 0.f;
-                float2 u[W];
+                float ur[W], ui[W], dr[3][W], di[3][W];
 #pragma unroll
-                for (int q = 0; q < W; ++q) u[q] = make_float2(0.f, 0.f);
-                u[0].x = 1.f;
-                if (mb == 0) acc[0].x += wsf;
-                RcUtot<TWOL, 1>::run(mb, rc_pairs(ck.ca, ck.cb), make_float2(wsf, wsf), u, acc);
+                for (int q = 0; q < W; ++q) ur[q] = ui[q] = 0.f;
+                ur[0] = 1.f;
+                if (mb == 0) accr[0] += wsf;
+                RcUtot<TWOL, 1>::run(mb, ck, wsf, ur, ui, dr, di, accr, acci);
             }
         }
     }
     float *sw = ut_smem + (size_t)wid * 32 * 2 * NACC;
 #pragma unroll
     for (int q = 0; q < NACC; ++q) {
-        sw[lane * 2 * NACC + 2 * q] = acc[q].x;
-        sw[lane * 2 * NACC + 2 * q + 1] = acc[q].y;
+        sw[lane * 2 * NACC + 2 * q] = accr[q];
+        sw[lane * 2 * NACC + 2 * q + 1] = acci[q];
     }
     __syncwarp();
     if (a >= A.natoms) return;
@@ -558,12 +558,12 @@ __global__ void __launch_bounds__(NT, (TWOL <= 8) ? 2 : 1) k_deidrj_rev(DArgs A,
             const int nlines = (A.nh * (int)sizeof(float2) + 127) / 128;
             for (int l = mb; l < nlines; l += RC::NCH) asm volatile("prefetch.global.L1 [%0];" ::"l"(yb + 128 * l));
         }
-        float2 u[W];
+        float ur[W], ui[W];
 #pragma unroll
-        for (int q = 0; q < W; ++q) u[q] = make_float2(0.f, 0.f);
-        u[0].x = 1.f;
+        for (int q = 0; q < W; ++q) ur[q] = ui[q] = 0.f;
+        ur[0] = 1.f;
         st[0] = make_float2(1.f, 0.f);  // level 0
-        RvFwd<TWOL, 1, NT>::run(mb, rc_pairs(ck.ca, ck.cb), u, st);
+        RvFwd<TWOL, 1, NT>::run(mb, ck, ur, ui, st);
         // backward sweep (packed pairs), the adjoint carry in g
         float2 g[W];
 #pragma unroll

@@ -41,9 +41,9 @@ __global__ void __launch_bounds__(NW * 32, (TWOL <= 6) ? 4 : ((TWOL == 8) ? 3 : 
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int a = blockIdx.x * NW + wid;
     const int grp = lane / RC::NCH, mb = lane - grp * RC::NCH;
-    float2 acc[NACC];
+    float accr[NACC], acci[NACC];
 #pragma unroll
-    for (int q = 0; q < NACC; ++q) acc[q] = make_float2(0.f, 0.f);
+    for (int q = 0; q < NACC; ++q) accr[q] = acci[q] = 0.f;
     if (a < A.natoms) {
         const int m0 = A.img_ptr[a], m1 = A.img_ptr[a + 1];
         float vi[3] = {0.f, 0.f, 0.f}, G[9];
@@ -104,34 +104,32 @@ __global__ void __launch_bounds__(NW * 32, (TWOL <= 6) ? 4 : ((TWOL == 8) ? 3 : 
                 const int src = sub + grp;
                 const bool ok = grp < RC::IPW && src < nimg;
                 const int sl = ok ? src : 0;
-                cx<float> ca, cb, da, db;
-                ca.re = __shfl_sync(0xffffffffu, ck0.ca.re, sl);
-                ca.im = __shfl_sync(0xffffffffu, ck0.ca.im, sl);
-                cb.re = __shfl_sync(0xffffffffu, ck0.cb.re, sl);
-                cb.im = __shfl_sync(0xffffffffu, ck0.cb.im, sl);
-                da.re = __shfl_sync(0xffffffffu, da0.re, sl);
-                da.im = __shfl_sync(0xffffffffu, da0.im, sl);
-                db.re = __shfl_sync(0xffffffffu, db0.re, sl);
-                db.im = __shfl_sync(0xffffffffu, db0.im, sl);
+                CK<float> ck;  // slot 0 of the derivatives holds the one direction
+                ck.ca.re = __shfl_sync(0xffffffffu, ck0.ca.re, sl);
+                ck.ca.im = __shfl_sync(0xffffffffu, ck0.ca.im, sl);
+                ck.cb.re = __shfl_sync(0xffffffffu, ck0.cb.re, sl);
+                ck.cb.im = __shfl_sync(0xffffffffu, ck0.cb.im, sl);
+                ck.cda[0].re = __shfl_sync(0xffffffffu, da0.re, sl);
+                ck.cda[0].im = __shfl_sync(0xffffffffu, da0.im, sl);
+                ck.cdb[0].re = __shfl_sync(0xffffffffu, db0.re, sl);
+                ck.cdb[0].im = __shfl_sync(0xffffffffu, db0.im, sl);
                 float a_du = __shfl_sync(0xffffffffu, a_du0, sl);
                 float a_d = __shfl_sync(0xffffffffu, a_d0, sl);
                 if (!ok) a_du = a_d = 0.f;
-                float2 u[W], d[1][W];
+                float ur[W], ui[W], dr[1][W], di[1][W];
 #pragma unroll
-                for (int q = 0; q < W; ++q) u[q] = d[0][q] = make_float2(0.f, 0.f);
-                u[0].x = 1.f;
-                if (mb == 0) acc[0].x += a_du;  // level 0: U = 1, dU = 0
-                const RcPairs dq[1] = {rc_pairs(da, db)};
-                RcJvp<TWOL, 1>::run(mb, rc_pairs(ca, cb), dq, make_float2(a_du, a_du), make_float2(a_d, a_d), u, d,
-                                    acc);
+                for (int q = 0; q < W; ++q) ur[q] = ui[q] = dr[0][q] = di[0][q] = 0.f;
+                ur[0] = 1.f;
+                if (mb == 0) accr[0] += a_du;  // level 0: U = 1, dU = 0
+                RcJvp<TWOL, 1>::run(mb, ck, a_du, a_d, ur, ui, dr, di, accr, acci);
             }
         }
     }
     float *sw = jv_smem + (size_t)wid * 32 * 2 * NACC;
 #pragma unroll
     for (int q = 0; q < NACC; ++q) {
-        sw[lane * 2 * NACC + 2 * q] = acc[q].x;
-        sw[lane * 2 * NACC + 2 * q + 1] = acc[q].y;
+        sw[lane * 2 * NACC + 2 * q] = accr[q];
+        sw[lane * 2 * NACC + 2 * q + 1] = acci[q];
     }
     __syncwarp();
     if (a >= A.natoms) return;

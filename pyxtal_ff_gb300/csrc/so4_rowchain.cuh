@@ -28,82 +28,77 @@ struct RowChain {
     static constexpr int W = TWOL + 1;         // longest row
 };
 
-// Coefficient pairs of the scaled step in packed FP32: with c = (cr, ci),
-//   c p = (cr, cr) p + (-ci, ci) swap(p),  -c p = (-cr, -cr) p + (ci, -ci) swap(p)
-// (elementwise products, swap(v) = (v.y, v.x)).
-struct RcPairs {
-    float2 ax, ayn, bxn, by;  // conj(a): (re, re), (-im, im); conj(b) negated: (-re, -re), (im, -im)
-};
-__device__ __forceinline__ RcPairs rc_pairs(const cx<float> &ca, const cx<float> &cb) {
-    RcPairs q;
-    q.ax = make_float2(ca.re, ca.re);
-    q.ayn = make_float2(-ca.im, ca.im);
-    q.bxn = make_float2(-cb.re, -cb.re);
-    q.by = make_float2(cb.im, -cb.im);
-    return q;
-}
-__device__ __forceinline__ float2 swap2(const float2 v) { return make_float2(v.y, v.x); }
-
-// Advance one image's chain `mb` from level L-1 to level L (in place), scaled rows in
-// packed pairs: V_L[ma] = conj(a) V_{L-1}[ma] - conj(b) V_{L-1}[ma-1].
-// u: the row of V; d[c]: the row of its derivative along direction c (q: the pairs of
-// conj(a), conj(b); dq[c]: those of their derivatives).  Lanes whose chain has not
-// started (mb > L/2) compute values nobody reads.
+// Advance one image's chain `mb` from level L-1 to level L (in place), scaled rows:
+// V_L[ma] = conj(a) V_{L-1}[ma] - conj(b) V_{L-1}[ma-1].
+// u, d0, d1, d2: the row (re, im) of V and of dV/dx, dV/dy, dV/dz.  Lanes whose chain
+// has not started (mb > L/2) compute values nobody reads.
 template <int TWOL, int L, bool DERIV, int NDER = 3>
-__device__ __forceinline__ void rc_level(int mb, const RcPairs &q, const RcPairs (&dq)[NDER], float2 (&u)[TWOL + 1],
-                                         float2 (&d)[NDER][TWOL + 1]) {
+__device__ __forceinline__ void rc_level(int mb, const CK<float> &ck, float (&ur)[TWOL + 1], float (&ui)[TWOL + 1],
+                                         float (&dr)[NDER][TWOL + 1], float (&di)[NDER][TWOL + 1]) {
     // descending in place: new[ma] uses old[ma] (a-term) and old[ma-1] (b-term)
 #pragma unroll
     for (int ma = L; ma >= 0; --ma) {
-        float2 v = make_float2(0.f, 0.f);
-        float2 e[NDER];
+        float vr = 0.f, vi = 0.f;
+        float er[NDER], ei[NDER];
 #pragma unroll
-        for (int c = 0; c < NDER; ++c) e[c] = make_float2(0.f, 0.f);
+        for (int c = 0; c < NDER; ++c) er[c] = ei[c] = 0.f;
         if (ma > 0) {
-            const float2 p = u[ma - 1], ps = swap2(p);
-            v = __ffma2_rn(q.bxn, p, __fmul2_rn(q.by, ps));
+            // - conj(b) * P[ma-1]
+            const float pr = ur[ma - 1], pi = ui[ma - 1];
+            vr = fmaf(ck.cb.im, pi, -ck.cb.re * pr);
+            vi = fmaf(-ck.cb.im, pr, -ck.cb.re * pi);
             if (DERIV) {
 #pragma unroll
                 for (int c = 0; c < NDER; ++c) {
-                    const float2 w = d[c][ma - 1], ws = swap2(w);
-                    e[c] = __ffma2_rn(dq[c].bxn, p, __ffma2_rn(dq[c].by, ps,
-                                      __ffma2_rn(q.bxn, w, __fmul2_rn(q.by, ws))));
+                    const float qr = dr[c][ma - 1], qi = di[c][ma - 1];
+                    er[c] = -(ck.cdb[c].re * pr - ck.cdb[c].im * pi + ck.cb.re * qr - ck.cb.im * qi);
+                    ei[c] = -(ck.cdb[c].re * pi + ck.cdb[c].im * pr + ck.cb.re * qi + ck.cb.im * qr);
                 }
             }
         }
         if (ma < L) {
-            const float2 p = u[ma], ps = swap2(p);
-            v = __ffma2_rn(q.ax, p, __ffma2_rn(q.ayn, ps, v));
+            // + conj(a) * P[ma]
+            const float pr = ur[ma], pi = ui[ma];
+            vr = fmaf(ck.ca.re, pr, fmaf(-ck.ca.im, pi, vr));
+            vi = fmaf(ck.ca.re, pi, fmaf(ck.ca.im, pr, vi));
             if (DERIV) {
 #pragma unroll
                 for (int c = 0; c < NDER; ++c) {
-                    const float2 w = d[c][ma], ws = swap2(w);
-                    e[c] = __ffma2_rn(dq[c].ax, p, __ffma2_rn(dq[c].ayn, ps,
-                                      __ffma2_rn(q.ax, w, __ffma2_rn(q.ayn, ws, e[c]))));
+                    const float qr = dr[c][ma], qi = di[c][ma];
+                    er[c] += ck.cda[c].re * pr - ck.cda[c].im * pi + ck.ca.re * qr - ck.ca.im * qi;
+                    ei[c] += ck.cda[c].re * pi + ck.cda[c].im * pr + ck.ca.re * qi + ck.ca.im * qr;
                 }
             }
         }
-        u[ma] = v;
+        ur[ma] = vr;
+        ui[ma] = vi;
         if (DERIV) {
 #pragma unroll
-            for (int c = 0; c < NDER; ++c) d[c][ma] = e[c];
+            for (int c = 0; c < NDER; ++c) {
+                dr[c][ma] = er[c];
+                di[c][ma] = ei[c];
+            }
         }
     }
     if ((L & 1) == 0 && 2 * mb == L) {
         // middle row: centre -> conj, upper half -> (-1)^(L/2+ma) conj(lower mirror)
         constexpr int H = L / 2;
-        u[H].y = -u[H].y;
+        ui[H] = -ui[H];
         if (DERIV) {
 #pragma unroll
-            for (int c = 0; c < NDER; ++c) d[c][H].y = -d[c][H].y;
+            for (int c = 0; c < NDER; ++c) di[c][H] = -di[c][H];
         }
 #pragma unroll
         for (int ma = H + 1; ma <= L; ++ma) {
             const float s = ((H + ma) & 1) ? -1.f : 1.f;
-            u[ma] = make_float2(s * u[L - ma].x, -s * u[L - ma].y);
+            ur[ma] = s * ur[L - ma];
+            ui[ma] = -s * ui[L - ma];
             if (DERIV) {
 #pragma unroll
-                for (int c = 0; c < NDER; ++c) d[c][ma] = make_float2(s * d[c][L - ma].x, -s * d[c][L - ma].y);
+                for (int c = 0; c < NDER; ++c) {
+                    dr[c][ma] = s * dr[c][L - ma];
+                    di[c][ma] = -s * di[c][L - ma];
+                }
             }
         }
     }
@@ -116,21 +111,28 @@ __device__ __forceinline__ void rc_level(int mb, const RcPairs &q, const RcPairs
 // values.  The source lane is never the taking lane, so writing slot c while
 // later shuffles read slots L-1-c of lane-1 is safe.
 template <int TWOL, int L, bool DERIV, int NDER = 3>
-__device__ __forceinline__ void rc_start(int mb, float2 (&u)[TWOL + 1], float2 (&d)[NDER][TWOL + 1]) {
+__device__ __forceinline__ void rc_start(int mb, float (&ur)[TWOL + 1], float (&ui)[TWOL + 1],
+                                         float (&dr)[NDER][TWOL + 1], float (&di)[NDER][TWOL + 1]) {
     constexpr int H = L / 2;
     const bool take = (mb == H);
 #pragma unroll
     for (int c = 0; c < L; ++c) {
         const float s = ((H + c) & 1) ? -1.f : 1.f;
-        const float vr = __shfl_up_sync(0xffffffffu, u[L - 1 - c].x, 1);
-        const float vi = __shfl_up_sync(0xffffffffu, u[L - 1 - c].y, 1);
-        if (take) u[c] = make_float2(s * vr, -s * vi);
+        const float vr = __shfl_up_sync(0xffffffffu, ur[L - 1 - c], 1);
+        const float vi = __shfl_up_sync(0xffffffffu, ui[L - 1 - c], 1);
+        if (take) {
+            ur[c] = s * vr;
+            ui[c] = -s * vi;
+        }
         if (DERIV) {
 #pragma unroll
             for (int k = 0; k < NDER; ++k) {
-                const float wr = __shfl_up_sync(0xffffffffu, d[k][L - 1 - c].x, 1);
-                const float wi = __shfl_up_sync(0xffffffffu, d[k][L - 1 - c].y, 1);
-                if (take) d[k][c] = make_float2(s * wr, -s * wi);
+                const float wr = __shfl_up_sync(0xffffffffu, dr[k][L - 1 - c], 1);
+                const float wi = __shfl_up_sync(0xffffffffu, di[k][L - 1 - c], 1);
+                if (take) {
+                    dr[k][c] = s * wr;
+                    di[k][c] = -s * wi;
+                }
             }
         }
     }
@@ -181,52 +183,59 @@ __device__ __forceinline__ int centre_of(const int32_t *img_ptr, int natoms, int
 __host__ __device__ constexpr int acc_block(int L) { return L * (L + 1) / 2; }
 
 // Levels L..TWOL of the U recursion (no derivatives); after each level the
-// lane adds w sfac V of its row into its accumulator pairs for that level.
+// lane adds w sfac U of its row into its accumulator for that level.
 template <int TWOL, int L>
 struct RcUtot {
-    __device__ __forceinline__ static void run(int mb, const RcPairs &q, const float2 wsf2, float2 (&u)[TWOL + 1],
-                                               float2 (&acc)[acc_block(TWOL + 1)]) {
-        float2 d[1][TWOL + 1];  // no derivative rows (not read)
-        const RcPairs dq[1] = {q};
-        if ((L & 1) == 0) rc_start<TWOL, L, false, 1>(mb, u, d);
-        rc_level<TWOL, L, false, 1>(mb, q, dq, u, d);
+    __device__ __forceinline__ static void run(int mb, const CK<float> &ck, float wsf, float (&ur)[TWOL + 1],
+                                               float (&ui)[TWOL + 1], float (&dr)[3][TWOL + 1],
+                                               float (&di)[3][TWOL + 1], float (&accr)[acc_block(TWOL + 1)],
+                                               float (&acci)[acc_block(TWOL + 1)]) {
+        if ((L & 1) == 0) rc_start<TWOL, L, false>(mb, ur, ui, dr, di);
+        rc_level<TWOL, L, false>(mb, ck, ur, ui, dr, di);
         if (2 * mb <= L) {
 #pragma unroll
-            for (int ma = 0; ma <= L; ++ma) acc[acc_block(L) + ma] = __ffma2_rn(wsf2, u[ma], acc[acc_block(L) + ma]);
+            for (int ma = 0; ma <= L; ++ma) {
+                accr[acc_block(L) + ma] += wsf * ur[ma];
+                acci[acc_block(L) + ma] += wsf * ui[ma];
+            }
         }
-        RcUtot<TWOL, L + 1>::run(mb, q, wsf2, u, acc);
+        RcUtot<TWOL, L + 1>::run(mb, ck, wsf, ur, ui, dr, di, accr, acci);
     }
 };
 template <int TWOL>
 struct RcUtot<TWOL, TWOL + 1> {
-    __device__ __forceinline__ static void run(int, const RcPairs &, const float2, float2 (&)[TWOL + 1],
-                                               float2 (&)[acc_block(TWOL + 1)]) {}
+    __device__ __forceinline__ static void run(int, const CK<float> &, float, float (&)[TWOL + 1], float (&)[TWOL + 1],
+                                               float (&)[3][TWOL + 1], float (&)[3][TWOL + 1],
+                                               float (&)[acc_block(TWOL + 1)], float (&)[acc_block(TWOL + 1)]) {}
 };
 
-// Levels L..TWOL with the derivative along one direction per image (dq: the pairs of
-// d conj(a), d conj(b) along it); after each level the lane adds
-//   a_du V + a_d dV   (a_du = w dsfac (r^ . dr_m), a_d = w sfac)
-// of its row into its accumulator pairs (the tangent of U_tot used by the JVP).
+// Levels L..TWOL with the derivative along one direction per image (ck.cda[0],
+// ck.cdb[0] hold d conj(a), d conj(b) along it); after each level the lane adds
+//   a_du U + a_d dU   (a_du = w dsfac (r^ . dr_m), a_d = w sfac)
+// of its row into its accumulator (the tangent of U_tot used by the JVP).
 template <int TWOL, int L>
 struct RcJvp {
-    __device__ __forceinline__ static void run(int mb, const RcPairs &q, const RcPairs (&dq)[1], const float2 adu2,
-                                               const float2 ad2, float2 (&u)[TWOL + 1], float2 (&d)[1][TWOL + 1],
-                                               float2 (&acc)[acc_block(TWOL + 1)]) {
-        if ((L & 1) == 0) rc_start<TWOL, L, true, 1>(mb, u, d);
-        rc_level<TWOL, L, true, 1>(mb, q, dq, u, d);
+    __device__ __forceinline__ static void run(int mb, const CK<float> &ck, float a_du, float a_d,
+                                               float (&ur)[TWOL + 1], float (&ui)[TWOL + 1],
+                                               float (&dr)[1][TWOL + 1], float (&di)[1][TWOL + 1],
+                                               float (&accr)[acc_block(TWOL + 1)], float (&acci)[acc_block(TWOL + 1)]) {
+        if ((L & 1) == 0) rc_start<TWOL, L, true, 1>(mb, ur, ui, dr, di);
+        rc_level<TWOL, L, true, 1>(mb, ck, ur, ui, dr, di);
         if (2 * mb <= L) {
 #pragma unroll
-            for (int ma = 0; ma <= L; ++ma)
-                acc[acc_block(L) + ma] = __ffma2_rn(adu2, u[ma], __ffma2_rn(ad2, d[0][ma], acc[acc_block(L) + ma]));
+            for (int ma = 0; ma <= L; ++ma) {
+                accr[acc_block(L) + ma] += a_du * ur[ma] + a_d * dr[0][ma];
+                acci[acc_block(L) + ma] += a_du * ui[ma] + a_d * di[0][ma];
+            }
         }
-        RcJvp<TWOL, L + 1>::run(mb, q, dq, adu2, ad2, u, d, acc);
+        RcJvp<TWOL, L + 1>::run(mb, ck, a_du, a_d, ur, ui, dr, di, accr, acci);
     }
 };
 template <int TWOL>
 struct RcJvp<TWOL, TWOL + 1> {
-    __device__ __forceinline__ static void run(int, const RcPairs &, const RcPairs (&)[1], const float2, const float2,
-                                               float2 (&)[TWOL + 1], float2 (&)[1][TWOL + 1],
-                                               float2 (&)[acc_block(TWOL + 1)]) {}
+    __device__ __forceinline__ static void run(int, const CK<float> &, float, float, float (&)[TWOL + 1],
+                                               float (&)[TWOL + 1], float (&)[1][TWOL + 1], float (&)[1][TWOL + 1],
+                                               float (&)[acc_block(TWOL + 1)], float (&)[acc_block(TWOL + 1)]) {}
 };
 
 // ---------------------------------------------------------------------------
@@ -242,25 +251,26 @@ struct RcJvp<TWOL, TWOL + 1> {
 // memory at st[(acc_block(L) + ma) * NT] (NT = threads per CTA, st = base + tid).
 template <int TWOL, int L, int NT>
 struct RvFwd {
-    __device__ __forceinline__ static void run(int mb, const RcPairs &q, float2 (&u)[TWOL + 1], float2 *st) {
-        float2 d[1][TWOL + 1];  // no derivative rows (not read)
-        const RcPairs dq[1] = {q};
+    __device__ __forceinline__ static void run(int mb, const CK<float> &ck, float (&ur)[TWOL + 1],
+                                               float (&ui)[TWOL + 1], float2 *st) {
+        float dr[3][TWOL + 1], di[3][TWOL + 1];  // unused (no derivatives)
         if ((L & 1) == 0) {
-            rc_start<TWOL, L, false, 1>(mb, u, d);
+            rc_start<TWOL, L, false>(mb, ur, ui, dr, di);
             if (mb == L / 2) {
 #pragma unroll
-                for (int c = 0; c < L; ++c) st[(acc_block(L - 1) + c) * NT] = u[c];
+                for (int c = 0; c < L; ++c) st[(acc_block(L - 1) + c) * NT] = make_float2(ur[c], ui[c]);
             }
         }
-        rc_level<TWOL, L, false, 1>(mb, q, dq, u, d);
+        rc_level<TWOL, L, false>(mb, ck, ur, ui, dr, di);
 #pragma unroll
-        for (int ma = 0; ma <= L; ++ma) st[(acc_block(L) + ma) * NT] = u[ma];
-        RvFwd<TWOL, L + 1, NT>::run(mb, q, u, st);
+        for (int ma = 0; ma <= L; ++ma) st[(acc_block(L) + ma) * NT] = make_float2(ur[ma], ui[ma]);
+        RvFwd<TWOL, L + 1, NT>::run(mb, ck, ur, ui, st);
     }
 };
 template <int TWOL, int NT>
 struct RvFwd<TWOL, TWOL + 1, NT> {
-    __device__ __forceinline__ static void run(int, const RcPairs &, float2 (&)[TWOL + 1], float2 *) {}
+    __device__ __forceinline__ static void run(int, const CK<float> &, float (&)[TWOL + 1], float (&)[TWOL + 1],
+                                               float2 *) {}
 };
 
 // Backward sweep, level L down to 1, in packed FP32 pairs.  g: on entry the adjoint of
