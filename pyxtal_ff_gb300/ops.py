@@ -8,6 +8,8 @@ they launch the CUDA kernels on torch's current stream):
   forward32(...)      -> (B, U_tot)                                         so4_forward32
   adjoint32(...)      -> (forces, virial)                                   so4_adjoint32
   jvp32(...)          -> dB                                                 so4_jvp32
+  forward / adjoint / adjoint_jvp: the same three under the operator set's names
+  contract_dxdr(...)  -> (forces, stress sums) from dxdr, rdxdr_atom         so4_contract_dxdr
 
 Autograd:
 
@@ -112,6 +114,37 @@ def adjoint32_op(ctx_key: int, utot: torch.Tensor, beta: torch.Tensor) -> tuple[
 def jvp32_op(ctx_key: int, utot: torch.Tensor, v: torch.Tensor, G: torch.Tensor) -> torch.Tensor:
     c = _CTX[ctx_key]
     return engine.jvp32(c.tab, c.prm, c.nb, c.w_nb, utot, v=v, G=G).clone()
+
+
+# The same operators under the names of the path's operator set (forward / adjoint /
+# adjoint_jvp), and the NN consumer's contraction of the plain path's outputs.
+@torch.library.custom_op(_NS + "::forward", mutates_args=())
+def forward_op(ctx_key: int) -> tuple[torch.Tensor, torch.Tensor]:
+    """B (N, nB) f32 and U_tot (kept for the adjoint): forward32."""
+    return forward32_op(ctx_key)
+
+
+@torch.library.custom_op(_NS + "::adjoint", mutates_args=())
+def adjoint_op(ctx_key: int, utot: torch.Tensor, beta: torch.Tensor) -> tuple[torch.Tensor, torch.Tensor]:
+    """Forces (N, 3) and virial (S, 3, 3) f64 for beta = dE/dB: adjoint32."""
+    return adjoint32_op(ctx_key, utot, beta)
+
+
+@torch.library.custom_op(_NS + "::adjoint_jvp", mutates_args=())
+def adjoint_jvp_op(ctx_key: int, utot: torch.Tensor, v: torch.Tensor, G: torch.Tensor) -> torch.Tensor:
+    """The adjoint's backward, dB along dr_m = (v_j - v_i) + G_s^T r_m: jvp32."""
+    return jvp32_op(ctx_key, utot, v, G)
+
+
+@torch.library.custom_op(_NS + "::contract_dxdr", mutates_args=())
+def contract_dxdr_op(ctx_key: int, beta: torch.Tensor, dxdr: torch.Tensor,
+                     rdxdr_atom: torch.Tensor) -> tuple[torch.Tensor, torch.Tensor]:
+    """Forces (N, 3) and per-structure stress sums (S, 6) from the plain path's dxdr and
+    per-atom rdxdr on the context's pair list (so4_contract_dxdr)."""
+    nb = _CTX[ctx_key].nb
+    f, st = engine.contract_dxdr(beta.contiguous(), nb.pair_ptr, nb.seq, nb.atom_struct, nb.atom_ptr_dev,
+                                 dxdr=dxdr.contiguous(), rdxdr_atom=rdxdr_atom.contiguous())
+    return f.clone(), st.clone()
 
 
 class SO4Descriptor(torch.autograd.Function):

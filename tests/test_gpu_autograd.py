@@ -120,3 +120,30 @@ def test_neighbor_and_plain_ops_match_engine(cuda_device):
         x2, dxdr2, rdxdr2 = engine.plain(ctx.tab, ctx.prm, nb, pos, ctx.w_nb, ctx.w_site, precision=prec)
         assert torch.equal(x, x2) and torch.equal(dxdr, dxdr2) and torch.equal(rdxdr, rdxdr2)
     ops.release(ctx)
+
+
+def test_operator_set_names_and_contraction_op(cuda_device):
+    # forward / adjoint / adjoint_jvp are the 32-bit operators under the operator set's
+    # names; contract_dxdr contracts the plain path's outputs on the context's pair list
+    _, _, p, ctx, x = _ctx()
+    k = ops.key(ctx)
+    xa, ua = torch.ops.so4gb300.forward(k)
+    xb, ub = torch.ops.so4gb300.forward32(k)
+    assert torch.equal(xa, xb) and torch.equal(ua, ub)
+    beta = torch.randn_like(xa)
+    fa, wa = torch.ops.so4gb300.adjoint(k, ua, beta)
+    fb, wb = torch.ops.so4gb300.adjoint32(k, ua, beta)
+    assert torch.equal(fa, fb) and torch.equal(wa, wb)
+    v = torch.randn((xa.shape[0], 3), dtype=torch.float64, device="cuda")
+    Gs = torch.randn((ctx.nb.nstruct, 3, 3), dtype=torch.float64, device="cuda")
+    assert torch.equal(torch.ops.so4gb300.adjoint_jvp(k, ua, v, Gs), torch.ops.so4gb300.jvp32(k, ua, v, Gs))
+    x64, dxdr, rdxdr = torch.ops.so4gb300.forward_deriv(k, p, 0)
+    rda = engine.rdxdr_atom(rdxdr, ctx.nb.pair_ptr, ctx.nb.natoms)
+    b64 = beta.double()
+    f, st = torch.ops.so4gb300.contract_dxdr(k, b64, dxdr, rda)
+    f2, st2 = engine.contract_dxdr(b64, ctx.nb.pair_ptr, ctx.nb.seq, ctx.nb.atom_struct, ctx.nb.atom_ptr_dev,
+                                   dxdr=dxdr, rdxdr_atom=rda)
+    assert torch.equal(f, f2) and torch.equal(st, st2)
+    # the FP64 contraction and the FP32 adjoint agree on the forces
+    assert (f - fa).abs().max().item() <= 2e-4 * fa.abs().max().item()
+    ops.release(ctx)
