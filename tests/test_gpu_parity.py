@@ -138,7 +138,9 @@ def test_fp64_plain_batched_vs_oracle(cuda_device):
         assert G.rel_err(rdxdr[p0:p1].cpu().numpy(), ref["rdxdr"]) < 1e-10
 
 
-@pytest.mark.parametrize("lmax,rc,w", [(3, 4.9, {"Si": 1.0, "O": 0.7}), (4, 5.0, {"Si": 1.0, "O": 0.5})])
+@pytest.mark.parametrize("lmax,rc,w", [(0, 4.0, {"Si": 1.0, "O": 0.6}), (1, 4.0, {"Si": 1.0, "O": 0.6}),
+                                       (2, 4.5, {"Si": 0.9, "O": 0.6}), (3, 4.9, {"Si": 1.0, "O": 0.7}),
+                                       (4, 5.0, {"Si": 1.0, "O": 0.5}), (5, 5.0, {"Si": 1.0, "O": 0.5})])
 def test_adjoint_fp32_vs_oracle_contraction(cuda_device, lmax, rc, w):
     structs = [S.diamond_si(2, 2, 1, sigma=0.1, rng=np.random.default_rng(5)), S.sio2_random(n_si=8, seed=9)]
     pos, cells, pbc, ptr = _batch_arrays(structs)
