@@ -166,14 +166,15 @@ def test_adjoint_fp32_vs_oracle_contraction(cuda_device, lmax, rc, w):
         assert ef < 2e-4 and ev < 2e-4
 
 
-def test_fused_linear_path_matches_unfused_and_oracle(cuda_device):
+@pytest.mark.parametrize("lmax", [2, 4, 5])
+def test_fused_linear_path_matches_unfused_and_oracle(cuda_device, lmax):
     structs = [S.diamond_si(2, 2, 1, sigma=0.1, rng=np.random.default_rng(8)), S.sio2_random(n_si=8, seed=10)]
     pos, cells, pbc, ptr = _batch_arrays(structs)
     numbers = np.concatenate([s.numbers for s in structs])
     symbols = sum([list(s.symbols) for s in structs], [])
     w = {"Si": 1.0, "O": 0.5}
-    tab = engine.tables(8)
-    prm = engine.params(8, 5.0, 0.99363, "cosine")
+    tab = engine.tables(2 * lmax)
+    prm = engine.params(2 * lmax, 5.0, 0.99363, "cosine")
     nb = engine.build_neighbors(torch.from_numpy(pos).cuda(), cells, pbc, ptr, 5.0)
     w_nb, w_site = engine.site_weights("SNAP", numbers, symbols, w)
     w_nb, w_site = torch.from_numpy(w_nb).cuda(), torch.from_numpy(w_site).cuda()
@@ -196,7 +197,7 @@ def test_fused_linear_path_matches_unfused_and_oracle(cuda_device):
     assert np.allclose(e4.cpu().numpy(), e_ref1, rtol=1e-12, atol=0)
     for s, st in enumerate(structs):
         a0, a1 = ptr[s], ptr[s + 1]
-        ref = O.forces_virial(st, beta[a0:a1].double().cpu().numpy(), kind="SNAP", lmax=4, rcut=5.0, weights=w,
+        ref = O.forces_virial(st, beta[a0:a1].double().cpu().numpy(), kind="SNAP", lmax=lmax, rcut=5.0, weights=w,
                               rfac0=0.99363)
         assert G.rel_err(x2[a0:a1].cpu().numpy(), ref["x"]) < 2e-5
         assert G.rel_err(f2[a0:a1].cpu().numpy(), ref["forces"]) < 2e-4
