@@ -344,6 +344,8 @@ __global__ void __launch_bounds__(ZW_THREADS, 2) k_zw32(ZLArgs A) {
     if (threadIdx.x == 0) s_unit = 0;
     zw_load_utot(A.utot, A.fmap, a0, A.natoms, A.nh, A.nu, Ub);
     if (MODE == 1 || MODE == 2) {
+        // unrolled: each iteration is a chain of dependent loads (block roles, then beta)
+#pragma unroll 4
         for (int idx = threadIdx.x; idx < 32 * A.nblk; idx += blockDim.x) {
             const int l = idx / A.nblk, b = idx - l * A.nblk;
             const int aa = a0 + l;
