@@ -304,7 +304,9 @@ struct RvBack {
             const float2 *Yr = Y + half_block(L) + mb * (L + 1);
 #pragma unroll
             for (int ma = 0; ma <= L; ++ma) {
-                const float2 y = __ldg(Yr + ma);
+                // the middle row of an even level carries no Y past its centre (not stored)
+                const bool none = (L & 1) == 0 && ma > H && mb == H;
+                const float2 y = none ? make_float2(0.f, 0.f) : __ldg(Yr + ma);
                 su = __ffma2_rn(st[(acc_block(L) + ma) * NT], y, su);
                 g[ma] = __fadd2_rn(g[ma], y);
             }

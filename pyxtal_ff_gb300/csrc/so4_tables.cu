@@ -11,6 +11,7 @@
 #include <string>
 #include <algorithm>
 #include <map>
+#include <tuple>
 #include <utility>
 
 #include "so4_common.cuh"
@@ -347,10 +348,14 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
     // values, so the smaller U is the one stepped) with the K values of U_a in a
     // register ring.  Ca[j][k] = cg(a, ma0 + k + d - lo - j, b, lo + j), 0 outside the
     // ranges, in rows of KP = K rounded up to 4 floats; the Ca table of a
-    // (block, ma0, K) is shared by every row.
+    // (block, ma0, K) is shared by every row.  The middle row of an even level
+    // (2 mb = lam) is cut at its centre: Y weighs its entries ma > lam / 2 by zero and B's
+    // section ends at the centre, so those entries are neither computed nor stored (the
+    // reverse sweep reads them as zero).
     std::vector<int4> wunit_y, wseg_y, wunit_b, wseg_b, wsub;
     std::vector<float> wca;
-    std::map<std::pair<int, int>, int> ca_off;  // (block, ma0) -> offset (K is fixed by lam and ma0)
+    std::map<std::tuple<int, int, int>, int> ca_off;  // (block, ma0, K) -> offset
+    auto row_len = [](int lam, int mb) { return (2 * mb == lam) ? lam / 2 + 1 : lam + 1; };
     auto cg_of = [&](const ZBlk &bk, int m1, int m2) {
         const int cgbase = t->idxcg_block[b3(ld, bk.l1, bk.l2, bk.l)];
         return t->cglist[cgbase + m1 * (bk.l2 + 1) + m2];
@@ -368,20 +373,21 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
     // unit of level lam_k that starts inside the B section, in (mb, ma0) order
     std::vector<int> nbu(ld, 0);
     for (int lam = 0; lam < ld; ++lam) {
-        const int n = lam + 1, ng = (n + ZW_KMAX - 1) / ZW_KMAX;
-        for (int mb = 0; 2 * mb <= lam; ++mb)
+        for (int mb = 0; 2 * mb <= lam; ++mb) {
+            const int n = row_len(lam, mb), ng = (n + ZW_KMAX - 1) / ZW_KMAX;
             for (int g = 0, ma0 = 0; g < ng; ++g) {
                 if (mb * (lam + 1) + ma0 < section_count(lam)) nbu[lam]++;
                 ma0 += n / ng + (g < n % ng ? 1 : 0);
             }
+        }
     }
     std::vector<int> bpos(t->n_b + 1, 0);
     for (int k = 0; k < t->n_b; ++k) bpos[k + 1] = bpos[k] + nbu[bent[k].lam[0]];
     t->n_bsec = bpos[t->n_b];
     for (int lam = 0; lam < ld; ++lam) {
         int bu = 0;  // index of the next B-section unit of this level
-        const int n = lam + 1, ng = (n + ZW_KMAX - 1) / ZW_KMAX;
-        for (int mb = 0; 2 * mb <= lam; ++mb)
+        for (int mb = 0; 2 * mb <= lam; ++mb) {
+            const int n = row_len(lam, mb), ng = (n + ZW_KMAX - 1) / ZW_KMAX;
             for (int g = 0, ma0 = 0; g < ng; ++g) {
                 WUnit u;
                 u.lam = lam;
@@ -404,7 +410,7 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
                     const int lo = std::max(0, u.ma0 + d - a), hi = std::min(b, u.ma0 + K - 1 + d);
                     const int S = hi - lo + 1;
                     if (S <= 0) continue;
-                    auto key = std::make_pair(bi, u.ma0);
+                    auto key = std::make_tuple(bi, u.ma0, K);
                     if (!ca_off.count(key)) {
                         ca_off[key] = (int)wca.size();
                         for (int j = 0; j < S; ++j)
@@ -448,6 +454,7 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
                 if (u.sb1 > u.sb0) wcb.push_back({-costb, (int)wun.size()});
                 wun.push_back(u);
             }
+        }
     }
     // order: by K (largest first), so the warps of a CTA, which take units in list order,
     // mostly run the same K specialisation at a time (fewer instruction-cache misses);
