@@ -65,11 +65,16 @@ def per_image_du(twol):
     return f
 
 
-def per_atom_z(twol):
+def _row_len(l, mb, cut_middle):
+    # the window kernels stop an even level's middle row at its centre
+    return l // 2 + 1 if (cut_middle and 2 * mb == l) else l + 1
+
+
+def per_atom_z(twol, cut_middle=False):
     f = 0
     for (l1, l2, l) in _blocks(twol):
         for mb in range(l // 2 + 1):
-            for ma in range(l + 1):
+            for ma in range(_row_len(l, mb, cut_middle)):
                 ma1min = max(0, (2 * ma - l - l2 + l1) // 2)
                 na = min(l1, (2 * ma - l + l2 + l1) // 2) - ma1min + 1
                 mb1min = max(0, (2 * mb - l - l2 + l1) // 2)
@@ -107,28 +112,44 @@ def per_image_db(twol):
     return f
 
 
-def per_atom_y(twol):
+def per_atom_y(twol, cut_middle=False):
     roles = 0
     for (l1, l2, l) in _blocks(twol):
         if l < l1:
             continue
         roles += 3
-    n = sizes(twol)
+    nz = sum(_row_len(l, mb, cut_middle) for (l1, l2, l) in _blocks(twol) for mb in range(l // 2 + 1))
     # each Y entry gathers one complex scale-add per contributing block entry
-    return 4 * n["n_z"] + 2 * roles
+    return 4 * nz + 2 * roles
+
+
+def per_image_rev(twol):
+    """The reverse-mode per-image contraction: the forward sweep of U, then per row entry
+    of every level the adjoint step (the gradient pairs of conj(a), conj(b): 16 flop; the
+    new adjoint a G - b H: 14) and the Y terms (f and the carry: 6), and the final
+    Jacobian dot products and weights (about 60)."""
+    f = per_image_u(twol)
+    for l in range(1, twol + 1):
+        for mb in range(l // 2 + 1):
+            f += 30 * l + 6 * (l + 1)
+    return f + 60
 
 
 def kernel_flops(twol, natoms, nimg):
-    """Algorithmic flops of one launch of each kernel for a batch."""
+    """Flops of one launch of each kernel for a batch, counted from the algorithm each
+    kernel runs (the window kernels' Z with middle rows cut at the centre, the reverse-mode
+    per-image contraction; an upper bound where the windows also skip the mirrored row
+    pairs of symmetric blocks)."""
     n = sizes(twol)
     u, du, z = per_image_u(twol), per_image_du(twol), per_atom_z(twol)
+    zc = per_atom_z(twol, cut_middle=True)
     utot_img = u + 6 * n["n_half"]
     return {
         "utot32": nimg * utot_img,
-        "linear_by32": natoms * (z + per_atom_b(twol) + per_atom_y(twol)),
-        "forward32": natoms * (z + per_atom_b(twol)) + nimg * utot_img,
-        "adjoint_y32": natoms * (z + per_atom_y(twol)),
-        "adjoint_deidrj32": nimg * (u + du + 16 * n["n_half"] + 24),
+        "linear_by32": natoms * (zc + per_atom_b(twol) + per_atom_y(twol, cut_middle=True)),
+        "forward32": natoms * (zc + per_atom_b(twol)) + nimg * utot_img,
+        "adjoint_y32": natoms * (zc + per_atom_y(twol, cut_middle=True)),
+        "adjoint_deidrj32": nimg * per_image_rev(twol),
         "plain": natoms * (z + per_atom_b(twol)) + nimg * (utot_img + u + du + per_image_db(twol)),
     }
 
