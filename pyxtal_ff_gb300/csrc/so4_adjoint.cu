@@ -684,8 +684,6 @@ __device__ __forceinline__ void group_atom_fv(int a, const int32_t *__restrict__
     for (int q = 0; q < 9; ++q) v[q] = 0.f;
     if (a >= 0) {
         const int m1 = __ldg(img_ptr + a + 1);
-        // a few images per lane: unrolled so their loads (and the reverse images') overlap
-#pragma unroll 4
         for (int m = __ldg(img_ptr + a) + (int)(threadIdx.x & (GSUB - 1)); m < m1; m += GSUB) {
             const float gm[3] = {__ldg(g + 3 * (size_t)m), __ldg(g + 3 * (size_t)m + 1), __ldg(g + 3 * (size_t)m + 2)};
             const float rm[3] = {(float)__ldg(img_r + 3 * (size_t)m), (float)__ldg(img_r + 3 * (size_t)m + 1),
@@ -781,9 +779,7 @@ __global__ void __launch_bounds__(GSS) k_struct_sum(const int *__restrict__ atom
     // chunk partials: thread t < NSLOT * GPART adds component q of chunks c0 + slot, c0 + slot + NSLOT, ...
     const int q = t % GPART, slot = t / GPART;
     if (slot < NSLOT) {
-        // independent loads, one running sum: unrolled so the loads are in flight together
         double acc = 0.0;
-#pragma unroll 8
         for (int c = c0 + slot; c <= c1; c += NSLOT) acc += __ldg(part + (size_t)GPART * c + q);
         red[slot][q] = acc;
     }
