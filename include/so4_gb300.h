@@ -88,7 +88,7 @@ typedef struct {
 int so4_tables_create(int twol, int normalize_u, so4_tables **out);
 int so4_tables_destroy(so4_tables *t);
 /* sizes[0..7] = idxu, idxu_half, idxz, nB, idxcg, number of Z blocks,
- * B-section entries per atom (scratch of so4_linear_by32), flattened Z terms */
+ * B-section entries per atom (scratch of so4_linear_by32), window sub-segments */
 int so4_tables_sizes(const so4_tables *t, int *sizes);
 /* host copies of the reference-visible tables (any pointer may be NULL):
  * cglist[idxcg] f64, idxb[nB*3], idxz[idxz*10], idxu_block[twol+1],

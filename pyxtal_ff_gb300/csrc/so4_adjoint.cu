@@ -60,11 +60,10 @@ int set_smem(K kern, size_t smem) {
 struct FwdArgs {
     so4_params prm;
     float psi_fac, rc32;  // rfac0 pi / rcut and rcut in FP32, set on the host
-    int natoms, nh, nu, nz, nB, nzB;
+    int natoms, nh, nu, nz, nB;
     const double *w_nb, *w_site, *img_r;
     const int32_t *img_ptr, *img_j;
     const float *cg, *rootpq;
-    const ZEnt *zent, *zentB;
     const BEnt *bent;
     SmallTables st;
     const int4 *hmap;  // per half entry: accumulator slot, row, diagonal flag, u_norm F, u_norm
@@ -202,9 +201,8 @@ int launch_utot_rc(const FwdArgs &A, cudaStream_t st) {
 struct ZLArgs {
     int natoms, nh, nu, nB, nblk, nunit;
     const float2 *utot;
-    const int *fmap, *term_ptr;
+    const int *fmap;
     const int4 *unit, *seg;
-    const ZTerm *terms;
     const BEnt *bent;
     const ZBlk *blk;
     const int *yptr, *ylist;
@@ -807,8 +805,6 @@ static ZLArgs zl_args(const so4_tables *t, int natoms) {
     Z.nB = t->n_b;
     Z.nblk = t->n_blk;
     Z.fmap = t->d_fmap;
-    Z.term_ptr = t->d_term_ptr;
-    Z.terms = t->d_terms;
     Z.bent = t->d_b;
     Z.blk = t->d_blk;
     Z.yptr = t->d_yblk_ptr;
@@ -877,9 +873,6 @@ extern "C" int so4_forward32(const so4_tables *t, const so4_params *p, int natom
     A.img_j = d_img_j;
     A.cg = t->d_cg32;
     A.rootpq = t->d_rootpq32;
-    A.zent = t->d_z;
-    A.zentB = t->d_zB;
-    A.nzB = t->n_zB;
     A.bent = t->d_b;
     fill_small_tables(t, A.st);
     A.hmap = t->d_hmap;
@@ -1159,9 +1152,6 @@ extern "C" int so4_utot32(const so4_tables *t, const so4_params *p, int natoms, 
     A.img_j = d_img_j;
     A.cg = t->d_cg32;
     A.rootpq = t->d_rootpq32;
-    A.zent = t->d_z;
-    A.zentB = t->d_zB;
-    A.nzB = t->n_zB;
     A.bent = t->d_b;
     fill_small_tables(t, A.st);
     A.hmap = t->d_hmap;

@@ -86,14 +86,6 @@ struct ZBlk {
     float role_f32[3];  // role_f in FP32 for the FP32 kernels (no FP64 conversion on the device)
 };
 
-// One product term of a Z entry: Z += c * U[i1] * U[i2] with c = cg_a * cg_b
-// and i1, i2 offsets in the full layout (compute_zi's two CG sums, SO4.py:1047-1066,
-// flattened into one list).
-struct ZTerm {
-    float c;
-    unsigned short i1, i2;
-};
-
 struct so4_tables {
     int twol, ldim, normalize_u;
     int n_u, n_half, n_z, n_b, n_cg, n_blk;
@@ -108,15 +100,10 @@ struct so4_tables {
     double *d_rootpq64 = nullptr;  // ldim x ldim
     float *d_rootpq32 = nullptr;
     ZEnt *d_z = nullptr;
-    ZEnt *d_zB = nullptr;       // entries of the blocks B reads (l >= l1)
-    int n_zB = 0;
     BEnt *d_b = nullptr;
     ZBlk *d_blk = nullptr;
     int *d_yblk_ptr = nullptr;  // ldim + 1 : blocks grouped by their third index
     int *d_yblk = nullptr;      // n_blk
-    // flattened Z terms and the work orders of the atoms-across-lanes kernels
-    ZTerm *d_terms = nullptr;
-    int *d_term_ptr = nullptr;  // n_z + 1
     int *d_fmap = nullptr;      // n_u: full entry -> half source | conj << 15 | negate << 14
     // n_half: per half entry (level L, row, ma) {L(L+1)/2 + ma | row << 8 | (ma == row) << 15,
     // bits of u_norm[L] F, bits of u_norm[L], 0}: where the row-chain kernels keep it and how
@@ -143,8 +130,7 @@ struct so4_tables {
     int *d_jpos = nullptr, *d_jbase = nullptr;
     float *d_jfac = nullptr;
     int n_wunit_j = 0, n_jslot = 0;
-    int n_terms = 0;
-    std::vector<int> term_ptr;
+    int n_wsub = 0;  // window sub-segments
 };
 
 // Window Z contractions: most entries per unit, and the zero rows kept before

@@ -85,16 +85,13 @@ void free_device(so4_tables *t) {
     cudaFree(t->d_rootpq64);
     cudaFree(t->d_rootpq32);
     cudaFree(t->d_z);
-    cudaFree(t->d_zB);
     cudaFree(t->d_b);
     cudaFree(t->d_blk);
     cudaFree(t->d_yblk_ptr);
     cudaFree(t->d_yblk);
-    cudaFree(t->d_terms);
     cudaFree(t->d_fmap);
     cudaFree(t->d_hmap);
     cudaFree(t->d_yscale);
-    cudaFree(t->d_term_ptr);
     cudaFree(t->d_bpos);
     cudaFree(t->d_wunit_y);
     cudaFree(t->d_wseg_y);
@@ -295,44 +292,6 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
             rp32[p * ld + q] = (float)rp64[p * ld + q];
         }
     std::vector<float> cg32(t->cglist.begin(), t->cglist.end());
-    std::vector<ZEnt> zentB;
-    for (const ZEnt &z : zent) {
-        const ZBlk &bk = blks[z.blk];
-        if (bk.l >= bk.l1) zentB.push_back(z);
-    }
-    t->n_zB = (int)zentB.size();
-
-    // flattened Z terms (full-layout offsets) and cost-ordered work lists
-    std::vector<ZTerm> terms;
-    t->term_ptr.assign(t->n_z + 1, 0);
-    for (int jz = 0; jz < t->n_z; ++jz) {
-        const int *q = &t->idxz[10 * jz];
-        const int l1 = q[0], l2 = q[1], l = q[2];
-        const int cgbase = t->idxcg_block[b3(ld, l1, l2, l)];
-        t->term_ptr[jz] = (int)terms.size();
-        for (int ib = 0; ib < q[8]; ++ib) {
-            const int mb1 = q[6] + ib, mb2 = q[7] - ib;
-            const double cgb = t->cglist[cgbase + mb1 * (l2 + 1) + mb2];
-            for (int ia = 0; ia < q[5]; ++ia) {
-                const int ma1 = q[3] + ia, ma2 = q[4] - ia;
-                const double cga = t->cglist[cgbase + ma1 * (l2 + 1) + ma2];
-                ZTerm zt;
-                zt.c = (float)(cga * cgb);
-                // offsets pre-scaled by the shared-memory row pitch of the lane-major U layout
-                zt.i1 = (unsigned short)((t->idxu_block[l1] + mb1 * (l1 + 1) + ma1) * 33);
-                zt.i2 = (unsigned short)((t->idxu_block[l2] + mb2 * (l2 + 1) + ma2) * 33);
-                terms.push_back(zt);
-            }
-        }
-        if (terms.size() % 2) {  // even length, so two terms load as one 16-byte word
-            ZTerm pad;
-            pad.c = 0.f;
-            pad.i1 = pad.i2 = 0;
-            terms.push_back(pad);
-        }
-    }
-    t->term_ptr[t->n_z] = (int)terms.size();
-    t->n_terms = (int)terms.size();
     // B component of each block (blocks with l >= l1)
     std::vector<int> blk_k(t->n_blk, -1);
     for (int k = 0; k < t->n_b; ++k)
@@ -483,6 +442,7 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
         }
     }
     t->n_wunit_y = (int)wunit_y.size();
+    t->n_wsub = (int)wsub.size();
     t->n_wunit_b = (int)wunit_b.size();
 
     // JVP lists: the section entries of every level (units starting in the B section) and
@@ -588,8 +548,6 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
     if (!rc) rc = upload(&t->d_fmap, fmap);
     if (!rc) rc = upload(&t->d_hmap, hmap);
     if (!rc) rc = upload(&t->d_yscale, yscale);
-    if (!rc) rc = upload(&t->d_terms, terms);
-    if (!rc) rc = upload(&t->d_term_ptr, t->term_ptr);
     if (!rc) rc = upload(&t->d_bpos, bpos);
     if (!rc) rc = upload(&t->d_wunit_y, wunit_y);
     if (!rc) rc = upload(&t->d_wseg_y, wseg_y);
@@ -607,7 +565,6 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
     if (!rc) rc = upload(&t->d_rootpq64, rp64);
     if (!rc) rc = upload(&t->d_rootpq32, rp32);
     if (!rc) rc = upload(&t->d_z, zent);
-    if (!rc) rc = upload(&t->d_zB, zentB);
     if (!rc) rc = upload(&t->d_b, bent);
     if (!rc) rc = upload(&t->d_blk, blks);
     if (!rc) rc = upload(&t->d_yblk_ptr, yptr);
@@ -637,7 +594,7 @@ extern "C" int so4_tables_sizes(const so4_tables *t, int *s) {
     s[4] = t->n_cg;
     s[5] = t->n_blk;
     s[6] = t->n_bsec;
-    s[7] = t->n_terms;
+    s[7] = t->n_wsub;
     return SO4_OK;
 }
 

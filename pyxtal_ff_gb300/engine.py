@@ -45,7 +45,7 @@ class Tables:
         s = (C.c_int * 8)()
         check(lib().so4_tables_sizes(h, s), "so4_tables_sizes")
         self.twol = int(twol)
-        self.n_u, self.n_half, self.n_z, self.nB, self.n_cg, self.n_blk, self.n_bsec, self.n_terms = [int(v) for v in s]
+        self.n_u, self.n_half, self.n_z, self.nB, self.n_cg, self.n_blk, self.n_bsec, self.n_wsub = [int(v) for v in s]
 
     def export(self):
         ld = self.twol + 1
