@@ -38,7 +38,7 @@ CONFIG = {"workload": "diamond-Si 20x20x10 (32000 atoms), SO4 lmax=4, rcut=5.0 A
 # DRAM bytes (read + write) per full launch of each stage's kernel: twice the figures of
 # the half-size launches (one graph branch each) captured with ncu and summarised in
 # profiles/k_zw32_k_deidrj_rev_k_utot_rc_si32000_lmax4.md (same workload)
-NCU_TRAFFIC = {"utot32": 25.8e6, "linear_by32": 47.2e6, "adjoint_deidrj32": 65.5e6}
+NCU_TRAFFIC = {"utot32": 25.8e6, "linear_by32": 49.5e6, "adjoint_deidrj32": 65.4e6}
 
 
 def workload():
