@@ -258,6 +258,21 @@ int so4_design_struct(int nstruct, int nB, int nelem, const int32_t *d_atom_ptr,
                       const double *d_x, const double *d_rdxdr_atom, const int64_t *d_energy_row,
                       const int64_t *d_stress_row, int64_t ncols, double *d_X, void *stream);
 
+/* The same rows for general features of the nB descriptors (order 2, quadratic SNAP:
+ * polynomialregression.py:488-559): d_feat[nfeat] = (d1, d2) per feature, (a, -1) for x_a,
+ * (d1, d1) for 0.5 x_d1^2, (d1, d2) for x_d1 x_d2; block e spans 1 + nfeat columns.  Force
+ * rows: -sum over the pairs pointing at the atom of d feature(x of the pair's centre) / d r
+ * (one CTA per atom); energy rows: the count and the sums of the features; stress rows:
+ * -sum of d feature along the per-atom Voigt rows. */
+int so4_design_forces_q(int natoms, int nB, int nfeat, int nelem, const int2 *d_feat, const int32_t *d_atom_struct,
+                        const int32_t *d_atom_ptr, const int32_t *d_pair_ptr, const int64_t *d_seq,
+                        const int32_t *d_species, const double *d_x, const double *d_dxdr, const int64_t *d_force_row,
+                        int64_t ncols, double *d_X, int *d_status, void *stream);
+int so4_design_struct_q(int nstruct, int nB, int nfeat, int nelem, const int2 *d_feat, const int32_t *d_atom_ptr,
+                        const int32_t *d_species, const double *d_x, const double *d_rdxdr_atom,
+                        const int64_t *d_energy_row, const int64_t *d_stress_row, int64_t ncols, double *d_X,
+                        void *stream);
+
 /* ------------------------------------------------------------ adjoint path */
 /* Forward (FP32): U_tot per centre in the half layout (d_utot[natoms*idxu_half*2]
  * f32, kept for the adjoint) and B (d_x[natoms*nB] f32).  Scratch:

@@ -101,6 +101,9 @@ def lib():
         "so4_contract_dxdr": (_i, [_i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
         "so4_design_forces": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, C.c_int64, _vp, _vp, _vp]),
         "so4_design_struct": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, C.c_int64, _vp, _vp]),
+        "so4_design_forces_q": (_i, [_i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, C.c_int64, _vp,
+                                     _vp, _vp]),
+        "so4_design_struct_q": (_i, [_i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, C.c_int64, _vp, _vp]),
         "so4_forward32_workspace_size": (_sz, [_vp, _i]),
         "so4_forward32": (_i, [_vp, C.POINTER(Params), _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
         "so4_adjoint_workspace_size": (_sz, [_vp, _i, _i64]),

@@ -287,7 +287,168 @@ __global__ void __launch_bounds__(DS) k_design_struct(int nB, const int32_t *ato
         }
 }
 
+// ---------------------------------------------------------------- quadratic features
+// Order 2 (polynomialregression.py:488-559): the features of descriptors x (length d) are
+// x_a (a < d), then for each d1 the square 0.5 x_d1^2 followed by the products
+// x_d1 x_d2 (d2 > d1).  feat[f] = (d1, d2): (a, -1) linear, (d1, d1) square, else product.
+// Their derivative along any descriptor derivative t (dxdr or rdxdr row) is t_a,
+// x_d1 t_d1, or x_d2 t_d1 + x_d1 t_d2, with x the centre atom's descriptors.
+__device__ __forceinline__ double qfeat_d(int2 f, const double *x, const double *t, int stride) {
+    if (f.y < 0) return t[stride * f.x];
+    if (f.x == f.y) return x[f.x] * t[stride * f.x];
+    return fma(x[f.y], t[stride * f.x], x[f.x] * t[stride * f.y]);
+}
+__device__ __forceinline__ double qfeat(int2 f, const double *x) {
+    if (f.y < 0) return x[f.x];
+    if (f.x == f.y) return 0.5 * x[f.x] * x[f.x];
+    return x[f.x] * x[f.y];
+}
+
+// Force rows for general features, one CTA per target atom m: for each pair p pointing
+// at m (the reverse of m's own pairs, in ascending source order), the pair's dxdr and the
+// source's descriptors are staged in shared memory and every thread adds, for the
+// outputs (element, feature, component) it owns, -d feature / d r of that source.
+constexpr int QT = 256, QMAXO = 16;  // threads; outputs per thread per pass
+__global__ void __launch_bounds__(QT) k_design_forces_q(int nB, int nfeat, int nelem, const int2 *feat,
+                                                       const int32_t *astruct, const int32_t *atom_ptr,
+                                                       const int32_t *pair_ptr, const int64_t *seq,
+                                                       const int32_t *species, const double *x,
+                                                       const double *dxdr, const int64_t *force_row,
+                                                       int64_t ncols, double *X, int *status) {
+    extern __shared__ double qsm[];  // dxdr row [3 nB], source descriptors [nB]
+    double *sd = qsm, *sx = qsm + 3 * nB;
+    __shared__ int s_p, s_e;
+    const int m = blockIdx.x, t = threadIdx.x;
+    const int s = astruct[m], base = atom_ptr[s];
+    const int64_t ml = m - base;
+    const int q0 = pair_ptr[m], q1 = pair_ptr[m + 1];
+    const int nout = nelem * nfeat * 3;
+    for (int o0 = 0; o0 < nout; o0 += QT * QMAXO) {
+        double acc[QMAXO];
+#pragma unroll
+        for (int k = 0; k < QMAXO; ++k) acc[k] = 0.0;
+        for (int q = q0; q < q1; ++q) {
+            if (t == 0) {
+                const int j = base + (int)seq[2 * (size_t)q + 1];
+                int p = -1, lo = pair_ptr[j], hi = pair_ptr[j + 1] - 1;
+                while (lo <= hi) {
+                    const int mid = (lo + hi) >> 1;
+                    const int64_t v = seq[2 * (size_t)mid + 1];
+                    if (v < ml) {
+                        lo = mid + 1;
+                    } else if (v > ml) {
+                        hi = mid - 1;
+                    } else {
+                        p = mid;
+                        break;
+                    }
+                }
+                const int e = species[j];
+                if (p < 0) atomicOr(status, 1 << SO4_ERR_REVERSE);
+                if (e < 0 || e >= nelem) {
+                    atomicOr(status, 1 << SO4_ERR_ARG);
+                    p = -1;
+                }
+                s_p = p;
+                s_e = e;
+            }
+            __syncthreads();
+            const int pp = s_p, ee = s_e;
+            if (pp >= 0) {
+                const int j = base + (int)seq[2 * (size_t)q + 1];
+                for (int i = t; i < 3 * nB; i += QT) sd[i] = dxdr[(size_t)pp * 3 * nB + i];
+                for (int i = t; i < nB; i += QT) sx[i] = x[(size_t)j * nB + i];
+            }
+            __syncthreads();
+            if (pp >= 0) {
+#pragma unroll
+                for (int k = 0; k < QMAXO; ++k) {
+                    const int o = o0 + t + QT * k;
+                    if (o < nout) {
+                        const int c = o % 3, f = (o / 3) % nfeat, e = o / (3 * nfeat);
+                        if (e == ee) acc[k] -= qfeat_d(__ldg(feat + f), sx, sd + c, 3);
+                    }
+                }
+            }
+            __syncthreads();
+        }
+        const int64_t row0 = force_row[s] + 3 * ml;
+#pragma unroll
+        for (int k = 0; k < QMAXO; ++k) {
+            const int o = o0 + t + QT * k;
+            if (o < nout) {
+                const int c = o % 3, f = (o / 3) % nfeat, e = o / (3 * nfeat);
+                X[(row0 + c) * ncols + (int64_t)e * (1 + nfeat) + 1 + f] = acc[k];
+            }
+        }
+    }
+}
+
+// Energy and stress rows for general features, one CTA per (structure, element): the energy
+// row gets the atom count and the sums of the features; the stress rows the sums of
+// -d feature along the per-atom Voigt rows.
+__global__ void __launch_bounds__(DS) k_design_struct_q(int nB, int nfeat, const int2 *feat,
+                                                        const int32_t *atom_ptr, const int32_t *species,
+                                                        const double *x, const double *rdxdr,
+                                                        const int64_t *energy_row, const int64_t *stress_row,
+                                                        int64_t ncols, double *X) {
+    const int s = blockIdx.x, e = blockIdx.y;
+    const int a0 = atom_ptr[s], a1 = atom_ptr[s + 1];
+    const int64_t col0 = (int64_t)e * (1 + nfeat);
+    const int64_t er = energy_row[s], sr = stress_row ? stress_row[s] : -1;
+    if (er >= 0)
+        for (int col = threadIdx.x; col <= nfeat; col += DS) {
+            double v = 0.0;
+            for (int i = a0; i < a1; ++i)
+                if (species[i] == e) v += (col == 0) ? 1.0 : qfeat(__ldg(feat + col - 1), x + (size_t)i * nB);
+            X[er * ncols + col0 + col] = v;
+        }
+    if (sr >= 0 && rdxdr)
+        for (int o = threadIdx.x; o < 6 * nfeat; o += DS) {
+            const int f = o / 6, v = o - 6 * f;
+            double acc = 0.0;
+            for (int i = a0; i < a1; ++i)
+                if (species[i] == e)
+                    acc -= qfeat_d(__ldg(feat + f), x + (size_t)i * nB, rdxdr + (size_t)i * 6 * nB + v, 6);
+            X[(sr + v) * ncols + col0 + 1 + f] = acc;
+        }
+}
+
 }  // namespace
+
+extern "C" int so4_design_forces_q(int natoms, int nB, int nfeat, int nelem, const int2 *d_feat,
+                                   const int32_t *d_atom_struct, const int32_t *d_atom_ptr, const int32_t *d_pair_ptr,
+                                   const int64_t *d_seq, const int32_t *d_species, const double *d_x,
+                                   const double *d_dxdr, const int64_t *d_force_row, int64_t ncols, double *d_X,
+                                   int *d_status, void *stream) {
+    if (natoms < 0 || nB <= 0 || nfeat <= 0 || nelem <= 0 || ncols < (int64_t)nelem * (1 + nfeat)) return SO4_ERR_ARG;
+    if (natoms == 0) return SO4_OK;
+    if (!d_feat || !d_atom_struct || !d_atom_ptr || !d_pair_ptr || !d_seq || !d_species || !d_x || !d_dxdr ||
+        !d_force_row || !d_X || !d_status)
+        return SO4_ERR_ARG;
+    const size_t smem = sizeof(double) * 4 * (size_t)nB;
+    if (smem > 48 * 1024) return SO4_ERR_UNSUPPORTED;
+    k_design_forces_q<<<natoms, QT, smem, (cudaStream_t)stream>>>(nB, nfeat, nelem, d_feat, d_atom_struct, d_atom_ptr,
+                                                                  d_pair_ptr, d_seq, d_species, d_x, d_dxdr,
+                                                                  d_force_row, ncols, d_X, d_status);
+    so4_count_launch();
+    return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
+}
+
+extern "C" int so4_design_struct_q(int nstruct, int nB, int nfeat, int nelem, const int2 *d_feat,
+                                   const int32_t *d_atom_ptr, const int32_t *d_species, const double *d_x,
+                                   const double *d_rdxdr_atom, const int64_t *d_energy_row,
+                                   const int64_t *d_stress_row, int64_t ncols, double *d_X, void *stream) {
+    if (nstruct < 0 || nB <= 0 || nfeat <= 0 || nelem <= 0 || ncols < (int64_t)nelem * (1 + nfeat)) return SO4_ERR_ARG;
+    if (nstruct == 0) return SO4_OK;
+    if (!d_feat || !d_atom_ptr || !d_species || !d_x || !d_energy_row || !d_X || (d_stress_row && !d_rdxdr_atom))
+        return SO4_ERR_ARG;
+    k_design_struct_q<<<dim3(nstruct, nelem), DS, 0, (cudaStream_t)stream>>>(nB, nfeat, d_feat, d_atom_ptr, d_species,
+                                                                             d_x, d_rdxdr_atom, d_energy_row,
+                                                                             d_stress_row, ncols, d_X);
+    so4_count_launch();
+    return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
+}
 
 extern "C" int so4_design_forces(int natoms, int nB, int nelem, const int32_t *d_atom_struct,
                                  const int32_t *d_atom_ptr, const int32_t *d_pair_ptr, const int64_t *d_seq,

@@ -403,6 +403,29 @@ def design_struct(X, ncols, nB, nelem, species, atom_ptr, x, rdxdr_atom, energy_
           "so4_design_struct")
 
 
+def design_forces_q(X, ncols, nB, feat, nelem, species, pair_ptr, seq, atom_struct, atom_ptr, x, dxdr, force_row):
+    """Force rows of the design matrix for the features feat (F, 2) i32 (so4_design_forces_q)."""
+    natoms = int(species.numel())
+    status = torch.zeros(1, dtype=torch.int32, device=X.device)
+    check(lib().so4_design_forces_q(natoms, nB, int(feat.shape[0]), nelem, _ptr(feat), _ptr(atom_struct),
+                                    _ptr(atom_ptr), _ptr(pair_ptr), _ptr(seq), _ptr(species), _ptr(x), _ptr(dxdr),
+                                    _ptr(force_row), int(ncols), _ptr(X), _ptr(status), _stream()),
+          "so4_design_forces_q")
+    bits = int(status.item())
+    if bits & (1 << _lib.SO4_ERR_REVERSE):
+        raise ValueError("so4_design_forces_q: a pair has no reverse pair (the pair list is not symmetric)")
+    if bits & (1 << _lib.SO4_ERR_ARG):
+        raise ValueError("so4_design_forces_q: an element index is out of range")
+
+
+def design_struct_q(X, ncols, nB, feat, nelem, species, atom_ptr, x, rdxdr_atom, energy_row, stress_row):
+    """Energy and stress rows per structure for the features feat (so4_design_struct_q)."""
+    nstruct = int(atom_ptr.numel()) - 1
+    check(lib().so4_design_struct_q(nstruct, nB, int(feat.shape[0]), nelem, _ptr(feat), _ptr(atom_ptr), _ptr(species),
+                                    _ptr(x), _ptr(rdxdr_atom), _ptr(energy_row), _ptr(stress_row), int(ncols),
+                                    _ptr(X), _stream()), "so4_design_struct_q")
+
+
 def forward32(tab, prm, nb: Neighbors, w_nb, w_site):
     """FP32 B (N,nB) and U_tot (N, n_half, 2) for the adjoint."""
     dev = w_nb.device

@@ -13,8 +13,11 @@ weighted, optionally L2/L1-regularised least squares (:240-260) on the GPU;
 The force and stress rows, which the reference fills with one np.where over all
 pairs per atom, come from so4_design_forces (one warp per target atom over its
 reverse pairs, per source element) and so4_design_struct; the per-atom energy rows
-of train=False are plain copies.  Order 2 (quadratic SNAP) is not on this path:
-constructing it raises NotImplementedError.
+of train=False are plain copies.  Order 2 (quadratic SNAP, :488-559) uses the features
+x_a, then per d1 the square 0.5 x_d1^2 and the products x_d1 x_d2 (d2 > d1) of the first
+d_max descriptors, with the force and stress rows from so4_design_forces_q and
+so4_design_struct_q (the derivative of a feature along a pair's dxdr uses the pair's
+centre descriptors, as the reference's does).
 """
 from __future__ import annotations
 
@@ -29,13 +32,11 @@ EV2GPA = 160.21766
 class PolynomialRegressionPotential:
     def __init__(self, elements, coef_=None, order=1, d_max=None, path="", force_coefficient=None,
                  stress_coefficient=None, stress_group=None, alpha=None, norm=2, device="cuda"):
-        if order == 2:
-            raise NotImplementedError("order 2 (quadratic) is not on this path")
-        if order != 1:
+        if order not in (1, 2):
             raise ValueError("Order must be 1 or 2")
         self.elements = sorted(elements)
         self.order = order
-        self.quadratic = False
+        self.quadratic = order == 2
         self.coef_ = None if coef_ is None else np.asarray(coef_, dtype=np.float64)
         self.d_max = d_max
         self.path = path
@@ -48,6 +49,17 @@ class PolynomialRegressionPotential:
         self.device = torch.device(device)
 
     # ------------------------------------------------------------ design matrix
+    @staticmethod
+    def features(d, quadratic):
+        """(F, 2) int32 feature table in the reference's column order: (a, -1) for x_a, then
+        per d1 (d1, d1) for 0.5 x_d1^2 and (d1, d2) for x_d1 x_d2, d2 > d1."""
+        f = [(a, -1) for a in range(d)]
+        if quadratic:
+            for d1 in range(d):
+                f.append((d1, d1))
+                f.extend((d1, d2) for d2 in range(d1 + 1, d))
+        return np.asarray(f, dtype=np.int32)
+
     def _stack(self, descs, d_max):
         """Concatenate structures on the device: x (N, d), dxdr (P, d, 3), seq (P, 2) local,
         rdxdr (N, d, 6), species (N,), atom / pair pointers."""
@@ -87,7 +99,9 @@ class PolynomialRegressionPotential:
             self.d_max = len(np.asarray(descs[0]["x"])[0])
         d = self.d_max
         ne = len(self.elements)
-        ncols = (1 + d) * ne
+        feat_np = self.features(d, self.quadratic)
+        nf = len(feat_np)
+        ncols = (1 + nf) * ne
         S = len(descs)
         st = self._stack(descs, d)
         nat = [int(np.asarray(dd["x"]).shape[0]) for dd in descs]
@@ -106,25 +120,40 @@ class PolynomialRegressionPotential:
         dev = self.device
         X = torch.zeros((r, ncols), dtype=torch.float64, device=dev)
         t64 = lambda v: torch.tensor(v, dtype=torch.int64, device=dev)  # noqa: E731
-        if not train:  # one energy row per atom: [1, x_i] in the atom's element block
+        feat = torch.from_numpy(feat_np).to(dev)
+        if not train:  # one energy row per atom: [1, features(x_i)] in the atom's element block
             if S != 1:
                 raise ValueError("train=False takes one structure")
             rows = torch.arange(nat[0], device=dev)
-            c0 = st["species"].long() * (1 + d)
+            c0 = st["species"].long() * (1 + nf)
             X[rows, c0] = 1.0
-            X[rows[:, None], c0[:, None] + 1 + torch.arange(d, device=dev)] = st["x"]
+            xv = st["x"]
+            f1, f2 = feat[:, 0].long(), feat[:, 1].long()
+            sq = (f2 == f1).to(xv.dtype)
+            quad = xv[:, f1] * xv[:, f2.clamp(min=0)] * (1.0 - 0.5 * sq)
+            vals = torch.where((f2 < 0)[None, :], xv[:, f1], quad)
+            X[rows[:, None], c0[:, None] + 1 + torch.arange(nf, device=dev)] = vals
         if fc and nat and sum(nat):
             if "dxdr" not in st:
                 raise ValueError("fc=True needs dxdr and seq")
-            engine.design_forces(X, ncols, d, ne, st["species"], st["pair_ptr"], st["seq"], st["atom_struct"],
-                                 st["atom_ptr"], st["dxdr"], t64(force_row))
+            if self.quadratic:
+                engine.design_forces_q(X, ncols, d, feat, ne, st["species"], st["pair_ptr"], st["seq"],
+                                       st["atom_struct"], st["atom_ptr"], st["x"], st["dxdr"], t64(force_row))
+            else:
+                engine.design_forces(X, ncols, d, ne, st["species"], st["pair_ptr"], st["seq"], st["atom_struct"],
+                                     st["atom_ptr"], st["dxdr"], t64(force_row))
         want_s = any(v >= 0 for v in stress_row)
         if train or want_s:
             if want_s and "rdxdr" not in st:
                 raise ValueError("sc=True needs per-atom rdxdr")
-            engine.design_struct(X, ncols, d, ne, st["species"], st["atom_ptr"], st["x"],
-                                 st.get("rdxdr") if want_s else None, t64(energy_row),
-                                 t64(stress_row) if want_s else None, )
+            rd = st.get("rdxdr") if want_s else None
+            srow = t64(stress_row) if want_s else None
+            if self.quadratic:
+                engine.design_struct_q(X, ncols, d, feat, ne, st["species"], st["atom_ptr"], st["x"], rd,
+                                       t64(energy_row), srow)
+            else:
+                engine.design_struct(X, ncols, d, ne, st["species"], st["atom_ptr"], st["x"], rd, t64(energy_row),
+                                     srow)
         return X
 
     def parse_descriptors(self, data, fc=True, sc=False, train=True):

@@ -6,7 +6,8 @@ tests/golden/nn_*.npz (which the reference's SNAP code computed):
   case, with the random coefficients stored there (pr_coef);
 - parse_descriptors(train=True) over a two-structure database (the NaCl and Si16
   cases, elements Cl, Na, Si; only the second in the stress group), written with the
-  standard-library shelve module as the reference reads it.
+  standard-library shelve module as the reference reads it;
+- the same for order 2 (quadratic features of the first d_max descriptors).
 
 Runs in the build container only (the reference tree must be readable); stand-ins as
 in make_golden_nn.py.
@@ -51,6 +52,21 @@ def main():
         key = name[3:]
         out[key + "_X"], out[key + "_energies"], out[key + "_forces"], out[key + "_stress"] = X, e, f, s
         print(key, X.shape, e.sum(), flush=True)
+    # order 2 (quadratic): the same per case, on the first few descriptors (d_max) so the
+    # fixture stays small, with random coefficients
+    for name, dmax in (("nn_nacl_snap", 6), ("nn_si16_snap", 5), ("nn_si432_snap", 5)):
+        d, desc = _desc(name)
+        pr = prmod.PR.__new__(prmod.PR)
+        pr.elements = sorted(set(desc["elements"]))
+        pr.quadratic, pr.d_max = True, dmax
+        nq = (dmax * dmax + 3 * dmax) // 2
+        pr.coef_ = np.random.default_rng(7).normal(size=len(pr.elements) * (1 + nq))
+        X = pr.parse_descriptors({"0": desc}, fc=True, sc=True, train=False)
+        e, f, s_ = pr.calculate_properties(desc, bforce=True, bstress=True)
+        key = "quad_" + name[3:]
+        out[key + "_X"], out[key + "_energies"], out[key + "_forces"], out[key + "_stress"] = X, e, f, s_
+        out[key + "_coef"], out[key + "_dmax"] = pr.coef_, np.int64(dmax)
+        print(key, X.shape, flush=True)
     # training matrix over two structures
     with tempfile.TemporaryDirectory() as tmp:
         db = shelve.open(os.path.join(tmp, "train"))
@@ -68,6 +84,10 @@ def main():
         X = pr.parse_descriptors("train", fc=True, sc=True, train=True)
         out["train_X"] = X
         print("train", X.shape, flush=True)
+        pr.quadratic, pr.d_max = True, 6
+        X = pr.parse_descriptors("train", fc=True, sc=True, train=True)
+        out["quad_train_X"] = X
+        print("quad train", X.shape, flush=True)
     np.savez_compressed(os.path.join(HERE, "pr_design.npz"), **out)
 
 

@@ -69,3 +69,33 @@ def test_linear_regression_matches_numpy(cuda_device):
             ref = np.linalg.lstsq(Xw.T @ Xw, Xw.T @ yw - alpha, rcond=None)[0]
         # the fitted values agree (X is rank deficient: both are minimum-norm solutions)
         assert G.rel_err(X @ got, X @ ref) < 1e-8
+
+
+@pytest.mark.parametrize("name", G.nn_names())
+def test_quadratic_predict_design_matrix_and_properties(cuda_device, name):
+    d, desc = _desc(name)
+    key = "quad_" + name[3:]
+    dmax = int(PR[key + "_dmax"])
+    pot = PolynomialRegressionPotential(sorted(set(desc["elements"])), coef_=PR[key + "_coef"], order=2, d_max=dmax)
+    X = pot.parse_descriptors({"0": desc}, fc=True, sc=True, train=False)
+    ref = PR[key + "_X"]
+    assert X.shape == ref.shape
+    assert G.rel_err(X, ref) < 1e-13, G.rel_err(X, ref)
+    e, f, s = pot.calculate_properties(desc, bforce=True, bstress=True)
+    assert G.rel_err(e, PR[key + "_energies"]) < 1e-12
+    assert G.rel_err(f, PR[key + "_forces"]) < 1e-12
+    assert G.rel_err(s, PR[key + "_stress"]) < 1e-12
+
+
+def test_quadratic_training_design_matrix(cuda_device):
+    data = {}
+    for i, (name, group) in enumerate((("nn_nacl_snap", "A"), ("nn_si16_snap", "B"))):
+        _, desc = _desc(name)
+        desc["group"] = group
+        data[str(i)] = desc
+    pot = PolynomialRegressionPotential(["Cl", "Na", "Si"], order=2, d_max=6, stress_group=["B"])
+    X = pot.parse_descriptors(data, fc=True, sc=True, train=True)
+    ref = PR["quad_train_X"]
+    assert X.shape == ref.shape
+    assert G.rel_err(X, ref) < 1e-13, G.rel_err(X, ref)
+
