@@ -1,4 +1,4 @@
-"""The reference's linear (polynomial order 1) potential, with its design matrix built
+"""The reference's polynomial (order 1 and 2) potential, with its design matrix built
 on the GPU.
 
 ``PolynomialRegressionPotential`` mirrors pyxtal_ff/models/polynomialregression.py
