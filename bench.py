@@ -454,7 +454,7 @@ def main():
     # ---- roofline of the dominant kernel (live CUDA events of the timed region)
     nb = calc.neighbors(batch, pos_dev)
     kf = flops.kernel_flops(2 * LMAX, nb.natoms, nb.nimg)     # the work the kernels' own algorithm does
-    ks = flops.survey_flops(2 * LMAX, nb.natoms, nb.nimg)     # the reference algorithm's tabulated work
+    ks = flops.tabulated_flops(2 * LMAX, nb.natoms, nb.nimg)     # the reference algorithm's tabulated work
     peaks = measured_peaks(torch)
     i_dom = int(np.argmax(stage_ms))
     dom = stage_names[i_dom]

@@ -157,17 +157,17 @@ def kernel_flops(twol, natoms, nimg):
 # Per-unit algorithmic work of the reference's algorithm as tabulated for this path
 # (U, dU, dudr, dB/dr and virial per neighbour image; Z, B and the adjoint per atom),
 # for lmax 3 and 4: the figures a launch's roofline is quoted against.
-SURVEY_UNITS = {
+TABULATED_UNITS = {
     6: dict(U=1240, dU=6696, dudr=4200, dB=24816, virial=1080, Z=98076, B=3824, adj_img=12600, adj_atom=200000),
     8: dict(U=2600, dU=14040, dudr=8550, dB=72072, virial=1980, Z=455702, B=11304, adj_img=27000, adj_atom=900000),
 }
 
 
-def survey_flops(twol, natoms, nimg):
+def tabulated_flops(twol, natoms, nimg):
     """Algorithmic flops of one launch of each stage from the tabulated per-unit work
     (None where the table has no entry for this twol): U_tot per image; Z + Y (+ B) per
     atom; the adjoint per image; the plain path's full per-image and per-atom work."""
-    t = SURVEY_UNITS.get(int(twol))
+    t = TABULATED_UNITS.get(int(twol))
     if t is None:
         return None
     return {

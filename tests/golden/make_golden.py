@@ -180,8 +180,8 @@ def _cases():
     c.append(("sio2_24_lmax4_snap", sio2, dict(kind="SNAP", lmax=4, rcut=5.0, weights={"Si": 1.0, "O": 0.5},
                                                rfac0=0.99363, big=True)))
     cfg0 = S.diamond_si(2, 2, 2, sigma=0.05, rng=np.random.default_rng(0))
-    c.append(("config0_w1", cfg0, dict(kind="SNAP", lmax=3, rcut=4.9, weights={"Si": 1.0}, rfac0=1.0, big=True)))
-    c.append(("config0_so4", cfg0, dict(kind="SO4", lmax=3, rcut=4.9, big=True)))
+    c.append(("si64_lmax3_snap_w1", cfg0, dict(kind="SNAP", lmax=3, rcut=4.9, weights={"Si": 1.0}, rfac0=1.0, big=True)))
+    c.append(("si64_lmax3_so4", cfg0, dict(kind="SO4", lmax=3, rcut=4.9, big=True)))
     return c
 
 

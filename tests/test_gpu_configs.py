@@ -1,12 +1,12 @@
-"""The survey's batched / autograd configurations at full size on the GPU.
+"""The batched and autograd workloads at full size on the GPU.
 
-config 1: 256 Si supercells (n_i in {1,2,3}, strain U(-0.03,0.03), sigma 0.08, seed 1),
-          lmax 3, rcut 4.9: FP32 plain x/dxdr/rdxdr vs the FP64 plain path of the same
-          batch (which is itself checked against the oracle at 1e-10), errors reported;
-          four structures also against the oracle.
-config 2: SiO2 648 atoms (2.2 g/cm^3, seed 2), lmax 4, rcut 5.0, weights Si 1.0 / O 0.5,
-          per-species MLP 2x16 tanh (Xavier, seed 3): autograd forces vs central finite
-          differences (h = 1e-4 A, FP64 energies) on 20 atoms and vs the FP64 dxdr . dE/dB.
+- 256 Si supercells (n_i in {1,2,3}, strain U(-0.03,0.03), sigma 0.08, seed 1), lmax 3,
+  rcut 4.9: FP32 plain x/dxdr/rdxdr vs the FP64 plain path of the same batch (which is
+  itself checked against the oracle at 1e-10), errors reported; four structures also
+  against the oracle.
+- SiO2 648 atoms (2.2 g/cm^3, seed 2), lmax 4, rcut 5.0, weights Si 1.0 / O 0.5,
+  per-species MLP 2x16 tanh (Xavier, seed 3): autograd forces vs central finite
+  differences (h = 1e-4 A, FP64 energies) on 20 atoms and vs the FP64 dxdr . dE/dB.
 """
 import numpy as np
 import pytest
@@ -21,7 +21,7 @@ from tests import goldens as G
 pytestmark = pytest.mark.gpu
 
 
-def test_config1_batched_fp32_plain(cuda_device):
+def test_256_si_supercells_batched_fp32_plain(cuda_device):
     structs = S.si_batch(256, seed=1, sizes=(1, 2, 3), strain=0.03, sigma=0.08)
     batch = Batch(structs)
     calc = SO4Calculator(lmax=3, rcut=4.9, kind="SNAP", weights={"Si": 1.0}, rfac0=1.0)
@@ -30,7 +30,7 @@ def test_config1_batched_fp32_plain(cuda_device):
     ex = G.rel_err(d32["x"].cpu().numpy(), d64["x"].cpu().numpy())
     ed = G.rel_err(d32["dxdr"].cpu().numpy(), d64["dxdr"].cpu().numpy())
     er = G.rel_err(d32["rdxdr"].cpu().numpy(), d64["rdxdr"].cpu().numpy())
-    print("config1 atoms", batch.natoms, "pairs", d64["seq"].shape[0], "rel err x %.2e dxdr %.2e rdxdr %.2e" % (ex, ed, er))
+    print("batched atoms", batch.natoms, "pairs", d64["seq"].shape[0], "rel err x %.2e dxdr %.2e rdxdr %.2e" % (ex, ed, er))
     assert ex < 2e-5 and ed < 2e-4 and er < 2e-4
     pptr = d64["pair_ptr"].cpu().numpy()
     for s in (0, 17, 100, 255):
@@ -65,7 +65,7 @@ class SpeciesMLP(torch.nn.Module):
         return out
 
 
-def test_config2_sio2_autograd_forces(cuda_device):
+def test_sio2_648_autograd_forces(cuda_device):
     atoms = S.sio2_random(n_si=216, density=2.2, dmin=1.4, seed=2)
     w = {"Si": 1.0, "O": 0.5}
     batch = Batch([atoms], species_order=["O", "Si"])
@@ -108,6 +108,6 @@ def test_config2_sio2_autograd_forces(cuda_device):
     c = contract_plain(d["x"], d["dxdr"], d["rdxdr"], d["seq"], d["pair_ptr"], batch.atom_ptr, beta64, batch.volumes)
     err_dx = float(np.abs(c["forces"].cpu().numpy() - F_auto).max())
     fmax = float(np.abs(F_auto).max())
-    print("config2 max|F| %.3f eV/A, FD err %.2e, dxdr.beta err %.2e" % (fmax, err_fd, err_dx))
+    print("SiO2 max|F| %.3f eV/A, FD err %.2e, dxdr.beta err %.2e" % (fmax, err_fd, err_dx))
     assert err_dx <= 1e-4 * max(1.0, fmax)
     assert err_fd <= 1e-3 * max(1.0, fmax)

@@ -1,4 +1,4 @@
-"""Force matching on the adjoint path (the survey's config 3).
+"""Force matching on the adjoint path (512 Si structures of 8-64 atoms, lmax 3).
 
 - The gradient of the training loss w.r.t. the model weights, computed with the
   adjoint forces and the JVP backward (FP32 kernels), matches the same loss built
@@ -62,11 +62,11 @@ def test_training_gradient_matches_fp64_plain_path(cuda_device):
         assert err < 1e-3, err
 
 
-def test_config3_full_step_runs_and_loss_decreases(cuda_device):
+def test_512_structure_training_step_runs_and_loss_decreases(cuda_device):
     structs = _structs(512, 4)
     fm = ForceMatching(structs, lmax=3, rcut=4.9, seed=4, lr=3e-3)
     losses = [fm.step().item() for _ in range(5)]
-    print("config3 atoms", fm.batch.natoms, "losses", ["%.4g" % v for v in losses])
+    print("training atoms", fm.batch.natoms, "losses", ["%.4g" % v for v in losses])
     assert np.all(np.isfinite(losses)) and losses[-1] < losses[0]
 
 

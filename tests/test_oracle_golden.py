@@ -36,7 +36,7 @@ def test_oracle_matches_reference(name):
     print(name, errs)
 
 
-def test_sizes_match_survey_counts():
+def test_sizes_match_reference_loop_counts():
     # idxu / idxz / idxcg / nB for lmax 3 and 4, counted from the reference's loops
     assert O.sizes(6) == dict(idxu=140, idxz=779, idxcg=1321, nB=30, idxu_half=78)
     assert O.sizes(8) == dict(idxu=285, idxz=2386, idxcg=4098, nB=55, idxu_half=155)
