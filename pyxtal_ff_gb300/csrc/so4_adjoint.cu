@@ -201,14 +201,14 @@ int launch_utot_rc(const FwdArgs &A, cudaStream_t st) {
 struct ZLArgs {
     int natoms, nh, nu, nB, nblk, nunit;
     const float2 *utot;
-    const int *fmap;
+    const int2 *hfull;
     const int4 *unit, *seg;
     const BEnt *bent;
     const ZBlk *blk;
     const int *yptr, *ylist;
     const float *beta;
     const int *bpos;  // nB + 1: first B partial slot of each component
-    int nbsec;
+    int nbsec;  // slots of the B partial (MODE 0, 2) or JVP (MODE 3) scratch
     SmallTables st;
     float *x;    // B out  (k_zb32, k_zby32)
     float2 *Y;   // Y out  (k_zy32, k_zby32)
@@ -261,11 +261,25 @@ __device__ __forceinline__ void zw_unit(const ZLArgs &A, const int4 un, const fl
         float2 z[K];
 #pragma unroll
         for (int k = 0; k < K; ++k) z[k] = make_float2(0.f, 0.f);
-        int4 hdn = (sg.x < sg.y) ? __ldg(A.wsub + sg.x) : make_int4(0, 0, 0, 0);
-        for (int r = sg.x; r < sg.y; ++r) {
-            const int4 hd = hdn;
-            if (r + 1 < sg.y) hdn = __ldg(A.wsub + r + 1);
-            zw_rows<K>(Ul, hd, ca, z);
+        // rows two at a time (they share the Ca table and S), the odd one alone; the two
+        // register rings fit without spills up to K = ZW_KPAIR
+        int r = sg.x;
+        int4 h1 = (r < sg.y) ? __ldg(A.wsub + r) : make_int4(0, 0, 0, 0);
+        if (K <= ZW_KPAIR) {
+            int4 h2 = (r + 1 < sg.y) ? __ldg(A.wsub + r + 1) : make_int4(0, 0, 0, 0);
+            for (; r + 1 < sg.y; r += 2) {
+                const int4 c1 = h1, c2 = h2;
+                if (r + 2 < sg.y) h1 = __ldg(A.wsub + r + 2);
+                if (r + 3 < sg.y) h2 = __ldg(A.wsub + r + 3);
+                zw_rows2<K>(Ul, c1, c2, ca, z);
+            }
+            if (r < sg.y) zw_rows<K>(Ul, h1, ca, z);
+        } else {
+            for (; r < sg.y; ++r) {
+                const int4 hd = h1;
+                if (r + 1 < sg.y) h1 = __ldg(A.wsub + r + 1);
+                zw_rows<K>(Ul, hd, ca, z);
+            }
         }
         if (MODE == 3) {
             // sum_e w_e Re(conj(dU[e]) Z[e]) over the unit's section entries, once per role of
@@ -322,7 +336,6 @@ __device__ __forceinline__ void zw_unit(const ZLArgs &A, const int4 un, const fl
     }
 }
 
-constexpr int ZW_THREADS = 256;  // 8 warps share one CTA's 32 atoms
 
 // Window form of k_zb32 / k_zy32 / k_zby32 (so4_zwin.cuh), 32 atoms per CTA.
 // MODE 0: B only (units of the B sections, B blocks only); 1: Y only; 2: Y and,
@@ -340,30 +353,73 @@ __global__ void __launch_bounds__(ZW_THREADS, 2) k_zw32(ZLArgs A) {
     float2 *Ub = zw_smem;
     float *coef = (float *)(Ub + (size_t)(A.nu + 2 * ZW_PAD) * ZL_PITCH);  // [nblk][33], MODE 1 and 2
     if (threadIdx.x == 0) s_unit = 0;
-    zw_load_utot(A.utot, A.fmap, a0, A.natoms, A.nh, A.nu, Ub);
-    if (MODE == 1 || MODE == 2) {
-        // unrolled: each iteration is a chain of dependent loads (block roles, then beta)
-#pragma unroll 4
-        for (int idx = threadIdx.x; idx < 32 * A.nblk; idx += blockDim.x) {
-            const int l = idx / A.nblk, b = idx - l * A.nblk;
-            const int aa = a0 + l;
-            float c = 0.f;
-            if (aa < A.natoms) {
-                const ZBlk &bk = A.blk[b];
-                for (int r = 0; r < bk.nrole; ++r)
-                    c += bk.role_f32[r] * __ldg(A.beta + (size_t)aa * A.nB + bk.role_k[r]);
-            }
-            coef[b * ZL_PITCH + l] = c;
-        }
-    }
     // the window coefficients (read at every step) in shared memory when they fit
     // (16-byte aligned for the float4 reads; the launch adds 16 bytes of slack)
     float *ca_s = reinterpret_cast<float *>((reinterpret_cast<uintptr_t>(coef + (size_t)A.nblk * ZL_PITCH) + 15) &
                                             ~(uintptr_t)15);
+    // Every independent global load of the prologue is in flight before any is waited on:
+    // the first ZW_CAR float4 per thread of the Ca table, the first ZW_BR values per thread
+    // of the 32 atoms' beta rows (one contiguous run; MODE 1 and 2 stage them in the Ca area
+    // when it can hold them), then the U tiles.  What exceeds the register batches (larger
+    // lmax) is copied by plain loops afterwards.
+    const bool staged = (MODE == 1 || MODE == 2) && CA_SMEM && 32 * A.nB <= A.nwca;
+    const int nca4 = CA_SMEM ? A.nwca / 4 : 0;
+    const float4 *csrc = reinterpret_cast<const float4 *>(A.wca);
+    float4 cr[ZW_CAR];
+#pragma unroll
+    for (int r = 0; r < ZW_CAR; ++r) {
+        const int i = threadIdx.x + r * ZW_THREADS;
+        cr[r] = (i < nca4) ? __ldg(csrc + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    const int nbt = staged ? min(32, A.natoms - a0) * A.nB : 0;
+    const float *bsrc = A.beta + (size_t)a0 * A.nB;
+    float br[ZW_BR];
+#pragma unroll
+    for (int r = 0; r < ZW_BR; ++r) {
+        const int i = threadIdx.x + r * ZW_THREADS;
+        br[r] = (i < nbt) ? __ldg(bsrc + i) : 0.f;
+    }
+    zw_load_utot(A.utot, A.hfull, a0, A.natoms, A.nh, A.nu, Ub);
+    if (MODE == 1 || MODE == 2) {
+        // coef[b][lane] = sum over the block's roles of role_f beta[atom][role_k], from the
+        // staged rows, else from global memory
+        if (staged) {
+#pragma unroll
+            for (int r = 0; r < ZW_BR; ++r) {
+                const int i = threadIdx.x + r * ZW_THREADS;
+                if (i < 32 * A.nB) ca_s[i] = br[r];
+            }
+            for (int i = threadIdx.x + ZW_BR * ZW_THREADS; i < 32 * A.nB; i += ZW_THREADS)
+                ca_s[i] = (i < nbt) ? __ldg(bsrc + i) : 0.f;
+            __syncthreads();
+        }
+        // one block per warp and step (its table entry is the same for all lanes), lane = atom
+#pragma unroll 4
+        for (int b = threadIdx.x >> 5; b < A.nblk; b += ZW_THREADS / 32) {
+            const ZBlk &bk = A.blk[b];
+            const int nr = bk.nrole;
+            float c = 0.f;
+            if (a < A.natoms) {
+#pragma unroll
+                for (int r = 0; r < 3; ++r) {
+                    if (r < nr) {
+                        const int k = bk.role_k[r];
+                        c += bk.role_f32[r] * (staged ? ca_s[lane * A.nB + k] : __ldg(A.beta + (size_t)a * A.nB + k));
+                    }
+                }
+            }
+            coef[b * ZL_PITCH + lane] = c;
+        }
+        if (staged) __syncthreads();  // before the Ca copy overwrites the staged beta
+    }
     if (CA_SMEM) {
-        const float4 *src = reinterpret_cast<const float4 *>(A.wca);
         float4 *dst = reinterpret_cast<float4 *>(ca_s);
-        for (int i = threadIdx.x; i < A.nwca / 4; i += blockDim.x) dst[i] = __ldg(src + i);
+#pragma unroll
+        for (int r = 0; r < ZW_CAR; ++r) {
+            const int i = threadIdx.x + r * ZW_THREADS;
+            if (i < nca4) dst[i] = cr[r];
+        }
+        for (int i = threadIdx.x + ZW_CAR * ZW_THREADS; i < nca4; i += ZW_THREADS) dst[i] = __ldg(csrc + i);
     }
     const float *ca = CA_SMEM ? ca_s : A.wca;
     __syncthreads();
@@ -383,36 +439,26 @@ __global__ void __launch_bounds__(ZW_THREADS, 2) k_zw32(ZLArgs A) {
     }
     if (MODE == 1) return;
     __syncthreads();
+    // the sums of the slots, staged in shared memory over the U tiles (no longer read) when
+    // they fit there (the host sizes the launch so), in the fixed slot order
+    float *stage = (float *)zw_smem;
     if (MODE == 3) {
         // dB_k: the sum of component k's slots (sections 0, 1, 2, each in unit order)
-        for (int idx = threadIdx.x; idx < 32 * A.nB; idx += blockDim.x) {
-            const int k = idx >> 5, aa = a0 + (idx & 31);
-            if (aa >= A.natoms) continue;
-            float acc = 0.f;
-            const int q1 = __ldg(A.jpos + k + 1);
-#pragma unroll 4
-            for (int q = __ldg(A.jpos + k); q < q1; ++q) acc += A.bc[(size_t)q * A.natoms + aa];
-            A.x[(size_t)aa * A.nB + k] = acc;
-        }
+        zw_slot_sums<1>(A.bc, A.jpos, A.nB, A.nbsec, A.natoms, a0, stage, [](int, int) { return 0.f; },
+                        [&](int k, int l, float acc, float) { A.x[(size_t)(a0 + l) * A.nB + k] = acc; });
         return;
     }
-    // B_k, and beta_k B_k kept in shared memory (over the U tiles, no longer read) for the energy
-    float *eb = (float *)zw_smem;  // [nB][33]
-    for (int idx = threadIdx.x; idx < 32 * A.nB; idx += blockDim.x) {
-        const int k = idx >> 5, l = idx & 31;
-        const int aa = a0 + l;
-        float acc = 0.f, e = 0.f;
-        if (aa < A.natoms) {
-            // the slots are independent loads: unrolled so they are in flight together
-            const int q1 = __ldg(A.bpos + k + 1);
-#pragma unroll 4
-            for (int q = __ldg(A.bpos + k); q < q1; ++q) acc += A.bc[(size_t)q * A.natoms + aa];
+    // B_k = 2 x the sum of its slots; in the fused pass also beta_k B_k per atom (beta read
+    // ahead with the slots), kept in shared memory after the staged slots for the energy
+    float *eb = stage + (size_t)A.nbsec * ZL_PITCH;  // [nB][33]
+    zw_slot_sums<ZW_BR>(
+        A.bc, A.bpos, A.nB, A.nbsec, A.natoms, a0, stage,
+        [&](int k, int l) { return (MODE == 2) ? __ldg(A.beta + (size_t)(a0 + l) * A.nB + k) : 0.f; },
+        [&](int k, int l, float acc, float bk) {
             acc *= 2.f;
-            A.x[(size_t)aa * A.nB + k] = acc;
-            if (MODE == 2) e = acc * __ldg(A.beta + (size_t)aa * A.nB + k);
-        }
-        if (MODE == 2) eb[k * ZL_PITCH + l] = e;
-    }
+            A.x[(size_t)(a0 + l) * A.nB + k] = acc;
+            if (MODE == 2) eb[k * ZL_PITCH + l] = acc * bk;
+        });
     if (MODE != 2 || A.eatom == nullptr) return;
     __syncthreads();
     if (threadIdx.x < 32 && a < A.natoms) {
@@ -804,7 +850,7 @@ static ZLArgs zl_args(const so4_tables *t, int natoms) {
     Z.nu = t->n_u;
     Z.nB = t->n_b;
     Z.nblk = t->n_blk;
-    Z.fmap = t->d_fmap;
+    Z.hfull = t->d_hfull;
     Z.bent = t->d_b;
     Z.blk = t->d_blk;
     Z.yptr = t->d_yblk_ptr;
@@ -817,8 +863,6 @@ static ZLArgs zl_args(const so4_tables *t, int natoms) {
     return Z;
 }
 
-// shared memory of k_zw32: padded U tiles and the per-block coefficients; the B
-// epilogue (with_b) reuses the U tiles for nB x 33 floats
 // Launch k_zw32<MODE> with the Ca table in shared memory when two CTAs per SM still fit.
 template <int MODE>
 static int launch_zw(const so4_tables *t, const ZLArgs &Z, int natoms, size_t smz, cudaStream_t st) {
@@ -838,9 +882,12 @@ static int launch_zw(const so4_tables *t, const ZLArgs &Z, int natoms, size_t sm
     return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
 }
 
-static size_t zw_smem_bytes(const so4_tables *t, bool with_b) {
+// shared memory of k_zw32 (without the Ca table): padded U tiles and the per-block
+// coefficients; the epilogue stages its slots over the U tiles
+static size_t zw_smem_bytes(const so4_tables *t, int nslot, bool with_eb) {
     size_t u = sizeof(float2) * (size_t)(t->n_u + 2 * ZW_PAD) * ZL_PITCH;
-    if (with_b) u = std::max(u, sizeof(float) * (size_t)t->n_b * ZL_PITCH);
+    // the epilogue stages nslot slot rows (and, in the fused pass, beta B) over the U tiles
+    u = std::max(u, sizeof(float) * (size_t)(nslot + (with_eb ? t->n_b : 0)) * ZL_PITCH);
     return u + sizeof(float) * (size_t)t->n_blk * ZL_PITCH;
 }
 
@@ -908,7 +955,7 @@ extern "C" int so4_forward32(const so4_tables *t, const so4_params *p, int natom
     Z.bpos = t->d_bpos;
     Z.nbsec = t->n_bsec;
     Z.bc = (float *)d_work;
-    const size_t smz = zw_smem_bytes(t, true);
+    const size_t smz = zw_smem_bytes(t, t->n_bsec, false);
     return launch_zw<0>(t, Z, natoms, smz, st);
 }
 
@@ -929,7 +976,7 @@ extern "C" int so4_adjoint_y32(const so4_tables *t, int natoms, const float *d_u
     Z.nunit = t->n_wunit_y;
     Z.beta = d_beta;
     Z.Y = (float2 *)d_y;
-    const size_t smz = zw_smem_bytes(t, false);
+    const size_t smz = zw_smem_bytes(t, 0, false);
     return launch_zw<1>(t, Z, natoms, smz, (cudaStream_t)stream);
 }
 
@@ -945,8 +992,9 @@ int so4_zw_jvp32(const so4_tables *t, int natoms, const float *d_utot, const flo
     Z.jpos = t->d_jpos;
     Z.jfac = t->d_jfac;
     Z.bc = d_slots;
+    Z.nbsec = t->n_jslot;  // the epilogue's slot count
     Z.x = d_dB;
-    return launch_zw<3>(t, Z, natoms, zw_smem_bytes(t, false), stream);
+    return launch_zw<3>(t, Z, natoms, zw_smem_bytes(t, t->n_jslot, false), stream);
 }
 
 extern "C" int so4_adjoint_deidrj32(const so4_tables *t, const so4_params *p, int natoms, const double *d_w_nb,
@@ -1197,7 +1245,7 @@ extern "C" int so4_linear_by32(const so4_tables *t, int natoms, const float *d_u
     Z.nbsec = t->n_bsec;
     Z.bc = d_bc;
     Z.eatom = d_eatom;
-    const size_t smz = zw_smem_bytes(t, true);
+    const size_t smz = zw_smem_bytes(t, t->n_bsec, true);
     return launch_zw<2>(t, Z, natoms, smz, (cudaStream_t)stream);
 }
 

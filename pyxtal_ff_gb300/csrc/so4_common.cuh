@@ -104,7 +104,8 @@ struct so4_tables {
     ZBlk *d_blk = nullptr;
     int *d_yblk_ptr = nullptr;  // ldim + 1 : blocks grouped by their third index
     int *d_yblk = nullptr;      // n_blk
-    int *d_fmap = nullptr;      // n_u: full entry -> half source | conj << 15 | negate << 14
+    // n_half: half entry -> {full position, mirror position | conj << 15 | negate << 14 or -1}
+    int2 *d_hfull = nullptr;
     // n_half: per half entry (level L, row, ma) {L(L+1)/2 + ma | row << 8 | (ma == row) << 15,
     // bits of u_norm[L] F, bits of u_norm[L], 0}: where the row-chain kernels keep it and how
     // it is finished (F the row scale of the scaled recursion, so4_tables.cu)
@@ -137,6 +138,7 @@ struct so4_tables {
 // and after the U tiles in shared memory (a window may reach ZW_KMAX - 1 entries
 // past either end of the full layout, always with a zero coefficient).
 constexpr int ZW_KMAX = 8;
+constexpr int ZW_KPAIR = 4;  // window units of K <= ZW_KPAIR walk their rows in pairs
 constexpr int ZW_PAD = ZW_KMAX - 1;
 
 // Table data every kernel stages into shared memory at start.

@@ -89,7 +89,7 @@ void free_device(so4_tables *t) {
     cudaFree(t->d_blk);
     cudaFree(t->d_yblk_ptr);
     cudaFree(t->d_yblk);
-    cudaFree(t->d_fmap);
+    cudaFree(t->d_hfull);
     cudaFree(t->d_hmap);
     cudaFree(t->d_yscale);
     cudaFree(t->d_bpos);
@@ -504,17 +504,17 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
         if (jwrites[q] != 1) jrc = SO4_ERR_UNSUPPORTED;
     t->n_wca = (int)wca.size();
 
-    std::vector<int> fmap(t->n_u);
+    // hfull: per half entry (l, mb <= l / 2, ma) its full-layout position and, for the rows
+    // below the middle, the position of its mirror (l, l - mb, l - ma) = (-1)^(mb + ma)
+    // conj U (conj << 15 | negate << 14), else -1; the window kernels scatter U_tot with it
+    std::vector<int2> hfull(t->n_half);
     for (int l = 0; l < ld; ++l)
-        for (int mb = 0; mb <= l; ++mb)
+        for (int mb = 0; 2 * mb <= l; ++mb)
             for (int ma = 0; ma <= l; ++ma) {
+                const int h = t->h_block[l] + mb * (l + 1) + ma;
                 const int f = t->idxu_block[l] + mb * (l + 1) + ma;
-                if (2 * mb <= l) {
-                    fmap[f] = t->h_block[l] + mb * (l + 1) + ma;
-                } else {
-                    const int src = t->h_block[l] + (l - mb) * (l + 1) + (l - ma);
-                    fmap[f] = src | (1 << 15) | ((((mb + ma) & 1) ? 1 : 0) << 14);
-                }
+                const int fm = t->idxu_block[l] + (l - mb) * (l + 1) + (l - ma);
+                hfull[h] = make_int2(f, (2 * mb < l) ? (fm | (1 << 15) | (((mb + ma) & 1) << 14)) : -1);
             }
 
     int rc = jrc;
@@ -545,7 +545,7 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
                 yscale.push_back((float)F);
             }
     }
-    if (!rc) rc = upload(&t->d_fmap, fmap);
+    if (!rc) rc = upload(&t->d_hfull, hfull);
     if (!rc) rc = upload(&t->d_hmap, hmap);
     if (!rc) rc = upload(&t->d_yscale, yscale);
     if (!rc) rc = upload(&t->d_bpos, bpos);

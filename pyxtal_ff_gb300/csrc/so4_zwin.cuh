@@ -12,15 +12,102 @@
 
 #include "so4_zlanes.cuh"
 
-// U tiles with ZW_PAD zero rows before and after: Ub[(ZW_PAD + f) * ZL_PITCH + lane]
-__device__ __forceinline__ void zw_load_utot(const float2 *__restrict__ utot, const int *__restrict__ fmap, int a0,
+constexpr int ZW_THREADS = 256;  // 8 warps share one CTA's 32 atoms
+constexpr int ZW_TPA = ZW_THREADS / 32;  // threads per atom in the U-tile load
+
+// U tiles with ZW_PAD zero rows before and after: Ub[(ZW_PAD + f) * ZL_PITCH + lane].
+// The half rows of the CTA's 32 consecutive atoms are one contiguous run of 32 nh values.
+// ZW_TPA threads share an atom (thread t: atom t / ZW_TPA, half entries t % ZW_TPA +
+// ZW_TPA i), each reading ZW_LD entries per round with independent loads, then writing
+// each to its full-layout position and, below the middle row, to its mirror (hfull);
+// atoms past natoms are zero.
+constexpr int ZW_LD = 10;
+constexpr int ZW_CAR = 8;  // Ca-table float4 per thread read ahead in the prologue
+constexpr int ZW_BR = 8;   // beta values per thread read ahead
+__device__ __forceinline__ void zw_load_utot(const float2 *__restrict__ utot, const int2 *__restrict__ hfull, int a0,
                                              int natoms, int nh, int nu, float2 *Ub) {
-    for (int idx = threadIdx.x; idx < 2 * ZW_PAD * ZL_PITCH; idx += blockDim.x) {
+    for (int idx = threadIdx.x; idx < 2 * ZW_PAD * ZL_PITCH; idx += ZW_THREADS) {
         const int r = idx / ZL_PITCH, c = idx - r * ZL_PITCH;
         const int row = (r < ZW_PAD) ? r : nu + r;  // rows 0.. ZW_PAD-1 and ZW_PAD+nu .. nu+2 ZW_PAD-1
         Ub[row * ZL_PITCH + c] = make_float2(0.f, 0.f);
     }
-    zl_load_utot(utot, fmap, a0, natoms, nh, nu, Ub + ZW_PAD * ZL_PITCH);
+    float2 *Uf = Ub + ZW_PAD * ZL_PITCH;
+    const int l = threadIdx.x / ZW_TPA;
+    const bool live = a0 + l < natoms;
+    const float2 *src = utot + (size_t)(a0 + l) * nh;
+    for (int h0 = threadIdx.x % ZW_TPA; h0 < nh; h0 += ZW_TPA * ZW_LD) {
+        float2 v[ZW_LD];
+#pragma unroll
+        for (int r = 0; r < ZW_LD; ++r) {
+            const int h = h0 + r * ZW_TPA;
+            v[r] = (live && h < nh) ? __ldg(src + h) : make_float2(0.f, 0.f);
+        }
+#pragma unroll
+        for (int r = 0; r < ZW_LD; ++r) {
+            const int h = h0 + r * ZW_TPA;
+            if (h < nh) {
+                const int2 m = __ldg(hfull + h);
+                Uf[m.x * ZL_PITCH + l] = v[r];
+                if (m.y >= 0) {
+                    float2 w = v[r];
+                    if (m.y & (1 << 15)) w.y = -w.y;
+                    if (m.y & (1 << 14)) {
+                        w.x = -w.x;
+                        w.y = -w.y;
+                    }
+                    Uf[(m.y & 0x3fff) * ZL_PITCH + l] = w;
+                }
+            }
+        }
+    }
+}
+
+// Per-atom sums of scratch slots: the sum of slots [pos[k], pos[k + 1]) of the slot-major
+// scratch sc[q * natoms + a0 + lane], for every k < ncomp and every lane with a0 + lane <
+// natoms, handed to f(k, lane, sum, pre(k, lane)).  The CTA copies its nslot x 32 values
+// into shared memory (stage: nslot x ZL_PITCH floats) with independent loads, issued
+// together with pre() of the thread's first NPRE (k, lane) pairs, then sums from there
+// in slot order.
+constexpr int ZW_SLD = 24;
+template <int NPRE, typename P, typename F>
+__device__ __forceinline__ void zw_slot_sums(const float *sc, const int *__restrict__ pos, int ncomp, int nslot,
+                                             int natoms, int a0, float *stage, P pre, F f) {
+    const int nl = min(32, natoms - a0);
+    float pv[NPRE];
+#pragma unroll
+    for (int r = 0; r < NPRE; ++r) {
+        const int idx = threadIdx.x + r * ZW_THREADS, k = idx >> 5, l = idx & 31;
+        pv[r] = (idx < 32 * ncomp && l < nl) ? pre(k, l) : 0.f;
+    }
+    for (int i0 = threadIdx.x; i0 < 32 * nslot; i0 += ZW_SLD * ZW_THREADS) {
+        float v[ZW_SLD];
+#pragma unroll
+        for (int r = 0; r < ZW_SLD; ++r) {
+            const int i = i0 + r * ZW_THREADS, q = i >> 5, l = i & 31;
+            v[r] = (i < 32 * nslot && l < nl) ? sc[(size_t)q * natoms + a0 + l] : 0.f;
+        }
+#pragma unroll
+        for (int r = 0; r < ZW_SLD; ++r) {
+            const int i = i0 + r * ZW_THREADS;
+            if (i < 32 * nslot) stage[(i >> 5) * ZL_PITCH + (i & 31)] = v[r];
+        }
+    }
+    __syncthreads();
+    auto sum = [&](int k, int l) {
+        float acc = 0.f;
+        const int q1 = __ldg(pos + k + 1);
+        for (int q = __ldg(pos + k); q < q1; ++q) acc += stage[q * ZL_PITCH + l];
+        return acc;
+    };
+#pragma unroll
+    for (int r = 0; r < NPRE; ++r) {
+        const int idx = threadIdx.x + r * ZW_THREADS, k = idx >> 5, l = idx & 31;
+        if (idx < 32 * ncomp && l < nl) f(k, l, sum(k, l), pv[r]);
+    }
+    for (int idx = threadIdx.x + NPRE * ZW_THREADS; idx < 32 * ncomp; idx += ZW_THREADS) {
+        const int k = idx >> 5, l = idx & 31;
+        if (l < nl) f(k, l, sum(k, l), pre(k, l));
+    }
 }
 
 // One sub-segment {f1 | f2 << 16, Ca offset, steps S, bits of Cb}: adds
@@ -71,6 +158,69 @@ __device__ __forceinline__ void zw_rows(const float2 *Ul, const int4 hd, const f
                 for (int k = 0; k < K; ++k) {
                     const int r = (k - t + K) % K;
                     const float2 p = __ffma2_rn(WY[r], as, __fmul2_rn(WX[r], a));
+                    z[k] = __ffma2_rn(make_float2(cc[k], cc[k]), p, z[k]);
+                }
+            }
+        }
+    }
+}
+
+// Two sub-segments of one segment together.  The rows of a segment share the Ca table
+// and the step count S (only f1, f2 and Cb differ), so per (step, entry) the two rows'
+// complex products are summed first and Ca[j][k] is applied once: five packed
+// instructions for two products instead of six, and the Ca loads serve both rows.
+template <int K>
+__device__ __forceinline__ void zw_rows2(const float2 *Ul, const int4 h1, const int4 h2,
+                                         const float *__restrict__ ca, float2 (&z)[K]) {
+    constexpr int KQ = (K + 3) / 4;
+    const int f1 = h1.x & 0xffff, f2 = (int)((unsigned)h1.x >> 16);
+    const int g1 = h2.x & 0xffff, g2 = (int)((unsigned)h2.x >> 16);
+    const int S = h1.z;
+    const float cb = __int_as_float(h1.w), db = __int_as_float(h2.w);
+    const float2 cb2 = make_float2(cb, cb), db2 = make_float2(db, db);
+    const float4 *cw = reinterpret_cast<const float4 *>(ca + h1.y);
+    float2 WX[K], WY[K], VX[K], VY[K];
+#pragma unroll
+    for (int k = 1; k < K; ++k) {
+        const float2 w = Ul[f2 + k * ZL_PITCH];
+        WX[k] = make_float2(w.x, w.x);
+        WY[k] = make_float2(-w.y, w.y);
+        const float2 v = Ul[g2 + k * ZL_PITCH];
+        VX[k] = make_float2(v.x, v.x);
+        VY[k] = make_float2(-v.y, v.y);
+    }
+    WX[0] = WY[0] = VX[0] = VY[0] = make_float2(0.f, 0.f);
+    for (int j0 = 0; j0 < S; j0 += K) {
+#pragma unroll
+        for (int t = 0; t < K; ++t) {
+            const int j = j0 + t;
+            if (j < S) {
+                const float2 w = Ul[f2 - j * ZL_PITCH];
+                WX[(K - t) % K] = make_float2(w.x, w.x);
+                WY[(K - t) % K] = make_float2(-w.y, w.y);
+                const float2 v = Ul[g2 - j * ZL_PITCH];
+                VX[(K - t) % K] = make_float2(v.x, v.x);
+                VY[(K - t) % K] = make_float2(-v.y, v.y);
+                const float2 a = __fmul2_rn(Ul[f1 + j * ZL_PITCH], cb2);
+                const float2 as = make_float2(a.y, a.x);
+                const float2 b = __fmul2_rn(Ul[g1 + j * ZL_PITCH], db2);
+                const float2 bs = make_float2(b.y, b.x);
+                float cc[4 * KQ];
+#pragma unroll
+                for (int q = 0; q < KQ; ++q) {
+                    const float4 c4 = cw[j * KQ + q];
+                    cc[4 * q] = c4.x;
+                    cc[4 * q + 1] = c4.y;
+                    cc[4 * q + 2] = c4.z;
+                    cc[4 * q + 3] = c4.w;
+                }
+#pragma unroll
+                for (int k = 0; k < K; ++k) {
+                    const int r = (k - t + K) % K;
+                    float2 p = __fmul2_rn(WX[r], a);
+                    p = __ffma2_rn(WY[r], as, p);
+                    p = __ffma2_rn(VX[r], b, p);
+                    p = __ffma2_rn(VY[r], bs, p);
                     z[k] = __ffma2_rn(make_float2(cc[k], cc[k]), p, z[k]);
                 }
             }
