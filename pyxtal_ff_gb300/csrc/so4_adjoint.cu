@@ -337,6 +337,19 @@ __device__ __forceinline__ void zw_unit(const ZLArgs &A, const int4 un, const fl
 }
 
 
+// zw_unit for the unit's K (1 <= k <= ZW_KMAX, from the work list)
+template <int MODE, int K = ZW_KMAX>
+__device__ __forceinline__ void zw_unit_k(int k, const ZLArgs &A, const int4 un, const float2 *Ul, const float *coef,
+                                          const float *__restrict__ ca, int a, int lane) {
+    if constexpr (K > 1) {
+        if (k != K) {
+            zw_unit_k<MODE, K - 1>(k, A, un, Ul, coef, ca, a, lane);
+            return;
+        }
+    }
+    zw_unit<MODE, K>(A, un, Ul, coef, ca, a, lane);
+}
+
 // Window form of k_zb32 / k_zy32 / k_zby32 (so4_zwin.cuh), 32 atoms per CTA.
 // MODE 0: B only (units of the B sections, B blocks only); 1: Y only; 2: Y and,
 // per (unit, B block), the unit's part of the section sum sum_e w_e Re(conj(U_lam[e]) Z[e])
@@ -426,16 +439,7 @@ __global__ void __launch_bounds__(ZW_THREADS, 2) k_zw32(ZLArgs A) {
     const float2 *Ul = Ub + lane;
     for (int u = zl_next(&s_unit); u < A.nunit; u = zl_next(&s_unit)) {
         const int4 un = __ldg(A.unit + u);
-        switch (un.x >> 24) {
-            case 1: zw_unit<MODE, 1>(A, un, Ul, coef, ca, a, lane); break;
-            case 2: zw_unit<MODE, 2>(A, un, Ul, coef, ca, a, lane); break;
-            case 3: zw_unit<MODE, 3>(A, un, Ul, coef, ca, a, lane); break;
-            case 4: zw_unit<MODE, 4>(A, un, Ul, coef, ca, a, lane); break;
-            case 5: zw_unit<MODE, 5>(A, un, Ul, coef, ca, a, lane); break;
-            case 6: zw_unit<MODE, 6>(A, un, Ul, coef, ca, a, lane); break;
-            case 7: zw_unit<MODE, 7>(A, un, Ul, coef, ca, a, lane); break;
-            default: zw_unit<MODE, 8>(A, un, Ul, coef, ca, a, lane); break;
-        }
+        zw_unit_k<MODE>(un.x >> 24, A, un, Ul, coef, ca, a, lane);
     }
     if (MODE == 1) return;
     __syncthreads();

@@ -137,8 +137,8 @@ struct so4_tables {
 // Window Z contractions: most entries per unit, and the zero rows kept before
 // and after the U tiles in shared memory (a window may reach ZW_KMAX - 1 entries
 // past either end of the full layout, always with a zero coefficient).
-constexpr int ZW_KMAX = 8;
-constexpr int ZW_KPAIR = 4;  // window units of K <= ZW_KPAIR walk their rows in pairs
+constexpr int ZW_KMAX = 5;
+constexpr int ZW_KPAIR = 5;  // window units of K <= ZW_KPAIR walk their rows in pairs (here every unit)
 constexpr int ZW_PAD = ZW_KMAX - 1;
 
 // Table data every kernel stages into shared memory at start.
