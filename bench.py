@@ -166,6 +166,50 @@ def kernels_back_to_back(calc, batch, pos_dev, beta_dev, reps=20):
     return out
 
 
+def run_ase_md(nstep=10):
+    """One MD step of the reference's published ASE example (1000-atom diamond Si, a = 5.659 A,
+    SNAP lmax 3, Rc 5.0, weight 1.0, NN 12-12 tanh, about 16 s per step on a CPU) through
+    PyXtalFFCalculator: the lattice displaced by sigma 0.1 A (about 1000 K), each step moves the
+    atoms by a further sigma 0.02 A, then one calculate() from host positions to host energies,
+    forces and stress.  Both routes: 'plain'
+    (FP64 descriptors with dxdr and per-atom rdxdr, the reference's arithmetic) and 'adjoint'
+    (FP32 adjoint forces).  Random-initialised network; descriptor range from the structure
+    itself; the ZBL base potential of the example is left out (not part of this path)."""
+    import torch
+    from pyxtal_ff_gb300 import structures as S
+    from pyxtal_ff_gb300.ase_calculator import ForceField, PyXtalFFCalculator, compute_descriptor
+    from pyxtal_ff_gb300.nn import NeuralNetworkPotential
+
+    rng = np.random.default_rng(21)
+    atoms = S.diamond_si(5, 5, 5, a=5.659, sigma=0.1, rng=rng)
+    desc = {"type": "SNAP", "Rc": 5.0, "cutoff": "cosine", "weights": {"Si": 1.0}, "base_potential": None,
+            "parameters": {"lmax": 3}}
+    x = compute_descriptor(desc, atoms)["x"]
+    lo, hi = x.min(0), x.max(0)
+    hi = np.where(hi > lo, hi, lo + 1.0)
+    torch.manual_seed(22)
+    nb = x.shape[1]
+    net = torch.nn.Sequential(torch.nn.Linear(nb, 12), torch.nn.Tanh(), torch.nn.Linear(12, 12), torch.nn.Tanh(),
+                              torch.nn.Linear(12, 1)).double()
+    base = atoms.positions.copy()
+    out = {"workload": "1000-atom diamond Si (5x5x5, a 5.659 A, sigma 0.1 A, 0.02 A more per step), SNAP "
+                       "lmax 3, Rc 5.0, NN 12-12 tanh (random init), energy + forces + stress per step, host "
+                       "positions in, host results out; ZBL base potential left out",
+           "published_cpu_s_per_step": 16.0, "published_source": "examples/Si-LAMMPS/README.md:28-40"}
+    for route in ("plain", "adjoint"):
+        ff = ForceField(desc, NeuralNetworkPotential({"Si": net}, {"Si": np.stack([lo, hi], 1)}))
+        calc = PyXtalFFCalculator(ff=ff, route=route)
+        ts = []
+        for it in range(nstep + 2):
+            atoms.positions = base + rng.normal(0.0, 0.02, size=base.shape)
+            t0 = time.perf_counter()
+            calc.calculate(atoms)
+            ts.append(time.perf_counter() - t0)
+        ms = 1e3 * float(np.median(ts[2:]))
+        out[route] = {"ms_per_step": ms, "speedup_vs_published": 16.0 / (ms * 1e-3)}
+    return out
+
+
 def measured_peaks(torch):
     """Measured denominators: HBM from MEASURED_PEAKS.json; FP32 / FP64 CUDA-core rates
     measured here with cuBLAS SGEMM (TF32 off) / DGEMM, since that file has none."""
@@ -583,6 +627,11 @@ def main():
                  "ms_per_step": tms, "atoms_per_s": fm.batch.natoms / (tms * 1e-3), "uncaptured_ms_per_step": t_eager}
         del fm
 
+    # ---- the reference's published MD workload through the ASE-calculator interface, extra line item
+    ase_md = None
+    if not args.no_train:
+        ase_md = run_ase_md()
+
     # ---- CPU baseline (the oracle, all host threads), rank 0 only
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -599,6 +648,7 @@ def main():
                 "pairs_per_s": ws * (nb.npair) * args.steps / (t_dev * 1e-3),
                 "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": int(launches),
                 "fp64_plain": fp64, "err_vs_fp64": err, "kernels": kernels, "train_step": train,
+                "ase_md_step": ase_md,
                 "peaks": {k: peaks[k] for k in ("hbm_gbs", "fp32_tflops", "fp64_tflops") if k in peaks}}
         print(json.dumps(line), flush=True)
     if ws > 1:
