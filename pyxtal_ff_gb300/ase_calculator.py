@@ -12,7 +12,8 @@ Two routes:
 - route='plain' (default, the reference's arithmetic): FP64 descriptors with dxdr
   and per-atom rdxdr from the CUDA plain path, contracted by so4_contract_dxdr;
 - route='adjoint': B in FP32, dE/dB from the networks, forces and virial by the
-  adjoint kernels (no dxdr), the path for MD-sized structures.
+  adjoint kernels (no dxdr), the path for MD-sized structures; repeated calls on one
+  layout (an MD loop) replay the step as a single CUDA graph.
 
 ASE is not a dependency: the class keeps ASE's calculator protocol
 (``calculate(atoms, properties, system_changes)``, ``results``,
@@ -84,6 +85,7 @@ class PyXtalFFCalculator:
         self.atoms = None
         self._atoms_obj = None
         self._calc = None
+        self._step, self._step_key, self._last_key = None, None, None
 
     def _ff(self):
         ff = self.parameters["ff"]
@@ -116,8 +118,24 @@ class PyXtalFFCalculator:
                                        rfac0=p.get("rfac", 0.99363), cutoff_function=f["cutoff"],
                                        normalize_U=p.get("normalize_U", False))
         batch = Batch([atoms])
-        model = ff.model.energy_model(batch.species_order)
-        r = self._calc.compute(batch, model)
+        # an MD or relaxation loop moves only the positions: from the second structure of one
+        # layout (cell, pbc, species, model) on, the step is one CUDA-graph replay
+        # (SO4Calculator.capture), bit for bit the uncaptured compute()
+        key = (batch.cells.tobytes(), np.asarray(batch.pbc).tobytes(), np.asarray(atoms.numbers).tobytes(),
+               id(ff.model))
+        if self._step is not None and self._step_key != key:
+            self._step = None
+        if self._step is None and self._last_key == key:
+            self._step = self._calc.capture(batch, ff.model.energy_model(batch.species_order))
+            self._step_key = key
+        self._last_key = key
+        r = None
+        if self._step is not None:
+            r = self._step(batch.positions)
+            if not self._step.check():  # the neighbour list outgrew the captured buffers
+                self._step, r = None, None
+        if r is None:
+            r = self._calc.compute(batch, ff.model.energy_model(batch.species_order))
         e_atom = r["energies"].double()
         symbols = np.asarray(_symbols(atoms))
         order = np.concatenate([np.nonzero(symbols == e)[0] for e in ff.model.elements])

@@ -202,12 +202,17 @@ def contract_plain(x, dxdr, rdxdr, seq, pair_ptr, atom_ptr, beta, volumes):
 class CapturedStep:
     """Energy, forces and stress of one batch layout as a single CUDA graph replay.
 
-    For a LinearModel and fixed cells / pbc / atom ranges (an MD or relaxation loop
-    moves only the positions), the whole step -- the three neighbour-list passes,
-    U_tot, the fused B + Y pass, the per-image dE/dr and the gather, then the
-    per-structure constant and the stress -- is captured once into a CUDA graph on
-    static device buffers; a step copies the positions in and replays it, with no
-    host synchronisation and no per-kernel launch cost.
+    For fixed cells / pbc / atom ranges (an MD or relaxation loop moves only the
+    positions), the whole step is captured once into a CUDA graph on static device
+    buffers; a step copies the positions in and replays it, with no host
+    synchronisation and no per-kernel launch cost.  For a LinearModel: the neighbour
+    list, U_tot, the fused B + Y pass, the per-image dE/dr and the gather, then the
+    per-structure constant and the stress, in parallel branches over ranges of atoms.
+    For any other model of (B, species) whose forward can be captured (no host
+    synchronisation; a species_index() method, as the NN potential's networks have,
+    supplies the atoms of each species once): the list, U_tot and B, the model and its
+    gradient dE/dB, Y, the per-image dE/dr and the gather, on one stream.  Either way the
+    results equal those of SO4Calculator.compute bit for bit.
 
     The image / pair buffers have a fixed capacity (the counts of the structure at
     capture time plus `headroom`); the true counts are only known on the device.
@@ -216,10 +221,12 @@ class CapturedStep:
     (`SO4Calculator.capture`); it raises for non-finite positions like the eager path.
     """
 
-    def __init__(self, calc: "SO4Calculator", batch: Batch, model: LinearModel, headroom=1.25, branches=2):
-        if not isinstance(model, LinearModel):
-            raise TypeError("graph capture covers the linear model (beta = dE/dB fixed)")
+    def __init__(self, calc: "SO4Calculator", batch: Batch, model, headroom=1.25, branches=2):
+        self.linear = isinstance(model, LinearModel)
         calc.prepare(batch)
+        # the graph reads these per-batch tensors by address: hold them, so that a later
+        # prepare() of another batch cannot free them under the graph
+        self._held = (calc._w_nb, calc._w_site, calc._species, calc._vol)
         dev = calc.device
         self.calc, self.batch = calc, batch
         self.layout = engine.layout(batch.cells, batch.pbc, batch.atom_ptr, calc.rcut, dev)
@@ -237,9 +244,27 @@ class CapturedStep:
         self.nl = engine.NeighborBuffers.allocate(lay, self.cap_m, self.cap_p, dev, slot_cap=self.slot_cap)
         L = engine.lib()
         tab = calc.tables
-        self.ws = torch.empty(L.so4_linear_workspace_size(tab.handle, N, self.cap_m), dtype=torch.uint8, device=dev)
-        self.beta = model.coef.detach()[calc._species].to(torch.float32).contiguous()
-        self.bias_s = (calc._counts @ model.bias.detach().double()).contiguous()
+        if self.linear:
+            self.ws = torch.empty(L.so4_linear_workspace_size(tab.handle, N, self.cap_m), dtype=torch.uint8,
+                                  device=dev)
+            self.beta = model.coef.detach()[calc._species].to(torch.float32).contiguous()
+            self.bias_s = (calc._counts @ model.bias.detach().double()).contiguous()
+        else:
+            # any model of (B, species) -> per-atom energy whose forward is capturable: B, the
+            # model and its gradient dE/dB, then the adjoint, as in the uncaptured compute();
+            # a model with species_index() gets the atoms of each species precomputed
+            self.model = model
+            self.index = model.species_index(calc._species) if hasattr(model, "species_index") else None
+            nh = tab.n_half
+            self.fws = torch.empty(max(L.so4_forward32_workspace_size(tab.handle, N), 1), dtype=torch.uint8,
+                                   device=dev)
+            self.utot = torch.empty((max(N, 1), nh, 2), dtype=torch.float32, device=dev)
+            self.ybuf = torch.empty((max(N, 1), nh, 2), dtype=torch.float32, device=dev)
+            self.beta = torch.empty((max(N, 1), tab.nB), dtype=torch.float32, device=dev)
+            self.eatom = torch.empty(max(N, 1), dtype=torch.float32, device=dev)
+            self.energies = torch.empty(max(N, 1), dtype=torch.float64, device=dev)
+            self.g = torch.empty((self.cap_m, 3), dtype=torch.float32, device=dev)
+            self.part = torch.empty(L.so4_gather_workspace_size(N), dtype=torch.uint8, device=dev)
         self.x = torch.empty((max(N, 1), tab.nB), dtype=torch.float32, device=dev)
         self.forces = torch.empty((max(N, 1), 3), dtype=torch.float64, device=dev)
         self.virial = torch.empty((max(S, 1), 3, 3), dtype=torch.float64, device=dev)
@@ -247,7 +272,7 @@ class CapturedStep:
         # Branches: after the neighbour list every stage up to the gather is independent per
         # centre, so consecutive ranges of atoms (cut at multiples of 32) run as parallel graph
         # branches and the tail of one branch's kernels overlaps the others' work.
-        self.branches = max(1, min(int(branches), N // 128))
+        self.branches = max(1, min(int(branches), N // 128)) if self.linear else 1
         if self.branches > 1:
             cuts = [0] + [min(N, (N * k // self.branches + 31) // 32 * 32) for k in range(1, self.branches)] + [N]
             self.chunks = [(a0, a1) for a0, a1 in zip(cuts[:-1], cuts[1:]) if a1 > a0]
@@ -283,6 +308,9 @@ class CapturedStep:
         b = self.nl
         _p = engine._ptr
         check = engine.check
+        if not self.linear:
+            self._enqueue_model()
+            return
         if self.branches == 1:
             engine.enqueue_neighbors(lay, self.pos, b, lite=True)
             check(L.so4_adjoint_linear32(tab.handle, C.byref(calc.params), lay.nstruct, _p(lay.atom_struct),
@@ -343,6 +371,36 @@ class CapturedStep:
         # same operations as the uncaptured path, so the two agree bit for bit
         self.stress[:S].copy_(-(self.virial[:S].reshape(S, 9)[:, self._voigt] / self.calc._vol[:, None]) * EV_A3_TO_GPA)
 
+    def _enqueue_model(self):
+        """The general-model step: neighbour list, U_tot and B (so4_forward32), the model and
+        beta = dE/dB by autograd, Y, the per-image dE/dr and the gather with the per-atom
+        energies -- the kernels and order of SO4Calculator.compute, so the two agree bit for bit."""
+        lay, calc, tab, L = self.layout, self.calc, self.calc.tables, engine.lib()
+        b, _p, check, st = self.nl, engine._ptr, engine.check, engine._stream()
+        N, S = lay.natoms, lay.nstruct
+        engine.enqueue_neighbors(lay, self.pos, b, lite=True)
+        check(L.so4_forward32(tab.handle, C.byref(calc.params), N, _p(calc._w_nb), _p(calc._w_site), _p(b.img_ptr),
+                              _p(b.img_j), _p(b.img_r), _p(self.utot), _p(self.x), _p(self.fws), self.fws.numel(), st),
+              "so4_forward32")
+        xg = self.x[:N].detach().requires_grad_(True)
+        with torch.enable_grad():
+            if self.index is not None:
+                e_atom = self.model(xg, calc._species, self.index)
+            else:
+                e_atom = self.model(xg, calc._species)
+            beta, = torch.autograd.grad(e_atom.sum(), xg)
+        self.beta[:N].copy_(beta)
+        self.energies[:N].copy_(e_atom.detach())
+        self.eatom[:N].copy_(e_atom.detach())
+        check(L.so4_adjoint_y32(tab.handle, N, _p(self.utot), _p(self.beta), _p(self.ybuf), st), "so4_adjoint_y32")
+        check(L.so4_adjoint_deidrj32(tab.handle, C.byref(calc.params), N, _p(calc._w_nb), _p(b.img_ptr),
+                                     _p(b.img_j), _p(b.img_r), self.cap_m, _p(self.ybuf), _p(self.g), st),
+              "so4_adjoint_deidrj32")
+        check(L.so4_adjoint_gather(N, S, _p(lay.atom_ptr_dev), _p(b.img_ptr), _p(b.img_rev), _p(b.img_r), _p(self.g),
+                                   _p(self.eatom), _p(self.part), _p(self.forces), _p(self.virial),
+                                   _p(self.energy), st), "so4_adjoint_gather")
+        self.stress[:S].copy_(-(self.virial[:S].reshape(S, 9)[:, self._voigt] / calc._vol[:, None]) * EV_A3_TO_GPA)
+
     def __call__(self, positions=None):
         """One step; positions (N,3) f64 from the host (pinned for an asynchronous copy)
         or the device, or None to reuse the last ones.  Returns views of the static
@@ -353,8 +411,11 @@ class CapturedStep:
             self.pos.copy_(positions, non_blocking=True)
         self.graph.replay()
         N, S = self.layout.natoms, self.layout.nstruct
-        return dict(energy=self.energy[:S], forces=self.forces[:N], virial=self.virial[:S], stress=self.stress[:S],
-                    x=self.x[:N])
+        out = dict(energy=self.energy[:S], forces=self.forces[:N], virial=self.virial[:S], stress=self.stress[:S],
+                   x=self.x[:N])
+        if not self.linear:
+            out["energies"] = self.energies[:N]
+        return out
 
     def check(self):
         """True if the last step's neighbour list fitted its buffers (raises on bad input)."""

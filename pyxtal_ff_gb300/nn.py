@@ -140,10 +140,18 @@ class _SpeciesNetworks(torch.nn.Module):
         self.species_order = species_order
         self.nets = torch.nn.ModuleList([pot.models[s] for s in species_order])
 
+    def species_index(self, species):
+        """The atoms of each species, in species_order (one synchronising nonzero each)."""
+        return [torch.nonzero(species == k).reshape(-1) for k in range(len(self.species_order))]
+
     def forward(self, x, species, index=None):
+        """index: the atoms of each species (a list of index tensors, as species_index
+        returns); given, the forward has no host synchronisation and can be graph-captured."""
         out = torch.zeros(x.shape[0], dtype=torch.float64, device=x.device)
+        if index is None:
+            index = self.species_index(species)
         for k, name in enumerate(self.species_order):
-            idx = torch.nonzero(species == k).reshape(-1)
+            idx = index[k]
             if idx.numel() == 0:
                 continue
             p = self.pot

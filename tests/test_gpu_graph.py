@@ -50,6 +50,42 @@ def test_graph_step_matches_eager_bitwise(cuda_device):
         _equal(res, calc.compute(batch, model, positions=pos))
 
 
+def test_graph_step_general_model_matches_eager_bitwise(cuda_device):
+    """An NN potential (two species, per-species networks) captured with its gradient dE/dB:
+    every output equals the uncaptured compute(), also after the same calculator prepared
+    another batch (the graph holds its per-batch tensors)."""
+    from pyxtal_ff_gb300.nn import NeuralNetworkPotential
+    structs = [S.diamond_si(2, 2, 2, sigma=0.1, rng=np.random.default_rng(1)), S.sio2_random(n_si=8, seed=2)]
+    batch, calc, _ = _setup(structs)
+    nB = calc.nB
+    torch.manual_seed(5)
+    nets = {e: torch.nn.Sequential(torch.nn.Linear(nB, 8), torch.nn.Tanh(), torch.nn.Linear(8, 1)).double()
+            for e in batch.species_order}
+    drange = {e: np.stack([np.zeros(nB), np.full(nB, 2.0)], 1) for e in nets}
+    pot = NeuralNetworkPotential(nets, drange)
+    model = pot.energy_model(batch.species_order)
+    step = calc.capture(batch, model)
+    keys = ("energy", "forces", "virial", "stress", "x", "energies")
+    res = {k: v.clone() for k, v in step().items()}
+    assert step.check()
+    ref = calc.compute(batch, model)
+    for k in keys:
+        assert torch.equal(res[k], ref[k]), k
+    rng = np.random.default_rng(11)
+    for _ in range(2):
+        pos = batch.positions + rng.normal(0, 0.02, size=batch.positions.shape)
+        res = {k: v.clone() for k, v in step(pos).items()}
+        assert step.check()
+        ref = calc.compute(batch, model, positions=pos)
+        for k in keys:
+            assert torch.equal(res[k], ref[k]), k
+    other = Batch([S.diamond_si(1, 1, 2, sigma=0.05, rng=np.random.default_rng(6))])
+    calc.compute(other, pot.energy_model(other.species_order))
+    res = {k: v.clone() for k, v in step(pos).items()}
+    for k in keys:
+        assert torch.equal(res[k], ref[k]), k
+
+
 def test_graph_step_reports_overflow_and_bad_input(cuda_device):
     structs = [S.diamond_si(2, 2, 2, sigma=0.05, rng=np.random.default_rng(5))]
     batch, calc, model = _setup(structs)

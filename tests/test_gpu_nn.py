@@ -74,6 +74,23 @@ def test_calculator_adjoint_route(cuda_device, name):
     assert G.rel_err(r["stress_ml"], d["stress"]) < 1e-4
 
 
+def test_calculator_adjoint_route_md_loop_replays_graph(cuda_device):
+    """Repeated calls on one layout (an MD loop) replay a captured step; every step equals
+    a fresh calculator's uncaptured result bit for bit."""
+    atoms, meta, d, nets, drange = G.load_nn("nn_si16_snap")
+    calc = PyXtalFFCalculator(ff=_ff(meta, nets, drange), route="adjoint")
+    base = atoms.positions.copy()
+    rng = np.random.default_rng(3)
+    for _ in range(4):
+        atoms.positions = base + rng.normal(0, 0.01, size=base.shape)
+        calc.calculate(atoms)
+        ref = PyXtalFFCalculator(ff=calc.parameters["ff"], route="adjoint")
+        ref.calculate(atoms)
+        for k in ("energies", "energy", "forces", "stress"):
+            assert np.array_equal(calc.results[k], ref.results[k]), k
+    assert calc._step is not None
+
+
 def test_contract_dxdr_large_two_species(cuda_device):
     from pyxtal_ff_gb300.calculator import Batch, SO4Calculator
     structs = [S.sio2_random(n_si=150, seed=7), S.diamond_si(2, 2, 3, sigma=0.1, rng=np.random.default_rng(8))]
