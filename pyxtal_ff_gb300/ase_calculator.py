@@ -122,7 +122,7 @@ class PyXtalFFCalculator:
         # layout (cell, pbc, species, model) on, the step is one CUDA-graph replay
         # (SO4Calculator.capture), bit for bit the uncaptured compute()
         key = (batch.cells.tobytes(), np.asarray(batch.pbc).tobytes(), np.asarray(atoms.numbers).tobytes(),
-               id(ff.model))
+               id(ff.model), tuple(id(ff.model.models[e]) for e in ff.model.elements))
         if self._step is not None and self._step_key != key:
             self._step = None
         if self._step is None and self._last_key == key:
