@@ -29,7 +29,7 @@ struct NLWork {
     int *bin_cur;    // nbins
     int *bin_atoms;  // natoms
     int *atom_bin;   // natoms
-    int *atom_shift; // 3 natoms
+    int4 *atom_shift; // natoms: the cell shifts (x, y, z, 0) that wrap each atom into its cell
     int *cnt;        // natoms (image or pair counts)
     float4 *pos32;   // natoms: FP32 copy of the positions for the prefilter
     unsigned long long *keys;  // nimg, or natoms * slot_cap in the slot mode
@@ -54,7 +54,7 @@ size_t carve(NLWork &w, void *base, int natoms, int nbins, int64_t nimg) {
     w.bin_cur = (int *)take(sizeof(int) * (nbins + 1));
     w.bin_atoms = (int *)take(sizeof(int) * (natoms + 1));
     w.atom_bin = (int *)take(sizeof(int) * (natoms + 1));
-    w.atom_shift = (int *)take(sizeof(int) * 3 * (natoms + 1));
+    w.atom_shift = (int4 *)take(sizeof(int4) * (natoms + 1));
     w.cnt = (int *)take(sizeof(int) * (natoms + 1));
     w.pos32 = (float4 *)take(sizeof(float4) * (natoms + 1));
     w.keys = (unsigned long long *)take(sizeof(unsigned long long) * (nimg + 1));
@@ -100,7 +100,7 @@ __global__ void k_bin(const so4_geom *geom, const double *pos, const int *astruc
     const so4_geom &g = geom[astruct[a]];
     const double r[3] = {pos[3 * a], pos[3 * a + 1], pos[3 * a + 2]};
     if (!isfinite(r[0]) || !isfinite(r[1]) || !isfinite(r[2])) flag(w.status, SO4_ERR_NONFINITE);
-    int b[3];
+    int b[3], shift[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
         double f = frac_k(g, r, k);
@@ -115,8 +115,9 @@ __global__ void k_bin(const so4_geom *geom, const double *pos, const int *astruc
             bk = min(max(bk, 0), g.nbin[k] - 1);
         }
         b[k] = bk;
-        w.atom_shift[3 * a + k] = sh;
+        shift[k] = sh;
     }
+    w.atom_shift[a] = make_int4(shift[0], shift[1], shift[2], 0);
     const int bin = g.bin_base + (b[0] * g.nbin[1] + b[1]) * g.nbin[2] + b[2];
     w.atom_bin[a] = bin;
     w.pos32[a] = make_float4((float)r[0], (float)r[1], (float)r[2], 0.f);
@@ -251,7 +252,7 @@ __global__ void k_scan_images(const so4_geom *geom, const double *pos, const int
     const float pimag = fmaxf(fabsf(pi32.x), fmaxf(fabsf(pi32.y), fabsf(pi32.z)));
     const int lb = w.atom_bin[a] - g.bin_base;
     const int bi[3] = {lb / (g.nbin[1] * g.nbin[2]), (lb / g.nbin[2]) % g.nbin[1], lb % g.nbin[2]};
-    const int si[3] = {w.atom_shift[3 * a], w.atom_shift[3 * a + 1], w.atom_shift[3 * a + 2]};
+    const int4 si = w.atom_shift[a];
     const int n1 = 2 * g.mshift[1] + 1, n2 = 2 * g.mshift[2] + 1;
     const int nq = (2 * g.mshift[0] + 1) * n1 * n2;
     const int64_t base = (MODE == 1) ? (int64_t)img_ptr[a] : ((MODE == 2) ? (int64_t)a * w.slot_cap : 0);
@@ -268,10 +269,14 @@ __global__ void k_scan_images(const so4_geom *geom, const double *pos, const int
             img[k] = (t - wk) / nb;
         }
         const int bin = g.bin_base + (tb[0] * g.nbin[1] + tb[1]) * g.nbin[2] + tb[2];
-        for (int s = w.bin_start[bin]; s < w.bin_start[bin + 1]; ++s) {
-            const int j = w.bin_atoms[s];
-            const int o[3] = {img[0] + w.atom_shift[3 * j] - si[0], img[1] + w.atom_shift[3 * j + 1] - si[1],
-                              img[2] + w.atom_shift[3 * j + 2] - si[2]};
+        // the next candidate's index is read one ahead, so its loads do not wait on it
+        const int s0 = w.bin_start[bin], s1 = w.bin_start[bin + 1];
+        int jn = (s0 < s1) ? w.bin_atoms[s0] : 0;
+        for (int s = s0; s < s1; ++s) {
+            const int j = jn;
+            if (s + 1 < s1) jn = w.bin_atoms[s + 1];
+            const int4 sj = w.atom_shift[j];
+            const int o[3] = {img[0] + sj.x - si.x, img[1] + sj.y - si.y, img[2] + sj.z - si.z};
             if (j == a && o[0] == 0 && o[1] == 0 && o[2] == 0) continue;
             // FP32 prefilter
             const float4 pj32 = w.pos32[j];
@@ -342,6 +347,16 @@ __global__ void k_sort(const so4_geom *geom, const double *pos, const int *astru
         return;
     }
     const double pi[3] = {pos[3 * a], pos[3 * a + 1], pos[3 * a + 2]};
+    // For the offset (0, 0, 0) image_vec's o . cell is, per component, a signed zero z: 0
+    // times a cell entry keeps the entry's sign, and the sum is -0 only if all three terms
+    // are.  p_j + z is then p_j itself, except -0 + +0 = +0, so r = p_j' - p_i with that one
+    // sign fix-up on the bits rounds exactly as image_vec does, with one FP64 operation per
+    // component instead of six (the FP64 pipe runs at 1/64 of FP32 on this GPU); in a cell
+    // larger than twice the cutoff almost every image has the zero offset.
+    bool zneg[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+        zneg[c] = signbit(g.cell[c]) && signbit(g.cell[3 + c]) && signbit(g.cell[6 + c]);
     // keys of this atom: compact at [p0, p1), or in its own slots
     const unsigned long long *kk = w.keys + ((w.slot_cap > 0) ? (int64_t)a * w.slot_cap - p0 : 0);
     for (int q = p0 + lane; q < p1; q += 32) {
@@ -359,7 +374,16 @@ __global__ void k_sort(const so4_geom *geom, const double *pos, const int *astru
         img_off[3 * dst + 2] = o2;
         const double pj[3] = {pos[3 * j], pos[3 * j + 1], pos[3 * j + 2]};
         double r[3];
-        image_vec(g, pi, pj, o0, o1, o2, r);
+        if ((o0 | o1 | o2) == 0) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                double p = pj[c];
+                if (!zneg[c] && __double_as_longlong(p) == (long long)0x8000000000000000ULL) p = 0.0;  // -0 + +0
+                r[c] = __dsub_rn(p, pi[c]);
+            }
+        } else {
+            image_vec(g, pi, pj, o0, o1, o2, r);
+        }
         img_r[3 * dst] = r[0];
         img_r[3 * dst + 1] = r[1];
         img_r[3 * dst + 2] = r[2];
