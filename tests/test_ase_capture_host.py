@@ -103,3 +103,21 @@ def test_new_layout_or_model_drops_the_graph():
     calc.parameters["ff"].model.models["Si"] = torch.nn.Sequential(torch.nn.Linear(nB, 1)).double()
     calc.calculate(b)
     assert fake.log[-1] == "compute" and calc._step is None
+
+
+def test_species_networks_precomputed_index_matches():
+    """The NN potential's networks with their species index lists supplied (the capturable
+    form) give the same per-atom energies as with the lists found by the forward itself."""
+    nB = 6
+    torch.manual_seed(0)
+    nets = {e: torch.nn.Sequential(torch.nn.Linear(nB, 3), torch.nn.Tanh(), torch.nn.Linear(3, 1)).double()
+            for e in ("O", "Si")}
+    drange = {e: np.stack([np.zeros(nB), np.full(nB, 2.0)], 1) for e in nets}
+    pot = NeuralNetworkPotential(nets, drange, device="cpu")
+    model = pot.energy_model(["O", "Si"])
+    species = torch.tensor([1, 0, 1, 1, 0, 1], dtype=torch.int64)  # interleaved elements
+    x = torch.rand((6, nB), dtype=torch.float32)
+    e0 = model(x, species)
+    e1 = model(x, species, model.species_index(species))
+    assert torch.equal(e0, e1)
+    assert e0.dtype == torch.float64 and e0.shape == (6,)
