@@ -575,6 +575,12 @@ def main():
                                "its DRAM traffic is far below the HBM roof",
                 "duration": "mean of 20 back-to-back launches replayed as one CUDA graph (no host gaps)",
                 "ms": sec * 1e3}
+        # the same launch against the HBM roof (ncu DRAM bytes per launch / its duration, of the
+        # measured copy rate): how far from memory bound the kernel is
+        tr, hbm = NCU_TRAFFIC.get(dom), peaks.get("hbm_gbs")
+        if tr and hbm:
+            roof["hbm"] = {"achieved_gbs": tr / sec / 1e9, "peak_gbs": hbm, "frac": tr / sec / 1e9 / hbm,
+                           "peak_source": peaks.get("source", "")}
     else:
         roof = {"kernel": dom, "bound": "latency", "achieved": None, "peak": None, "unit": None, "frac": None,
                 "traffic": None}
