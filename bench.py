@@ -50,6 +50,24 @@ def workload():
     return atoms, coef
 
 
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo), for the CPU baseline's record."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return None
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -244,13 +262,34 @@ def measured_peaks(torch):
 # ----------------------------------------------------------------- CPU side
 def cpu_run(atoms, coef, nthreads):
     """The oracle (C restatement of the reference path, FP64) on every centre of the
-    workload: energy, forces and the contracted virial."""
+    workload: B, energy, forces and the contracted virial.  Returns (seconds, results)."""
     from oracle import oracle as O
     t0 = time.perf_counter()
     beta = np.broadcast_to(coef, (len(atoms), len(coef)))
-    O.forces_virial(atoms, beta, kind="SNAP", lmax=LMAX, rcut=RCUT, weights={"Si": 1.0}, rfac0=1.0,
-                    nthreads=nthreads)
-    return time.perf_counter() - t0
+    ref = O.forces_virial(atoms, beta, kind="SNAP", lmax=LMAX, rcut=RCUT, weights={"Si": 1.0}, rfac0=1.0,
+                          nthreads=nthreads)
+    return time.perf_counter() - t0, ref
+
+
+def errors_vs(got, ref):
+    """Errors of one GPU path (host arrays: x, energy, forces, stress in GPa) against
+    reference results of the same shapes: max abs and max-normalised relative."""
+    def rel(a, b):
+        return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+    return {"force_max_abs_eV_per_A": float(np.max(np.abs(got["forces"] - ref["forces"]))),
+            "force_max_rel": rel(got["forces"], ref["forces"]),
+            "stress_max_abs_GPa": float(np.max(np.abs(got["stress"] - ref["stress"]))),
+            "stress_max_rel": rel(got["stress"], ref["stress"]),
+            "energy_rel": abs(got["energy"] - ref["energy"]) / abs(ref["energy"]),
+            "B_max_rel": rel(got["x"], ref["x"])}
+
+
+def oracle_results(ref):
+    """The oracle's results in the GPU paths' units: stress (1, 6) GPa in the reference's
+    Voigt order and sign, from its virial (which carries 1/V)."""
+    from pyxtal_ff_gb300.calculator import EV_A3_TO_GPA, VOIGT
+    return {"x": ref["x"], "energy": float(ref["energy"]), "forces": ref["forces"],
+            "stress": -(ref["virial"].reshape(1, 9)[:, VOIGT]) * EV_A3_TO_GPA}
 
 
 def run_reference(args, ws, rank):
@@ -260,7 +299,7 @@ def run_reference(args, ws, rank):
     nth = os.cpu_count() or 1
     for _ in range(args.warmup):
         cpu_run(atoms, coef, nth)
-    times = [cpu_run(atoms, coef, nth) for _ in range(args.steps)]
+    times = [cpu_run(atoms, coef, nth)[0] for _ in range(args.steps)]
     t = float(np.sum(times))
     value = len(atoms) * args.steps / t
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "atoms/s", "n_gpus": args.gpus,
@@ -268,6 +307,7 @@ def run_reference(args, ws, rank):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded)", "config": CONFIG,
             "cpu_baseline": {"value": value, "unit": "atoms/s", "cores": nth, "kind": "port",
+                             "cpu_model": cpu_model(),
                              "sample": "all 32000 centres of the workload per step (oracle, OpenMP)"},
             "e2e": {"value": value, "unit": "atoms/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -545,12 +585,13 @@ def main():
     res_eager = calc.compute(batch, model)
     graph_equals_eager = all(torch.equal(res[k], res_eager[k]) for k in ("energy", "forces", "virial", "x"))
     e64 = float((d64["x"].double() @ coef_t).sum())
-    err = {"force_max_abs_eV_per_A": float((res["forces"] - c64["forces"]).abs().max()),
-           "force_max_rel": float((res["forces"] - c64["forces"]).abs().max() / c64["forces"].abs().max()),
-           "stress_max_abs_GPa": float((res["stress"] - stress64).abs().max()),
-           "energy_rel": abs(float(res["energy"].sum()) - e64) / abs(e64),
-           "B_max_rel": float((res["x"].double() - d64["x"]).abs().max() / d64["x"].abs().max()),
-           "graph_bitwise_equals_uncaptured": bool(graph_equals_eager)}
+    # host copies of both GPU paths' results (the oracle comparison comes after the CPU leg)
+    got32 = {"x": res["x"].double().cpu().numpy(), "energy": float(res["energy"].sum()) - bias0,
+             "forces": res["forces"].cpu().numpy(), "stress": res["stress"].cpu().numpy()}
+    got64 = {"x": d64["x"].cpu().numpy(), "energy": e64, "forces": c64["forces"].cpu().numpy(),
+             "stress": stress64.cpu().numpy()}
+    err = errors_vs(got32, got64)
+    err["graph_bitwise_equals_uncaptured"] = bool(graph_equals_eager)
     del d64, c64
     fp64 = {"ms_per_step": ms64, "atoms_per_s": ws * natoms / (ms64 * 1e-3),
             "speedup_fp32_adjoint_over_fp64_plain": ms64 / (t_dev / args.steps)}
@@ -639,12 +680,20 @@ def main():
         ase_md = run_ase_md()
 
     # ---- CPU baseline (the oracle, all host threads), rank 0 only
+    # its results pin both GPU paths at the full workload: err_vs_oracle
     cpu = None
+    err_oracle = None
     if rank == 0 and not args.no_cpu:
         nth = os.cpu_count() or 1
-        tcpu = cpu_run(atoms, coef, nth)
+        tcpu, ref = cpu_run(atoms, coef, nth)
         cpu = {"value": natoms / tcpu, "unit": "atoms/s", "cores": nth, "kind": "port",
+               "cpu_model": cpu_model(),
                "sample": "all 32000 centres of the workload, one evaluation (oracle, OpenMP, FP64)"}
+        ro = oracle_results(ref)
+        err_oracle = {"fp32_adjoint": errors_vs(got32, ro), "fp64_plain": errors_vs(got64, ro),
+                      "oracle": "the C restatement of the reference path (FP64) on all 32000 centres",
+                      "targets": {"fp32_adjoint": "force <= 1e-4 eV/A, stress <= 1e-3 GPa",
+                                  "fp64_plain": "<= 1e-10 relative on every array"}}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "atoms/s", "n_gpus": ws, "steps": args.steps,
@@ -653,7 +702,8 @@ def main():
                 "data": "synthetic (seeded diamond-Si, sigma 0.1 A)", "config": CONFIG,
                 "pairs_per_s": ws * (nb.npair) * args.steps / (t_dev * 1e-3),
                 "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": int(launches),
-                "fp64_plain": fp64, "err_vs_fp64": err, "kernels": kernels, "train_step": train,
+                "fp64_plain": fp64, "err_vs_oracle": err_oracle, "err_vs_fp64": err, "kernels": kernels,
+                "train_step": train,
                 "ase_md_step": ase_md,
                 "peaks": {k: peaks[k] for k in ("hbm_gbs", "fp32_tflops", "fp64_tflops") if k in peaks}}
         print(json.dumps(line), flush=True)

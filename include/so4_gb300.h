@@ -368,7 +368,8 @@ int so4_jvp32(const so4_tables *t, const so4_params *p, const int *d_atom_struct
  * a fixed array of SO4_NOALLOC_SCRATCH_BYTES that every GPU loading the library
  * holds until exit.  Problems whose so4_adjoint_workspace_size() exceeds it
  * return SO4_ERR_TOO_LARGE.  The first call on each device looks up the
- * array's address (make it before any stream capture); calls that overlap on
+ * array's address (make it before any stream capture) and keeps it, so the
+ * entry point must not be used across a cudaDeviceReset; calls that overlap on
  * the GPU race on the shared array.  Allocates nothing. */
 #define SO4_NOALLOC_SCRATCH_BYTES (64u << 20)
 int so4_adjoint32_noalloc(const so4_tables *t, const so4_params *p, int nstruct, const int *d_atom_struct,

@@ -1117,7 +1117,10 @@ extern "C" int so4_adjoint32(const so4_tables *t, const so4_params *p, int nstru
 //
 // The device address of the array is looked up with cudaGetSymbolAddress the
 // first time the entry point runs on each device (with that device current);
-// that first call should come before any stream capture.
+// that first call should come before any stream capture.  The address is kept
+// for the life of the process: after cudaDeviceReset (or any teardown of the
+// device's primary context) the module is loaded again at another address, so
+// the entry point must not be used across a device reset.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[SO4_NOALLOC_SCRATCH_BYTES];
 
 #include <mutex>

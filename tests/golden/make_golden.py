@@ -1,7 +1,7 @@
 """Generate the golden vectors in tests/golden/ by running the REFERENCE itself.
 
-This script runs only in the build container, where the reference source tree
-is readable (default /root/reference, or $PYXTAL_FF_REF).  It imports the
+This script runs only where the reference source tree is readable; its root
+(the directory holding ``pyxtal_ff/``) must be given in $PYXTAL_FF_REF.  It imports the
 reference's own descriptor modules unchanged --
 ``pyxtal_ff/descriptors/SO4.py``, ``SNAP.py``, ``angular_momentum.py``,
 ``utils.py`` -- with three stand-ins for what this container lacks:
@@ -25,7 +25,7 @@ reference.npz with the reference's factorial table and CG lists.  Large cases
 keep x and seq in full, the pair arrays of the first centres, and per-atom /
 whole-array reductions of the rest.
 
-    python tests/golden/make_golden.py [--only name ...]
+    PYXTAL_FF_REF=<reference root> python tests/golden/make_golden.py [--only name ...]
 """
 import argparse
 import builtins
@@ -43,7 +43,12 @@ sys.path.insert(0, REPO)
 
 from pyxtal_ff_gb300 import structures as S  # noqa: E402
 
-REF = os.environ.get("PYXTAL_FF_REF", "/root/reference")
+def reference_root():
+    """The reference's source root, from $PYXTAL_FF_REF (required: there is no default)."""
+    ref = os.environ.get("PYXTAL_FF_REF")
+    if not ref or not os.path.isdir(os.path.join(ref, "pyxtal_ff", "descriptors")):
+        raise SystemExit("set PYXTAL_FF_REF to the reference's source root (the directory holding pyxtal_ff/)")
+    return ref
 
 
 # --------------------------------------------------------------------------- stubs
@@ -140,12 +145,13 @@ def _int_range(*args):
 
 
 def load_reference():
+    ref = reference_root()
     _install_numba_stub()
     _install_ase_stub()
     pkg = types.ModuleType("pyxtal_ff")
-    pkg.__path__ = [os.path.join(REF, "pyxtal_ff")]
+    pkg.__path__ = [os.path.join(ref, "pyxtal_ff")]
     sub = types.ModuleType("pyxtal_ff.descriptors")
-    sub.__path__ = [os.path.join(REF, "pyxtal_ff", "descriptors")]
+    sub.__path__ = [os.path.join(ref, "pyxtal_ff", "descriptors")]
     sys.modules["pyxtal_ff"] = pkg
     sys.modules["pyxtal_ff.descriptors"] = sub
     import importlib

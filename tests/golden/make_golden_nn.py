@@ -3,8 +3,8 @@ REFERENCE's own ``NeuralNetwork.calculate_properties``
 (pyxtal_ff/models/neuralnetwork.py:579-678) on descriptors the reference's SO4/SNAP
 code computed.
 
-Runs only in the build container, where the reference tree is readable (default
-/root/reference, or $PYXTAL_FF_REF).  Besides the descriptor stand-ins of
+Runs only where the reference tree is readable; its root must be given in
+$PYXTAL_FF_REF.  Besides the descriptor stand-ins of
 make_golden.py (numba, ASE, float range), the NN module needs stand-ins for what
 this container lacks and calculate_properties never calls: matplotlib (plotting),
 ``pyxtal_ff.models.optimizers.regressor`` (training) and
@@ -38,7 +38,6 @@ sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 import make_golden  # noqa: E402
 from pyxtal_ff_gb300 import structures as S  # noqa: E402
 
-REF = make_golden.REF
 
 
 def _install_nn_stubs():
@@ -54,7 +53,7 @@ def _install_nn_stubs():
                       ("matplotlib.ticker", tk)):
         sys.modules[name] = mod
     models = types.ModuleType("pyxtal_ff.models")
-    models.__path__ = [os.path.join(REF, "pyxtal_ff", "models")]
+    models.__path__ = [os.path.join(make_golden.reference_root(), "pyxtal_ff", "models")]
     sys.modules["pyxtal_ff.models"] = models
     opt = types.ModuleType("pyxtal_ff.models.optimizers")
     opt.__path__ = []
