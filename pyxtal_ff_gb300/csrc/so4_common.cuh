@@ -111,6 +111,15 @@ struct so4_tables {
     // it is finished (F the row scale of the scaled recursion, so4_tables.cu)
     int4 *d_hmap = nullptr;
     float *d_yscale = nullptr;  // n_half: the row-scale F of each half entry (so4_tables.cu)
+    double *d_yscale64 = nullptr;  // the same in FP64 (the plain path's scaled derivative pass)
+    // The plain path's dB/dr sections: every distinct Z block they read, contracted once per
+    // image by one lane of a warp, {first Z entry, half offset, entry count, level}, listed
+    // lane by lane (lane l owns [psec_ptr[l], psec_ptr[l + 1])) with the lanes' entry counts
+    // balanced; ksec[3 k + s]: the list position of component k's section s.
+    int4 *d_psec = nullptr;
+    int *d_psec_ptr = nullptr;  // 33
+    int *d_ksec = nullptr;      // 3 nB
+    int n_psec = 0;
     // B partial slots of the window kernels: one per (window unit, B block), component k
     // owning slots [bpos[k], bpos[k + 1]) in row order
     int *d_bpos = nullptr;  // nB + 1
@@ -340,6 +349,114 @@ __device__ void warp_uarray(const SmallTables &st, const T *rootpq, const CK<T> 
                     for (int c = 0; c < 3; ++c) {
                         const cx<T> dP = prev_row(dH + c * n_half + st.h_block[l - 1], l, mb, ma);
                         dv[c] = cadd(dv[c], cscale(cadd(cmul(ck.cda[c], P), cmul(ck.ca, dP)), rp));
+                    }
+                }
+            }
+            Hl[e] = v;
+            if (DERIV) {
+#pragma unroll
+                for (int c = 0; c < 3; ++c) dH[c * n_half + st.h_block[l] + e] = dv[c];
+            }
+        }
+        __syncwarp();
+        if ((l & 1) == 0) {
+            // middle row mb = l/2: centre -> conj, upper half -> mirror of lower half
+            const int mid = (l / 2) * ncol;
+            const int h = l / 2;
+            for (int ma = h + lane; ma <= l; ma += 32) {
+                const int src = (ma == h) ? ma : (l - ma);
+                const bool neg = ((h + ma) & 1) != 0;
+                cx<T> v = cconj(Hl[mid + src]);
+                if (neg && ma != h) {
+                    v.re = -v.re;
+                    v.im = -v.im;
+                }
+                Hl[mid + ma] = v;
+                if (DERIV) {
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        cx<T> *dHl = dH + c * n_half + st.h_block[l];
+                        cx<T> dv = cconj(dHl[mid + src]);
+                        if (neg && ma != h) {
+                            dv.re = -dv.re;
+                            dv.im = -dv.im;
+                        }
+                        dHl[mid + ma] = dv;
+                    }
+                }
+            }
+            __syncwarp();
+        }
+    }
+}
+
+// acc += a b and acc -= a b on complex values, as four FMAs each.
+template <typename T>
+__device__ __forceinline__ void cmac(cx<T> &acc, const cx<T> &a, const cx<T> &b) {
+    acc.re = fma(a.re, b.re, fma(-a.im, b.im, acc.re));
+    acc.im = fma(a.re, b.im, fma(a.im, b.re, acc.im));
+}
+template <typename T>
+__device__ __forceinline__ void cmsub(cx<T> &acc, const cx<T> &a, const cx<T> &b) {
+    acc.re = fma(-a.re, b.re, fma(a.im, b.im, acc.re));
+    acc.im = fma(-a.re, b.im, fma(-a.im, b.re, acc.im));
+}
+
+// warp_uarray in the scaled form V_l[mb][ma] = U_l[mb][ma] / F, F = sqrt(C(l, mb) / C(l, ma))
+// (C binomial; the row-scale table of so4_tables.cu).  The recursion's coefficients
+// rootpq[l-ma][l-mb] and rootpq[ma][l-mb] cancel against the scale:
+//   V_l[mb][ma] = conj(a) V_{l-1}[mb][ma] - conj(b) V_{l-1}[mb][ma-1],
+// and the chain-start mirror and the middle-row symmetry keep their form, because
+// C(l, ma) = C(l, l - ma).  So U = F V, and a contraction Re sum conj(dU) Z equals
+// Re sum conj(dV) (F Z): callers pre-scale Z by F instead of unscaling every row.
+// 56 FMAs per entry with DERIV against about 92 operations in warp_uarray.
+template <typename T, bool DERIV>
+__device__ void warp_vrows(const SmallTables &st, const CK<T> &ck, cx<T> *H, cx<T> *dH, int n_half, int lane) {
+    const int ldim = st.twol + 1;
+    if (lane == 0) {
+        H[0] = mk<T>(T(1), T(0));
+        if (DERIV) {
+            dH[0] = mk<T>(T(0), T(0));
+            dH[n_half] = mk<T>(T(0), T(0));
+            dH[2 * n_half] = mk<T>(T(0), T(0));
+        }
+    }
+    __syncwarp();
+    for (int l = 1; l < ldim; ++l) {
+        const int ncol = l + 1;
+        const int n = (l / 2 + 1) * ncol;
+        cx<T> *Hl = H + st.h_block[l];
+        const cx<T> *Hp = H + st.h_block[l - 1];
+        for (int e = lane; e < n; e += 32) {
+            const int mb = e / ncol;
+            const int ma = e - mb * ncol;
+            cx<T> v = mk<T>(T(0), T(0));
+            cx<T> dv[3];
+            if (DERIV) {
+#pragma unroll
+                for (int c = 0; c < 3; ++c) dv[c] = mk<T>(T(0), T(0));
+            }
+            if (ma > 0) {
+                const cx<T> P = prev_row(Hp, l, mb, ma - 1);
+                cmsub(v, ck.cb, P);
+                if (DERIV) {
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        const cx<T> dP = prev_row(dH + c * n_half + st.h_block[l - 1], l, mb, ma - 1);
+                        cmsub(dv[c], ck.cdb[c], P);
+                        cmsub(dv[c], ck.cb, dP);
+                    }
+                }
+            }
+            if (ma < l) {
+                const cx<T> P = prev_row(Hp, l, mb, ma);
+                cmac(v, ck.ca, P);
+                if (DERIV) {
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        const cx<T> dP = prev_row(dH + c * n_half + st.h_block[l - 1], l, mb, ma);
+                        cmac(dv[c], ck.cda[c], P);
+                        cmac(dv[c], ck.ca, dP);
                     }
                 }
             }

@@ -7,8 +7,12 @@
 //      partials are added in warp order (deterministic);
 //   2. all Z entries (compute_zi, :1020-1068) into shared memory;
 //   3. B (compute_bi, :1071-1111);
-//   4. warps split the pairs; per image: U and dU (the recursions :840-987),
-//      then each lane owns bispectrum components k and forms
+//   4. warps split the pairs; per image: U and dU (the recursions :840-987) in the
+//      scaled row form of warp_vrows, contracted with Z pre-scaled by the row scale.
+//      The sections S(Z block) = Re sum' conj(dU_lam) Z of every distinct block the
+//      components read are formed once per image (lanes take the blocks, balanced by
+//      entry count: several components share a block), then each lane owns
+//      bispectrum components k and forms
 //      dB_k/dr = 2 S_l + 2 (l+1)/(l1+1) S_l1 + 2 (l+1)/(l2+1) S_l2  (:1113-1227)
 //      with S_lam = w u_norm Re sum' conj(sfac dU + dsfac r^ U) Z (dudr, :1001-1018);
 //      per pair it keeps D = sum t and E = sum r (x) t over the pair's images;
@@ -33,6 +37,10 @@ struct PlainArgs {
     const double *pos, *w_nb, *w_site, *img_r;
     const int32_t *img_ptr, *img_j, *pair_ptr, *pair_img, *nsite;
     const T *cg, *rootpq;
+    const T *fscale;  // n_half: the row scale F of each half entry (U = F V)
+    const int4 *psec;  // distinct Z blocks of the dB/dr sections, lane by lane (so4_tables.cu)
+    const int *psec_ptr, *ksec;
+    int n_psec;
     const ZEnt *zent;
     const BEnt *bent;
     SmallTables st;
@@ -58,6 +66,7 @@ __global__ void __launch_bounds__(NW * 32) k_plain(PlainArgs<T> A) {
     cx<T> *dHw = Hw + nh;
     T *Dsum = (T *)(Z + nz + NW * 4 * nh);  // [NW][nB][3]
     T *Eself = Dsum + NW * nB * 3;           // [nB][9]
+    T *Sw = Eself + nB * 9 + wid * 4 * A.n_psec;  // per warp: [n_psec][4] section sums of one image
     for (int q = tid; q < ldim * ldim; q += NW * 32) rootpq[q] = A.rootpq[q];
     __syncthreads();
 
@@ -76,6 +85,11 @@ __global__ void __launch_bounds__(NW * 32) k_plain(PlainArgs<T> A) {
     // ---- 3. B
     block_b<T, NW, T>(A.bent, nB, Uh, Z, A.x + (size_t)a * nB);
     if (!A.want_deriv) return;
+    // the derivative pass carries the rows in the scaled form V (warp_vrows): Z times the
+    // row scale F of its half entry, so that Re conj(dU) Z = Re conj(dV) (F Z)
+    __syncthreads();
+    for (int q = tid; q < nz; q += NW * 32) Z[q] = cscale(Z[q], A.fscale[A.zent[q].jh]);
+    __syncthreads();
 
     // ---- 4. dB/dr per image, accumulated per pair
     const double Ri[3] = {A.pos[3 * a], A.pos[3 * a + 1], A.pos[3 * a + 2]};
@@ -101,7 +115,41 @@ __global__ void __launch_bounds__(NW * 32) k_plain(PlainArgs<T> A) {
             if (r < T(1e-8)) continue;
             CK<T> ck;
             make_ck<T, true>(x, y, z, r, psi_fac * r, ck);
-            warp_uarray<T, true>(st, rootpq, ck, Hw, dHw, nh, lane);
+            warp_vrows<T, true>(st, ck, Hw, dHw, nh, lane);
+            // every distinct Z block of the sections once: lane `lane` contracts its share of
+            // the list, four sums per block (U and the three dU components) into Sw
+            const int u1 = __ldg(A.psec_ptr + lane + 1);
+            for (int u = __ldg(A.psec_ptr + lane); u < u1; ++u) {
+                const int4 ps = __ldg(A.psec + u);  // first Z entry, half offset, entries, level
+                const int zo = ps.x, h = ps.y, cnt = ps.z, lam = ps.w;
+                T su = T(0), s0 = T(0), s1 = T(0), s2 = T(0);
+                // entries of weight 1 as two FMAs per accumulator; an even level's section
+                // ends at the middle-row centre, weight 1/2, added after the loop
+                const int cfull = (lam & 1) ? cnt : cnt - 1;
+                for (int e = 0; e < cfull; ++e) {
+                    const cx<T> zv = Z[zo + e];
+                    const cx<T> hv = Hw[h + e], d0 = dHw[h + e], d1 = dHw[nh + h + e], d2 = dHw[2 * nh + h + e];
+                    su = fma(hv.re, zv.re, fma(hv.im, zv.im, su));
+                    s0 = fma(d0.re, zv.re, fma(d0.im, zv.im, s0));
+                    s1 = fma(d1.re, zv.re, fma(d1.im, zv.im, s1));
+                    s2 = fma(d2.re, zv.re, fma(d2.im, zv.im, s2));
+                }
+                if (cfull < cnt) {
+                    const int e = cfull;
+                    const cx<T> zv = Z[zo + e];
+                    const T zr = T(0.5) * zv.re, zi = T(0.5) * zv.im;
+                    const cx<T> hv = Hw[h + e], d0 = dHw[h + e], d1 = dHw[nh + h + e], d2 = dHw[2 * nh + h + e];
+                    su = fma(hv.re, zr, fma(hv.im, zi, su));
+                    s0 = fma(d0.re, zr, fma(d0.im, zi, s0));
+                    s1 = fma(d1.re, zr, fma(d1.im, zi, s1));
+                    s2 = fma(d2.re, zr, fma(d2.im, zi, s2));
+                }
+                Sw[4 * u] = su;
+                Sw[4 * u + 1] = s0;
+                Sw[4 * u + 2] = s1;
+                Sw[4 * u + 3] = s2;
+            }
+            __syncwarp();
             T sf, dsf;
             cutoff_fn<T>(cid, r, rc, sf, dsf);
             const T wj = (T)A.w_nb[A.img_j[m]];
@@ -114,20 +162,11 @@ __global__ void __launch_bounds__(NW * 32) k_plain(PlainArgs<T> A) {
                 T t[3] = {T(0), T(0), T(0)};
 #pragma unroll
                 for (int sec = 0; sec < 3; ++sec) {
-                    const int lam = be.lam[sec], cnt = be.cnt[sec], h = be.h[sec], zo = be.z[sec];
-                    T su = T(0), s0 = T(0), s1 = T(0), s2 = T(0);
-                    for (int e = 0; e < cnt; ++e) {
-                        const cx<T> zv = Z[zo + e];
-                        T wt = ((lam % 2 == 0) && e == cnt - 1) ? T(0.5) : T(1);
-                        su += wt * redot(Hw[h + e], zv);
-                        s0 += wt * redot(dHw[h + e], zv);
-                        s1 += wt * redot(dHw[nh + h + e], zv);
-                        s2 += wt * redot(dHw[2 * nh + h + e], zv);
-                    }
-                    const T f = wj * (T)st.unorm[lam] * (T)be.fac[sec];
-                    t[0] += f * (sf * s0 + dsf * gr[0] * su);
-                    t[1] += f * (sf * s1 + dsf * gr[1] * su);
-                    t[2] += f * (sf * s2 + dsf * gr[2] * su);
+                    const T *S = Sw + 4 * __ldg(A.ksec + 3 * k + sec);
+                    const T f = wj * (T)st.unorm[be.lam[sec]] * (T)be.fac[sec];
+                    t[0] += f * (sf * S[1] + dsf * gr[0] * S[0]);
+                    t[1] += f * (sf * S[2] + dsf * gr[1] * S[0]);
+                    t[2] += f * (sf * S[3] + dsf * gr[2] * S[0]);
                 }
                 const T rv[3] = {x, y, z};
 #pragma unroll
@@ -195,7 +234,7 @@ size_t plain_smem_bytes(const so4_tables *t, int NW) {
     const int ld = t->ldim;
     size_t b = sizeof(T) * ((ld * ld + 1) & ~1);
     b += sizeof(cx<T>) * ((size_t)t->n_half + t->n_u + t->n_z + (size_t)NW * 4 * t->n_half);
-    b += sizeof(T) * ((size_t)NW * t->n_b * 3 + (size_t)t->n_b * 9);
+    b += sizeof(T) * ((size_t)NW * t->n_b * 3 + (size_t)t->n_b * 9 + (size_t)NW * 4 * t->n_psec);
     return b;
 }
 
@@ -236,6 +275,11 @@ int run_plain(const so4_tables *t, const so4_params *p, const so4_geom *geom, co
     A.nsite = nsite;
     A.cg = (const T *)(sizeof(T) == 8 ? (const void *)t->d_cg64 : (const void *)t->d_cg32);
     A.rootpq = (const T *)(sizeof(T) == 8 ? (const void *)t->d_rootpq64 : (const void *)t->d_rootpq32);
+    A.fscale = (const T *)(sizeof(T) == 8 ? (const void *)t->d_yscale64 : (const void *)t->d_yscale);
+    A.psec = t->d_psec;
+    A.psec_ptr = t->d_psec_ptr;
+    A.ksec = t->d_ksec;
+    A.n_psec = t->n_psec;
     A.zent = t->d_z;
     A.bent = t->d_b;
     fill_small_tables(t, A.st);

@@ -92,6 +92,10 @@ void free_device(so4_tables *t) {
     cudaFree(t->d_hfull);
     cudaFree(t->d_hmap);
     cudaFree(t->d_yscale);
+    cudaFree(t->d_yscale64);
+    cudaFree(t->d_psec);
+    cudaFree(t->d_psec_ptr);
+    cudaFree(t->d_ksec);
     cudaFree(t->d_bpos);
     cudaFree(t->d_wunit_y);
     cudaFree(t->d_wseg_y);
@@ -275,6 +279,46 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
                 }
         }
     }
+    // The plain path's dB/dr: the three sections of every component read Z blocks that
+    // several components share (165 sections over 125 distinct blocks at lmax 4), and the
+    // components' section sizes differ several-fold.  So each distinct block is contracted
+    // once per image, the blocks dealt to the 32 lanes of a warp largest first, each to the
+    // lane with the fewest entries so far (ties: the lower lane), and listed lane by lane.
+    std::vector<int4> usec;  // {first Z entry, half offset, entry count, level}
+    std::vector<int> ksec_u(3 * (size_t)t->n_b);
+    for (int k = 0; k < t->n_b; ++k)
+        for (int s = 0; s < 3; ++s) {
+            int u = 0;
+            while (u < (int)usec.size() && usec[u].x != bent[k].z[s]) ++u;
+            if (u == (int)usec.size()) usec.push_back(make_int4(bent[k].z[s], bent[k].h[s], bent[k].cnt[s], bent[k].lam[s]));
+            ksec_u[3 * k + s] = u;
+        }
+    std::vector<int> order(usec.size());
+    for (size_t u = 0; u < usec.size(); ++u) order[u] = (int)u;
+    std::stable_sort(order.begin(), order.end(), [&](int p, int q) { return usec[p].z > usec[q].z; });
+    std::vector<int> lane_of(usec.size()), load(32, 0);
+    for (int u : order) {
+        int best = 0;
+        for (int l = 1; l < 32; ++l)
+            if (load[l] < load[best]) best = l;
+        lane_of[u] = best;
+        load[best] += usec[u].z;
+    }
+    std::vector<int4> psec;
+    std::vector<int> psec_ptr(33, 0), pos_of(usec.size());
+    for (int l = 0; l < 32; ++l) {
+        psec_ptr[l] = (int)psec.size();
+        for (int u : order)
+            if (lane_of[u] == l) {
+                pos_of[u] = (int)psec.size();
+                psec.push_back(usec[u]);
+            }
+    }
+    psec_ptr[32] = (int)psec.size();
+    std::vector<int> ksec(3 * (size_t)t->n_b);
+    for (size_t i = 0; i < ksec.size(); ++i) ksec[i] = pos_of[ksec_u[i]];
+    t->n_psec = (int)psec.size();
+
     // blocks grouped by their third index (the level of Y they feed)
     std::vector<int> yptr(ld + 1, 0), ylist;
     for (int lam = 0; lam < ld; ++lam) {
@@ -532,6 +576,7 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
     };
     std::vector<int4> hmap;
     std::vector<float> yscale;
+    std::vector<double> yscale64;
     for (int l = 0; l < ld; ++l) {
         const float un = (float)t->unorm_l[l];
         for (int mb = 0; 2 * mb <= l; ++mb)
@@ -543,11 +588,13 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
                 std::memcpy(&b_un, &un, sizeof b_un);
                 hmap.push_back(make_int4((l * (l + 1) / 2 + ma) | (mb << 8) | ((ma == mb ? 1 : 0) << 15), b_unf, b_un, 0));
                 yscale.push_back((float)F);
+                yscale64.push_back(F);
             }
     }
     if (!rc) rc = upload(&t->d_hfull, hfull);
     if (!rc) rc = upload(&t->d_hmap, hmap);
     if (!rc) rc = upload(&t->d_yscale, yscale);
+    if (!rc) rc = upload(&t->d_yscale64, yscale64);
     if (!rc) rc = upload(&t->d_bpos, bpos);
     if (!rc) rc = upload(&t->d_wunit_y, wunit_y);
     if (!rc) rc = upload(&t->d_wseg_y, wseg_y);
@@ -566,6 +613,9 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
     if (!rc) rc = upload(&t->d_rootpq32, rp32);
     if (!rc) rc = upload(&t->d_z, zent);
     if (!rc) rc = upload(&t->d_b, bent);
+    if (!rc) rc = upload(&t->d_psec, psec);
+    if (!rc) rc = upload(&t->d_psec_ptr, psec_ptr);
+    if (!rc) rc = upload(&t->d_ksec, ksec);
     if (!rc) rc = upload(&t->d_blk, blks);
     if (!rc) rc = upload(&t->d_yblk_ptr, yptr);
     if (!rc) rc = upload(&t->d_yblk, ylist);
