@@ -68,6 +68,21 @@ def cpu_model():
     return None
 
 
+def reference_python_record():
+    """Timings of the reference's own Python code (numba unavailable: CPython + NumPy) and of
+    the oracle on one thread of the same host, taken where the reference source can be
+    imported (tests/golden/time_reference.py writes tests/golden/reference_timing.json); a
+    side record, not measured in this run."""
+    try:
+        with open(os.path.join(HERE, "tests", "golden", "reference_timing.json")) as fh:
+            d = json.load(fh)
+    except (OSError, ValueError):
+        return None
+    d["note"] = ("measured by tests/golden/time_reference.py on the host named here, not in this run: the "
+                 "reference's source tree is not present on the GPU host")
+    return d
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -309,7 +324,8 @@ def run_reference(args, ws, rank):
             "cpu_baseline": {"value": value, "unit": "atoms/s", "cores": nth, "kind": "port",
                              "cpu_model": cpu_model(),
                              "sample": "all 32000 centres of the workload per step (oracle, OpenMP)"},
-            "e2e": {"value": value, "unit": "atoms/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "e2e": {"value": value, "unit": "atoms/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "reference_python": reference_python_record()}
     print(json.dumps(line), flush=True)
 
 
@@ -363,6 +379,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-train", action="store_true", help="skip the training-step leg")
+    ap.add_argument("--no-tune", action="store_true", help="default launch shapes instead of the autotuner's choice")
     ap.add_argument("--quick", action="store_true",
                     help="device-resident steps only (no e2e, FP64, CPU or peak legs); for profiler runs")
     ap.add_argument("--contract-cells", type=int, default=0,
@@ -393,13 +410,21 @@ def main():
     def max_over_ranks(v):
         return replicas.max_over_ranks(v, device=dev)
 
-    from pyxtal_ff_gb300 import _lib, engine, flops
+    from pyxtal_ff_gb300 import _lib, autotune, engine, flops
     from pyxtal_ff_gb300.calculator import EV_A3_TO_GPA, Batch, LinearModel, SO4Calculator
 
     atoms, coef = workload()
     batch = Batch([atoms])
     calc = SO4Calculator(lmax=LMAX, rcut=RCUT, kind="SNAP", weights={"Si": 1.0}, rfac0=1.0, device=dev)
     model = LinearModel(coef).to(dev)
+    # launch shapes: the autotuner's choice for this workload, searched afresh (outside every
+    # timed region; each candidate checked against the FP64 plain path first)
+    tuning = None
+    if not args.no_tune:
+        rep = autotune.autotune_step(calc, batch, model, use_cache=False)
+        tuning = {"choice": rep["choice"], "ms": rep["ms"], "default_ms": rep["default_ms"],
+                  "evaluated": len(rep["evaluated"]),
+                  "rejected": sum(1 for e in rep["evaluated"] if e["ms"] is None)}
     calc.prepare(batch)
     pos_dev = torch.from_numpy(batch.positions).to(dev)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
@@ -653,7 +678,21 @@ def main():
         from pyxtal_ff_gb300 import structures as S
         from pyxtal_ff_gb300.train import ForceMatching
         tstructs = S.si_batch(512, seed=4, sizes=range(1, 9), max_cells=8, strain=0.04, sigma=0.1)
-        fm = ForceMatching(tstructs, lmax=3, rcut=4.9, seed=4)
+        tbatch = Batch(tstructs)
+        tchoice, ttune = None, None
+        if not args.no_tune:
+            from pyxtal_ff_gb300.train import stillinger_weber
+            targets = stillinger_weber(tbatch)
+            tcalc = SO4Calculator(lmax=3, rcut=4.9, kind="SNAP", weights={"Si": 1.0}, rfac0=1.0, device=dev)
+            rep = autotune.autotune_training(
+                lambda c: ForceMatching(tbatch, lmax=3, rcut=4.9, seed=4, targets=targets, tuning=c), tcalc, tbatch,
+                use_cache=False)
+            tchoice = autotune.Choice.from_dict(rep["choice"])
+            ttune = {"choice": rep["choice"], "ms": rep["ms"], "default_ms": rep["default_ms"],
+                     "evaluated": len(rep["evaluated"]),
+                     "rejected": sum(1 for e in rep["evaluated"] if e["ms"] is None)}
+            del tcalc
+        fm = ForceMatching(tbatch, lmax=3, rcut=4.9, seed=4, tuning=tchoice)
 
         def time_steps(nstep=10):
             for _ in range(2):
@@ -671,7 +710,8 @@ def main():
         tms = time_steps()
         train = {"workload": "512 Si structures (8-64 atoms, 22256 atoms), SO4 lmax 3, rcut 4.9, MLP 30-30 tanh, "
                              "loss MSE(E/atom)+0.1 MSE(F), Adam; B and U_tot held on device; one CUDA graph per step",
-                 "ms_per_step": tms, "atoms_per_s": fm.batch.natoms / (tms * 1e-3), "uncaptured_ms_per_step": t_eager}
+                 "ms_per_step": tms, "atoms_per_s": fm.batch.natoms / (tms * 1e-3), "uncaptured_ms_per_step": t_eager,
+                 "tuning": ttune}
         del fm
 
     # ---- the reference's published MD workload through the ASE-calculator interface, extra line item
@@ -704,7 +744,7 @@ def main():
                 "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": int(launches),
                 "fp64_plain": fp64, "err_vs_oracle": err_oracle, "err_vs_fp64": err, "kernels": kernels,
                 "train_step": train,
-                "ase_md_step": ase_md,
+                "ase_md_step": ase_md, "tuning": tuning, "reference_python": reference_python_record(),
                 "peaks": {k: peaks[k] for k in ("hbm_gbs", "fp32_tflops", "fp64_tflops") if k in peaks}}
         print(json.dumps(line), flush=True)
     if ws > 1:

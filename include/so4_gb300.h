@@ -87,6 +87,30 @@ typedef struct {
  * normalize_u selects u_norm = 4 pi / sqrt(l+1) (SO4.py:1304-1311). */
 int so4_tables_create(int twol, int normalize_u, so4_tables **out);
 int so4_tables_destroy(so4_tables *t);
+
+/* Launch shapes of the FP32 kernels, chosen per (lmax, workload, device) by the
+ * autotuner (pyxtal_ff_gb300/autotune.py).  No counterpart in the reference, whose
+ * serial driver loop (SO4.py:1414-1548) has nothing to tune.  Zero in a field selects
+ * the default.
+ *   wkmax       entries per window unit of the Z pass, 1..5 (default 5): the window
+ *               work lists are built for it (a smaller unit: more units, fewer
+ *               registers per ring, other rounding of the Z sums);
+ *   rev_threads threads per CTA of the per-image pass, 128 or 256 (default 256 up to
+ *               twol 8, 128 above; only twol 6 and 8 have both);
+ *   utot_warps  warps (centres) per CTA of the U_tot pass, 2, 4 or 8 (default 4; only
+ *               twol 6 and 8 have all three). */
+typedef struct {
+    int wkmax;
+    int rev_threads;
+    int utot_warps;
+} so4_tuning;
+/* so4_tables_create with a tuning (NULL: the defaults).  SO4_ERR_ARG for a value
+ * outside the ranges above; SO4_ERR_UNSUPPORTED for a CTA shape not built for this
+ * twol, or for a wkmax whose window kernels (more units, so more B / JVP slots staged
+ * in shared memory) would not fit where the default ones do. */
+int so4_tables_create_tuned(int twol, int normalize_u, const so4_tuning *tune, so4_tables **out);
+/* The tuning a handle was built with, defaults filled in. */
+int so4_tables_get_tuning(const so4_tables *t, so4_tuning *out);
 /* sizes[0..7] = idxu, idxu_half, idxz, nB, idxcg, number of Z blocks,
  * B-section entries per atom (scratch of so4_linear_by32), window sub-segments */
 int so4_tables_sizes(const so4_tables *t, int *sizes);
@@ -380,6 +404,19 @@ int so4_adjoint32_noalloc(const so4_tables *t, const so4_params *p, int nstruct,
 
 /* Number of kernels this library has launched since it was loaded. */
 long long so4_launch_count(void);
+
+/* Programmatic dependent launch for the calling host thread's launches of U_tot
+ * (so4_utot32 and the forward), the window Z pass (so4_linear_by32, so4_adjoint_y32
+ * and the other window modes) and the per-image pass (so4_adjoint_deidrj32): with
+ * on != 0 each may be scheduled while the kernel before it in the stream finishes
+ * (its set-up overlaps that kernel's tail) and waits on the device for that kernel's
+ * results before reading them.  Off by default.  Only turn it on for a stream in which
+ * nothing between two of these launches writes the constant inputs they read before
+ * that wait (tables, beta): the captured step of a linear energy (a fixed beta) is
+ * such a stream.  No counterpart in the reference (its driver loop,
+ * pyxtal_ff/descriptors/SO4.py:1414-1548, is one serial CPU loop).  Returns the
+ * previous setting. */
+int so4_set_pdl(int on);
 
 /* Library version string. */
 const char *so4_version(void);

@@ -61,6 +61,11 @@ class Params(C.Structure):
     _fields_ = [("twol", C.c_int), ("cutoff_id", C.c_int), ("rcut", C.c_double), ("rfac0", C.c_double)]
 
 
+class Tuning(C.Structure):
+    """so4_tuning: launch shapes of the FP32 kernels (0 = the default)."""
+    _fields_ = [("wkmax", C.c_int), ("rev_threads", C.c_int), ("utot_warps", C.c_int)]
+
+
 _lib = None
 _vp, _i, _sz, _i64, _d = C.c_void_p, C.c_int, C.c_size_t, C.c_int64, C.c_double
 
@@ -77,6 +82,8 @@ def lib():
     sig = {
         "so4_version": (C.c_char_p, []),
         "so4_tables_create": (_i, [_i, _i, C.POINTER(_vp)]),
+        "so4_tables_create_tuned": (_i, [_i, _i, C.POINTER(Tuning), C.POINTER(_vp)]),
+        "so4_tables_get_tuning": (_i, [_vp, C.POINTER(Tuning)]),
         "so4_tables_destroy": (_i, [_vp]),
         "so4_tables_sizes": (_i, [_vp, C.POINTER(_i)]),
         "so4_tables_export": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp]),
@@ -112,6 +119,7 @@ def lib():
         "so4_gather_workspace_size": (_sz, [_i]),
         "so4_adjoint_gather": (_i, [_i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
         "so4_launch_count": (C.c_longlong, []),
+        "so4_set_pdl": (C.c_int, [C.c_int]),
         "so4_jvp_workspace_size": (_sz, [_vp, _i]),
         "so4_linear_workspace_size": (_sz, [_vp, _i, _i64]),
         "so4_utot32": (_i, [_vp, C.POINTER(Params), _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),

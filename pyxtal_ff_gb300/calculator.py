@@ -46,6 +46,8 @@ class Batch:
     """Host description of a batch of structures (cells, pbc, atom ranges, species)."""
 
     def __init__(self, structures, species_order=None):
+        structures = list(structures)
+        self.structures = structures
         pos, cells, pbcs, nums, syms = [], [], [], [], []
         for s in structures:
             p, c, b, n, y = as_arrays(s)
@@ -84,7 +86,7 @@ class SO4Calculator:
     """
 
     def __init__(self, lmax=3, rcut=3.5, kind="SO4", weights=None, rfac0=0.99363, cutoff_function="cosine",
-                 normalize_U=False, device="cuda"):
+                 normalize_U=False, device="cuda", tuning=None):
         engine.require_cuda()
         if kind not in ("SO4", "SNAP"):
             raise ValueError("kind must be 'SO4' or 'SNAP'")
@@ -98,11 +100,21 @@ class SO4Calculator:
         self.rfac0 = 1.0 if kind == "SO4" else float(rfac0)
         self.cutoff_function = cutoff_function
         self.device = torch.device(device)
-        with torch.cuda.device(self.device):
-            self.tables = engine.tables(self.twol, normalize_U)
+        self.normalize_U = bool(normalize_U)
         self.params = engine.params(self.twol, self.rcut, self.rfac0, cutoff_function)
         self._ws = None
         self._batch_key = None
+        self.set_tuning(tuning)
+
+    def set_tuning(self, tuning=None):
+        """Launch shapes (an autotune.Choice, e.g. from autotune.autotune_step; None: the
+        defaults): the kernels' tables and the captured step's branches and PDL."""
+        self.tuning = tuning
+        with torch.cuda.device(self.device):
+            self.tables = engine.tables(self.twol, self.normalize_U, None if tuning is None else tuning.kernel_tuning())
+        self.branches = 2 if tuning is None else int(tuning.branches)
+        self.pdl = False if tuning is None else bool(tuning.pdl)
+        self._ws = None
 
     @property
     def nB(self):
@@ -124,10 +136,12 @@ class SO4Calculator:
             self._batch_key = batch
         return self
 
-    def capture(self, batch: Batch, model, headroom=1.25, branches=2):
+    def capture(self, batch: Batch, model, headroom=1.25, branches=None, pdl=None):
         """The whole energy / forces / stress step of this batch layout as one CUDA graph
-        (see CapturedStep); call the result with new positions."""
-        return CapturedStep(self, batch, model, headroom=headroom, branches=branches)
+        (see CapturedStep); call the result with new positions.  branches / pdl default to
+        the calculator's tuning (2 and off untuned)."""
+        return CapturedStep(self, batch, model, headroom=headroom, branches=self.branches if branches is None else branches,
+                            pdl=self.pdl if pdl is None else pdl)
 
     def neighbors(self, batch: Batch, positions):
         return engine.build_neighbors(positions, batch.cells, batch.pbc, batch.atom_ptr, self.rcut, device=self.device)
@@ -221,8 +235,11 @@ class CapturedStep:
     (`SO4Calculator.capture`); it raises for non-finite positions like the eager path.
     """
 
-    def __init__(self, calc: "SO4Calculator", batch: Batch, model, headroom=1.25, branches=2):
+    def __init__(self, calc: "SO4Calculator", batch: Batch, model, headroom=1.25, branches=2, pdl=False):
         self.linear = isinstance(model, LinearModel)
+        # programmatic dependent launch between U_tot, the window pass and the per-image pass
+        # (so4_set_pdl): only for a linear energy, whose beta is fixed for the whole step
+        self.pdl = bool(pdl) and self.linear
         calc.prepare(batch)
         # the graph reads these per-batch tensors by address: hold them, so that a later
         # prepare() of another batch cannot free them under the graph
@@ -304,13 +321,21 @@ class CapturedStep:
         self.launches = int(L.so4_launch_count() - c0)  # kernels of this library in one replay
 
     def _enqueue(self):
+        if not self.linear:
+            self._enqueue_model()
+            return
+        L = engine.lib()
+        prev = L.so4_set_pdl(1 if self.pdl else 0)
+        try:
+            self._enqueue_linear()
+        finally:
+            L.so4_set_pdl(prev)
+
+    def _enqueue_linear(self):
         lay, calc, tab, L = self.layout, self.calc, self.calc.tables, engine.lib()
         b = self.nl
         _p = engine._ptr
         check = engine.check
-        if not self.linear:
-            self._enqueue_model()
-            return
         if self.branches == 1:
             engine.enqueue_neighbors(lay, self.pos, b, lite=True)
             check(L.so4_adjoint_linear32(tab.handle, C.byref(calc.params), lay.nstruct, _p(lay.atom_struct),

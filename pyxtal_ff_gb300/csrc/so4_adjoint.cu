@@ -98,7 +98,7 @@ __global__ void __launch_bounds__(NWF * 32) k_utot32(FwdArgs A) {
 // order, the self term f_c(0) w_site is put on the diagonal and u_norm applied
 // (SO4.py:1480-1505, 560-597).
 template <int TWOL, int NW>
-__global__ void __launch_bounds__(NW * 32, (TWOL <= 8) ? 4 : 1) k_utot_rc(FwdArgs A) {
+__global__ void __launch_bounds__(NW * 32, (TWOL <= 8) ? 16 / NW : 1) k_utot_rc(FwdArgs A) {
     using RC = RowChain<TWOL>;
     constexpr int W = TWOL + 1, NACC = acc_block(TWOL + 1);
     extern __shared__ __align__(16) float ut_smem[];  // [NW][32][2 * NACC]
@@ -108,6 +108,7 @@ __global__ void __launch_bounds__(NW * 32, (TWOL <= 8) ? 4 : 1) k_utot_rc(FwdArg
     float accr[NACC], acci[NACC];
 #pragma unroll
     for (int q = 0; q < NACC; ++q) accr[q] = acci[q] = 0.f;
+    pdl_wait();  // the neighbour list comes from the kernel before
     if (a < A.natoms) {
         const int m0 = A.img_ptr[a], m1 = A.img_ptr[a + 1];
         // Cayley-Klein parameters and weights of up to 32 images at once, one per lane;
@@ -157,6 +158,7 @@ __global__ void __launch_bounds__(NW * 32, (TWOL <= 8) ? 4 : 1) k_utot_rc(FwdArg
             }
         }
     }
+    pdl_trigger();  // the next kernel may start its set-up during this epilogue
     float *sw = ut_smem + (size_t)wid * 32 * 2 * NACC;
 #pragma unroll
     for (int q = 0; q < NACC; ++q) {
@@ -187,15 +189,22 @@ __global__ void __launch_bounds__(NW * 32, (TWOL <= 8) ? 4 : 1) k_utot_rc(FwdArg
     }
 }
 
-template <int TWOL>
-int launch_utot_rc(const FwdArgs &A, cudaStream_t st) {
-    constexpr int NW = 4;
+template <int TWOL, int NW>
+int launch_utot_rc_nw(const FwdArgs &A, cudaStream_t st) {
     const size_t smem = sizeof(float) * NW * 32 * 2 * acc_block(TWOL + 1);
     int rc = set_smem(k_utot_rc<TWOL, NW>, smem);
     if (rc) return rc;
-    k_utot_rc<TWOL, NW><<<(A.natoms + NW - 1) / NW, NW * 32, smem, st>>>(A);
-    so4_count_launch();
-    return SO4_OK;
+    return so4_launch_pdl(k_utot_rc<TWOL, NW>, dim3((A.natoms + NW - 1) / NW), dim3(NW * 32), smem, st, A);
+}
+
+// nw: warps (centres) per CTA, from the tables' tuning; 2 and 8 are built for twol 6 and 8
+template <int TWOL>
+int launch_utot_rc(const FwdArgs &A, int nw, cudaStream_t st) {
+    if constexpr (TWOL == 6 || TWOL == 8) {
+        if (nw == 2) return launch_utot_rc_nw<TWOL, 2>(A, st);
+        if (nw == 8) return launch_utot_rc_nw<TWOL, 8>(A, st);
+    }
+    return launch_utot_rc_nw<TWOL, 4>(A, st);
 }
 
 struct ZLArgs {
@@ -392,6 +401,7 @@ __global__ void __launch_bounds__(ZW_THREADS, 2) k_zw32(ZLArgs A) {
         const int i = threadIdx.x + r * ZW_THREADS;
         br[r] = (i < nbt) ? __ldg(bsrc + i) : 0.f;
     }
+    pdl_wait();  // U_tot (and, in the JVP, dU) come from the kernel before
     zw_load_utot(A.utot, A.hfull, a0, A.natoms, A.nh, A.nu, Ub);
     if (MODE == 1 || MODE == 2) {
         // coef[b][lane] = sum over the block's roles of role_f beta[atom][role_k], from the
@@ -441,6 +451,7 @@ __global__ void __launch_bounds__(ZW_THREADS, 2) k_zw32(ZLArgs A) {
         const int4 un = __ldg(A.unit + u);
         zw_unit_k<MODE>(un.x >> 24, A, un, Ul, coef, ca, a, lane);
     }
+    pdl_trigger();  // the next kernel may start its set-up during the slot sums
     if (MODE == 1) return;
     __syncthreads();
     // the sums of the slots, staged in shared memory over the U tiles (no longer read) when
@@ -551,7 +562,7 @@ __global__ void __launch_bounds__(NWD * 32) k_deidrj(DArgs A) {
 // U rows are kept in shared memory by the forward sweep; one backward sweep of Y
 // gives the gradients with respect to conj(a), conj(b).
 template <int TWOL, int NT>
-__global__ void __launch_bounds__(NT, (TWOL <= 8) ? 2 : 1) k_deidrj_rev(DArgs A, int64_t nimg) {
+__global__ void __launch_bounds__(NT, (TWOL <= 8) ? 512 / NT : 1) k_deidrj_rev(DArgs A, int64_t nimg) {
     using RC = RowChain<TWOL>;
     constexpr int W = TWOL + 1;
     constexpr int NIT = 32 / RC::IPW, PASS = NIT * RC::IPW;  // images per warp: one per lane
@@ -559,6 +570,7 @@ __global__ void __launch_bounds__(NT, (TWOL <= 8) ? 2 : 1) k_deidrj_rev(DArgs A,
     float2 *st = rv_smem + threadIdx.x;
     const int lane = threadIdx.x & 31;
     const int64_t wg = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    pdl_wait();  // Y comes from the kernel before
     const int grp = lane / RC::NCH, mb = lane - grp * RC::NCH;
     // the images are [img_ptr[0], img_ptr[natoms]) (img_ptr may point into a longer list
     // for a range of centres); nimg bounds their count (a capacity will do).  Warps past
@@ -661,10 +673,9 @@ __global__ void __launch_bounds__(NT, (TWOL <= 8) ? 2 : 1) k_deidrj_rev(DArgs A,
     }
 }
 
-template <int TWOL>
-int launch_deidrj_rev(const DArgs &D, int64_t nimg, cudaStream_t st) {
+template <int TWOL, int NT>
+int launch_deidrj_rev_nt(const DArgs &D, int64_t nimg, cudaStream_t st) {
     using RC = RowChain<TWOL>;
-    constexpr int NT = (TWOL <= 8) ? 256 : 128;
     if (nimg <= 0) return SO4_OK;
     const size_t smem = sizeof(float2) * (size_t)acc_block(TWOL + 1) * NT;
     const int rc = so4_set_smem((const void *)k_deidrj_rev<TWOL, NT>, smem);
@@ -672,9 +683,17 @@ int launch_deidrj_rev(const DArgs &D, int64_t nimg, cudaStream_t st) {
     constexpr int PASS = (32 / RC::IPW) * RC::IPW;  // images per warp (k_deidrj_rev)
     const int64_t warps = (nimg + PASS - 1) / PASS;
     const int64_t blocks = (warps + NT / 32 - 1) / (NT / 32);
-    k_deidrj_rev<TWOL, NT><<<(unsigned)blocks, NT, smem, st>>>(D, nimg);
-    so4_count_launch();
-    return SO4_OK;
+    return so4_launch_pdl(k_deidrj_rev<TWOL, NT>, dim3((unsigned)blocks), dim3(NT), smem, st, D, nimg);
+}
+
+// nt: threads per CTA, from the tables' tuning (256 up to twol 8, 128 above; both for twol 6, 8)
+template <int TWOL>
+int launch_deidrj_rev(const DArgs &D, int64_t nimg, int nt, cudaStream_t st) {
+    if constexpr (TWOL == 6 || TWOL == 8) {
+        if (nt == 128) return launch_deidrj_rev_nt<TWOL, 128>(D, nimg, st);
+        return launch_deidrj_rev_nt<TWOL, 256>(D, nimg, st);
+    }
+    return launch_deidrj_rev_nt<TWOL, (TWOL <= 8) ? 256 : 128>(D, nimg, st);
 }
 
 
@@ -876,14 +895,11 @@ static int launch_zw(const so4_tables *t, const ZLArgs &Z, int natoms, size_t sm
     if (2 * (with_ca + 1024) <= 228 * 1024) {
         rc = set_smem(k_zw32<MODE, true>, with_ca);
         if (rc) return rc;
-        k_zw32<MODE, true><<<groups, ZW_THREADS, with_ca, st>>>(Z);
-    } else {
-        rc = set_smem(k_zw32<MODE, false>, smz);
-        if (rc) return rc;
-        k_zw32<MODE, false><<<groups, ZW_THREADS, smz, st>>>(Z);
+        return so4_launch_pdl(k_zw32<MODE, true>, dim3(groups), dim3(ZW_THREADS), with_ca, st, Z);
     }
-    so4_count_launch();
-    return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
+    rc = set_smem(k_zw32<MODE, false>, smz);
+    if (rc) return rc;
+    return so4_launch_pdl(k_zw32<MODE, false>, dim3(groups), dim3(ZW_THREADS), smz, st, Z);
 }
 
 // shared memory of k_zw32 (without the Ca table): padded U tiles and the per-block
@@ -893,6 +909,16 @@ static size_t zw_smem_bytes(const so4_tables *t, int nslot, bool with_eb) {
     // the epilogue stages nslot slot rows (and, in the fused pass, beta B) over the U tiles
     u = std::max(u, sizeof(float) * (size_t)(nslot + (with_eb ? t->n_b : 0)) * ZL_PITCH);
     return u + sizeof(float) * (size_t)t->n_blk * ZL_PITCH;
+}
+
+// Dynamic shared memory the window kernels need in each mode (without the Ca table, which
+// they drop when it does not fit): B only, Y only, B + Y, JVP.  The check of a tuned
+// table's work lists.
+void so4_zw_smem_modes(const so4_tables *t, size_t out[4]) {
+    out[0] = zw_smem_bytes(t, t->n_bsec, false);
+    out[1] = zw_smem_bytes(t, 0, false);
+    out[2] = zw_smem_bytes(t, t->n_bsec, true);
+    out[3] = zw_smem_bytes(t, t->n_jslot, false);
 }
 
 extern "C" size_t so4_forward32_workspace_size(const so4_tables *t, int natoms) {
@@ -933,12 +959,12 @@ extern "C" int so4_forward32(const so4_tables *t, const so4_params *p, int natom
     A.rc32 = (float)p->rcut;
     int rc = SO4_OK;
     switch (t->twol) {
-        case 2: rc = launch_utot_rc<2>(A, st); break;
-        case 4: rc = launch_utot_rc<4>(A, st); break;
-        case 6: rc = launch_utot_rc<6>(A, st); break;
-        case 8: rc = launch_utot_rc<8>(A, st); break;
-        case 10: rc = launch_utot_rc<10>(A, st); break;
-        case 12: rc = launch_utot_rc<12>(A, st); break;
+        case 2: rc = launch_utot_rc<2>(A, t->tune.utot_warps, st); break;
+        case 4: rc = launch_utot_rc<4>(A, t->tune.utot_warps, st); break;
+        case 6: rc = launch_utot_rc<6>(A, t->tune.utot_warps, st); break;
+        case 8: rc = launch_utot_rc<8>(A, t->tune.utot_warps, st); break;
+        case 10: rc = launch_utot_rc<10>(A, t->tune.utot_warps, st); break;
+        case 12: rc = launch_utot_rc<12>(A, t->tune.utot_warps, st); break;
         default: {
             const size_t smu =
                 sizeof(float) * rootpq_floats(t->ldim) + sizeof(cx<float>) * ((size_t)t->n_half * (1 + 2 * NWF));
@@ -1025,12 +1051,12 @@ extern "C" int so4_adjoint_deidrj32(const so4_tables *t, const so4_params *p, in
     cudaStream_t st = (cudaStream_t)stream;
     int rc = SO4_OK;
     switch (t->twol) {
-        case 2: rc = launch_deidrj_rev<2>(D, nimg, st); break;
-        case 4: rc = launch_deidrj_rev<4>(D, nimg, st); break;
-        case 6: rc = launch_deidrj_rev<6>(D, nimg, st); break;
-        case 8: rc = launch_deidrj_rev<8>(D, nimg, st); break;
-        case 10: rc = launch_deidrj_rev<10>(D, nimg, st); break;
-        case 12: rc = launch_deidrj_rev<12>(D, nimg, st); break;
+        case 2: rc = launch_deidrj_rev<2>(D, nimg, t->tune.rev_threads, st); break;
+        case 4: rc = launch_deidrj_rev<4>(D, nimg, t->tune.rev_threads, st); break;
+        case 6: rc = launch_deidrj_rev<6>(D, nimg, t->tune.rev_threads, st); break;
+        case 8: rc = launch_deidrj_rev<8>(D, nimg, t->tune.rev_threads, st); break;
+        case 10: rc = launch_deidrj_rev<10>(D, nimg, t->tune.rev_threads, st); break;
+        case 12: rc = launch_deidrj_rev<12>(D, nimg, t->tune.rev_threads, st); break;
         default: {
             const size_t smd = sizeof(float) * rootpq_floats(t->ldim) +
                                sizeof(cx<float>) * ((size_t)t->n_half + (size_t)NWD * 4 * t->n_half);
@@ -1217,12 +1243,12 @@ extern "C" int so4_utot32(const so4_tables *t, const so4_params *p, int natoms, 
     cudaStream_t st = (cudaStream_t)stream;
     int rc = SO4_OK;
     switch (t->twol) {
-        case 2: rc = launch_utot_rc<2>(A, st); break;
-        case 4: rc = launch_utot_rc<4>(A, st); break;
-        case 6: rc = launch_utot_rc<6>(A, st); break;
-        case 8: rc = launch_utot_rc<8>(A, st); break;
-        case 10: rc = launch_utot_rc<10>(A, st); break;
-        case 12: rc = launch_utot_rc<12>(A, st); break;
+        case 2: rc = launch_utot_rc<2>(A, t->tune.utot_warps, st); break;
+        case 4: rc = launch_utot_rc<4>(A, t->tune.utot_warps, st); break;
+        case 6: rc = launch_utot_rc<6>(A, t->tune.utot_warps, st); break;
+        case 8: rc = launch_utot_rc<8>(A, t->tune.utot_warps, st); break;
+        case 10: rc = launch_utot_rc<10>(A, t->tune.utot_warps, st); break;
+        case 12: rc = launch_utot_rc<12>(A, t->tune.utot_warps, st); break;
         default: {
             const size_t smu =
                 sizeof(float) * rootpq_floats(t->ldim) + sizeof(cx<float>) * ((size_t)t->n_half * (1 + 2 * NWF));

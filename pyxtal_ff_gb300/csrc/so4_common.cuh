@@ -8,6 +8,8 @@
 //                the inversion-symmetry copy of SO4.py:908-925.
 #pragma once
 
+#include <utility>
+
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <vector>
@@ -88,6 +90,7 @@ struct ZBlk {
 
 struct so4_tables {
     int twol, ldim, normalize_u;
+    so4_tuning tune;  // launch shapes, defaults filled in (so4_tables_create_tuned)
     int n_u, n_half, n_z, n_b, n_cg, n_blk;
     // host copies (reference-visible)
     std::vector<double> cglist;
@@ -514,8 +517,39 @@ __host__ __device__ __forceinline__ int section_count(int lam) {
 // status word at the start of every workspace
 #define SO4_WS_HEADER 256
 
+// Dynamic shared memory of the window kernels in each of their four modes (so4_adjoint.cu).
+void so4_zw_smem_modes(const so4_tables *t, size_t out[4]);
+
 // number of kernels this library has launched (so4_launch_count)
 void so4_count_launch(int n = 1);
+
+// Programmatic dependent launch (PDL).  While so4_set_pdl(1) is in effect on the calling
+// host thread, so4_launch_pdl gives its launch the programmatic-stream-serialization
+// attribute: the kernel may be scheduled as soon as every CTA of the kernel before it in
+// the stream has called pdl_trigger() (or exited), and runs its code up to pdl_wait()
+// while that kernel finishes.  A kernel launched this way calls pdl_wait() before it
+// reads anything an earlier kernel of the stream writes and before its first global
+// store; what it does before (index set-up, loads of constant tables) overlaps the
+// previous kernel's tail.  Launched without the attribute, pdl_wait() returns at once.
+int so4_pdl_on();
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+template <typename... KArgs, typename... Args>
+int so4_launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, Args &&...args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = so4_pdl_on() ? 1 : 0;
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
+    so4_count_launch();
+    return e == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
+}
 // Raise a kernel's dynamic shared-memory limit to at least smem bytes on the current
 // device.  The attribute is set only when the limit grows, so launches after the
 // first make no runtime call besides the launch (safe inside stream capture).

@@ -112,16 +112,58 @@ void free_device(so4_tables *t) {
 
 }  // namespace
 
+// The defaults of so4_tuning for one twol, and whether a requested tuning is built.
+static so4_tuning tuning_defaults(int twol) {
+    so4_tuning d;
+    d.wkmax = ZW_KMAX;
+    d.rev_threads = (twol <= 8) ? 256 : 128;
+    d.utot_warps = 4;
+    return d;
+}
+
+static int tuning_resolve(int twol, const so4_tuning *req, so4_tuning &out) {
+    out = tuning_defaults(twol);
+    if (!req) return SO4_OK;
+    if (req->wkmax < 0 || req->wkmax > ZW_KMAX || req->rev_threads < 0 || req->utot_warps < 0) return SO4_ERR_ARG;
+    if (req->rev_threads && req->rev_threads != 128 && req->rev_threads != 256) return SO4_ERR_ARG;
+    if (req->utot_warps && req->utot_warps != 2 && req->utot_warps != 4 && req->utot_warps != 8) return SO4_ERR_ARG;
+    if (req->wkmax) out.wkmax = req->wkmax;
+    const bool shapes = (twol == 6 || twol == 8);  // the twol with every launch shape instantiated
+    if (req->rev_threads && req->rev_threads != out.rev_threads) {
+        if (!shapes) return SO4_ERR_UNSUPPORTED;
+        out.rev_threads = req->rev_threads;
+    }
+    if (req->utot_warps && req->utot_warps != out.utot_warps) {
+        if (!shapes) return SO4_ERR_UNSUPPORTED;
+        out.utot_warps = req->utot_warps;
+    }
+    return SO4_OK;
+}
+
 extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
+    return so4_tables_create_tuned(twol, normalize_u, nullptr, out);
+}
+
+extern "C" int so4_tables_get_tuning(const so4_tables *t, so4_tuning *out) {
+    if (!t || !out) return SO4_ERR_ARG;
+    *out = t->tune;
+    return SO4_OK;
+}
+
+extern "C" int so4_tables_create_tuned(int twol, int normalize_u, const so4_tuning *tune, so4_tables **out) {
     if (!out) return SO4_ERR_ARG;
     *out = nullptr;
     if (twol < 0) return SO4_ERR_ARG;
     if (twol > SO4_TWOL_MAX) return SO4_ERR_UNSUPPORTED;
+    so4_tuning tn;
+    const int trc = tuning_resolve(twol, tune, tn);
+    if (trc) return trc;
     so4_tables *t = new so4_tables();
     const int ld = twol + 1;
     t->twol = twol;
     t->ldim = ld;
     t->normalize_u = normalize_u ? 1 : 0;
+    t->tune = tn;
 
     // idxcg_block and CG list (SO4.py:1269-1285, 410-480)
     t->idxcg_block.assign(ld * ld * ld, 0);
@@ -345,8 +387,8 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
     // Window work lists.  For block (a, b, lam) with d = (a + b - lam) / 2, the Z entry
     // (ma, mb) is (SO4.py:1042-1063)
     //   sum_{mb1} Cb(mb, mb1) sum_{ma2} Ca(ma, ma2) U_a[ma + d - ma2, mb1] U_b[ma2, mb + d - mb1].
-    // A unit holds K <= ZW_KMAX consecutive entries ma0.. of one half row (rows longer
-    // than ZW_KMAX are cut into near-equal parts).  Per block and per mb1 a sub-segment
+    // A unit holds K <= wkmax (<= ZW_KMAX) consecutive entries ma0.. of one half row (rows
+    // longer than wkmax are cut into near-equal parts).  Per block and per mb1 a sub-segment
     // walks ma2 = lo .. hi (the union of the entries' ranges, at most b + 1 <= a + 1
     // values, so the smaller U is the one stepped) with the K values of U_a in a
     // register ring.  Ca[j][k] = cg(a, ma0 + k + d - lo - j, b, lo + j), 0 outside the
@@ -375,9 +417,10 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
     // B partial slots: component k owns nbu(lam_k) consecutive slots, one per window
     // unit of level lam_k that starts inside the B section, in (mb, ma0) order
     std::vector<int> nbu(ld, 0);
+    const int wk = t->tune.wkmax;  // entries per unit at most (ZW_KMAX unless tuned lower)
     for (int lam = 0; lam < ld; ++lam) {
         for (int mb = 0; 2 * mb <= lam; ++mb) {
-            const int n = row_len(lam, mb), ng = (n + ZW_KMAX - 1) / ZW_KMAX;
+            const int n = row_len(lam, mb), ng = (n + wk - 1) / wk;
             for (int g = 0, ma0 = 0; g < ng; ++g) {
                 if (mb * (lam + 1) + ma0 < section_count(lam)) nbu[lam]++;
                 ma0 += n / ng + (g < n % ng ? 1 : 0);
@@ -390,7 +433,7 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
     for (int lam = 0; lam < ld; ++lam) {
         int bu = 0;  // index of the next B-section unit of this level
         for (int mb = 0; 2 * mb <= lam; ++mb) {
-            const int n = row_len(lam, mb), ng = (n + ZW_KMAX - 1) / ZW_KMAX;
+            const int n = row_len(lam, mb), ng = (n + wk - 1) / wk;
             for (int g = 0, ma0 = 0; g < ng; ++g) {
                 WUnit u;
                 u.lam = lam;
@@ -619,6 +662,23 @@ extern "C" int so4_tables_create(int twol, int normalize_u, so4_tables **out) {
     if (!rc) rc = upload(&t->d_blk, blks);
     if (!rc) rc = upload(&t->d_yblk_ptr, yptr);
     if (!rc) rc = upload(&t->d_yblk, ylist);
+    // a unit cap below the default means more units and so more B / JVP slots, which the
+    // window kernels stage in shared memory: refuse a tuning whose window kernels would not
+    // run in every mode where the default ones do
+    if (!rc && t->tune.wkmax != ZW_KMAX) {
+        size_t mt[4], md[4];
+        so4_zw_smem_modes(t, mt);
+        if (std::max(std::max(mt[0], mt[1]), std::max(mt[2], mt[3])) > 227 * 1024) {
+            so4_tuning d = tuning_defaults(twol);
+            so4_tables *t0 = nullptr;
+            if (so4_tables_create_tuned(twol, normalize_u, &d, &t0) == SO4_OK) {
+                so4_zw_smem_modes(t0, md);
+                for (int q = 0; q < 4; ++q)
+                    if (mt[q] > 227 * 1024 && md[q] <= 227 * 1024) rc = SO4_ERR_UNSUPPORTED;
+                so4_tables_destroy(t0);
+            }
+        }
+    }
     if (rc) {
         free_device(t);
         delete t;
@@ -697,4 +757,14 @@ int so4_set_smem(const void *kern, size_t smem) {
     return SO4_OK;
 }
 void so4_count_launch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+// Programmatic dependent launch of the kernels that support it (so4_launch_pdl), for the
+// launches this host thread makes while it is on.
+static thread_local int g_pdl = 0;
+int so4_pdl_on() { return g_pdl; }
+extern "C" int so4_set_pdl(int on) {
+    const int prev = g_pdl;
+    g_pdl = on ? 1 : 0;
+    return prev;
+}
 extern "C" long long so4_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }

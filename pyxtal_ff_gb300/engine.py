@@ -15,7 +15,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from ._lib import Geom, Params, check, lib
+from ._lib import Geom, Params, Tuning, check, lib
 
 CUTOFF_IDS = {"cosine": 1, "tanh": 2, "poly1": 3, "poly2": 4, "poly3": 5, "poly4": 6, "exp": 7}
 
@@ -36,12 +36,21 @@ def require_cuda():
 
 # ---------------------------------------------------------------------- tables
 class Tables:
-    """Device-resident CG / rootpq / index tables for one (twol, normalize_U)."""
+    """Device-resident CG / rootpq / index tables for one (twol, normalize_U), built for
+    one tuning of the FP32 kernels' launch shapes (None: the defaults; see so4_tuning)."""
 
-    def __init__(self, twol, normalize_u=False):
+    def __init__(self, twol, normalize_u=False, tuning=None):
         h = C.c_void_p()
-        check(lib().so4_tables_create(int(twol), int(bool(normalize_u)), C.byref(h)), "so4_tables_create")
+        if tuning is None:
+            check(lib().so4_tables_create(int(twol), int(bool(normalize_u)), C.byref(h)), "so4_tables_create")
+        else:
+            tn = Tuning(int(tuning[0]), int(tuning[1]), int(tuning[2]))
+            check(lib().so4_tables_create_tuned(int(twol), int(bool(normalize_u)), C.byref(tn), C.byref(h)),
+                  "so4_tables_create_tuned")
         self.handle = h
+        tn = Tuning()
+        check(lib().so4_tables_get_tuning(h, C.byref(tn)), "so4_tables_get_tuning")
+        self.tuning = (tn.wkmax, tn.rev_threads, tn.utot_warps)  # (wkmax, rev_threads, utot_warps), resolved
         s = (C.c_int * 8)()
         check(lib().so4_tables_sizes(h, s), "so4_tables_sizes")
         self.twol = int(twol)
@@ -71,11 +80,14 @@ class Tables:
 _TABLES = {}
 
 
-def tables(twol, normalize_u=False):
-    key = (int(twol), bool(normalize_u), torch.cuda.current_device())
+def tables(twol, normalize_u=False, tuning=None):
+    """The tables of (twol, normalize_u) on the current device, built once per tuning
+    ((wkmax, rev_threads, utot_warps) with 0 for a default, or None for all defaults)."""
+    tkey = None if tuning is None else tuple(int(v) for v in tuning)
+    key = (int(twol), bool(normalize_u), torch.cuda.current_device(), tkey)
     t = _TABLES.get(key)
     if t is None:
-        t = Tables(twol, normalize_u)
+        t = Tables(twol, normalize_u, tkey)
         _TABLES[key] = t
     return t
 

@@ -43,9 +43,10 @@ class Context:
 
     @classmethod
     def build(cls, positions, cells, pbc, atom_ptr, numbers, symbols, *, lmax, rcut, kind="SO4", weights=None,
-              rfac0=0.99363, cutoff_function="cosine", normalize_U=False):
+              rfac0=0.99363, cutoff_function="cosine", normalize_U=False, tuning=None):
+        """tuning: an autotune.Choice (its kernel launch shapes) or None for the defaults."""
         twol = int(round(2 * lmax))
-        tab = engine.tables(twol, normalize_U)
+        tab = engine.tables(twol, normalize_U, None if tuning is None else tuning.kernel_tuning())
         prm = engine.params(twol, rcut, 1.0 if kind == "SO4" else rfac0, cutoff_function)
         nb = engine.build_neighbors(positions.detach(), cells, pbc, atom_ptr, rcut, device=positions.device)
         w_nb, w_site = engine.site_weights(kind, numbers, symbols, weights)

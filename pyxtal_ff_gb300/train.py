@@ -114,13 +114,14 @@ class ForceMatching:
     as a CUDA graph for the fixed batch; later ``step()`` calls replay it."""
 
     def __init__(self, structures, *, lmax=3, rcut=4.9, kind="SNAP", weights=None, rfac0=1.0, hidden=(30, 30),
-                 seed=0, lr=1e-3, force_weight=0.1, targets=None, device="cuda"):
+                 seed=0, lr=1e-3, force_weight=0.1, targets=None, device="cuda", tuning=None):
         self.device = torch.device(device)
-        self.batch = Batch(structures)
+        self.batch = structures if isinstance(structures, Batch) else Batch(structures)
         b = self.batch
         pos = torch.from_numpy(b.positions).to(self.device)
         self.ctx = ops.Context.build(pos, b.cells, b.pbc, b.atom_ptr, b.numbers, b.symbols, lmax=lmax, rcut=rcut,
-                                     kind=kind, weights=weights or {s: 1.0 for s in set(b.symbols)}, rfac0=rfac0)
+                                     kind=kind, weights=weights or {s: 1.0 for s in set(b.symbols)}, rfac0=rfac0,
+                                     tuning=tuning)
         x, utot = engine.forward32(self.ctx.tab, self.ctx.prm, self.ctx.nb, self.ctx.w_nb, self.ctx.w_site)
         self.ctx.utot = utot
         self.x = x
