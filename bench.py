@@ -271,7 +271,70 @@ def measured_peaks(torch):
         peaks[name] = 2.0 * n ** 3 / (best * 1e-3) / 1e12
         del a, b
     torch.backends.cuda.matmul.allow_tf32 = prev
+    peaks.update(fma_peaks(torch))
     return peaks
+
+
+def fma_peaks(torch):
+    """The FP32 and FP64 FMA pipes measured directly (so4_peak_fma: 8 CTAs of 256 threads
+    per SM, 8 independent FMA chains per thread), best of 3 launches of about 10 ms."""
+    import ctypes as C
+    from pyxtal_ff_gb300 import _lib
+    from pyxtal_ff_gb300.engine import _stream
+    L = _lib.lib()
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    blocks = 8 * sms
+    out = torch.empty(blocks * 256, dtype=torch.float32, device="cuda")
+    res = {}
+    for name, kind, iters in (("fp32_ffma2_tflops", 0, 80000), ("fp32_ffma_tflops", 1, 80000),
+                              ("fp64_dfma_tflops", 2, 2400)):
+        flop = C.c_double()
+        best = 1e9
+        for _ in range(4):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            _lib.check(L.so4_peak_fma(kind, iters, blocks, C.c_void_p(out.data_ptr()), C.byref(flop), _stream()),
+                       "so4_peak_fma")
+            e1.record()
+            e1.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+        res[name] = flop.value / (best * 1e-3) / 1e12
+    res["fp32_fma_tflops"] = max(res["fp32_ffma2_tflops"], res["fp32_ffma_tflops"])
+    return res
+
+
+def nl_back_to_back(step, reps=20):
+    """Mean duration (ms) of the captured step's neighbour list in its one-branch form (bins and
+    per-atom keys, sort with the FP64 image vectors, reverse images, summary), `reps` times back to
+    back in one CUDA graph, and its algorithmic bytes: positions read, per image j, offset (3 x i32),
+    vector (3 x f64) and reverse index written, per atom the image pointer."""
+    import torch
+    from pyxtal_ff_gb300 import engine
+    lay, b = step.layout, step.nl
+    for _ in range(3):
+        engine.enqueue_neighbors(lay, step.pos, b, lite=True)
+    torch.cuda.synchronize()
+    gr = torch.cuda.CUDAGraph()
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        engine.enqueue_neighbors(lay, step.pos, b, lite=True)
+    torch.cuda.current_stream().wait_stream(side)
+    torch.cuda.synchronize()
+    with torch.cuda.graph(gr):
+        for _ in range(reps):
+            engine.enqueue_neighbors(lay, step.pos, b, lite=True)
+    gr.replay()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    gr.replay()
+    e1.record()
+    e1.synchronize()
+    M = int(b.summary_dev().cpu()[0])
+    N = lay.natoms
+    nbytes = 24 * N + 4 * (N + 1) + M * (4 + 12 + 24 + 4)
+    return e0.elapsed_time(e1) / reps, nbytes, M
 
 
 # ----------------------------------------------------------------- CPU side
@@ -371,6 +434,32 @@ def run_contract(args):
                       "gbs": byt / (ms * 1e-3) / 1e9}), flush=True)
 
 
+def run_profile_case(which):
+    """Small cases of single kernels for ncu captures (summaries under profiles/)."""
+    import torch
+    from pyxtal_ff_gb300 import engine, ops
+    from pyxtal_ff_gb300 import structures as S
+    from pyxtal_ff_gb300.calculator import Batch, SO4Calculator
+    if which == "plain":
+        batch = Batch([S.diamond_si(8, 8, 4, sigma=0.1, rng=np.random.default_rng(5))])
+        calc = SO4Calculator(lmax=LMAX, rcut=RCUT, kind="SNAP", weights={"Si": 1.0}, rfac0=1.0)
+        for _ in range(2):
+            d = calc.descriptors(batch, precision="fp64")
+            torch.cuda.synchronize()
+            del d
+    else:
+        batch = Batch([S.diamond_si(16, 16, 8, sigma=0.1, rng=np.random.default_rng(5))])
+        p = torch.from_numpy(batch.positions).cuda()
+        ctx = ops.Context.build(p, batch.cells, batch.pbc, batch.atom_ptr, batch.numbers, batch.symbols, lmax=LMAX,
+                                rcut=RCUT, kind="SNAP", weights={"Si": 1.0}, rfac0=1.0)
+        x, utot = engine.forward32(ctx.tab, ctx.prm, ctx.nb, ctx.w_nb, ctx.w_site)
+        v = torch.from_numpy(np.random.default_rng(1).normal(size=(batch.natoms, 3))).cuda()
+        for _ in range(3):
+            engine.jvp32(ctx.tab, ctx.prm, ctx.nb, ctx.w_nb, utot, v=v)
+        torch.cuda.synchronize()
+    print(json.dumps({"profile_case": which, "atoms": batch.natoms}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -382,6 +471,10 @@ def main():
     ap.add_argument("--no-tune", action="store_true", help="default launch shapes instead of the autotuner's choice")
     ap.add_argument("--quick", action="store_true",
                     help="device-resident steps only (no e2e, FP64, CPU or peak legs); for profiler runs")
+    ap.add_argument("--profile-case", choices=["plain", "jvp"], default=None,
+                    help="only a small case for profiler runs: 'plain' = two FP64 plain-path evaluations of a "
+                         "2,048-atom diamond-Si cell, 'jvp' = the FP32 forward and three JVPs of a 16,384-atom "
+                         "cell (lmax 4, rcut 5.0)")
     ap.add_argument("--contract-cells", type=int, default=0,
                     help="only the NN consumer's dxdr contraction (so4_contract_dxdr) on an N x N x 10 diamond-Si "
                          "cell at lmax 4 (a small case for profiler runs)")
@@ -392,6 +485,9 @@ def main():
         return
     if args.contract_cells:
         run_contract(args)
+        return
+    if args.profile_case:
+        run_profile_case(args.profile_case)
         return
 
     import torch
@@ -496,6 +592,7 @@ def main():
         stage_ms += np.array([ev[i].elapsed_time(ev[i + 1]) for i in range(nev - 1)])
     stage_ms /= args.steps
     b2b_ms = kernels_back_to_back(calc, batch, pos_dev, beta_dev)
+    nl_ms, nl_bytes, nl_images = nl_back_to_back(step)
     if args.quick:
         clocks.stop()
         if rank == 0:
@@ -637,6 +734,9 @@ def main():
                 "work": "tabulated per-unit work of the reference algorithm x units per launch",
                 "achieved_executed": kf[dom] / sec / 1e12,
                 "frac_executed": kf[dom] / sec / 1e12 / peaks["fp32_tflops"],
+                "frac_vs_fma_loop": achieved / peaks["fp32_fma_tflops"],
+                "frac_executed_vs_fma_loop": kf[dom] / sec / 1e12 / peaks["fp32_fma_tflops"],
+                "fma_loop_tflops": peaks["fp32_fma_tflops"],
                 "peak_source": "cuBLAS SGEMM (TF32 off) measured in this run; the kernel is FP32-FMA bound, "
                                "its DRAM traffic is far below the HBM roof",
                 "duration": "mean of 20 back-to-back launches replayed as one CUDA graph (no host gaps)",
@@ -669,8 +769,30 @@ def main():
         "bytes": cbytes, "what": "forces and stress of the reference NN consumer from the FP64 dxdr (%.2f GB) and "
                                  "per-atom rdxdr; bytes = dxdr + rdxdr_atom + beta + seq + outputs; FP64 pipe and "
                                  "HBM bound it about equally on GB300" % (8e-9 * nbp.npair * nB * 3)}
+    # the neighbour list against the HBM roof: it moves 44 B per image and runs far below that
+    # roof, bound by the latency of its per-centre bin walks (profiles/k_scan_images_k_sort_*)
+    kernels["neighbors_lite"] = {
+        "ms_back_to_back": nl_ms, "bytes": nl_bytes, "images": nl_images,
+        "gbs": nl_bytes / (nl_ms * 1e-3) / 1e9, "frac_hbm": nl_bytes / (nl_ms * 1e-3) / 1e9 / peaks["hbm_gbs"],
+        "bound": "latency (per-centre bin walk), not HBM",
+        "what": "one-branch form of the captured step's list: bins + per-atom keys, sort with FP64 image vectors, "
+                "reverse images, summary; bytes = positions + image pointer + 44 B per image written"}
+    for nme in ("utot32", "linear_by32", "adjoint_deidrj32"):
+        if "tflops_executed" in kernels.get(nme, {}):
+            kernels[nme]["frac_executed_vs_fma_loop"] = kernels[nme]["tflops_executed"] / peaks["fp32_fma_tflops"]
+            kernels[nme]["frac_vs_fma_loop"] = kernels[nme]["tflops"] / peaks["fp32_fma_tflops"]
+    # the per-kernel times are full-size launches back to back; the step runs each of them as two
+    # half-size launches in parallel graph branches, plus the list and the gather
+    kernels["step_reconciliation"] = {
+        "sum_of_back_to_back_kernels_ms": float(sum(b2b_ms.values())) + nl_ms,
+        "gather_ms_eager": float(stage_ms[stage_names.index("gather")]),
+        "step_ms": t_dev / args.steps,
+        "note": "U_tot, window and per-image kernels back to back at full size, plus the one-branch "
+                "neighbour list; the captured step runs two branches over the atom halves, so kernel tails "
+                "overlap and the step is close to this sum plus the gather"}
     kernels["plain_fp64"] = {"ms": ms64, "tflops_fp64_incl_nl_contraction": ks["plain"] / (ms64 * 1e-3) / 1e12,
-                             "frac_fp64": ks["plain"] / (ms64 * 1e-3) / 1e12 / peaks["fp64_tflops"]}
+                             "frac_fp64": ks["plain"] / (ms64 * 1e-3) / 1e12 / peaks["fp64_tflops"],
+                             "frac_fp64_vs_dfma_loop": ks["plain"] / (ms64 * 1e-3) / 1e12 / peaks["fp64_dfma_tflops"]}
 
     # ---- force-matching training step (512 Si structures of 8-64 atoms, lmax 3), extra line item
     train = None
@@ -745,7 +867,8 @@ def main():
                 "fp64_plain": fp64, "err_vs_oracle": err_oracle, "err_vs_fp64": err, "kernels": kernels,
                 "train_step": train,
                 "ase_md_step": ase_md, "tuning": tuning, "reference_python": reference_python_record(),
-                "peaks": {k: peaks[k] for k in ("hbm_gbs", "fp32_tflops", "fp64_tflops") if k in peaks}}
+                "peaks": {k: peaks[k] for k in ("hbm_gbs", "fp32_tflops", "fp64_tflops", "fp32_ffma2_tflops",
+                                                "fp32_ffma_tflops", "fp64_dfma_tflops") if k in peaks}}
         print(json.dumps(line), flush=True)
     if ws > 1:
         dist.destroy_process_group()

@@ -402,6 +402,13 @@ int so4_adjoint32_noalloc(const so4_tables *t, const so4_params *p, int nstruct,
                           int64_t nimg, const float *d_utot, const float *d_beta, double *d_forces,
                           double *d_virial, void *stream);
 
+/* FMA throughput loop (measurement aid, no counterpart in the reference): blocks CTAs
+ * of 256 threads, each thread running 8 independent FMA chains for `iters` iterations;
+ * kind 0 packed FP32 pairs (fma.rn.f32x2), 1 scalar FP32, 2 FP64.  Writes one float per
+ * thread to d_out[blocks * 256] and the launch's flop count to *h_flop; time it on
+ * `stream`. */
+int so4_peak_fma(int kind, int iters, int blocks, float *d_out, double *h_flop, void *stream);
+
 /* Number of kernels this library has launched since it was loaded. */
 long long so4_launch_count(void);
 

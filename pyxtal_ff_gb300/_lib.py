@@ -120,6 +120,7 @@ def lib():
         "so4_adjoint_gather": (_i, [_i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
         "so4_launch_count": (C.c_longlong, []),
         "so4_set_pdl": (C.c_int, [C.c_int]),
+        "so4_peak_fma": (_i, [_i, _i, _i, _vp, C.POINTER(C.c_double), _vp]),
         "so4_jvp_workspace_size": (_sz, [_vp, _i]),
         "so4_linear_workspace_size": (_sz, [_vp, _i, _i64]),
         "so4_utot32": (_i, [_vp, C.POINTER(Params), _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),

@@ -15,7 +15,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libso4gb300.so")
-SOURCES = ["so4_tables.cu", "so4_nlist.cu", "so4_plain.cu", "so4_adjoint.cu", "so4_jvp.cu", "so4_consumer.cu"]
+SOURCES = ["so4_tables.cu", "so4_nlist.cu", "so4_plain.cu", "so4_adjoint.cu", "so4_jvp.cu", "so4_consumer.cu",
+           "so4_peak.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
 

@@ -232,6 +232,7 @@ struct ZLArgs {
     const int *jbase, *jpos;
     const float *jfac;
     const float *yscale;  // n_half: Y is stored times the row scale F of its entry
+    int stage_cap;        // MODE 3: slot rows the epilogue stages at a time (those fitting over the U tiles)
 };
 
 
@@ -458,9 +459,11 @@ __global__ void __launch_bounds__(ZW_THREADS, 2) k_zw32(ZLArgs A) {
     // they fit there (the host sizes the launch so), in the fixed slot order
     float *stage = (float *)zw_smem;
     if (MODE == 3) {
-        // dB_k: the sum of component k's slots (sections 0, 1, 2, each in unit order)
-        zw_slot_sums<1>(A.bc, A.jpos, A.nB, A.nbsec, A.natoms, a0, stage, [](int, int) { return 0.f; },
-                        [&](int k, int l, float acc, float) { A.x[(size_t)(a0 + l) * A.nB + k] = acc; });
+        // dB_k: the sum of component k's slots (sections 0, 1, 2, each in unit order), staged a
+        // chunk of components at a time over the U tiles, so the JVP mode needs no more shared
+        // memory than the others
+        zw_slot_sums_chunked(A.bc, A.jpos, A.nB, A.natoms, a0, stage, A.stage_cap,
+                             [&](int k, int l, float acc) { A.x[(size_t)(a0 + l) * A.nB + k] = acc; });
         return;
     }
     // B_k = 2 x the sum of its slots; in the fused pass also beta_k B_k per atom (beta read
@@ -918,8 +921,11 @@ void so4_zw_smem_modes(const so4_tables *t, size_t out[4]) {
     out[0] = zw_smem_bytes(t, t->n_bsec, false);
     out[1] = zw_smem_bytes(t, 0, false);
     out[2] = zw_smem_bytes(t, t->n_bsec, true);
-    out[3] = zw_smem_bytes(t, t->n_jslot, false);
+    out[3] = zw_smem_bytes(t, 0, false);  // the JVP stages its slots in chunks over the U tiles
 }
+
+// Slot rows the JVP epilogue stages at a time: those that fit over the padded U tiles.
+static int zw_stage_cap(const so4_tables *t) { return 2 * (t->n_u + 2 * ZW_PAD); }
 
 extern "C" size_t so4_forward32_workspace_size(const so4_tables *t, int natoms) {
     if (!t || natoms < 0) return 0;
@@ -1023,8 +1029,10 @@ int so4_zw_jvp32(const so4_tables *t, int natoms, const float *d_utot, const flo
     Z.jfac = t->d_jfac;
     Z.bc = d_slots;
     Z.nbsec = t->n_jslot;  // the epilogue's slot count
+    Z.stage_cap = zw_stage_cap(t);
+    if (t->n_jmax > Z.stage_cap) return SO4_ERR_UNSUPPORTED;  // a component's slots must fit one chunk
     Z.x = d_dB;
-    return launch_zw<3>(t, Z, natoms, zw_smem_bytes(t, t->n_jslot, false), stream);
+    return launch_zw<3>(t, Z, natoms, zw_smem_bytes(t, 0, false), stream);
 }
 
 extern "C" int so4_adjoint_deidrj32(const so4_tables *t, const so4_params *p, int natoms, const double *d_w_nb,

@@ -143,6 +143,7 @@ struct so4_tables {
     int *d_jpos = nullptr, *d_jbase = nullptr;
     float *d_jfac = nullptr;
     int n_wunit_j = 0, n_jslot = 0;
+    int n_jmax = 0;  // the most slots one component owns
     int n_wsub = 0;  // window sub-segments
 };
 

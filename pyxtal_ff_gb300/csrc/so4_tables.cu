@@ -553,6 +553,7 @@ extern "C" int so4_tables_create_tuned(int twol, int normalize_u, const so4_tuni
         jpos[k + 1] = base;
     }
     t->n_jslot = jpos[t->n_b];
+    for (int k = 0; k < t->n_b; ++k) t->n_jmax = std::max(t->n_jmax, jpos[k + 1] - jpos[k]);
     for (int bi = 0; bi < t->n_blk; ++bi)
         for (int r = blks[bi].nrole; r < 3; ++r) jbase[3 * bi + r] = -1;  // no role r
     std::vector<std::pair<long, int>> wcj;

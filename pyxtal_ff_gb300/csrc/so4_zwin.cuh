@@ -110,6 +110,49 @@ __device__ __forceinline__ void zw_slot_sums(const float *sc, const int *__restr
     }
 }
 
+// zw_slot_sums without its single staging pass: components are taken in chunks whose slots
+// (at most `cap` of them, the slot rows that fit in `stage`) are staged together, summed,
+// and the stage reused for the next chunk.  Every component owns at most cap slots (the
+// host checks it).  f(k, lane, sum) for every k < ncomp and lane with a0 + lane < natoms.
+template <typename F>
+__device__ __forceinline__ void zw_slot_sums_chunked(const float *sc, const int *__restrict__ pos, int ncomp,
+                                                     int natoms, int a0, float *stage, int cap, F f) {
+    const int nl = min(32, natoms - a0);
+    int k0 = 0;
+    while (k0 < ncomp) {
+        // the chunk [k0, k1): as many whole components as fit (the same k1 in every thread)
+        const int q0 = __ldg(pos + k0);
+        int k1 = k0 + 1;
+        while (k1 < ncomp && __ldg(pos + k1 + 1) - q0 <= cap) ++k1;
+        const int nq = __ldg(pos + k1) - q0;
+        for (int i0 = threadIdx.x; i0 < 32 * nq; i0 += ZW_SLD * ZW_THREADS) {
+            float v[ZW_SLD];
+#pragma unroll
+            for (int r = 0; r < ZW_SLD; ++r) {
+                const int i = i0 + r * ZW_THREADS, q = i >> 5, l = i & 31;
+                v[r] = (i < 32 * nq && l < nl) ? sc[(size_t)(q0 + q) * natoms + a0 + l] : 0.f;
+            }
+#pragma unroll
+            for (int r = 0; r < ZW_SLD; ++r) {
+                const int i = i0 + r * ZW_THREADS;
+                if (i < 32 * nq) stage[(i >> 5) * ZL_PITCH + (i & 31)] = v[r];
+            }
+        }
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < 32 * (k1 - k0); idx += ZW_THREADS) {
+            const int k = k0 + (idx >> 5), l = idx & 31;
+            if (l < nl) {
+                float acc = 0.f;
+                const int qa = __ldg(pos + k) - q0, qb = __ldg(pos + k + 1) - q0;
+                for (int q = qa; q < qb; ++q) acc += stage[q * ZL_PITCH + l];
+                f(k, l, acc);
+            }
+        }
+        __syncthreads();  // before the next chunk overwrites the stage
+        k0 = k1;
+    }
+}
+
 // One sub-segment {f1 | f2 << 16, Ca offset, steps S, bits of Cb}: adds
 // Cb sum_j Ca[j][k] U_a[f2 - j + k] U_b[f1 + j] to z[k] = (re, im), k < K, for this
 // lane's atom (offsets in Ub rows, pre-scaled by the pitch; Ul = Ub + lane).  Ca rows
