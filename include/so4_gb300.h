@@ -227,7 +227,9 @@ int so4_status_read(const void *d_work, size_t work_bytes, void *stream, int *h_
  * number; SNAP: weights[symbol]); d_w_site[natoms]: site weight (SO4: atomic
  * number; SNAP: 1).  want_deriv / want_stress as the reference's flags; dxdr
  * and rdxdr may be NULL when not wanted.  Output element type is double
- * (precision 0) or float (precision 1). */
+ * (precision 0) or float (precision 1).  Scratch: so4_plain_workspace_size()
+ * bytes -- a status header, and at twol 12, where the FP64 path's Z does not fit in
+ * shared memory, one global Z slot per CTA of the launch (min(natoms, 2 x SMs)). */
 size_t so4_plain_workspace_size(const so4_tables *t, int natoms);
 int so4_plain(const so4_tables *t, const so4_params *p, int precision, const so4_geom *d_geom,
               const int *d_atom_struct, int natoms, const double *d_pos, const double *d_w_nb,

@@ -46,30 +46,20 @@ struct PlainArgs {
     SmallTables st;
     int want_deriv, want_stress;
     T *x, *dxdr, *rdxdr;
+    cx<T> *zg;  // global Z slots (k_plain<..., true>), one per CTA
 };
 
+// One centre atom: steps 1-5 above.  Z is in shared memory, or (when it does not fit
+// beside the rest) in this CTA's slot of a global scratch; HB holds the per-warp H / dH
+// buffers (and, during step 1, the per-warp U_tot partials).
 template <typename T, int NW, int KS>
-__global__ void __launch_bounds__(NW * 32) k_plain(PlainArgs<T> A) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ SmallTables st;
+__device__ __forceinline__ void plain_centre(const PlainArgs<T> &A, int a, const SmallTables &st, const T *rootpq,
+                                             cx<T> *Uh, cx<T> *Uf, cx<T> *Z, cx<T> *HB, T *Dsum, T *Eself,
+                                             T *Sw) {
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    const int a = blockIdx.x;
-    if (tid == 0) st = A.st;
-    const int ldim = A.st.twol + 1;
     const int nh = A.n_half, nu = A.n_u, nz = A.n_z, nB = A.n_b;
-    // carve shared memory
-    T *rootpq = (T *)smem_raw;
-    cx<T> *Uh = (cx<T> *)(rootpq + ((ldim * ldim + 1) & ~1));
-    cx<T> *Uf = Uh + nh;
-    cx<T> *Z = Uf + nu;
-    cx<T> *Hw = Z + nz + wid * 4 * nh;  // per warp: H[nh], dH[3 nh]
+    cx<T> *Hw = HB + wid * 4 * nh;  // per warp: H[nh], dH[3 nh]
     cx<T> *dHw = Hw + nh;
-    T *Dsum = (T *)(Z + nz + NW * 4 * nh);  // [NW][nB][3]
-    T *Eself = Dsum + NW * nB * 3;           // [nB][9]
-    T *Sw = Eself + nB * 9 + wid * 4 * A.n_psec;  // per warp: [n_psec][4] section sums of one image
-    for (int q = tid; q < ldim * ldim; q += NW * 32) rootpq[q] = A.rootpq[q];
-    __syncthreads();
-
     const so4_geom &g = A.geom[A.astruct[a]];
     const T rc = (T)A.prm.rcut;
     const T psi_fac = (T)(A.prm.rfac0 * SO4_PI / A.prm.rcut);
@@ -77,8 +67,8 @@ __global__ void __launch_bounds__(NW * 32) k_plain(PlainArgs<T> A) {
     const int m0 = A.img_ptr[a], m1 = A.img_ptr[a + 1];
 
     // ---- 1. U_tot (per-warp partials live in the dH buffers, unused until step 4)
-    block_utot<T, NW>(st, rootpq, a, A.img_r, A.img_j, m0, m1, A.w_nb, A.w_site[a], rc, psi_fac, cid, nh,
-                      Z + nz, Z + nz + nh, 4 * nh, Uh);
+    block_utot<T, NW>(st, rootpq, a, A.img_r, A.img_j, m0, m1, A.w_nb, A.w_site[a], rc, psi_fac, cid, nh, HB,
+                      HB + nh, 4 * nh, Uh);
     block_expand<T, NW>(st, Uh, nu, Uf);
     // ---- 2. Z
     block_z<T, NW>(A.zent, nz, A.cg, Uf, Z);
@@ -229,23 +219,65 @@ __global__ void __launch_bounds__(NW * 32) k_plain(PlainArgs<T> A) {
     }
 }
 
+// ZG false: one CTA per centre, Z in shared memory.  ZG true: gridDim.x CTAs take the centres
+// in turn, each with its own Z slot of nz entries in A.zg (the FP64 path above twol 10, where
+// Z alone is 95-207 KB): resident CTAs keep their slots in L2.
+template <typename T, int NW, int KS, bool ZG>
+__global__ void __launch_bounds__(NW * 32) k_plain(PlainArgs<T> A) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ SmallTables st;
+    const int tid = threadIdx.x, wid = tid >> 5;
+    if (tid == 0) st = A.st;
+    const int ldim = A.st.twol + 1;
+    const int nh = A.n_half, nu = A.n_u, nz = A.n_z, nB = A.n_b;
+    // carve shared memory
+    T *rootpq = (T *)smem_raw;
+    cx<T> *Uh = (cx<T> *)(rootpq + ((ldim * ldim + 1) & ~1));
+    cx<T> *Uf = Uh + nh;
+    cx<T> *Zs = Uf + nu;
+    cx<T> *HB = Zs + (ZG ? 0 : nz);
+    T *Dsum = (T *)(HB + NW * 4 * nh);  // [NW][nB][3]
+    T *Eself = Dsum + NW * nB * 3;      // [nB][9]
+    T *Sw = Eself + nB * 9 + wid * 4 * A.n_psec;  // per warp: [n_psec][4] section sums of one image
+    for (int q = tid; q < ldim * ldim; q += NW * 32) rootpq[q] = A.rootpq[q];
+    __syncthreads();
+    cx<T> *Z = ZG ? A.zg + (size_t)blockIdx.x * nz : Zs;
+    for (int a = blockIdx.x; a < A.natoms; a += gridDim.x) {
+        plain_centre<T, NW, KS>(A, a, st, rootpq, Uh, Uf, Z, HB, Dsum, Eself, Sw);
+        __syncthreads();  // before the next centre reuses the buffers
+    }
+}
+
 template <typename T>
-size_t plain_smem_bytes(const so4_tables *t, int NW) {
+size_t plain_smem_bytes(const so4_tables *t, int NW, bool zg = false) {
     const int ld = t->ldim;
     size_t b = sizeof(T) * ((ld * ld + 1) & ~1);
-    b += sizeof(cx<T>) * ((size_t)t->n_half + t->n_u + t->n_z + (size_t)NW * 4 * t->n_half);
+    b += sizeof(cx<T>) * ((size_t)t->n_half + t->n_u + (zg ? 0 : t->n_z) + (size_t)NW * 4 * t->n_half);
     b += sizeof(T) * ((size_t)NW * t->n_b * 3 + (size_t)t->n_b * 9 + (size_t)NW * 4 * t->n_psec);
     return b;
 }
 
-template <typename T, int NW, int KS>
-int launch_plain(const PlainArgs<T> &A, size_t smem, cudaStream_t st) {
-    auto kern = k_plain<T, NW, KS>;
+template <typename T, int NW, int KS, bool ZG = false>
+int launch_plain(const PlainArgs<T> &A, size_t smem, int grid, cudaStream_t st) {
+    auto kern = k_plain<T, NW, KS, ZG>;
     const int rc = so4_set_smem((const void *)kern, smem);
     if (rc) return rc;
-    kern<<<A.natoms, NW * 32, smem, st>>>(A);
+    kern<<<grid, NW * 32, smem, st>>>(A);
     so4_count_launch();
     return cudaGetLastError() == cudaSuccess ? SO4_OK : SO4_ERR_CUDA;
+}
+
+constexpr int PLAIN_NW = 4;
+
+// Global Z slots of the FP64 path where Z does not fit in shared memory beside the rest
+// (twol 12): one per CTA of a grid of min(natoms, 2 x SMs) CTAs.  0 where Z fits.
+int plain_zslots(const so4_tables *t, int natoms) {
+    if (plain_smem_bytes<double>(t, PLAIN_NW) <= 227 * 1024) return 0;
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+                                                  cudaSuccess)
+        sms = 160;
+    return std::max(1, std::min(natoms, 2 * sms));
 }
 
 template <typename T>
@@ -253,8 +285,8 @@ int run_plain(const so4_tables *t, const so4_params *p, const so4_geom *geom, co
               const double *pos, const double *w_nb, const double *w_site, const int32_t *img_ptr,
               const int32_t *img_j, const double *img_r, const int32_t *pair_ptr, const int32_t *pair_img,
               const int32_t *nsite, int want_deriv, int want_stress, void *x, void *dxdr, void *rdxdr,
-              cudaStream_t st) {
-    constexpr int NW = 4;
+              void *work, size_t work_bytes, cudaStream_t st) {
+    constexpr int NW = PLAIN_NW;
     PlainArgs<T> A;
     A.prm = *p;
     A.natoms = natoms;
@@ -288,23 +320,34 @@ int run_plain(const so4_tables *t, const so4_params *p, const so4_geom *geom, co
     A.x = (T *)x;
     A.dxdr = (T *)dxdr;
     A.rdxdr = (T *)rdxdr;
+    A.zg = nullptr;
     const size_t smem = plain_smem_bytes<T>(t, NW);
-    if (smem > 227 * 1024) return SO4_ERR_UNSUPPORTED;
-    if (natoms == 0) return SO4_OK;
     const int ks = (t->n_b + 31) / 32;
-    if (ks <= 1) return launch_plain<T, NW, 1>(A, smem, st);
-    if (ks <= 2) return launch_plain<T, NW, 2>(A, smem, st);
-    if (ks <= 3) return launch_plain<T, NW, 3>(A, smem, st);
-    if (ks <= 5) return launch_plain<T, NW, 5>(A, smem, st);
+    if (smem > 227 * 1024) {
+        // Z in global slots: built for the FP64 path at twol 12 (nB 140); FP32 fits in shared memory
+        const size_t smg = plain_smem_bytes<T>(t, NW, true);
+        if (sizeof(T) != 8 || smg > 227 * 1024 || ks != 5) return SO4_ERR_UNSUPPORTED;
+        if (natoms == 0) return SO4_OK;
+        const int slots = plain_zslots(t, natoms);
+        if (!work || work_bytes < SO4_WS_HEADER + sizeof(cx<T>) * (size_t)slots * t->n_z) return SO4_ERR_WORKSPACE;
+        A.zg = (cx<T> *)((char *)work + SO4_WS_HEADER);
+        if constexpr (sizeof(T) == 8) return launch_plain<T, NW, 5, true>(A, smg, slots, st);
+        return SO4_ERR_UNSUPPORTED;
+    }
+    if (natoms == 0) return SO4_OK;
+    if (ks <= 1) return launch_plain<T, NW, 1>(A, smem, natoms, st);
+    if (ks <= 2) return launch_plain<T, NW, 2>(A, smem, natoms, st);
+    if (ks <= 3) return launch_plain<T, NW, 3>(A, smem, natoms, st);
+    if (ks <= 5) return launch_plain<T, NW, 5>(A, smem, natoms, st);
     return SO4_ERR_UNSUPPORTED;
 }
 
 }  // namespace
 
 extern "C" size_t so4_plain_workspace_size(const so4_tables *t, int natoms) {
-    (void)t;
-    (void)natoms;
-    return SO4_WS_HEADER;
+    if (!t || natoms < 0) return SO4_WS_HEADER;
+    // the FP64 path's global Z slots where Z does not fit in shared memory (twol 12)
+    return SO4_WS_HEADER + sizeof(cx<double>) * (size_t)plain_zslots(t, natoms) * t->n_z;
 }
 
 extern "C" int so4_plain(const so4_tables *t, const so4_params *p, int precision, const so4_geom *d_geom,
@@ -313,8 +356,6 @@ extern "C" int so4_plain(const so4_tables *t, const so4_params *p, int precision
                          const double *d_img_r, const int32_t *d_pair_ptr, const int32_t *d_pair_img,
                          const int32_t *d_nsite, int want_deriv, int want_stress, void *d_x, void *d_dxdr,
                          void *d_rdxdr, void *d_work, size_t work_bytes, void *stream) {
-    (void)d_work;
-    (void)work_bytes;
     if (!t || !p || natoms < 0 || !d_x) return SO4_ERR_ARG;
     if (p->twol != t->twol) return SO4_ERR_ARG;
     if (p->cutoff_id < 1 || p->cutoff_id > 7) return SO4_ERR_UNSUPPORTED;
@@ -325,11 +366,11 @@ extern "C" int so4_plain(const so4_tables *t, const so4_params *p, int precision
     if (precision == 0)
         return run_plain<double>(t, p, d_geom, d_astruct, natoms, d_pos, d_w_nb, d_w_site, d_img_ptr, d_img_j, d_img_r,
                                  d_pair_ptr, d_pair_img, d_nsite, want_deriv, want_deriv && want_stress, d_x, d_dxdr,
-                                 d_rdxdr, st);
+                                 d_rdxdr, d_work, work_bytes, st);
     if (precision == 1)
         return run_plain<float>(t, p, d_geom, d_astruct, natoms, d_pos, d_w_nb, d_w_site, d_img_ptr, d_img_j, d_img_r,
                                 d_pair_ptr, d_pair_img, d_nsite, want_deriv, want_deriv && want_stress, d_x, d_dxdr,
-                                d_rdxdr, st);
+                                d_rdxdr, d_work, work_bytes, st);
     return SO4_ERR_ARG;
 }
 
