@@ -98,11 +98,16 @@ int so4_tables_destroy(so4_tables *t);
  *   rev_threads threads per CTA of the per-image pass, 128 or 256 (default 256 up to
  *               twol 8, 128 above; only twol 6 and 8 have both);
  *   utot_warps  warps (centres) per CTA of the U_tot pass, 2, 4 or 8 (default 4; only
- *               twol 6 and 8 have all three). */
+ *               twol 6 and 8 have all three);
+ *   rev_pair    layout of the per-image pass: 1 two lanes per image (its row chains
+ *               shared out so the lanes' work per level is even), 2 one lane per row
+ *               chain (built for every twol; rev_threads applies to it); 0 the default,
+ *               two lanes where built (twol 6 and 8). */
 typedef struct {
     int wkmax;
     int rev_threads;
     int utot_warps;
+    int rev_pair;
 } so4_tuning;
 /* so4_tables_create with a tuning (NULL: the defaults).  SO4_ERR_ARG for a value
  * outside the ranges above; SO4_ERR_UNSUPPORTED for a CTA shape not built for this

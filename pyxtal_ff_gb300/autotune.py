@@ -10,6 +10,7 @@ device.  The knobs:
                built for it; so4_tuning.wkmax)
   rev_threads  threads per CTA of the per-image dE/dr pass, 128 or 256
   utot_warps   centres per CTA of the U_tot pass, 2, 4 or 8
+  rev_pair     layout of the per-image pass: 1 two lanes per image, 2 one lane per row chain
   branches     parallel graph branches of the captured linear step, 1..4
   pdl          programmatic dependent launch between that step's kernels
 
@@ -33,7 +34,7 @@ from dataclasses import dataclass
 
 import numpy as np
 
-SPACE_ORDER = ("branches", "wkmax", "rev_threads", "utot_warps", "pdl")
+SPACE_ORDER = ("branches", "wkmax", "rev_pair", "rev_threads", "utot_warps", "pdl")
 
 
 @dataclass(frozen=True)
@@ -44,10 +45,11 @@ class Choice:
     utot_warps: int = 4
     branches: int = 2
     pdl: bool = False
+    rev_pair: int = 0
 
     def kernel_tuning(self):
-        """(wkmax, rev_threads, utot_warps) for engine.tables / so4_tables_create_tuned."""
-        return (int(self.wkmax), int(self.rev_threads), int(self.utot_warps))
+        """(wkmax, rev_threads, utot_warps, rev_pair) for engine.tables / so4_tables_create_tuned."""
+        return (int(self.wkmax), int(self.rev_threads), int(self.utot_warps), int(self.rev_pair))
 
     def as_dict(self):
         return dataclasses.asdict(self)
@@ -66,6 +68,7 @@ def search_space(twol, linear=True):
         "wkmax": (5, 4, 3),
         "rev_threads": ((256, 128) if shapes else (0,)),
         "utot_warps": ((4, 2, 8) if shapes else (4,)),
+        "rev_pair": ((0, 1, 2) if shapes else (0,)),
         "pdl": (False, True) if linear else (False,),
     }
 

@@ -15,6 +15,7 @@
 #include <algorithm>
 
 #include "so4_atom.cuh"
+#include "so4_rev2.cuh"
 #include "so4_rowchain.cuh"
 #include "so4_zwin.cuh"
 
@@ -676,6 +677,130 @@ __global__ void __launch_bounds__(NT, (TWOL <= 8) ? 512 / NT : 1) k_deidrj_rev(D
     }
 }
 
+// k_deidrj_rev with two lanes per image (so4_rev2.cuh): a warp takes 32 images, one per lane
+// for the set-up as above, then two iterations of 16 images, lane = 2 image + role.
+template <int TWOL, int NT>
+__global__ void __launch_bounds__(NT, 2) k_deidrj_rev2(DArgs A, int64_t nimg) {
+    using Y = rev2::Layout<TWOL>;
+    constexpr int W = TWOL + 1, NS = Y::NS;
+    constexpr int IPI = 16, PASS = 32;  // images per iteration (two lanes each) and per warp
+    extern __shared__ __align__(16) float2 rv_smem[];  // [Y::SLOTW][NT]
+    float2 *st = rv_smem + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const int64_t wg = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    pdl_wait();  // Y comes from the kernel before
+    const int role = lane & 1, pimg = lane >> 1;
+    int ch[NS];
+#pragma unroll
+    for (int q = 0; q < NS; ++q) ch[q] = -1;
+#pragma unroll
+    for (int c = 0; c < Y::NCH; ++c)
+        if (rev2::role_of(c) == role) ch[rev2::slot_of(c)] = c;
+    const int64_t mbase = __ldg(A.img_ptr);
+    const int64_t mtot = min(nimg, (int64_t)__ldg(A.img_ptr + A.natoms) - mbase);
+    const int64_t p0 = wg * PASS;  // this warp's first image, relative to mbase
+    if (p0 >= mtot) return;
+    const int64_t mo = mbase + p0 + lane;
+    const bool own = p0 + lane < mtot;
+    float x = 1.f, y = 0.f, z = 0.f, wj = 0.f;
+    int centre = 0;
+    if (own) {
+        x = (float)A.img_r[3 * mo];
+        y = (float)A.img_r[3 * mo + 1];
+        z = (float)A.img_r[3 * mo + 2];
+        wj = (float)A.w_nb[A.img_j[mo]];
+        centre = centre_of(A.img_ptr, A.natoms, (int)mo, (int)mbase, mtot);
+    }
+    float r = sqrtf(x * x + y * y + z * z);
+    const bool skip = !(r >= 1e-8f);  // SO4.py:1441 skips r < 1e-8
+    if (skip) {
+        x = 1.f;
+        y = z = 0.f;
+        r = 1.f;
+    }
+    CK<float> ck0;
+    make_ck<float, true>(x, y, z, r, A.psi_fac * r, ck0);
+    const int nit = (int)min((int64_t)(PASS / IPI), (mtot - p0 + IPI - 1) / IPI);
+    for (int it = 0; it < nit; ++it) {
+        const int src = it * IPI + pimg;  // owning lane of this lane's image
+        const bool valid = p0 + src < mtot;
+        const int sl = valid ? src : 0;
+        CK<float> ck;
+        ck.ca.re = __shfl_sync(0xffffffffu, ck0.ca.re, sl);
+        ck.ca.im = __shfl_sync(0xffffffffu, ck0.ca.im, sl);
+        ck.cb.re = __shfl_sync(0xffffffffu, ck0.cb.re, sl);
+        ck.cb.im = __shfl_sync(0xffffffffu, ck0.cb.im, sl);
+        const int c_it = __shfl_sync(0xffffffffu, centre, sl);
+        if (valid) {
+            // the backward sweep reads this centre's Y level by level: ask for its lines now
+            const char *yb = reinterpret_cast<const char *>(A.Y + (size_t)c_it * A.nh);
+            const int nlines = (A.nh * (int)sizeof(float2) + 127) / 128;
+            for (int l = role; l < nlines; l += 2) asm volatile("prefetch.global.L1 [%0];" ::"l"(yb + 128 * l));
+        }
+        float ur[NS][W], ui[NS][W];
+#pragma unroll
+        for (int q = 0; q < NS; ++q)
+#pragma unroll
+            for (int e = 0; e < W; ++e) ur[q][e] = ui[q][e] = 0.f;
+        if (role == 0) {
+            ur[0][0] = 1.f;  // level 0 of chain 0
+            st[Y::idx(0, 0) * NT] = make_float2(1.f, 0.f);
+        }
+        rev2::Fwd<TWOL, 1, NT>::run(role, ch, ck, ur, ui, st);
+        float2 g[NS][W];
+#pragma unroll
+        for (int q = 0; q < NS; ++q)
+#pragma unroll
+            for (int e = 0; e < W; ++e) g[q][e] = make_float2(0.f, 0.f);
+        const float2 *Yc = A.Y + (size_t)c_it * A.nh;
+        const float2 z2 = make_float2(0.f, 0.f);
+        float2 su2 = z2, sa1 = z2, sa2 = z2, sb1 = z2, sb2 = z2;
+        rev2::Back<TWOL, TWOL, NT>::run(role, ch, rv_pairs(ck), Yc, st, g, su2, sa1, sa2, sb1, sb2);
+        float tu = su2.x + su2.y, t0 = sa1.x + sa1.y, t1 = sa2.x - sa2.y;
+        float t2 = -(sb1.x + sb1.y), t3 = -(sb2.x - sb2.y);
+        // the pair's two lanes: both hold the image's sums
+        tu += __shfl_xor_sync(0xffffffffu, tu, 1);
+        t0 += __shfl_xor_sync(0xffffffffu, t0, 1);
+        t1 += __shfl_xor_sync(0xffffffffu, t1, 1);
+        t2 += __shfl_xor_sync(0xffffffffu, t2, 1);
+        t3 += __shfl_xor_sync(0xffffffffu, t3, 1);
+        // the owning lanes of this iteration's images take the sums of their pair
+        const int ol = lane - it * IPI;
+        const bool mine = own && ol >= 0 && ol < IPI;
+        const int from = mine ? 2 * ol : 0;
+        tu = __shfl_sync(0xffffffffu, tu, from);
+        t0 = __shfl_sync(0xffffffffu, t0, from);
+        t1 = __shfl_sync(0xffffffffu, t1, from);
+        t2 = __shfl_sync(0xffffffffu, t2, from);
+        t3 = __shfl_sync(0xffffffffu, t3, from);
+        if (mine) {
+            float sf, dsf;
+            cutoff_fn<float>(A.prm.cutoff_id, r, A.rc32, sf, dsf);
+            const float xr[3] = {x / r, y / r, z / r};
+            float gv[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const float sc = t0 * ck0.cda[c].re + t1 * ck0.cda[c].im + t2 * ck0.cdb[c].re + t3 * ck0.cdb[c].im;
+                gv[c] = skip ? 0.f : wj * (sf * sc + dsf * xr[c] * tu);
+            }
+            A.g[3 * mo] = gv[0];
+            A.g[3 * mo + 1] = gv[1];
+            A.g[3 * mo + 2] = gv[2];
+        }
+    }
+}
+
+template <int TWOL, int NT>
+int launch_deidrj_rev2(const DArgs &D, int64_t nimg, cudaStream_t st) {
+    if (nimg <= 0) return SO4_OK;
+    const size_t smem = sizeof(float2) * (size_t)rev2::Layout<TWOL>::SLOTW * NT;
+    const int rc = so4_set_smem((const void *)k_deidrj_rev2<TWOL, NT>, smem);
+    if (rc) return rc;
+    const int64_t warps = (nimg + 31) / 32;
+    const int64_t blocks = (warps + NT / 32 - 1) / (NT / 32);
+    return so4_launch_pdl(k_deidrj_rev2<TWOL, NT>, dim3((unsigned)blocks), dim3(NT), smem, st, D, nimg);
+}
+
 template <int TWOL, int NT>
 int launch_deidrj_rev_nt(const DArgs &D, int64_t nimg, cudaStream_t st) {
     using RC = RowChain<TWOL>;
@@ -689,10 +814,13 @@ int launch_deidrj_rev_nt(const DArgs &D, int64_t nimg, cudaStream_t st) {
     return so4_launch_pdl(k_deidrj_rev<TWOL, NT>, dim3((unsigned)blocks), dim3(NT), smem, st, D, nimg);
 }
 
-// nt: threads per CTA, from the tables' tuning (256 up to twol 8, 128 above; both for twol 6, 8)
+// nt: threads per CTA, from the tables' tuning (256 up to twol 8, 128 above; both for twol 6, 8);
+// pair: two lanes per image (k_deidrj_rev2, twol 6 and 8: 256 threads at twol 6, 128 at 8,
+// two CTAs per SM either way) instead of one lane per row chain
 template <int TWOL>
-int launch_deidrj_rev(const DArgs &D, int64_t nimg, int nt, cudaStream_t st) {
+int launch_deidrj_rev(const DArgs &D, int64_t nimg, int nt, int pair, cudaStream_t st) {
     if constexpr (TWOL == 6 || TWOL == 8) {
+        if (pair) return launch_deidrj_rev2<TWOL, (TWOL == 6) ? 256 : 128>(D, nimg, st);
         if (nt == 128) return launch_deidrj_rev_nt<TWOL, 128>(D, nimg, st);
         return launch_deidrj_rev_nt<TWOL, 256>(D, nimg, st);
     }
@@ -1059,12 +1187,12 @@ extern "C" int so4_adjoint_deidrj32(const so4_tables *t, const so4_params *p, in
     cudaStream_t st = (cudaStream_t)stream;
     int rc = SO4_OK;
     switch (t->twol) {
-        case 2: rc = launch_deidrj_rev<2>(D, nimg, t->tune.rev_threads, st); break;
-        case 4: rc = launch_deidrj_rev<4>(D, nimg, t->tune.rev_threads, st); break;
-        case 6: rc = launch_deidrj_rev<6>(D, nimg, t->tune.rev_threads, st); break;
-        case 8: rc = launch_deidrj_rev<8>(D, nimg, t->tune.rev_threads, st); break;
-        case 10: rc = launch_deidrj_rev<10>(D, nimg, t->tune.rev_threads, st); break;
-        case 12: rc = launch_deidrj_rev<12>(D, nimg, t->tune.rev_threads, st); break;
+        case 2: rc = launch_deidrj_rev<2>(D, nimg, t->tune.rev_threads, t->tune.rev_pair == 1, st); break;
+        case 4: rc = launch_deidrj_rev<4>(D, nimg, t->tune.rev_threads, t->tune.rev_pair == 1, st); break;
+        case 6: rc = launch_deidrj_rev<6>(D, nimg, t->tune.rev_threads, t->tune.rev_pair == 1, st); break;
+        case 8: rc = launch_deidrj_rev<8>(D, nimg, t->tune.rev_threads, t->tune.rev_pair == 1, st); break;
+        case 10: rc = launch_deidrj_rev<10>(D, nimg, t->tune.rev_threads, t->tune.rev_pair == 1, st); break;
+        case 12: rc = launch_deidrj_rev<12>(D, nimg, t->tune.rev_threads, t->tune.rev_pair == 1, st); break;
         default: {
             const size_t smd = sizeof(float) * rootpq_floats(t->ldim) +
                                sizeof(cx<float>) * ((size_t)t->n_half + (size_t)NWD * 4 * t->n_half);

@@ -112,12 +112,16 @@ void free_device(so4_tables *t) {
 
 }  // namespace
 
+// Default layout of the per-image pass at twol 6 and 8 (1: two lanes per image).
+#define REV_PAIR_DEFAULT 1
+
 // The defaults of so4_tuning for one twol, and whether a requested tuning is built.
 static so4_tuning tuning_defaults(int twol) {
     so4_tuning d;
     d.wkmax = ZW_KMAX;
     d.rev_threads = (twol <= 8) ? 256 : 128;
     d.utot_warps = 4;
+    d.rev_pair = (twol == 6 || twol == 8) ? REV_PAIR_DEFAULT : 2;
     return d;
 }
 
@@ -125,6 +129,7 @@ static int tuning_resolve(int twol, const so4_tuning *req, so4_tuning &out) {
     out = tuning_defaults(twol);
     if (!req) return SO4_OK;
     if (req->wkmax < 0 || req->wkmax > ZW_KMAX || req->rev_threads < 0 || req->utot_warps < 0) return SO4_ERR_ARG;
+    if (req->rev_pair < 0 || req->rev_pair > 2) return SO4_ERR_ARG;
     if (req->rev_threads && req->rev_threads != 128 && req->rev_threads != 256) return SO4_ERR_ARG;
     if (req->utot_warps && req->utot_warps != 2 && req->utot_warps != 4 && req->utot_warps != 8) return SO4_ERR_ARG;
     if (req->wkmax) out.wkmax = req->wkmax;
@@ -136,6 +141,10 @@ static int tuning_resolve(int twol, const so4_tuning *req, so4_tuning &out) {
     if (req->utot_warps && req->utot_warps != out.utot_warps) {
         if (!shapes) return SO4_ERR_UNSUPPORTED;
         out.utot_warps = req->utot_warps;
+    }
+    if (req->rev_pair && req->rev_pair != out.rev_pair) {
+        if (!shapes) return SO4_ERR_UNSUPPORTED;
+        out.rev_pair = req->rev_pair;
     }
     return SO4_OK;
 }

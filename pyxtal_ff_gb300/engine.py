@@ -44,13 +44,15 @@ class Tables:
         if tuning is None:
             check(lib().so4_tables_create(int(twol), int(bool(normalize_u)), C.byref(h)), "so4_tables_create")
         else:
-            tn = Tuning(int(tuning[0]), int(tuning[1]), int(tuning[2]))
+            t4 = tuple(tuning) + (0,) * (4 - len(tuning))
+            tn = Tuning(int(t4[0]), int(t4[1]), int(t4[2]), int(t4[3]))
             check(lib().so4_tables_create_tuned(int(twol), int(bool(normalize_u)), C.byref(tn), C.byref(h)),
                   "so4_tables_create_tuned")
         self.handle = h
         tn = Tuning()
         check(lib().so4_tables_get_tuning(h, C.byref(tn)), "so4_tables_get_tuning")
-        self.tuning = (tn.wkmax, tn.rev_threads, tn.utot_warps)  # (wkmax, rev_threads, utot_warps), resolved
+        # (wkmax, rev_threads, utot_warps, rev_pair), resolved
+        self.tuning = (tn.wkmax, tn.rev_threads, tn.utot_warps, tn.rev_pair)
         s = (C.c_int * 8)()
         check(lib().so4_tables_sizes(h, s), "so4_tables_sizes")
         self.twol = int(twol)
@@ -82,7 +84,8 @@ _TABLES = {}
 
 def tables(twol, normalize_u=False, tuning=None):
     """The tables of (twol, normalize_u) on the current device, built once per tuning
-    ((wkmax, rev_threads, utot_warps) with 0 for a default, or None for all defaults)."""
+    ((wkmax, rev_threads, utot_warps[, rev_pair]) with 0 for a default, or None for all
+    defaults)."""
     tkey = None if tuning is None else tuple(int(v) for v in tuning)
     key = (int(twol), bool(normalize_u), torch.cuda.current_device(), tkey)
     t = _TABLES.get(key)

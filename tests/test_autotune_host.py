@@ -22,12 +22,13 @@ def _cost(best):
         t += 0.07 * (c.rev_threads != best.rev_threads)
         t += 0.03 * abs(c.utot_warps - best.utot_warps) / 2
         t += 0.02 * (c.pdl != best.pdl)
+        t += 0.04 * (c.rev_pair != best.rev_pair)
         return t
     return f, calls
 
 
 def test_coordinate_descent_finds_the_separable_optimum_and_evaluates_each_choice_once():
-    best = T.Choice(wkmax=3, rev_threads=128, utot_warps=8, branches=3, pdl=True)
+    best = T.Choice(wkmax=3, rev_threads=128, utot_warps=8, branches=3, pdl=True, rev_pair=2)
     f, calls = _cost(best)
     start = T.default_choice(8)
     got, t, table = T.coordinate_descent(f, start, T.search_space(8))
@@ -65,8 +66,8 @@ def test_min_gain_keeps_the_default_on_a_flat_cost():
 
 def test_search_space_by_twol_and_step_kind():
     s8, s4 = T.search_space(8), T.search_space(4)
-    assert s8["rev_threads"] == (256, 128) and s8["utot_warps"] == (4, 2, 8)
-    assert s4["rev_threads"] == (0,) and s4["utot_warps"] == (4,)
+    assert s8["rev_threads"] == (256, 128) and s8["utot_warps"] == (4, 2, 8) and s8["rev_pair"] == (0, 1, 2)
+    assert s4["rev_threads"] == (0,) and s4["utot_warps"] == (4,) and s4["rev_pair"] == (0,)
     m = T.search_space(6, linear=False)
     assert m["branches"] == (1,) and m["pdl"] == (False,)
     assert T.default_choice(8, linear=False).branches == 1
@@ -101,6 +102,9 @@ def test_workload_key_classes():
 
 
 def test_choice_dict_round_trip_and_kernel_tuning():
-    ch = T.Choice(wkmax=4, rev_threads=128, utot_warps=8, branches=1, pdl=True)
+    ch = T.Choice(wkmax=4, rev_threads=128, utot_warps=8, branches=1, pdl=True, rev_pair=1)
     assert T.Choice.from_dict(ch.as_dict()) == ch
-    assert ch.kernel_tuning() == (4, 128, 8)
+    assert ch.kernel_tuning() == (4, 128, 8, 1)
+    # a cached choice written before a knob existed reads back with that knob's default
+    old = {"wkmax": 4, "rev_threads": 128, "utot_warps": 8, "branches": 1, "pdl": True}
+    assert T.Choice.from_dict(old).rev_pair == 0

@@ -2,8 +2,9 @@
 
 - so4_tables_create_tuned: out-of-range values -> SO4_ERR_ARG; a CTA shape that is not
   built for this twol -> SO4_ERR_UNSUPPORTED; the resolved tuning reads back.
-- Each non-default kernel shape (window units of 3 and 4 entries, 128-thread
-  per-image CTAs, 2 and 8 centres per U_tot CTA) at lmax 3 and 4: B, forces and
+- Each kernel shape (window units of 3 and 4 entries, 128-thread per-image CTAs, 2 and 8
+  centres per U_tot CTA, the per-image pass with two lanes per image or one lane per row
+  chain) at lmax 3 and 4: B, forces and
   virial against the oracle's contraction (2e-4 relative; B 2e-5), and the JVP
   against the oracle's dxdr / rdxdr (2e-4).
 - autotune_step on a small batch: every evaluated candidate passed its check or was
@@ -38,13 +39,16 @@ def test_tuned_tables_validate_their_arguments(cuda_device):
     for unsupported in [(0, 128, 0), (0, 0, 8)]:
         assert L.so4_tables_create_tuned(4, 0, C.byref(_lib.Tuning(*unsupported)), C.byref(h)) == \
             _lib.SO4_ERR_UNSUPPORTED
-    assert engine.Tables(8, False, (3, 128, 2)).tuning == (3, 128, 2)
-    assert engine.Tables(8, False, None).tuning == (5, 256, 4)
-    assert engine.Tables(10, False, (4, 0, 0)).tuning == (4, 128, 4)
+    assert engine.Tables(8, False, (3, 128, 2, 1)).tuning == (3, 128, 2, 1)
+    assert engine.Tables(8, False, None).tuning[:3] == (5, 256, 4)
+    assert engine.Tables(10, False, (4, 0, 0)).tuning == (4, 128, 4, 2)
+    assert L.so4_tables_create_tuned(8, 0, C.byref(_lib.Tuning(0, 0, 0, 3)), C.byref(h)) == _lib.SO4_ERR_ARG
+    assert L.so4_tables_create_tuned(4, 0, C.byref(_lib.Tuning(0, 0, 0, 1)), C.byref(h)) == _lib.SO4_ERR_UNSUPPORTED
 
 
 @pytest.mark.parametrize("lmax", [3, 4])
-@pytest.mark.parametrize("tuning", [(3, 0, 0), (4, 128, 2), (5, 128, 8), (3, 256, 8)])
+@pytest.mark.parametrize("tuning", [(3, 0, 0, 0), (4, 128, 2, 2), (5, 128, 8, 2), (3, 256, 8, 2), (5, 0, 4, 1),
+                                    (4, 0, 2, 1)])
 def test_tuned_kernels_match_the_oracle(cuda_device, lmax, tuning):
     structs = _structs()
     pos = np.concatenate([s.positions for s in structs])
@@ -55,7 +59,7 @@ def test_tuned_kernels_match_the_oracle(cuda_device, lmax, tuning):
     symbols = sum([list(s.symbols) for s in structs], [])
     rc = 4.9
     p = torch.from_numpy(pos).cuda()
-    choice = autotune.Choice(wkmax=tuning[0], rev_threads=tuning[1], utot_warps=tuning[2])
+    choice = autotune.Choice(wkmax=tuning[0], rev_threads=tuning[1], utot_warps=tuning[2], rev_pair=tuning[3])
     ctx = ops.Context.build(p, cells, pbc, ptr, numbers, symbols, lmax=lmax, rcut=rc, kind="SNAP", weights=W,
                             tuning=choice)
     assert ctx.tab.tuning[0] == tuning[0]
