@@ -215,6 +215,8 @@ struct ZLArgs {
     const int4 *unit, *seg;
     const BEnt *bent;
     const ZBlk *blk;
+    const int4 *blk_rk;    // per block: role components (so4_tables: d_blk_rk)
+    const float4 *blk_rf;  // per block: role factors
     const int *yptr, *ylist;
     const float *beta;
     const int *bpos;  // nB + 1: first B partial slot of each component
@@ -418,19 +420,25 @@ __global__ void __launch_bounds__(ZW_THREADS, 2) k_zw32(ZLArgs A) {
                 ca_s[i] = (i < nbt) ? __ldg(bsrc + i) : 0.f;
             __syncthreads();
         }
-        // one block per warp and step (its table entry is the same for all lanes), lane = atom
+        // one block per warp and step (its table entry is the same for all lanes), lane = atom;
+        // the packed role table (missing roles: factor 0 on a present component) takes two
+        // independent loads per block instead of a chain of dependent reads of the block record
 #pragma unroll 4
         for (int b = threadIdx.x >> 5; b < A.nblk; b += ZW_THREADS / 32) {
-            const ZBlk &bk = A.blk[b];
-            const int nr = bk.nrole;
+            const int4 rk = __ldg(A.blk_rk + b);
+            const float4 rf = __ldg(A.blk_rf + b);
             float c = 0.f;
             if (a < A.natoms) {
-#pragma unroll
-                for (int r = 0; r < 3; ++r) {
-                    if (r < nr) {
-                        const int k = bk.role_k[r];
-                        c += bk.role_f32[r] * (staged ? ca_s[lane * A.nB + k] : __ldg(A.beta + (size_t)a * A.nB + k));
-                    }
+                if (staged) {
+                    const float *bl = ca_s + lane * A.nB;
+                    c = fmaf(rf.x, bl[rk.x], c);
+                    c = fmaf(rf.y, bl[rk.y], c);
+                    c = fmaf(rf.z, bl[rk.z], c);
+                } else {
+                    const float *bl = A.beta + (size_t)a * A.nB;
+                    c = fmaf(rf.x, __ldg(bl + rk.x), c);
+                    c = fmaf(rf.y, __ldg(bl + rk.y), c);
+                    c = fmaf(rf.z, __ldg(bl + rk.z), c);
                 }
             }
             coef[b * ZL_PITCH + lane] = c;
@@ -1007,6 +1015,8 @@ static ZLArgs zl_args(const so4_tables *t, int natoms) {
     Z.hfull = t->d_hfull;
     Z.bent = t->d_b;
     Z.blk = t->d_blk;
+    Z.blk_rk = t->d_blk_rk;
+    Z.blk_rf = t->d_blk_rf;
     Z.yptr = t->d_yblk_ptr;
     Z.ylist = t->d_yblk;
     Z.wsub = t->d_wsub;

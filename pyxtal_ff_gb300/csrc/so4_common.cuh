@@ -105,6 +105,10 @@ struct so4_tables {
     ZEnt *d_z = nullptr;
     BEnt *d_b = nullptr;
     ZBlk *d_blk = nullptr;
+    // per Z block, packed for the window kernels' coefficient loop: the components of its
+    // roles {k0, k1, k2, nrole} (missing roles repeat k0) and their FP32 factors (0 when missing)
+    int4 *d_blk_rk = nullptr;
+    float4 *d_blk_rf = nullptr;
     int *d_yblk_ptr = nullptr;  // ldim + 1 : blocks grouped by their third index
     int *d_yblk = nullptr;      // n_blk
     // n_half: half entry -> {full position, mirror position | conj << 15 | negate << 14 or -1}

@@ -87,6 +87,8 @@ void free_device(so4_tables *t) {
     cudaFree(t->d_z);
     cudaFree(t->d_b);
     cudaFree(t->d_blk);
+    cudaFree(t->d_blk_rk);
+    cudaFree(t->d_blk_rf);
     cudaFree(t->d_yblk_ptr);
     cudaFree(t->d_yblk);
     cudaFree(t->d_hfull);
@@ -670,6 +672,23 @@ extern "C" int so4_tables_create_tuned(int twol, int normalize_u, const so4_tuni
     if (!rc) rc = upload(&t->d_psec_ptr, psec_ptr);
     if (!rc) rc = upload(&t->d_ksec, ksec);
     if (!rc) rc = upload(&t->d_blk, blks);
+    if (!rc) {
+        std::vector<int4> rk(t->n_blk);
+        std::vector<float4> rf(t->n_blk);
+        for (int bi = 0; bi < t->n_blk; ++bi) {
+            const ZBlk &bk = blks[bi];
+            int k[3];
+            float f[3];
+            for (int r = 0; r < 3; ++r) {
+                k[r] = (r < bk.nrole) ? bk.role_k[r] : (bk.nrole > 0 ? bk.role_k[0] : 0);
+                f[r] = (r < bk.nrole) ? bk.role_f32[r] : 0.f;
+            }
+            rk[bi] = make_int4(k[0], k[1], k[2], bk.nrole);
+            rf[bi] = make_float4(f[0], f[1], f[2], 0.f);
+        }
+        rc = upload(&t->d_blk_rk, rk);
+        if (!rc) rc = upload(&t->d_blk_rf, rf);
+    }
     if (!rc) rc = upload(&t->d_yblk_ptr, yptr);
     if (!rc) rc = upload(&t->d_yblk, ylist);
     // a unit cap below the default means more units and so more B / JVP slots, which the
