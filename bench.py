@@ -35,10 +35,10 @@ CONFIG = {"workload": "diamond-Si 20x20x10 (32000 atoms), SO4 lmax=4, rcut=5.0 A
                   "dE/dr, gather (compensated FP32 per atom, FP64 across atoms)"}
 
 
-# DRAM bytes (read + write) per full launch of each stage's kernel: twice the figures of
-# the half-size launches (one graph branch each) captured with ncu and summarised in
-# profiles/k_zw32_k_deidrj_rev_k_utot_rc_si32000_lmax4.md (same workload)
-NCU_TRAFFIC = {"utot32": 25.8e6, "linear_by32": 50.6e6, "adjoint_deidrj32": 65.4e6}
+# DRAM bytes (read + write) per full launch of each stage's kernel: the figures of the
+# one-kernel captures of a 16,384-atom case (profiles/k_utot_rc_k_zw32_k_deidrj_rev2_si16384_lmax4.md),
+# times 1.95 for the atoms and images of the 32,000-atom workload
+NCU_TRAFFIC = {"utot32": 25.8e6, "linear_by32": 51.0e6, "adjoint_deidrj32": 68.2e6}
 
 
 def workload():
@@ -447,6 +447,15 @@ def run_profile_case(which):
             d = calc.descriptors(batch, precision="fp64")
             torch.cuda.synchronize()
             del d
+    elif which == "linear":
+        batch = Batch([S.diamond_si(16, 16, 8, sigma=0.1, rng=np.random.default_rng(5))])
+        p = torch.from_numpy(batch.positions).cuda()
+        ctx = ops.Context.build(p, batch.cells, batch.pbc, batch.atom_ptr, batch.numbers, batch.symbols, lmax=LMAX,
+                                rcut=RCUT, kind="SNAP", weights={"Si": 1.0}, rfac0=1.0)
+        beta = torch.from_numpy(np.random.default_rng(6).normal(0, 0.01, (batch.natoms, ctx.tab.nB))).float().cuda()
+        for _ in range(3):
+            engine.adjoint_linear32(ctx.tab, ctx.prm, ctx.nb, ctx.w_nb, ctx.w_site, beta)
+        torch.cuda.synchronize()
     else:
         batch = Batch([S.diamond_si(16, 16, 8, sigma=0.1, rng=np.random.default_rng(5))])
         p = torch.from_numpy(batch.positions).cuda()
@@ -471,10 +480,11 @@ def main():
     ap.add_argument("--no-tune", action="store_true", help="default launch shapes instead of the autotuner's choice")
     ap.add_argument("--quick", action="store_true",
                     help="device-resident steps only (no e2e, FP64, CPU or peak legs); for profiler runs")
-    ap.add_argument("--profile-case", choices=["plain", "jvp"], default=None,
+    ap.add_argument("--profile-case", choices=["plain", "jvp", "linear"], default=None,
                     help="only a small case for profiler runs: 'plain' = two FP64 plain-path evaluations of a "
                          "2,048-atom diamond-Si cell, 'jvp' = the FP32 forward and three JVPs of a 16,384-atom "
-                         "cell (lmax 4, rcut 5.0)")
+                         "cell, 'linear' = three fused linear-energy evaluations (U_tot, window B + Y, "
+                         "per-image pass, gather) of the 16,384-atom cell (lmax 4, rcut 5.0)")
     ap.add_argument("--contract-cells", type=int, default=0,
                     help="only the NN consumer's dxdr contraction (so4_contract_dxdr) on an N x N x 10 diamond-Si "
                          "cell at lmax 4 (a small case for profiler runs)")
