@@ -688,7 +688,7 @@ __global__ void __launch_bounds__(NT, (TWOL <= 8) ? 512 / NT : 1) k_deidrj_rev(D
 // k_deidrj_rev with two lanes per image (so4_rev2.cuh): a warp takes 32 images, one per lane
 // for the set-up as above, then two iterations of 16 images, lane = 2 image + role.
 template <int TWOL, int NT>
-__global__ void __launch_bounds__(NT, 2) k_deidrj_rev2(DArgs A, int64_t nimg) {
+__global__ void __launch_bounds__(NT, (TWOL == 8) ? 3 : 2) k_deidrj_rev2(DArgs A, int64_t nimg) {
     using Y = rev2::Layout<TWOL>;
     constexpr int W = TWOL + 1, NS = Y::NS;
     constexpr int IPI = 16, PASS = 32;  // images per iteration (two lanes each) and per warp
@@ -763,7 +763,7 @@ __global__ void __launch_bounds__(NT, 2) k_deidrj_rev2(DArgs A, int64_t nimg) {
         const float2 *Yc = A.Y + (size_t)c_it * A.nh;
         const float2 z2 = make_float2(0.f, 0.f);
         float2 su2 = z2, sa1 = z2, sa2 = z2, sb1 = z2, sb2 = z2;
-        rev2::Back<TWOL, TWOL, NT>::run(role, ch, rv_pairs(ck), Yc, st, g, su2, sa1, sa2, sb1, sb2);
+        rev2::Back<TWOL, TWOL, NT>::run(role, ch, rv_pairs(ck), Yc, st, ur, ui, g, su2, sa1, sa2, sb1, sb2);
         float tu = su2.x + su2.y, t0 = sa1.x + sa1.y, t1 = sa2.x - sa2.y;
         float t2 = -(sb1.x + sb1.y), t3 = -(sb2.x - sb2.y);
         // the pair's two lanes: both hold the image's sums
@@ -823,8 +823,8 @@ int launch_deidrj_rev_nt(const DArgs &D, int64_t nimg, cudaStream_t st) {
 }
 
 // nt: threads per CTA, from the tables' tuning (256 up to twol 8, 128 above; both for twol 6, 8);
-// pair: two lanes per image (k_deidrj_rev2, twol 6 and 8: 256 threads at twol 6, 128 at 8,
-// two CTAs per SM either way) instead of one lane per row chain
+// pair: two lanes per image (k_deidrj_rev2, twol 6 and 8: 256 threads at twol 6 with two
+// CTAs per SM, 128 at 8 with three) instead of one lane per row chain
 template <int TWOL>
 int launch_deidrj_rev(const DArgs &D, int64_t nimg, int nt, int pair, cudaStream_t st) {
     if constexpr (TWOL == 6 || TWOL == 8) {

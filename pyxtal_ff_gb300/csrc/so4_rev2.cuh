@@ -16,10 +16,12 @@
 // The recursion itself is the scaled one of so4_rowchain.cuh (rc_level), and the backward
 // sweep the same adjoint steps as RvBack, slot by slot.
 //
-// Each lane keeps the rows it computes in shared memory, slot s from level base(s) on:
-// slot s's region starts at SOFF(s) and row (L, ma) sits at SOFF(s) + acc_block(L) -
-// acc_block(base(s)) + ma; at a chain start the mirrored starting row is stored as level
-// L - 1 of the new chain's slot (101 entries per lane at TWOL 8, 50 at TWOL 6).
+// Each lane keeps the rows it computes in shared memory, slot s from level base(s) up to
+// TWOL - 1: slot s's region starts at SOFF(s) and row (L, ma) sits at SOFF(s) + acc_block(L)
+// - acc_block(base(s)) + ma; at a chain start the mirrored starting row is stored as level
+// L - 1 of the new chain's slot.  The rows of level TWOL are not stored: they are still in
+// the forward sweep's registers when the backward sweep starts there (74 entries per lane at
+// TWOL 8, 36 at TWOL 6).
 #pragma once
 
 #include "so4_rowchain.cuh"
@@ -60,7 +62,7 @@ struct Layout {
     }
     __host__ __device__ static constexpr int soff(int s) {
         int o = 0;
-        for (int q = 0; q < s; ++q) o += acc_block(TWOL + 1) - acc_block(base(q));
+        for (int q = 0; q < s; ++q) o += acc_block(TWOL) - acc_block(base(q));
         return o;
     }
     static constexpr int SLOTW = soff(NS);  // stored entries per lane
@@ -103,7 +105,7 @@ struct Fwd {
         for (int s = 0; s < Y::NS; ++s) {
             if (Y::act(s) <= L) {
                 rc_level<TWOL, L, false>(ch[s], ck, ur[s], ui[s], dr, di);
-                if (ch[s] >= 0 && 2 * ch[s] <= L) {
+                if (L < TWOL && ch[s] >= 0 && 2 * ch[s] <= L) {
 #pragma unroll
                     for (int ma = 0; ma <= L; ++ma) st[(Y::idx(s, L) + ma) * NT] = make_float2(ur[s][ma], ui[s][ma]);
                 }
@@ -126,6 +128,7 @@ struct Back {
     using Y = Layout<TWOL>;
     __device__ __forceinline__ static void run(int role, const int (&ch)[Y::NS], const RvPairs &q,
                                                const float2 *__restrict__ Yc, const float2 *st,
+                                               const float (&ur)[Y::NS][TWOL + 1], const float (&ui)[Y::NS][TWOL + 1],
                                                float2 (&g)[Y::NS][TWOL + 1], float2 &su, float2 &sa1, float2 &sa2,
                                                float2 &sb1, float2 &sb2) {
         constexpr int H = L / 2;
@@ -140,7 +143,9 @@ struct Back {
                         // the middle row of an even level carries no Y past its centre (not stored)
                         const bool none = (L & 1) == 0 && ma > H && mb == H;
                         const float2 y = none ? make_float2(0.f, 0.f) : __ldg(Yr + ma);
-                        su = __ffma2_rn(st[(Y::idx(s, L) + ma) * NT], y, su);
+                        // level TWOL from the forward sweep's registers, lower levels from shared memory
+                        const float2 row = (L == TWOL) ? make_float2(ur[s][ma], ui[s][ma]) : st[(Y::idx(s, L) + ma) * NT];
+                        su = __ffma2_rn(row, y, su);
                         g[s][ma] = __fadd2_rn(g[s][ma], y);
                     }
                     if ((L & 1) == 0 && mb == H) {
@@ -189,7 +194,7 @@ struct Back {
                 }
             }
         }
-        Back<TWOL, L - 1, NT>::run(role, ch, q, Yc, st, g, su, sa1, sa2, sb1, sb2);
+        Back<TWOL, L - 1, NT>::run(role, ch, q, Yc, st, ur, ui, g, su, sa1, sa2, sb1, sb2);
     }
 };
 template <int TWOL, int NT>
@@ -197,6 +202,7 @@ struct Back<TWOL, 0, NT> {
     using Y = Layout<TWOL>;
     __device__ __forceinline__ static void run(int role, const int (&)[Y::NS], const RvPairs &,
                                                const float2 *__restrict__ Yc, const float2 *,
+                                               const float (&)[Y::NS][TWOL + 1], const float (&)[Y::NS][TWOL + 1],
                                                float2 (&)[Y::NS][TWOL + 1], float2 &su, float2 &, float2 &,
                                                float2 &, float2 &) {
         if (role == 0) su.x += __ldg(Yc).x;  // level 0: U = 1 (chain 0, lane A)
