@@ -142,9 +142,10 @@ class Clocks:
 
 # ----------------------------------------------------------------- peaks
 def kernels_back_to_back(calc, batch, pos_dev, beta_dev, reps=20):
-    """Mean launch duration (ms) of the three adjoint kernels, each called `reps` times back to
-    back through its C-ABI entry and replayed as one CUDA graph, so no host launch gap enters
-    (the eager stage table includes them)."""
+    """Mean launch duration (ms) of the three adjoint kernels and of the JVP (two launches:
+    the per-image tangent pass and the window pass), each called `reps` times back to back
+    through its C-ABI entry and replayed as one CUDA graph, so no host launch gap enters (the
+    eager stage table includes them)."""
     import ctypes as C
     import torch
     from pyxtal_ff_gb300 import _lib
@@ -161,6 +162,9 @@ def kernels_back_to_back(calc, batch, pos_dev, beta_dev, reps=20):
     bc = torch.empty((tab.n_bsec, N), dtype=torch.float32, device=dev)
     eatom = torch.empty(N, dtype=torch.float32, device=dev)
     g = torch.empty((M, 3), dtype=torch.float32, device=dev)
+    v = torch.from_numpy(np.random.default_rng(7).normal(size=(N, 3))).to(dev)
+    dB = torch.empty((N, tab.nB), dtype=torch.float32, device=dev)
+    jws = torch.empty(L.so4_jvp_workspace_size(tab.handle, N), dtype=torch.uint8, device=dev)
     w_nb, w_site = calc._w_nb, calc._w_site
     calls = {
         "utot32": lambda: check(L.so4_utot32(tab.handle, C.byref(prm), N, _ptr(w_nb), _ptr(w_site), _ptr(nb.img_ptr),
@@ -170,6 +174,10 @@ def kernels_back_to_back(calc, batch, pos_dev, beta_dev, reps=20):
         "adjoint_deidrj32": lambda: check(L.so4_adjoint_deidrj32(tab.handle, C.byref(prm), N, _ptr(w_nb),
                                                                  _ptr(nb.img_ptr), _ptr(nb.img_j), _ptr(nb.img_r), M,
                                                                  _ptr(y), _ptr(g), _stream()), "so4_adjoint_deidrj32"),
+        # the training path's backward (forces' tangent through B), on the same structure
+        "jvp32": lambda: check(L.so4_jvp32(tab.handle, C.byref(prm), _ptr(nb.atom_struct), N, _ptr(w_nb),
+                                           _ptr(nb.img_ptr), _ptr(nb.img_j), _ptr(nb.img_r), _ptr(utot), _ptr(v),
+                                           _ptr(None), _ptr(dB), _ptr(jws), jws.numel(), _stream()), "so4_jvp32"),
     }
     out = {}
     for name, f in calls.items():
@@ -447,6 +455,14 @@ def run_profile_case(which):
             d = calc.descriptors(batch, precision="fp64")
             torch.cuda.synchronize()
             del d
+    elif which == "nl":
+        from pyxtal_ff_gb300.calculator import LinearModel
+        batch = Batch([S.diamond_si(16, 16, 8, sigma=0.1, rng=np.random.default_rng(5))])
+        calc = SO4Calculator(lmax=LMAX, rcut=RCUT, kind="SNAP", weights={"Si": 1.0}, rfac0=1.0)
+        step = calc.capture(batch, LinearModel(np.zeros(calc.nB)).cuda(), branches=1)
+        for _ in range(3):
+            engine.enqueue_neighbors(step.layout, step.pos, step.nl, lite=True)
+        torch.cuda.synchronize()
     elif which == "linear":
         batch = Batch([S.diamond_si(16, 16, 8, sigma=0.1, rng=np.random.default_rng(5))])
         p = torch.from_numpy(batch.positions).cuda()
@@ -480,11 +496,12 @@ def main():
     ap.add_argument("--no-tune", action="store_true", help="default launch shapes instead of the autotuner's choice")
     ap.add_argument("--quick", action="store_true",
                     help="device-resident steps only (no e2e, FP64, CPU or peak legs); for profiler runs")
-    ap.add_argument("--profile-case", choices=["plain", "jvp", "linear"], default=None,
+    ap.add_argument("--profile-case", choices=["plain", "jvp", "linear", "nl"], default=None,
                     help="only a small case for profiler runs: 'plain' = two FP64 plain-path evaluations of a "
                          "2,048-atom diamond-Si cell, 'jvp' = the FP32 forward and three JVPs of a 16,384-atom "
                          "cell, 'linear' = three fused linear-energy evaluations (U_tot, window B + Y, "
-                         "per-image pass, gather) of the 16,384-atom cell (lmax 4, rcut 5.0)")
+                         "per-image pass, gather) of the 16,384-atom cell, 'nl' = three one-branch neighbour "
+                         "lists of the captured step on the 16,384-atom cell (lmax 4, rcut 5.0)")
     ap.add_argument("--contract-cells", type=int, default=0,
                     help="only the NN consumer's dxdr contraction (so4_contract_dxdr) on an N x N x 10 diamond-Si "
                          "cell at lmax 4 (a small case for profiler runs)")
@@ -785,16 +802,27 @@ def main():
         "ms_back_to_back": nl_ms, "bytes": nl_bytes, "images": nl_images,
         "gbs": nl_bytes / (nl_ms * 1e-3) / 1e9, "frac_hbm": nl_bytes / (nl_ms * 1e-3) / 1e9 / peaks["hbm_gbs"],
         "bound": "latency (per-centre bin walk), not HBM",
+        "traffic": 25.9e6, "traffic_unit": "DRAM bytes per full list: scan + sort + reverse images of a 16,384-atom "
+                                           "list from ncu (profiles/k_scan_images_k_sort_k_rev_si16384_dram.md) x 1.95; "
+                                           "below the algorithmic bytes because the outputs stay in L2",
         "what": "one-branch form of the captured step's list: bins + per-atom keys, sort with FP64 image vectors, "
                 "reverse images, summary; bytes = positions + image pointer + 44 B per image written"}
-    for nme in ("utot32", "linear_by32", "adjoint_deidrj32"):
-        if "tflops_executed" in kernels.get(nme, {}):
-            kernels[nme]["frac_executed_vs_fma_loop"] = kernels[nme]["tflops_executed"] / peaks["fp32_fma_tflops"]
-            kernels[nme]["frac_vs_fma_loop"] = kernels[nme]["tflops"] / peaks["fp32_fma_tflops"]
+    # the JVP (training's backward) on the same structure: executed work only (the reference has
+    # no such step: its trainer back-propagates through stored dxdr)
+    kernels["jvp32"] = {"ms_back_to_back": b2b_ms["jvp32"],
+                        "tflops_executed": kf["jvp32"] / (b2b_ms["jvp32"] * 1e-3) / 1e12,
+                        "what": "so4_jvp32 with a per-atom tangent: per-image tangent pass + window pass"}
+    kernels["jvp32"]["frac_executed"] = kernels["jvp32"]["tflops_executed"] / peaks["fp32_tflops"]
+    for nme in ("utot32", "linear_by32", "adjoint_deidrj32", "jvp32"):
+        k = kernels.get(nme, {})
+        if "tflops_executed" in k:
+            k["frac_executed_vs_fma_loop"] = k["tflops_executed"] / peaks["fp32_fma_tflops"]
+        if "tflops" in k:
+            k["frac_vs_fma_loop"] = k["tflops"] / peaks["fp32_fma_tflops"]
     # the per-kernel times are full-size launches back to back; the step runs each of them as two
     # half-size launches in parallel graph branches, plus the list and the gather
     kernels["step_reconciliation"] = {
-        "sum_of_back_to_back_kernels_ms": float(sum(b2b_ms.values())) + nl_ms,
+        "sum_of_back_to_back_kernels_ms": float(sum(v for k, v in b2b_ms.items() if k != "jvp32")) + nl_ms,
         "gather_ms_eager": float(stage_ms[stage_names.index("gather")]),
         "step_ms": t_dev / args.steps,
         "note": "U_tot, window and per-image kernels back to back at full size, plus the one-branch "

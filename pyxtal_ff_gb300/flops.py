@@ -135,6 +135,12 @@ def per_image_rev(twol):
     return f + 60
 
 
+def per_image_jvp(twol):
+    """The JVP's per-image pass: the U recursion, its tangent along one direction (one
+    component of the dU recursion) and the tangent of U_tot accumulated (8 per half entry)."""
+    return per_image_u(twol) + per_image_du(twol) // 3 + 8 * sizes(twol)["n_half"]
+
+
 def kernel_flops(twol, natoms, nimg):
     """Flops of one launch of each kernel for a batch, counted from the algorithm each
     kernel runs (the window kernels' Z with middle rows cut at the centre, the reverse-mode
@@ -150,6 +156,9 @@ def kernel_flops(twol, natoms, nimg):
         "forward32": natoms * (zc + per_atom_b(twol)) + nimg * utot_img,
         "adjoint_y32": natoms * (zc + per_atom_y(twol, cut_middle=True)),
         "adjoint_deidrj32": nimg * per_image_rev(twol),
+        # the JVP: the per-image tangent pass, then the window pass's Z once per atom contracted
+        # with the tangent per (block, role) like Y (so4_jvp32)
+        "jvp32": nimg * per_image_jvp(twol) + natoms * (zc + per_atom_y(twol, cut_middle=True)),
         "plain": natoms * (z + per_atom_b(twol)) + nimg * (utot_img + u + du + per_image_db(twol)),
     }
 
