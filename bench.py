@@ -455,6 +455,14 @@ def run_profile_case(which):
             d = calc.descriptors(batch, precision="fp64")
             torch.cuda.synchronize()
             del d
+    elif which == "train":
+        from pyxtal_ff_gb300.train import ForceMatching
+        batch = Batch(S.si_batch(512, seed=4, sizes=range(1, 9), max_cells=8, strain=0.04, sigma=0.1))
+        fm = ForceMatching(batch, lmax=3, rcut=4.9, seed=4)
+        fm.capture(warmup=2)
+        for _ in range(3):
+            fm.step()
+        torch.cuda.synchronize()
     elif which == "nl":
         from pyxtal_ff_gb300.calculator import LinearModel
         batch = Batch([S.diamond_si(16, 16, 8, sigma=0.1, rng=np.random.default_rng(5))])
@@ -496,12 +504,13 @@ def main():
     ap.add_argument("--no-tune", action="store_true", help="default launch shapes instead of the autotuner's choice")
     ap.add_argument("--quick", action="store_true",
                     help="device-resident steps only (no e2e, FP64, CPU or peak legs); for profiler runs")
-    ap.add_argument("--profile-case", choices=["plain", "jvp", "linear", "nl"], default=None,
+    ap.add_argument("--profile-case", choices=["plain", "jvp", "linear", "nl", "train"], default=None,
                     help="only a small case for profiler runs: 'plain' = two FP64 plain-path evaluations of a "
                          "2,048-atom diamond-Si cell, 'jvp' = the FP32 forward and three JVPs of a 16,384-atom "
                          "cell, 'linear' = three fused linear-energy evaluations (U_tot, window B + Y, "
                          "per-image pass, gather) of the 16,384-atom cell, 'nl' = three one-branch neighbour "
-                         "lists of the captured step on the 16,384-atom cell (lmax 4, rcut 5.0)")
+                         "lists of the captured step on the 16,384-atom cell (lmax 4, rcut 5.0), 'train' = the "
+                         "force-matching training step (512 Si structures, lmax 3) captured, then three replays")
     ap.add_argument("--contract-cells", type=int, default=0,
                     help="only the NN consumer's dxdr contraction (so4_contract_dxdr) on an N x N x 10 diamond-Si "
                          "cell at lmax 4 (a small case for profiler runs)")

@@ -74,6 +74,29 @@ def stillinger_weber(batch: Batch, device="cuda", params=SW_SI):
     return energy.detach(), (-forces).detach()
 
 
+class RowChunkedLinear(torch.nn.Linear):
+    """nn.Linear computed over chunks of `rows` input rows with one batched matmul.
+
+    The trainer's layers are tall and narrow (tens of thousands of atoms by 30 features), so
+    the gradient of a weight is a 30 x 30 product summed over all the atoms; as one GEMM that
+    reduction runs on a handful of thread blocks.  Chunked, autograd forms it as one product
+    per chunk (in parallel) and a sum over the chunks, at every order of differentiation the
+    force-matching loss needs.  The parameters and results are those of nn.Linear (up to the
+    order of the sums)."""
+
+    rows = 512
+
+    def forward(self, x):
+        n = x.shape[0]
+        if x.dim() != 2 or n < 4 * self.rows:
+            return super().forward(x)
+        c = (n + self.rows - 1) // self.rows
+        xp = torch.nn.functional.pad(x, (0, 0, 0, c * self.rows - n)).view(c, self.rows, self.in_features)
+        y = torch.bmm(xp, self.weight.t().unsqueeze(0).expand(c, self.in_features, self.out_features))
+        y = y.reshape(c * self.rows, self.out_features)[:n]
+        return y + self.bias if self.bias is not None else y
+
+
 class SpeciesMLP(torch.nn.Module):
     """Per-species MLP on B (nB -> hidden... -> 1, tanh), Xavier-uniform weights from a seed."""
 
@@ -84,9 +107,9 @@ class SpeciesMLP(torch.nn.Module):
         for _ in range(nspecies):
             layers, n_in = [], nB
             for h in hidden:
-                layers += [torch.nn.Linear(n_in, h), torch.nn.Tanh()]
+                layers += [RowChunkedLinear(n_in, h), torch.nn.Tanh()]
                 n_in = h
-            layers.append(torch.nn.Linear(n_in, 1))
+            layers.append(RowChunkedLinear(n_in, 1))
             net = torch.nn.Sequential(*layers)
             for m in net:
                 if isinstance(m, torch.nn.Linear):
