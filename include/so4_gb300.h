@@ -102,12 +102,22 @@ int so4_tables_destroy(so4_tables *t);
  *   rev_pair    layout of the per-image pass: 1 two lanes per image (its row chains
  *               shared out so the lanes' work per level is even), 2 one lane per row
  *               chain (built for every twol; rev_threads applies to it); 0 the default,
- *               two lanes where built (twol 6 and 8). */
+ *               two lanes where built (twol 6 and 8);
+ *   zw_atoms    atoms per CTA of the window Z pass (so4_forward32, so4_adjoint_y32,
+ *               so4_linear_by32, so4_jvp32): 32, one per lane, two CTAs per SM; or 64,
+ *               two per lane (their real and imaginary parts packed in FP32 pairs), one
+ *               CTA per SM, up to twol 8, where its U tiles fit in shared memory
+ *               (default 64 up to twol 8, 32 above);
+ *   zw_threads  threads per CTA of the 64-atom window pass, 256 or 512 (default 512:
+ *               16 warps at 128 registers).
+ * Every layout gives the same bits. */
 typedef struct {
     int wkmax;
     int rev_threads;
     int utot_warps;
     int rev_pair;
+    int zw_atoms;
+    int zw_threads;
 } so4_tuning;
 /* so4_tables_create with a tuning (NULL: the defaults).  SO4_ERR_ARG for a value
  * outside the ranges above; SO4_ERR_UNSUPPORTED for a CTA shape not built for this

@@ -63,7 +63,8 @@ class Params(C.Structure):
 
 class Tuning(C.Structure):
     """so4_tuning: launch shapes of the FP32 kernels (0 = the default)."""
-    _fields_ = [("wkmax", C.c_int), ("rev_threads", C.c_int), ("utot_warps", C.c_int), ("rev_pair", C.c_int)]
+    _fields_ = [("wkmax", C.c_int), ("rev_threads", C.c_int), ("utot_warps", C.c_int), ("rev_pair", C.c_int),
+                ("zw_atoms", C.c_int), ("zw_threads", C.c_int)]
 
 
 _lib = None

@@ -11,6 +11,9 @@ device.  The knobs:
   rev_threads  threads per CTA of the per-image dE/dr pass, 128 or 256
   utot_warps   centres per CTA of the U_tot pass, 2, 4 or 8
   rev_pair     layout of the per-image pass: 1 two lanes per image, 2 one lane per row chain
+  zw_atoms     atoms per CTA of the window Z pass: 32 (one per lane) or 64 (two per lane,
+               up to twol 8)
+  zw_threads   threads per CTA of the 64-atom window pass, 256 or 512
   branches     parallel graph branches of the captured linear step, 1..4
   pdl          programmatic dependent launch between that step's kernels
 
@@ -34,7 +37,7 @@ from dataclasses import dataclass
 
 import numpy as np
 
-SPACE_ORDER = ("branches", "wkmax", "rev_pair", "rev_threads", "utot_warps", "pdl")
+SPACE_ORDER = ("branches", "wkmax", "zw_atoms", "zw_threads", "rev_pair", "rev_threads", "utot_warps", "pdl")
 
 
 @dataclass(frozen=True)
@@ -46,10 +49,14 @@ class Choice:
     branches: int = 2
     pdl: bool = False
     rev_pair: int = 0
+    zw_atoms: int = 0
+    zw_threads: int = 0
 
     def kernel_tuning(self):
-        """(wkmax, rev_threads, utot_warps, rev_pair) for engine.tables / so4_tables_create_tuned."""
-        return (int(self.wkmax), int(self.rev_threads), int(self.utot_warps), int(self.rev_pair))
+        """(wkmax, rev_threads, utot_warps, rev_pair, zw_atoms, zw_threads) for engine.tables /
+        so4_tables_create_tuned."""
+        return (int(self.wkmax), int(self.rev_threads), int(self.utot_warps), int(self.rev_pair),
+                int(self.zw_atoms), int(self.zw_threads))
 
     def as_dict(self):
         return dataclasses.asdict(self)
@@ -69,6 +76,8 @@ def search_space(twol, linear=True):
         "rev_threads": ((256, 128) if shapes else (0,)),
         "utot_warps": ((4, 2, 8) if shapes else (4,)),
         "rev_pair": ((0, 1, 2) if shapes else (0,)),
+        "zw_atoms": ((32, 64) if twol <= 8 else (0,)),
+        "zw_threads": ((256, 512) if twol <= 8 else (0,)),
         "pdl": (False, True) if linear else (False,),
     }
 

@@ -18,6 +18,7 @@
 #include "so4_rev2.cuh"
 #include "so4_rowchain.cuh"
 #include "so4_zwin.cuh"
+#include "so4_zwin2.cuh"
 
 namespace {
 
@@ -326,7 +327,7 @@ __device__ __forceinline__ void zw_unit(const ZLArgs &A, const int4 un, const fl
                 const int off = off0 + k;
                 if (off < cnt) {
                     const float2 uv = ul[k * ZL_PITCH];
-                    const float d = uv.x * z[k].x + uv.y * z[k].y;
+                    const float d = __fmaf_rn(uv.y, z[k].y, __fmul_rn(uv.x, z[k].x));
                     v += ((lam & 1) == 0 && off == cnt - 1) ? 0.5f * d : d;
                 }
             }
@@ -345,6 +346,11 @@ __device__ __forceinline__ void zw_unit(const ZLArgs &A, const int4 un, const fl
             // times the row scale F: the reverse sweep contracts the scaled rows with it
             const float s = un_l * wmid * __ldg(ys + k);
             Yo[k] = make_float2(s * y[k].x, s * y[k].y);
+        }
+        // no unit computes the upper half of an even level's middle row (its Y is zero): the
+        // unit ending at the row's centre writes those zeros, so every Y entry is defined
+        if (2 * mb == lam && ma0 + K - 1 == lam / 2) {
+            for (int ma = lam / 2 + 1; ma <= lam; ++ma) Yo[ma - ma0] = make_float2(0.f, 0.f);
         }
     }
 }
@@ -380,9 +386,11 @@ __global__ void __launch_bounds__(ZW_THREADS, 2) k_zw32(ZLArgs A) {
     float *coef = (float *)(Ub + (size_t)(A.nu + 2 * ZW_PAD) * ZL_PITCH);  // [nblk][33], MODE 1 and 2
     if (threadIdx.x == 0) s_unit = 0;
     // the window coefficients (read at every step) in shared memory when they fit
-    // (16-byte aligned for the float4 reads; the launch adds 16 bytes of slack)
-    float *ca_s = reinterpret_cast<float *>((reinterpret_cast<uintptr_t>(coef + (size_t)A.nblk * ZL_PITCH) + 15) &
-                                            ~(uintptr_t)15);
+    // (16-byte aligned for the float4 reads; the launch adds 16 bytes of slack).  Offset
+    // arithmetic on the shared array, not integer casts, so that the compiler keeps the
+    // shared address space and issues shared loads for the table
+    float *ca_s = reinterpret_cast<float *>(zw_smem) +
+                  ((2 * (size_t)(A.nu + 2 * ZW_PAD) * ZL_PITCH + (size_t)A.nblk * ZL_PITCH + 3) & ~(size_t)3);
     // Every independent global load of the prologue is in flight before any is waited on:
     // the first ZW_CAR float4 per thread of the Ca table, the first ZW_BR values per thread
     // of the 32 atoms' beta rows (one contiguous run; MODE 1 and 2 stage them in the Ca area
@@ -495,6 +503,255 @@ __global__ void __launch_bounds__(ZW_THREADS, 2) k_zw32(ZLArgs A) {
     }
 }
 
+
+// zw_unit with two atoms per lane (so4_zwin2.cuh): the lane's atoms are a = a0 + lane
+// and a + 32; every per-atom quantity is a pair (atom a, atom a + 32).
+template <int MODE, int K>
+__device__ __forceinline__ void zw2_unit(const ZLArgs &A, const int4 un, const float4 *Ul, const float2 *coef,
+                                         const float *__restrict__ ca, int a, int lane) {
+    const int lam = un.x & 0xff, mb = (un.x >> 8) & 0xff, ma0 = (un.x >> 16) & 0xff;
+    const int off0 = mb * (lam + 1) + ma0;
+    const int cnt = section_count(lam);
+    const int b = a + 32;
+    float2 yr[K], yi[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) yr[k] = yi[k] = make_float2(0.f, 0.f);
+    // MODE 3: w_e dU[e] of the unit's entries for both atoms (0 past the section's end)
+    float2 dr[K], di[K];
+    if (MODE == 3) {
+        const size_t hb = A.st.h_block[lam] + off0;
+        const float2 *dp = A.dU + (size_t)min(a, A.natoms - 1) * A.nh + hb;
+        const float2 *dq = A.dU + (size_t)min(b, A.natoms - 1) * A.nh + hb;
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const int off = off0 + k;
+            float2 d = make_float2(0.f, 0.f), e = make_float2(0.f, 0.f);
+            if (off < cnt) {
+                d = __ldg(dp + k);
+                e = __ldg(dq + k);
+            }
+            const float w = ((lam & 1) == 0 && off == cnt - 1) ? 0.5f : 1.f;
+            dr[k] = make_float2(w * d.x, w * e.x);
+            di[k] = make_float2(w * d.y, w * e.y);
+        }
+    }
+    int4 sgn = (un.y < un.z) ? __ldg(A.seg + un.y) : make_int4(0, 0, 0, -1);
+    for (int q = un.y; q < un.z; ++q) {
+        const int4 sg = sgn;
+        if (q + 1 < un.z) sgn = __ldg(A.seg + q + 1);
+        float2 zr[K], zi[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) zr[k] = zi[k] = make_float2(0.f, 0.f);
+        int r = sg.x;
+        int4 h1 = (r < sg.y) ? __ldg(A.wsub + r) : make_int4(0, 0, 0, 0);
+        if (K <= ZW_KPAIR) {
+            int4 h2 = (r + 1 < sg.y) ? __ldg(A.wsub + r + 1) : make_int4(0, 0, 0, 0);
+            for (; r + 1 < sg.y; r += 2) {
+                const int4 c1 = h1, c2 = h2;
+                if (r + 2 < sg.y) h1 = __ldg(A.wsub + r + 2);
+                if (r + 3 < sg.y) h2 = __ldg(A.wsub + r + 3);
+                zw2_rows2<K>(Ul, c1, c2, ca, zr, zi);
+            }
+            if (r < sg.y) zw2_rows<K>(Ul, h1, ca, zr, zi);
+        } else {
+            for (; r < sg.y; ++r) {
+                const int4 hd = h1;
+                if (r + 1 < sg.y) h1 = __ldg(A.wsub + r + 1);
+                zw2_rows<K>(Ul, hd, ca, zr, zi);
+            }
+        }
+        if (MODE == 3) {
+            float2 v = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int k = 0; k < K; ++k) v = __ffma2_rn(dr[k], zr[k], __ffma2_rn(di[k], zi[k], v));
+#pragma unroll
+            for (int t = 0; t < 3; ++t) {
+                const int jb = __ldg(A.jbase + 3 * sg.z + t);
+                if (jb < 0) break;
+                const float f = __ldg(A.jfac + 3 * sg.z + t);
+                float *row = A.bc + (size_t)(jb + sg.w) * A.natoms;
+                if (a < A.natoms) row[a] = f * v.x;
+                if (b < A.natoms) row[b] = f * v.y;
+            }
+        }
+        if (MODE == 1 || MODE == 2) {
+            const float2 c = coef[sg.z * ZL_PITCH + lane];
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                yr[k] = __ffma2_rn(c, zr[k], yr[k]);
+                yi[k] = __ffma2_rn(c, zi[k], yi[k]);
+            }
+        }
+        if ((MODE == 0 || MODE == 2) && sg.w >= 0) {
+            const float4 *ul = Ul + (ZW_PAD + A.st.u_block[lam] + off0) * ZL_PITCH;
+            float v = 0.f, w = 0.f;
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                const int off = off0 + k;
+                if (off < cnt) {
+                    const float4 uv = ul[k * ZL_PITCH];
+                    const float d = __fmaf_rn(uv.z, zi[k].x, __fmul_rn(uv.x, zr[k].x));
+                    const float e = __fmaf_rn(uv.w, zi[k].y, __fmul_rn(uv.y, zr[k].y));
+                    const bool half = (lam & 1) == 0 && off == cnt - 1;
+                    v += half ? 0.5f * d : d;
+                    w += half ? 0.5f * e : e;
+                }
+            }
+            float *row = A.bc + (size_t)sg.w * A.natoms;
+            if (a < A.natoms) row[a] = v;
+            if (b < A.natoms) row[b] = w;
+        }
+    }
+    if (MODE == 1 || MODE == 2) {
+        const float un_l = __int_as_float(un.w);
+        const size_t hb = A.st.h_block[lam] + off0;
+        const float *ys = A.yscale + hb;
+        float2 *Ya = A.Y + (size_t)a * A.nh + hb;
+        float2 *Yb = A.Y + (size_t)b * A.nh + hb;
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const int ma = ma0 + k;
+            const float wmid = (2 * mb < lam) ? 1.f : ((2 * ma < lam) ? 1.f : ((2 * ma == lam) ? 0.5f : 0.f));
+            const float s = un_l * wmid * __ldg(ys + k);
+            if (a < A.natoms) Ya[k] = make_float2(s * yr[k].x, s * yi[k].x);
+            if (b < A.natoms) Yb[k] = make_float2(s * yr[k].y, s * yi[k].y);
+        }
+        if (2 * mb == lam && ma0 + K - 1 == lam / 2) {  // the zero upper half of the middle row
+            for (int ma = lam / 2 + 1; ma <= lam; ++ma) {
+                if (a < A.natoms) Ya[ma - ma0] = make_float2(0.f, 0.f);
+                if (b < A.natoms) Yb[ma - ma0] = make_float2(0.f, 0.f);
+            }
+        }
+    }
+}
+
+template <int MODE, int K = ZW_KMAX>
+__device__ __forceinline__ void zw2_unit_k(int k, const ZLArgs &A, const int4 un, const float4 *Ul,
+                                           const float2 *coef, const float *__restrict__ ca, int a, int lane) {
+    if constexpr (K > 1) {
+        if (k != K) {
+            zw2_unit_k<MODE, K - 1>(k, A, un, Ul, coef, ca, a, lane);
+            return;
+        }
+    }
+    zw2_unit<MODE, K>(A, un, Ul, coef, ca, a, lane);
+}
+
+// k_zw32 with two atoms per lane: 64 atoms per CTA of NT threads, one CTA per SM (the
+// two-atom U tiles of twol 8 take 155 KB).  The same work lists, modes and outputs.
+template <int MODE, bool CA_SMEM, int NT>
+__global__ void __launch_bounds__(NT, 1) k_zw64(ZLArgs A) {
+    extern __shared__ __align__(16) float4 zw2_smem[];
+    __shared__ int s_unit;
+    const int lane = threadIdx.x & 31;
+    const int a0 = blockIdx.x * ZW2_ATOMS, a = a0 + lane;
+    float4 *Uq = zw2_smem;
+    const size_t ntile = (size_t)(A.nu + 2 * ZW_PAD) * ZL_PITCH;  // float4
+    float2 *coef = reinterpret_cast<float2 *>(zw2_smem + ntile);  // [nblk][33] pairs, MODE 1 and 2
+    if (threadIdx.x == 0) s_unit = 0;
+    float *ca_s = reinterpret_cast<float *>(zw2_smem) + ((4 * ntile + 2 * (size_t)A.nblk * ZL_PITCH + 3) & ~(size_t)3);
+    const bool staged = (MODE == 1 || MODE == 2) && CA_SMEM && ZW2_ATOMS * A.nB <= A.nwca;
+    const int nca4 = CA_SMEM ? A.nwca / 4 : 0;
+    const float4 *csrc = reinterpret_cast<const float4 *>(A.wca);
+    float4 cr[ZW_CAR];
+#pragma unroll
+    for (int r = 0; r < ZW_CAR; ++r) {
+        const int i = threadIdx.x + r * NT;
+        cr[r] = (i < nca4) ? __ldg(csrc + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    const int nbt = staged ? min(ZW2_ATOMS, A.natoms - a0) * A.nB : 0;
+    const float *bsrc = A.beta + (size_t)a0 * A.nB;
+    float br[ZW_BR];
+#pragma unroll
+    for (int r = 0; r < ZW_BR; ++r) {
+        const int i = threadIdx.x + r * NT;
+        br[r] = (i < nbt) ? __ldg(bsrc + i) : 0.f;
+    }
+    pdl_wait();
+    zw2_load_utot<NT>(A.utot, A.hfull, a0, A.natoms, A.nh, A.nu, Uq);
+    if (MODE == 1 || MODE == 2) {
+        if (staged) {
+#pragma unroll
+            for (int r = 0; r < ZW_BR; ++r) {
+                const int i = threadIdx.x + r * NT;
+                if (i < ZW2_ATOMS * A.nB) ca_s[i] = br[r];
+            }
+            for (int i = threadIdx.x + ZW_BR * NT; i < ZW2_ATOMS * A.nB; i += NT)
+                ca_s[i] = (i < nbt) ? __ldg(bsrc + i) : 0.f;
+            __syncthreads();
+        }
+        // coef[b][lane] = (c of atom a, c of atom a + 32), c = sum over the block's roles
+        // of role_f beta[atom][role_k], in the order of k_zw32
+#pragma unroll 4
+        for (int bk = threadIdx.x >> 5; bk < A.nblk; bk += NT / 32) {
+            const int4 rk = __ldg(A.blk_rk + bk);
+            const float4 rf = __ldg(A.blk_rf + bk);
+            float c[2] = {0.f, 0.f};
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int at = a + 32 * h;
+                if (at < A.natoms) {
+                    if (staged) {
+                        const float *bl = ca_s + (lane + 32 * h) * A.nB;
+                        c[h] = fmaf(rf.x, bl[rk.x], c[h]);
+                        c[h] = fmaf(rf.y, bl[rk.y], c[h]);
+                        c[h] = fmaf(rf.z, bl[rk.z], c[h]);
+                    } else {
+                        const float *bl = A.beta + (size_t)at * A.nB;
+                        c[h] = fmaf(rf.x, __ldg(bl + rk.x), c[h]);
+                        c[h] = fmaf(rf.y, __ldg(bl + rk.y), c[h]);
+                        c[h] = fmaf(rf.z, __ldg(bl + rk.z), c[h]);
+                    }
+                }
+            }
+            coef[bk * ZL_PITCH + lane] = make_float2(c[0], c[1]);
+        }
+        if (staged) __syncthreads();
+    }
+    if (CA_SMEM) {
+        float4 *dst = reinterpret_cast<float4 *>(ca_s);
+#pragma unroll
+        for (int r = 0; r < ZW_CAR; ++r) {
+            const int i = threadIdx.x + r * NT;
+            if (i < nca4) dst[i] = cr[r];
+        }
+        for (int i = threadIdx.x + ZW_CAR * NT; i < nca4; i += NT) dst[i] = __ldg(csrc + i);
+    }
+    const float *ca = CA_SMEM ? ca_s : A.wca;
+    __syncthreads();
+    const float4 *Ul = Uq + lane;
+    for (int u = zl_next(&s_unit); u < A.nunit; u = zl_next(&s_unit)) {
+        const int4 un = __ldg(A.unit + u);
+        zw2_unit_k<MODE>(un.x >> 24, A, un, Ul, coef, ca, a, lane);
+    }
+    pdl_trigger();
+    if (MODE == 1) return;
+    __syncthreads();
+    float *stage = reinterpret_cast<float *>(zw2_smem);
+    if (MODE == 3) {
+        zw_slot_sums_chunked<ZW2_ATOMS, NT>(
+            A.bc, A.jpos, A.nB, A.natoms, a0, stage, A.stage_cap,
+            [&](int k, int l, float acc) { A.x[(size_t)(a0 + l) * A.nB + k] = acc; });
+        return;
+    }
+    float *eb = stage + (size_t)A.nbsec * ZW2_SP;  // [nB][65]
+    zw_slot_sums<ZW_BR, ZW2_ATOMS, NT>(
+        A.bc, A.bpos, A.nB, A.nbsec, A.natoms, a0, stage,
+        [&](int k, int l) { return (MODE == 2) ? __ldg(A.beta + (size_t)(a0 + l) * A.nB + k) : 0.f; },
+        [&](int k, int l, float acc, float bk) {
+            acc *= 2.f;
+            A.x[(size_t)(a0 + l) * A.nB + k] = acc;
+            if (MODE == 2) eb[k * ZW2_SP + l] = acc * bk;
+        });
+    if (MODE != 2 || A.eatom == nullptr) return;
+    __syncthreads();
+    if (threadIdx.x < ZW2_ATOMS && a0 + (int)threadIdx.x < A.natoms) {
+        float e = 0.f;
+        for (int k = 0; k < A.nB; ++k) e += eb[k * ZW2_SP + threadIdx.x];
+        A.eatom[a0 + threadIdx.x] = e;
+    }
+}
+
 struct DArgs {
     so4_params prm;
     float psi_fac, rc32;  // rfac0 pi / rcut and rcut in FP32, set on the host
@@ -504,11 +761,14 @@ struct DArgs {
     const float *rootpq;
     SmallTables st;
     const float2 *Y;
+    const float *yscale;  // n_half: the row scale F by which the window kernels stored Y
     float *g;
 };
 
 // One CTA per centre, warps over its images: U and dU by the recursion, then
-// dE/dr_image = w_j (sfac Re sum conj(dU) Y + dsfac r^ Re sum conj(U) Y).
+// dE/dr_image = w_j (sfac Re sum conj(dU) Y + dsfac r^ Re sum conj(U) Y).  The recursion
+// gives U itself, not the scaled rows the row-chain kernels contract, so Y is taken back
+// from its stored form (times the row scale F) to Y / F.
 __global__ void __launch_bounds__(NWD * 32) k_deidrj(DArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ SmallTables st;
@@ -523,7 +783,10 @@ __global__ void __launch_bounds__(NWD * 32) k_deidrj(DArgs A) {
     cx<float> *dHw = Hw + nh;
     for (int q = tid; q < ldim * ldim; q += NWD * 32) rootpq[q] = A.rootpq[q];
     const float2 *Yg = A.Y + (size_t)a * nh;
-    for (int e = tid; e < nh; e += NWD * 32) Ys[e] = mk<float>(Yg[e].x, Yg[e].y);
+    for (int e = tid; e < nh; e += NWD * 32) {
+        const float f = __ldg(A.yscale + e);
+        Ys[e] = mk<float>(Yg[e].x / f, Yg[e].y / f);
+    }
     __syncthreads();
     const float rc = (float)A.prm.rcut;
     const float psi_fac = (float)(A.prm.rfac0 * SO4_PI / A.prm.rcut);
@@ -1027,29 +1290,21 @@ static ZLArgs zl_args(const so4_tables *t, int natoms) {
     return Z;
 }
 
-// Launch k_zw32<MODE> with the Ca table in shared memory when two CTAs per SM still fit.
-template <int MODE>
-static int launch_zw(const so4_tables *t, const ZLArgs &Z, int natoms, size_t smz, cudaStream_t st) {
-    const size_t with_ca = smz + 16 + sizeof(float) * (size_t)t->n_wca;
-    const int groups = (natoms + 31) / 32;
-    int rc;
-    if (2 * (with_ca + 1024) <= 228 * 1024) {
-        rc = set_smem(k_zw32<MODE, true>, with_ca);
-        if (rc) return rc;
-        return so4_launch_pdl(k_zw32<MODE, true>, dim3(groups), dim3(ZW_THREADS), with_ca, st, Z);
-    }
-    rc = set_smem(k_zw32<MODE, false>, smz);
-    if (rc) return rc;
-    return so4_launch_pdl(k_zw32<MODE, false>, dim3(groups), dim3(ZW_THREADS), smz, st, Z);
+// shared memory of k_zw32 (without the Ca table): padded U tiles and the per-block
+// coefficients; the epilogue stages nslot slot rows (and, in the fused pass, beta B) over
+// the U tiles.  k_zw64: the two-atom tiles (a float4 per entry and lane), coefficient
+// pairs, stage rows of 65 floats.
+static size_t zw_smem_bytes(const so4_tables *t, int nslot, bool with_eb) {
+    const size_t rows = (size_t)(t->n_u + 2 * ZW_PAD) * ZL_PITCH, nst = nslot + (with_eb ? t->n_b : 0);
+    if (t->tune.zw_atoms == ZW2_ATOMS)
+        return std::max(sizeof(float4) * rows, sizeof(float) * nst * ZW2_SP) + sizeof(float2) * (size_t)t->n_blk * ZL_PITCH;
+    return std::max(sizeof(float2) * rows, sizeof(float) * nst * ZL_PITCH) + sizeof(float) * (size_t)t->n_blk * ZL_PITCH;
 }
 
-// shared memory of k_zw32 (without the Ca table): padded U tiles and the per-block
-// coefficients; the epilogue stages its slots over the U tiles
-static size_t zw_smem_bytes(const so4_tables *t, int nslot, bool with_eb) {
-    size_t u = sizeof(float2) * (size_t)(t->n_u + 2 * ZW_PAD) * ZL_PITCH;
-    // the epilogue stages nslot slot rows (and, in the fused pass, beta B) over the U tiles
-    u = std::max(u, sizeof(float) * (size_t)(nslot + (with_eb ? t->n_b : 0)) * ZL_PITCH);
-    return u + sizeof(float) * (size_t)t->n_blk * ZL_PITCH;
+// Slot rows the JVP epilogue stages at a time: those that fit over the padded U tiles.
+static int zw_stage_cap(const so4_tables *t) {
+    const size_t rows = (size_t)(t->n_u + 2 * ZW_PAD) * ZL_PITCH;
+    return (t->tune.zw_atoms == ZW2_ATOMS) ? (int)(4 * rows / ZW2_SP) : (int)(2 * rows / ZL_PITCH);
 }
 
 // Dynamic shared memory the window kernels need in each mode (without the Ca table, which
@@ -1062,8 +1317,45 @@ void so4_zw_smem_modes(const so4_tables *t, size_t out[4]) {
     out[3] = zw_smem_bytes(t, 0, false);  // the JVP stages its slots in chunks over the U tiles
 }
 
-// Slot rows the JVP epilogue stages at a time: those that fit over the padded U tiles.
-static int zw_stage_cap(const so4_tables *t) { return 2 * (t->n_u + 2 * ZW_PAD); }
+// k_zw64 with NT threads, the Ca table in shared memory when the one CTA per SM still
+// fits with it
+template <int MODE, int NT>
+static int launch_zw64(const so4_tables *t, const ZLArgs &Z, int natoms, size_t smz, cudaStream_t st) {
+    const size_t with_ca = smz + 16 + sizeof(float) * (size_t)t->n_wca;
+    const int groups = (natoms + ZW2_ATOMS - 1) / ZW2_ATOMS;
+    int rc;
+    if (with_ca <= 227 * 1024) {
+        rc = set_smem(k_zw64<MODE, true, NT>, with_ca);
+        if (rc) return rc;
+        return so4_launch_pdl(k_zw64<MODE, true, NT>, dim3(groups), dim3(NT), with_ca, st, Z);
+    }
+    rc = set_smem(k_zw64<MODE, false, NT>, smz);
+    if (rc) return rc;
+    return so4_launch_pdl(k_zw64<MODE, false, NT>, dim3(groups), dim3(NT), smz, st, Z);
+}
+
+// Launch the window kernel of the tables' layout: k_zw64 (two atoms per lane) or k_zw32
+// with the Ca table in shared memory when two CTAs per SM still fit.  nslot: the slot
+// rows its epilogue stages; with_eb: and beta B.
+template <int MODE>
+static int launch_zw(const so4_tables *t, const ZLArgs &Z, int natoms, int nslot, bool with_eb, cudaStream_t st) {
+    const size_t smz = zw_smem_bytes(t, nslot, with_eb);
+    if (t->tune.zw_atoms == ZW2_ATOMS) {
+        if (t->tune.zw_threads == 512) return launch_zw64<MODE, 512>(t, Z, natoms, smz, st);
+        return launch_zw64<MODE, 256>(t, Z, natoms, smz, st);
+    }
+    const size_t with_ca = smz + 16 + sizeof(float) * (size_t)t->n_wca;
+    const int groups = (natoms + 31) / 32;
+    int rc;
+    if (2 * (with_ca + 1024) <= 228 * 1024) {
+        rc = set_smem(k_zw32<MODE, true>, with_ca);
+        if (rc) return rc;
+        return so4_launch_pdl(k_zw32<MODE, true>, dim3(groups), dim3(ZW_THREADS), with_ca, st, Z);
+    }
+    rc = set_smem(k_zw32<MODE, false>, smz);
+    if (rc) return rc;
+    return so4_launch_pdl(k_zw32<MODE, false>, dim3(groups), dim3(ZW_THREADS), smz, st, Z);
+}
 
 extern "C" size_t so4_forward32_workspace_size(const so4_tables *t, int natoms) {
     if (!t || natoms < 0) return 0;
@@ -1129,8 +1421,7 @@ extern "C" int so4_forward32(const so4_tables *t, const so4_params *p, int natom
     Z.bpos = t->d_bpos;
     Z.nbsec = t->n_bsec;
     Z.bc = (float *)d_work;
-    const size_t smz = zw_smem_bytes(t, t->n_bsec, false);
-    return launch_zw<0>(t, Z, natoms, smz, st);
+    return launch_zw<0>(t, Z, natoms, t->n_bsec, false, st);
 }
 
 extern "C" size_t so4_adjoint_workspace_size(const so4_tables *t, int natoms, int64_t nimg) {
@@ -1150,8 +1441,7 @@ extern "C" int so4_adjoint_y32(const so4_tables *t, int natoms, const float *d_u
     Z.nunit = t->n_wunit_y;
     Z.beta = d_beta;
     Z.Y = (float2 *)d_y;
-    const size_t smz = zw_smem_bytes(t, 0, false);
-    return launch_zw<1>(t, Z, natoms, smz, (cudaStream_t)stream);
+    return launch_zw<1>(t, Z, natoms, 0, false, (cudaStream_t)stream);
 }
 
 int so4_zw_jvp32(const so4_tables *t, int natoms, const float *d_utot, const float *d_du, float *d_slots, float *d_dB,
@@ -1170,7 +1460,7 @@ int so4_zw_jvp32(const so4_tables *t, int natoms, const float *d_utot, const flo
     Z.stage_cap = zw_stage_cap(t);
     if (t->n_jmax > Z.stage_cap) return SO4_ERR_UNSUPPORTED;  // a component's slots must fit one chunk
     Z.x = d_dB;
-    return launch_zw<3>(t, Z, natoms, zw_smem_bytes(t, 0, false), stream);
+    return launch_zw<3>(t, Z, natoms, 0, false, stream);
 }
 
 extern "C" int so4_adjoint_deidrj32(const so4_tables *t, const so4_params *p, int natoms, const double *d_w_nb,
@@ -1193,6 +1483,7 @@ extern "C" int so4_adjoint_deidrj32(const so4_tables *t, const so4_params *p, in
     D.psi_fac = (float)(p->rfac0 * SO4_PI / p->rcut);
     D.rc32 = (float)p->rcut;
     D.Y = (const float2 *)d_y;
+    D.yscale = t->d_yscale;
     D.g = d_g;
     cudaStream_t st = (cudaStream_t)stream;
     int rc = SO4_OK;
@@ -1424,8 +1715,7 @@ extern "C" int so4_linear_by32(const so4_tables *t, int natoms, const float *d_u
     Z.nbsec = t->n_bsec;
     Z.bc = d_bc;
     Z.eatom = d_eatom;
-    const size_t smz = zw_smem_bytes(t, t->n_bsec, true);
-    return launch_zw<2>(t, Z, natoms, smz, (cudaStream_t)stream);
+    return launch_zw<2>(t, Z, natoms, t->n_bsec, true, (cudaStream_t)stream);
 }
 
 extern "C" int so4_adjoint_linear32(const so4_tables *t, const so4_params *p, int nstruct, const int *d_atom_struct,

@@ -116,6 +116,10 @@ void free_device(so4_tables *t) {
 
 // Default layout of the per-image pass at twol 6 and 8 (1: two lanes per image).
 #define REV_PAIR_DEFAULT 1
+// Default atoms per CTA of the window Z pass up to twol 8 (32 or 64), and threads per
+// CTA of the 64-atom pass (256 or 512).
+#define ZW_ATOMS_DEFAULT 64
+#define ZW_THREADS_DEFAULT 512
 
 // The defaults of so4_tuning for one twol, and whether a requested tuning is built.
 static so4_tuning tuning_defaults(int twol) {
@@ -124,6 +128,8 @@ static so4_tuning tuning_defaults(int twol) {
     d.rev_threads = (twol <= 8) ? 256 : 128;
     d.utot_warps = 4;
     d.rev_pair = (twol == 6 || twol == 8) ? REV_PAIR_DEFAULT : 2;
+    d.zw_atoms = (twol <= 8) ? ZW_ATOMS_DEFAULT : 32;
+    d.zw_threads = ZW_THREADS_DEFAULT;
     return d;
 }
 
@@ -131,7 +137,7 @@ static int tuning_resolve(int twol, const so4_tuning *req, so4_tuning &out) {
     out = tuning_defaults(twol);
     if (!req) return SO4_OK;
     if (req->wkmax < 0 || req->wkmax > ZW_KMAX || req->rev_threads < 0 || req->utot_warps < 0) return SO4_ERR_ARG;
-    if (req->rev_pair < 0 || req->rev_pair > 2) return SO4_ERR_ARG;
+    if (req->rev_pair < 0 || req->rev_pair > 2 || req->zw_atoms < 0 || req->zw_threads < 0) return SO4_ERR_ARG;
     if (req->rev_threads && req->rev_threads != 128 && req->rev_threads != 256) return SO4_ERR_ARG;
     if (req->utot_warps && req->utot_warps != 2 && req->utot_warps != 4 && req->utot_warps != 8) return SO4_ERR_ARG;
     if (req->wkmax) out.wkmax = req->wkmax;
@@ -148,6 +154,13 @@ static int tuning_resolve(int twol, const so4_tuning *req, so4_tuning &out) {
         if (!shapes) return SO4_ERR_UNSUPPORTED;
         out.rev_pair = req->rev_pair;
     }
+    if (req->zw_atoms && req->zw_atoms != 32 && req->zw_atoms != 64) return SO4_ERR_ARG;
+    if (req->zw_threads && req->zw_threads != 256 && req->zw_threads != 512) return SO4_ERR_ARG;
+    if (req->zw_atoms) {
+        if (req->zw_atoms == 64 && twol > 8) return SO4_ERR_UNSUPPORTED;  // the tiles exceed shared memory
+        out.zw_atoms = req->zw_atoms;
+    }
+    if (req->zw_threads) out.zw_threads = req->zw_threads;
     return SO4_OK;
 }
 
@@ -692,9 +705,10 @@ extern "C" int so4_tables_create_tuned(int twol, int normalize_u, const so4_tuni
     if (!rc) rc = upload(&t->d_yblk_ptr, yptr);
     if (!rc) rc = upload(&t->d_yblk, ylist);
     // a unit cap below the default means more units and so more B / JVP slots, which the
-    // window kernels stage in shared memory: refuse a tuning whose window kernels would not
-    // run in every mode where the default ones do
-    if (!rc && t->tune.wkmax != ZW_KMAX) {
+    // window kernels stage in shared memory, and the other window layout has other tiles:
+    // refuse a tuning whose window kernels would not run in every mode where the default
+    // ones do
+    if (!rc && (t->tune.wkmax != ZW_KMAX || t->tune.zw_atoms != tuning_defaults(twol).zw_atoms)) {
         size_t mt[4], md[4];
         so4_zw_smem_modes(t, mt);
         if (std::max(std::max(mt[0], mt[1]), std::max(mt[2], mt[3])) > 227 * 1024) {

@@ -63,49 +63,50 @@ __device__ __forceinline__ void zw_load_utot(const float2 *__restrict__ utot, co
 }
 
 // Per-atom sums of scratch slots: the sum of slots [pos[k], pos[k + 1]) of the slot-major
-// scratch sc[q * natoms + a0 + lane], for every k < ncomp and every lane with a0 + lane <
-// natoms, handed to f(k, lane, sum, pre(k, lane)).  The CTA copies its nslot x 32 values
-// into shared memory (stage: nslot x ZL_PITCH floats) with independent loads, issued
-// together with pre() of the thread's first NPRE (k, lane) pairs, then sums from there
-// in slot order.
+// scratch sc[q * natoms + a0 + l], for every k < ncomp and every l < NA with a0 + l <
+// natoms, handed to f(k, l, sum, pre(k, l)).  The CTA (NT threads, NA atoms) copies its
+// nslot x NA values into shared memory (stage: nslot x (NA + 1) floats) with independent
+// loads, issued together with pre() of the thread's first NPRE (k, l) pairs, then sums from
+// there in slot order.
 constexpr int ZW_SLD = 24;
-template <int NPRE, typename P, typename F>
+template <int NPRE, int NA = 32, int NT = ZW_THREADS, typename P, typename F>
 __device__ __forceinline__ void zw_slot_sums(const float *sc, const int *__restrict__ pos, int ncomp, int nslot,
                                              int natoms, int a0, float *stage, P pre, F f) {
-    const int nl = min(32, natoms - a0);
+    constexpr int SP = NA + 1;
+    const int nl = min(NA, natoms - a0);
     float pv[NPRE];
 #pragma unroll
     for (int r = 0; r < NPRE; ++r) {
-        const int idx = threadIdx.x + r * ZW_THREADS, k = idx >> 5, l = idx & 31;
-        pv[r] = (idx < 32 * ncomp && l < nl) ? pre(k, l) : 0.f;
+        const int idx = threadIdx.x + r * NT, k = idx / NA, l = idx % NA;
+        pv[r] = (idx < NA * ncomp && l < nl) ? pre(k, l) : 0.f;
     }
-    for (int i0 = threadIdx.x; i0 < 32 * nslot; i0 += ZW_SLD * ZW_THREADS) {
+    for (int i0 = threadIdx.x; i0 < NA * nslot; i0 += ZW_SLD * NT) {
         float v[ZW_SLD];
 #pragma unroll
         for (int r = 0; r < ZW_SLD; ++r) {
-            const int i = i0 + r * ZW_THREADS, q = i >> 5, l = i & 31;
-            v[r] = (i < 32 * nslot && l < nl) ? sc[(size_t)q * natoms + a0 + l] : 0.f;
+            const int i = i0 + r * NT, q = i / NA, l = i % NA;
+            v[r] = (i < NA * nslot && l < nl) ? sc[(size_t)q * natoms + a0 + l] : 0.f;
         }
 #pragma unroll
         for (int r = 0; r < ZW_SLD; ++r) {
-            const int i = i0 + r * ZW_THREADS;
-            if (i < 32 * nslot) stage[(i >> 5) * ZL_PITCH + (i & 31)] = v[r];
+            const int i = i0 + r * NT;
+            if (i < NA * nslot) stage[(i / NA) * SP + (i % NA)] = v[r];
         }
     }
     __syncthreads();
     auto sum = [&](int k, int l) {
         float acc = 0.f;
         const int q1 = __ldg(pos + k + 1);
-        for (int q = __ldg(pos + k); q < q1; ++q) acc += stage[q * ZL_PITCH + l];
+        for (int q = __ldg(pos + k); q < q1; ++q) acc += stage[q * SP + l];
         return acc;
     };
 #pragma unroll
     for (int r = 0; r < NPRE; ++r) {
-        const int idx = threadIdx.x + r * ZW_THREADS, k = idx >> 5, l = idx & 31;
-        if (idx < 32 * ncomp && l < nl) f(k, l, sum(k, l), pv[r]);
+        const int idx = threadIdx.x + r * NT, k = idx / NA, l = idx % NA;
+        if (idx < NA * ncomp && l < nl) f(k, l, sum(k, l), pv[r]);
     }
-    for (int idx = threadIdx.x + NPRE * ZW_THREADS; idx < 32 * ncomp; idx += ZW_THREADS) {
-        const int k = idx >> 5, l = idx & 31;
+    for (int idx = threadIdx.x + NPRE * NT; idx < NA * ncomp; idx += NT) {
+        const int k = idx / NA, l = idx % NA;
         if (l < nl) f(k, l, sum(k, l), pre(k, l));
     }
 }
@@ -113,11 +114,12 @@ __device__ __forceinline__ void zw_slot_sums(const float *sc, const int *__restr
 // zw_slot_sums without its single staging pass: components are taken in chunks whose slots
 // (at most `cap` of them, the slot rows that fit in `stage`) are staged together, summed,
 // and the stage reused for the next chunk.  Every component owns at most cap slots (the
-// host checks it).  f(k, lane, sum) for every k < ncomp and lane with a0 + lane < natoms.
-template <typename F>
+// host checks it).  f(k, l, sum) for every k < ncomp and l < NA with a0 + l < natoms.
+template <int NA = 32, int NT = ZW_THREADS, typename F>
 __device__ __forceinline__ void zw_slot_sums_chunked(const float *sc, const int *__restrict__ pos, int ncomp,
                                                      int natoms, int a0, float *stage, int cap, F f) {
-    const int nl = min(32, natoms - a0);
+    constexpr int SP = NA + 1;
+    const int nl = min(NA, natoms - a0);
     int k0 = 0;
     while (k0 < ncomp) {
         // the chunk [k0, k1): as many whole components as fit (the same k1 in every thread)
@@ -125,26 +127,26 @@ __device__ __forceinline__ void zw_slot_sums_chunked(const float *sc, const int 
         int k1 = k0 + 1;
         while (k1 < ncomp && __ldg(pos + k1 + 1) - q0 <= cap) ++k1;
         const int nq = __ldg(pos + k1) - q0;
-        for (int i0 = threadIdx.x; i0 < 32 * nq; i0 += ZW_SLD * ZW_THREADS) {
+        for (int i0 = threadIdx.x; i0 < NA * nq; i0 += ZW_SLD * NT) {
             float v[ZW_SLD];
 #pragma unroll
             for (int r = 0; r < ZW_SLD; ++r) {
-                const int i = i0 + r * ZW_THREADS, q = i >> 5, l = i & 31;
-                v[r] = (i < 32 * nq && l < nl) ? sc[(size_t)(q0 + q) * natoms + a0 + l] : 0.f;
+                const int i = i0 + r * NT, q = i / NA, l = i % NA;
+                v[r] = (i < NA * nq && l < nl) ? sc[(size_t)(q0 + q) * natoms + a0 + l] : 0.f;
             }
 #pragma unroll
             for (int r = 0; r < ZW_SLD; ++r) {
-                const int i = i0 + r * ZW_THREADS;
-                if (i < 32 * nq) stage[(i >> 5) * ZL_PITCH + (i & 31)] = v[r];
+                const int i = i0 + r * NT;
+                if (i < NA * nq) stage[(i / NA) * SP + (i % NA)] = v[r];
             }
         }
         __syncthreads();
-        for (int idx = threadIdx.x; idx < 32 * (k1 - k0); idx += ZW_THREADS) {
-            const int k = k0 + (idx >> 5), l = idx & 31;
+        for (int idx = threadIdx.x; idx < NA * (k1 - k0); idx += NT) {
+            const int k = k0 + idx / NA, l = idx % NA;
             if (l < nl) {
                 float acc = 0.f;
                 const int qa = __ldg(pos + k) - q0, qb = __ldg(pos + k + 1) - q0;
-                for (int q = qa; q < qb; ++q) acc += stage[q * ZL_PITCH + l];
+                for (int q = qa; q < qb; ++q) acc += stage[q * SP + l];
                 f(k, l, acc);
             }
         }

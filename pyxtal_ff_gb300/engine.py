@@ -44,15 +44,15 @@ class Tables:
         if tuning is None:
             check(lib().so4_tables_create(int(twol), int(bool(normalize_u)), C.byref(h)), "so4_tables_create")
         else:
-            t4 = tuple(tuning) + (0,) * (4 - len(tuning))
-            tn = Tuning(int(t4[0]), int(t4[1]), int(t4[2]), int(t4[3]))
+            t6 = tuple(tuning) + (0,) * (6 - len(tuning))
+            tn = Tuning(*(int(v) for v in t6[:6]))
             check(lib().so4_tables_create_tuned(int(twol), int(bool(normalize_u)), C.byref(tn), C.byref(h)),
                   "so4_tables_create_tuned")
         self.handle = h
         tn = Tuning()
         check(lib().so4_tables_get_tuning(h, C.byref(tn)), "so4_tables_get_tuning")
-        # (wkmax, rev_threads, utot_warps, rev_pair), resolved
-        self.tuning = (tn.wkmax, tn.rev_threads, tn.utot_warps, tn.rev_pair)
+        # (wkmax, rev_threads, utot_warps, rev_pair, zw_atoms, zw_threads), resolved
+        self.tuning = (tn.wkmax, tn.rev_threads, tn.utot_warps, tn.rev_pair, tn.zw_atoms, tn.zw_threads)
         s = (C.c_int * 8)()
         check(lib().so4_tables_sizes(h, s), "so4_tables_sizes")
         self.twol = int(twol)

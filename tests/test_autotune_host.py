@@ -68,6 +68,8 @@ def test_search_space_by_twol_and_step_kind():
     s8, s4 = T.search_space(8), T.search_space(4)
     assert s8["rev_threads"] == (256, 128) and s8["utot_warps"] == (4, 2, 8) and s8["rev_pair"] == (0, 1, 2)
     assert s4["rev_threads"] == (0,) and s4["utot_warps"] == (4,) and s4["rev_pair"] == (0,)
+    assert s8["zw_atoms"] == (32, 64) and s8["zw_threads"] == (256, 512)
+    assert T.search_space(10)["zw_atoms"] == (0,)  # the 64-atom tiles exceed shared memory above twol 8
     m = T.search_space(6, linear=False)
     assert m["branches"] == (1,) and m["pdl"] == (False,)
     assert T.default_choice(8, linear=False).branches == 1
@@ -104,7 +106,8 @@ def test_workload_key_classes():
 def test_choice_dict_round_trip_and_kernel_tuning():
     ch = T.Choice(wkmax=4, rev_threads=128, utot_warps=8, branches=1, pdl=True, rev_pair=1)
     assert T.Choice.from_dict(ch.as_dict()) == ch
-    assert ch.kernel_tuning() == (4, 128, 8, 1)
+    assert ch.kernel_tuning() == (4, 128, 8, 1, 0, 0)
+    assert T.Choice(zw_atoms=64, zw_threads=512).kernel_tuning()[4:] == (64, 512)
     # a cached choice written before a knob existed reads back with that knob's default
     old = {"wkmax": 4, "rev_threads": 128, "utot_warps": 8, "branches": 1, "pdl": True}
     assert T.Choice.from_dict(old).rev_pair == 0

@@ -39,9 +39,9 @@ def test_tuned_tables_validate_their_arguments(cuda_device):
     for unsupported in [(0, 128, 0), (0, 0, 8)]:
         assert L.so4_tables_create_tuned(4, 0, C.byref(_lib.Tuning(*unsupported)), C.byref(h)) == \
             _lib.SO4_ERR_UNSUPPORTED
-    assert engine.Tables(8, False, (3, 128, 2, 1)).tuning == (3, 128, 2, 1)
+    assert engine.Tables(8, False, (3, 128, 2, 1)).tuning[:4] == (3, 128, 2, 1)
     assert engine.Tables(8, False, None).tuning[:3] == (5, 256, 4)
-    assert engine.Tables(10, False, (4, 0, 0)).tuning == (4, 128, 4, 2)
+    assert engine.Tables(10, False, (4, 0, 0)).tuning == (4, 128, 4, 2, 32, 512)
     assert L.so4_tables_create_tuned(8, 0, C.byref(_lib.Tuning(0, 0, 0, 3)), C.byref(h)) == _lib.SO4_ERR_ARG
     assert L.so4_tables_create_tuned(4, 0, C.byref(_lib.Tuning(0, 0, 0, 1)), C.byref(h)) == _lib.SO4_ERR_UNSUPPORTED
 

@@ -1,0 +1,126 @@
+"""The window Z pass with two atoms per lane (k_zw64) against the one-atom kernel (k_zw32).
+
+Per atom both layouts perform the same products and sums in the same order, so every
+output that goes through the window pass is bitwise equal:
+- B and U_tot of so4_forward32 (window mode 0);
+- forces and virial of so4_adjoint32 (mode 1, the Y build, then the per-image pass);
+- B, forces, virial and energy of the fused so4_adjoint_linear32 (mode 2);
+- the JVP dB of so4_jvp32 (mode 3; built for even twol).
+Batches are ragged so that the last 64-atom CTA is partly empty (63, 64, 65, 240 atoms,
+several structures), at twol 3 to 8, with 256 and 512 threads per CTA.  Creation refuses
+the 64-atom layout above twol 8 (its tiles exceed shared memory) and values other than
+32 / 64 atoms and 256 / 512 threads.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+import torch
+
+from pyxtal_ff_gb300 import _lib, autotune, engine, ops
+from pyxtal_ff_gb300 import structures as S
+
+pytestmark = pytest.mark.gpu
+W = {"Si": 1.0, "O": 0.5}
+
+
+def _batches():
+    return {
+        63: [S.sio2_random(n_si=21, seed=3)],
+        64: [S.diamond_si(2, 2, 2, sigma=0.1, rng=np.random.default_rng(5))],
+        65: [S.diamond_si(2, 2, 1, sigma=0.1, rng=np.random.default_rng(6)), S.sio2_random(n_si=11, seed=7)],
+        240: [S.diamond_si(3, 3, 3, sigma=0.1, rng=np.random.default_rng(8)), S.sio2_random(n_si=8, seed=9)],
+    }
+
+
+def _ctx(structs, twol, choice):
+    pos = np.concatenate([s.positions for s in structs])
+    cells = np.stack([s.get_cell() for s in structs])
+    ptr = np.concatenate([[0], np.cumsum([len(s) for s in structs])])
+    numbers = np.concatenate([s.numbers for s in structs])
+    symbols = sum([list(s.symbols) for s in structs], [])
+    return ops.Context.build(torch.from_numpy(pos).cuda(), cells, np.ones((len(structs), 3), np.int32), ptr, numbers,
+                             symbols, lmax=twol / 2, rcut=4.7, kind="SNAP", weights=W, tuning=choice)
+
+
+def _outputs(structs, twol, choice):
+    ctx = _ctx(structs, twol, choice)
+    n = ctx.nb.natoms
+    x, utot = engine.forward32(ctx.tab, ctx.prm, ctx.nb, ctx.w_nb, ctx.w_site)
+    rng = np.random.default_rng(twol)
+    beta = torch.from_numpy(rng.normal(0, 0.01, size=(n, ctx.tab.nB))).float().cuda()
+    f, vir = engine.adjoint32(ctx.tab, ctx.prm, ctx.nb, ctx.w_nb, utot, beta)
+    xl, fl, vl, el = engine.adjoint_linear32(ctx.tab, ctx.prm, ctx.nb, ctx.w_nb, ctx.w_site, beta)
+    out = {"x": x, "utot": utot, "f": f, "vir": vir, "xl": xl, "fl": fl, "vl": vl, "el": el}
+    if twol % 2 == 0:  # the JVP is built for even twol
+        v = torch.from_numpy(rng.normal(size=(n, 3))).cuda()
+        G = torch.from_numpy(rng.normal(size=(len(structs), 3, 3)) * 0.01).cuda()
+        out["dB"] = engine.jvp32(ctx.tab, ctx.prm, ctx.nb, ctx.w_nb, utot, v=v, G=G)
+    torch.cuda.synchronize()
+    return ctx.tab.tuning, out
+
+
+@pytest.mark.parametrize("twol", [3, 4, 7, 8])
+@pytest.mark.parametrize("natoms", [63, 64, 65, 240])
+def test_two_atom_window_pass_is_bitwise_equal(cuda_device, twol, natoms):
+    structs = _batches()[natoms]
+    t32, ref = _outputs(structs, twol, autotune.Choice(zw_atoms=32))
+    assert t32[4] == 32
+    for nt in (256, 512):
+        t64, got = _outputs(structs, twol, autotune.Choice(zw_atoms=64, zw_threads=nt))
+        assert t64[4:] == (64, nt)
+        for k, a in ref.items():
+            assert a.shape == got[k].shape
+            assert torch.equal(a, got[k]), "%s differs (twol %d, %d atoms, %d threads)" % (k, twol, natoms, nt)
+        assert torch.isfinite(got["fl"]).all() and got["x"].abs().sum() > 0
+
+
+def test_two_atom_layout_creation_rules(cuda_device):
+    L = _lib.lib()
+    h = C.c_void_p()
+    assert L.so4_tables_create_tuned(10, 0, C.byref(_lib.Tuning(0, 0, 0, 0, 64, 0)), C.byref(h)) == \
+        _lib.SO4_ERR_UNSUPPORTED
+    for bad in [(0, 0, 0, 0, 48, 0), (0, 0, 0, 0, 64, 384), (0, 0, 0, 0, -1, 0)]:
+        assert L.so4_tables_create_tuned(8, 0, C.byref(_lib.Tuning(*bad)), C.byref(h)) == _lib.SO4_ERR_ARG
+    assert engine.Tables(8, False, (0, 0, 0, 0, 64, 512)).tuning[4:] == (64, 512)
+    assert engine.Tables(10, False, None).tuning[4] == 32
+    assert engine.Tables(8, False, None).tuning[4:] == (64, 512)
+
+
+@pytest.mark.parametrize("twol", [3, 5, 8])
+@pytest.mark.parametrize("zw_atoms", [32, 64])
+def test_y_is_defined_everywhere_and_forces_ignore_scratch(cuda_device, twol, zw_atoms):
+    # Y of so4_adjoint_y32 covers every half-layout entry (the upper half of an even
+    # level's middle row as zeros), so neither a caller of Y nor the per-image pass (the
+    # generic per-centre kernel at odd twol reads every entry) sees uninitialised memory:
+    # the forces are the same bits whatever the workspace held, and match the oracle (at odd
+    # twol the generic kernel takes Y back from its stored, row-scaled form)
+    from oracle import oracle as O
+    from tests import goldens as G
+    structs = _batches()[65]
+    ctx = _ctx(structs, twol, autotune.Choice(zw_atoms=zw_atoms))
+    n = ctx.nb.natoms
+    L = _lib.lib()
+    x, utot = engine.forward32(ctx.tab, ctx.prm, ctx.nb, ctx.w_nb, ctx.w_site)
+    beta_np = np.random.default_rng(11).normal(0, 0.01, size=(n, ctx.tab.nB))
+    beta = torch.from_numpy(beta_np).float().cuda()
+    y = torch.full((n, ctx.tab.n_half, 2), float("nan"), dtype=torch.float32, device="cuda")
+    engine.check(L.so4_adjoint_y32(ctx.tab.handle, n, engine._ptr(utot), engine._ptr(beta), engine._ptr(y),
+                                   engine._stream()), "so4_adjoint_y32")
+    assert not torch.isnan(y).any()
+    need = L.so4_adjoint_workspace_size(ctx.tab.handle, n, ctx.nb.nimg)
+    got = []
+    for fill in (0, 0xFF, 0x3F):
+        ws = torch.full((need,), fill, dtype=torch.uint8, device="cuda")
+        f, vir = engine.adjoint32(ctx.tab, ctx.prm, ctx.nb, ctx.w_nb, utot, beta, workspace=ws)
+        got.append((f.clone(), vir.clone()))
+    for f, vir in got[1:]:
+        assert torch.equal(f, got[0][0]) and torch.equal(vir, got[0][1])
+    f, vir = got[0][0].cpu().numpy(), got[0][1].cpu().numpy()
+    ptr = np.concatenate([[0], np.cumsum([len(s) for s in structs])])
+    for s, st in enumerate(structs):
+        a0, a1 = ptr[s], ptr[s + 1]
+        ref = O.forces_virial(st, beta_np[a0:a1], kind="SNAP", lmax=twol / 2, rcut=4.7, weights=W, rfac0=0.99363)
+        assert G.rel_err(x[a0:a1].cpu().numpy(), ref["x"]) < 2e-5
+        assert G.rel_err(f[a0:a1], ref["forces"]) < 2e-4
+        assert G.rel_err(vir[s] / ctx.nb.vol[s], ref["virial"]) < 2e-4
