@@ -11,6 +11,7 @@
 #include <string>
 #include <algorithm>
 #include <map>
+#include <queue>
 #include <tuple>
 #include <utility>
 
@@ -526,16 +527,51 @@ extern "C" int so4_tables_create_tuned(int twol, int normalize_u, const so4_tuni
             }
         }
     }
-    // order: by K (largest first), so the warps of a CTA, which take units in list order,
-    // mostly run the same K specialisation at a time (fewer instruction-cache misses);
-    // within one K, most expensive first
     auto by_k_cost = [&](const std::pair<long, int> &x, const std::pair<long, int> &y) {
         const int kx = wun[x.second].nk, ky = wun[y.second].nk;
         if (kx != ky) return kx > ky;
         return x.first < y.first;
     };
-    std::stable_sort(wcy.begin(), wcy.end(), by_k_cost);
-    std::stable_sort(wcb.begin(), wcb.end(), by_k_cost);
+    // The warps of a CTA take units in list order, each the next one when it is free, and
+    // the CTA ends with its last warp.  Units are grouped by K (largest first: the warps of
+    // a CTA mostly run one K specialisation at a time, so fewer instruction-cache misses),
+    // most expensive first within a K; then swaps of two units of the same K that make the
+    // simulated finish time, by the cost model, earlier for the layout's warps per CTA.
+    const int zwarps = (t->tune.zw_atoms == 64 ? t->tune.zw_threads : 256) / 32;
+    auto order_units = [&](std::vector<std::pair<long, int>> &wc) {
+        auto finish = [&](const std::vector<std::pair<long, int>> &v) {
+            std::priority_queue<long, std::vector<long>, std::greater<long>> free_at;
+            for (int w = 0; w < zwarps; ++w) free_at.push(0);
+            long end = 0;
+            for (auto &e : v) {
+                const long t0 = free_at.top();
+                free_at.pop();
+                free_at.push(t0 - e.first);  // e.first = -cost
+                end = std::max(end, t0 - e.first);
+            }
+            return end;
+        };
+        std::stable_sort(wc.begin(), wc.end(), by_k_cost);
+        long best = finish(wc);
+        for (int pass = 0; pass < 3; ++pass) {
+            bool better = false;
+            for (size_t i = 0; i < wc.size(); ++i)
+                for (size_t j = i + 1; j < wc.size(); ++j) {
+                    if (wc[i].first == wc[j].first || wun[wc[i].second].nk != wun[wc[j].second].nk) continue;
+                    std::swap(wc[i], wc[j]);
+                    const long f = finish(wc);
+                    if (f < best) {
+                        best = f;
+                        better = true;
+                    } else {
+                        std::swap(wc[i], wc[j]);
+                    }
+                }
+            if (!better) break;
+        }
+    };
+    order_units(wcy);
+    order_units(wcb);
     for (int pass = 0; pass < 2; ++pass) {
         auto &order = pass ? wcb : wcy;
         auto &units = pass ? wunit_b : wunit_y;
@@ -589,7 +625,7 @@ extern "C" int so4_tables_create_tuned(int twol, int normalize_u, const so4_tuni
             if (blks[segy_all[q].z].nrole > 0) c += segy_cost[q];
         wcj.push_back({-c, ui});
     }
-    std::stable_sort(wcj.begin(), wcj.end(), by_k_cost);
+    order_units(wcj);
     std::vector<int4> wunit_j, wseg_j;
     std::vector<int> jwrites(jpos[t->n_b], 0);
     for (auto &v : wcj) {
