@@ -94,22 +94,22 @@ __global__ void __launch_bounds__(NWF * 32) k_utot32(FwdArgs A) {
     for (int e = tid; e < nh; e += NWF * 32) ug[e] = make_float2(Uh[e].re, Uh[e].im);
 }
 
-// U_tot with the row-chain recursion: one warp per centre, RowChain<TWOL>::IPW
-// images per round.  Each lane accumulates w_j sfac U over its images for its
-// chain's rows; the image groups are then added through shared memory in group
-// order, the self term f_c(0) w_site is put on the diagonal and u_norm applied
-// (SO4.py:1480-1505, 560-597).
+// U_tot with the row-chain recursion: one warp per centre, UtotLanes<TWOL>::IPW
+// images per round (lanes per image: one per row chain; at twol 8 the last lane runs the
+// last two chains).  Each lane accumulates w_j sfac U over its images for its chain's rows;
+// the image groups are then added through shared memory in group order, the self term
+// f_c(0) w_site is put on the diagonal and u_norm applied (SO4.py:1480-1505, 560-597).
 template <int TWOL, int NW>
 __global__ void __launch_bounds__(NW * 32, (TWOL <= 8) ? 16 / NW : 1) k_utot_rc(FwdArgs A) {
-    using RC = RowChain<TWOL>;
+    using UL = UtotLanes<TWOL>;
     constexpr int W = TWOL + 1, NACC = acc_block(TWOL + 1);
     extern __shared__ __align__(16) float ut_smem[];  // [NW][32][2 * NACC]
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int a = blockIdx.x * NW + wid;
-    const int grp = lane / RC::NCH, mb = lane - grp * RC::NCH;
-    float accr[NACC], acci[NACC];
+    const int grp = lane / UL::LPI, mb = lane - grp * UL::LPI;
+    float2 acc[NACC];
 #pragma unroll
-    for (int q = 0; q < NACC; ++q) accr[q] = acci[q] = 0.f;
+    for (int q = 0; q < NACC; ++q) acc[q] = make_float2(0.f, 0.f);
     pdl_wait();  // the neighbour list comes from the kernel before
     if (a < A.natoms) {
         const int m0 = A.img_ptr[a], m1 = A.img_ptr[a + 1];
@@ -139,10 +139,10 @@ __global__ void __launch_bounds__(NW * 32, (TWOL <= 8) ? 16 / NW : 1) k_utot_rc(
                 make_ck<float, false>(x, y, z, r, A.psi_fac * r, ck0);
             }
             const int nimg = min(32, m1 - base);
-            for (int sub = 0; sub < nimg; sub += RC::IPW) {
+            for (int sub = 0; sub < nimg; sub += UL::IPW) {
                 // lane (grp, mb) takes image sub + grp; lanes past the images take a zero weight
                 const int src = sub + grp;
-                const bool ok = grp < RC::IPW && src < nimg;
+                const bool ok = grp < UL::IPW && src < nimg;
                 const int sl = ok ? src : 0;
                 CK<float> ck;
                 ck.ca.re = __shfl_sync(0xffffffffu, ck0.ca.re, sl);
@@ -151,22 +151,19 @@ __global__ void __launch_bounds__(NW * 32, (TWOL <= 8) ? 16 / NW : 1) k_utot_rc(
                 ck.cb.im = __shfl_sync(0xffffffffu, ck0.cb.im, sl);
                 float wsf = __shfl_sync(0xffffffffu, wsf0, sl);
                 if (!ok) wsf = 0.f;
-                float ur[W], ui[W], dr[3][W], di[3][W];
+                float2 u[W];
 #pragma unroll
-                for (int q = 0; q < W; ++q) ur[q] = ui[q] = 0.f;
-                ur[0] = 1.f;
-                if (mb == 0) accr[0] += wsf;
-                RcUtot<TWOL, 1>::run(mb, ck, wsf, ur, ui, dr, di, accr, acci);
+                for (int q = 0; q < W; ++q) u[q] = make_float2(0.f, 0.f);
+                u[0].x = 1.f;
+                if (mb == 0) acc[0].x += wsf;
+                RcUtot2<TWOL, 1>::run(mb, ck, wsf, u, acc);
             }
         }
     }
     pdl_trigger();  // the next kernel may start its set-up during this epilogue
-    float *sw = ut_smem + (size_t)wid * 32 * 2 * NACC;
+    float2 *sw = reinterpret_cast<float2 *>(ut_smem) + (size_t)wid * 32 * NACC;
 #pragma unroll
-    for (int q = 0; q < NACC; ++q) {
-        sw[lane * 2 * NACC + 2 * q] = accr[q];
-        sw[lane * 2 * NACC + 2 * q + 1] = acci[q];
-    }
+    for (int q = 0; q < NACC; ++q) sw[lane * NACC + q] = acc[q];
     __syncwarp();
     if (a >= A.natoms) return;
     float f0, df0;
@@ -176,12 +173,13 @@ __global__ void __launch_bounds__(NW * 32, (TWOL <= 8) ? 16 / NW : 1) k_utot_rc(
     for (int e = lane; e < A.nh; e += 32) {
         const int4 h = __ldg(A.hmap + e);
         const int slot = h.x & 0xff, row = (h.x >> 8) & 0x7f;
+        const int ln = UL::lane_of(row), sq = UL::slot_of(row, slot);
         float sr = 0.f, si = 0.f;
 #pragma unroll
-        for (int g = 0; g < RC::IPW; ++g) {
-            const float *src = sw + (g * RC::NCH + row) * 2 * NACC + 2 * slot;
-            sr += src[0];
-            si += src[1];
+        for (int g = 0; g < UL::IPW; ++g) {
+            const float2 v = sw[(g * UL::LPI + ln) * NACC + sq];
+            sr += v.x;
+            si += v.y;
         }
         // sums of scaled rows: times u_norm F; the self term (diagonal) times u_norm
         const float unf = __int_as_float(h.y), un = __int_as_float(h.z);

@@ -209,6 +209,111 @@ struct RcUtot<TWOL, TWOL + 1> {
                                                float (&)[acc_block(TWOL + 1)], float (&)[acc_block(TWOL + 1)]) {}
 };
 
+// ---------------------------------------------------------------------------
+// U_tot (no derivatives), rows as (re, im) pairs so that the weighted accumulation is one
+// packed FMA per entry; the recursion and the chain start are rc_level / rc_start's own
+// operations on the pair's halves.
+//
+// Lanes per image: one per row chain, except at TWOL 8, where the last lane of an image
+// runs chains 3 and 4 (UtotLanes::LPI = 4, eight images per pass instead of six): chain 4
+// exists at level 8 only and starts from chain 3's row of level 7, which that lane holds.
+// Its accumulators take chain 4's level-8 row in slots 0..8, which chain 3 (levels 6..8,
+// slots acc_block(6)..) leaves free.
+template <int TWOL>
+struct UtotLanes {
+    static constexpr int NCH = TWOL / 2 + 1;
+    static constexpr bool PAIR = (TWOL == 8);  // the last lane also runs the last chain
+    static constexpr int LPI = PAIR ? NCH - 1 : NCH;  // lanes per image
+    static constexpr int IPW = 32 / LPI;              // images per pass
+    // lane (within the image) and accumulator slot of the entry (chain mb, level L, ma)
+    __host__ __device__ static constexpr int lane_of(int mb) { return (PAIR && mb == NCH - 1) ? LPI - 1 : mb; }
+    __host__ __device__ static constexpr int slot_of(int mb, int slot) {
+        return (PAIR && mb == NCH - 1) ? slot - acc_block(TWOL) : slot;
+    }
+};
+
+template <int TWOL, int L>
+__device__ __forceinline__ void rc2_level(int mb, const CK<float> &ck, float2 (&u)[TWOL + 1]) {
+#pragma unroll
+    for (int ma = L; ma >= 0; --ma) {
+        float vr = 0.f, vi = 0.f;
+        if (ma > 0) {
+            const float pr = u[ma - 1].x, pi = u[ma - 1].y;
+            vr = fmaf(ck.cb.im, pi, -ck.cb.re * pr);
+            vi = fmaf(-ck.cb.im, pr, -ck.cb.re * pi);
+        }
+        if (ma < L) {
+            const float pr = u[ma].x, pi = u[ma].y;
+            vr = fmaf(ck.ca.re, pr, fmaf(-ck.ca.im, pi, vr));
+            vi = fmaf(ck.ca.re, pi, fmaf(ck.ca.im, pr, vi));
+        }
+        u[ma] = make_float2(vr, vi);
+    }
+    if ((L & 1) == 0 && 2 * mb == L) {
+        constexpr int H = L / 2;
+        u[H].y = -u[H].y;
+#pragma unroll
+        for (int ma = H + 1; ma <= L; ++ma) {
+            const float s = ((H + ma) & 1) ? -1.f : 1.f;
+            u[ma] = make_float2(s * u[L - ma].x, -s * u[L - ma].y);
+        }
+    }
+}
+
+// the start of chain H = L/2 from row H-1 of level L-1, mirrored: from lane - 1 (shuffle)
+template <int TWOL, int L>
+__device__ __forceinline__ void rc2_start(int mb, float2 (&u)[TWOL + 1]) {
+    constexpr int H = L / 2;
+    const bool take = (mb == H);
+#pragma unroll
+    for (int c = 0; c < L; ++c) {
+        const float s = ((H + c) & 1) ? -1.f : 1.f;
+        const float vr = __shfl_up_sync(0xffffffffu, u[L - 1 - c].x, 1);
+        const float vi = __shfl_up_sync(0xffffffffu, u[L - 1 - c].y, 1);
+        if (take) u[c] = make_float2(s * vr, -s * vi);
+    }
+}
+
+// Levels L..TWOL of one image's chain mb (lane chain; with UtotLanes::PAIR the lane of
+// chain NCH-2 also runs chain NCH-1 at level TWOL), accumulating wsf times each row.
+template <int TWOL, int L>
+struct RcUtot2 {
+    using UL = UtotLanes<TWOL>;
+    __device__ __forceinline__ static void run(int mb, const CK<float> &ck, float wsf, float2 (&u)[TWOL + 1],
+                                               float2 (&acc)[acc_block(TWOL + 1)]) {
+        const float2 w2 = make_float2(wsf, wsf);
+        if constexpr (UL::PAIR && L == TWOL) {
+            // the last chain (c = TWOL/2) from this lane's own row of level TWOL-1 (chain c-1)
+            constexpr int H = L / 2;
+            if (mb == H - 1) {
+                float2 t[TWOL + 1];
+#pragma unroll
+                for (int c = 0; c < L; ++c) {
+                    const float s = ((H + c) & 1) ? -1.f : 1.f;
+                    t[c] = make_float2(s * u[L - 1 - c].x, -s * u[L - 1 - c].y);
+                }
+                t[L] = make_float2(0.f, 0.f);
+                rc2_level<TWOL, L>(H, ck, t);
+#pragma unroll
+                for (int ma = 0; ma <= L; ++ma) acc[ma] = __ffma2_rn(w2, t[ma], acc[ma]);
+            }
+        } else if constexpr ((L & 1) == 0) {
+            rc2_start<TWOL, L>(mb, u);
+        }
+        rc2_level<TWOL, L>(mb, ck, u);
+        if (2 * mb <= L) {
+#pragma unroll
+            for (int ma = 0; ma <= L; ++ma) acc[acc_block(L) + ma] = __ffma2_rn(w2, u[ma], acc[acc_block(L) + ma]);
+        }
+        RcUtot2<TWOL, L + 1>::run(mb, ck, wsf, u, acc);
+    }
+};
+template <int TWOL>
+struct RcUtot2<TWOL, TWOL + 1> {
+    __device__ __forceinline__ static void run(int, const CK<float> &, float, float2 (&)[TWOL + 1],
+                                               float2 (&)[acc_block(TWOL + 1)]) {}
+};
+
 // Levels L..TWOL with the derivative along one direction per image (ck.cda[0],
 // ck.cdb[0] hold d conj(a), d conj(b) along it); after each level the lane adds
 //   a_du U + a_d dU   (a_du = w dsfac (r^ . dr_m), a_d = w sfac)
