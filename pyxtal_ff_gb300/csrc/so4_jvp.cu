@@ -32,18 +32,18 @@ struct JArgs {
     float *dB;
 };
 
-// tangent of U_tot, one warp per centre (same layout as k_utot_rc)
+// tangent of U_tot, one warp per centre (same lanes as k_utot_rc: UtotLanes)
 template <int TWOL, int NW>
 __global__ void __launch_bounds__(NW * 32, (TWOL <= 6) ? 4 : ((TWOL == 8) ? 3 : 1)) k_jvp_du_rc(JArgs A) {
-    using RC = RowChain<TWOL>;
+    using UL = UtotLanes<TWOL>;
     constexpr int W = TWOL + 1, NACC = acc_block(TWOL + 1);
     extern __shared__ __align__(16) float jv_smem[];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int a = blockIdx.x * NW + wid;
-    const int grp = lane / RC::NCH, mb = lane - grp * RC::NCH;
-    float accr[NACC], acci[NACC];
+    const int grp = lane / UL::LPI, mb = lane - grp * UL::LPI;
+    float2 acc[NACC];
 #pragma unroll
-    for (int q = 0; q < NACC; ++q) accr[q] = acci[q] = 0.f;
+    for (int q = 0; q < NACC; ++q) acc[q] = make_float2(0.f, 0.f);
     if (a < A.natoms) {
         const int m0 = A.img_ptr[a], m1 = A.img_ptr[a + 1];
         float vi[3] = {0.f, 0.f, 0.f}, G[9];
@@ -100,9 +100,9 @@ __global__ void __launch_bounds__(NW * 32, (TWOL <= 6) ? 4 : ((TWOL == 8) ? 3 : 
                 db0.im += d[c] * ck0.cdb[c].im;
             }
             const int nimg = min(32, m1 - base);
-            for (int sub = 0; sub < nimg; sub += RC::IPW) {
+            for (int sub = 0; sub < nimg; sub += UL::IPW) {
                 const int src = sub + grp;
-                const bool ok = grp < RC::IPW && src < nimg;
+                const bool ok = grp < UL::IPW && src < nimg;
                 const int sl = ok ? src : 0;
                 CK<float> ck;  // slot 0 of the derivatives holds the one direction
                 ck.ca.re = __shfl_sync(0xffffffffu, ck0.ca.re, sl);
@@ -116,33 +116,31 @@ __global__ void __launch_bounds__(NW * 32, (TWOL <= 6) ? 4 : ((TWOL == 8) ? 3 : 
                 float a_du = __shfl_sync(0xffffffffu, a_du0, sl);
                 float a_d = __shfl_sync(0xffffffffu, a_d0, sl);
                 if (!ok) a_du = a_d = 0.f;
-                float ur[W], ui[W], dr[1][W], di[1][W];
+                float2 u[W], du[W];
 #pragma unroll
-                for (int q = 0; q < W; ++q) ur[q] = ui[q] = dr[0][q] = di[0][q] = 0.f;
-                ur[0] = 1.f;
-                if (mb == 0) accr[0] += a_du;  // level 0: U = 1, dU = 0
-                RcJvp<TWOL, 1>::run(mb, ck, a_du, a_d, ur, ui, dr, di, accr, acci);
+                for (int q = 0; q < W; ++q) u[q] = du[q] = make_float2(0.f, 0.f);
+                u[0].x = 1.f;
+                if (mb == 0) acc[0].x += a_du;  // level 0: U = 1, dU = 0
+                RcJvp2<TWOL, 1>::run(mb, ck, a_du, a_d, u, du, acc);
             }
         }
     }
-    float *sw = jv_smem + (size_t)wid * 32 * 2 * NACC;
+    float2 *sw = reinterpret_cast<float2 *>(jv_smem) + (size_t)wid * 32 * NACC;
 #pragma unroll
-    for (int q = 0; q < NACC; ++q) {
-        sw[lane * 2 * NACC + 2 * q] = accr[q];
-        sw[lane * 2 * NACC + 2 * q + 1] = acci[q];
-    }
+    for (int q = 0; q < NACC; ++q) sw[lane * NACC + q] = acc[q];
     __syncwarp();
     if (a >= A.natoms) return;
     float2 *out = A.dU + (size_t)a * A.nh;
     for (int e = lane; e < A.nh; e += 32) {
         const int4 h = __ldg(A.hmap + e);
         const int slot = h.x & 0xff, row = (h.x >> 8) & 0x7f;
+        const int ln = UL::lane_of(row), sq = UL::slot_of(row, slot);
         float sr = 0.f, si = 0.f;
 #pragma unroll
-        for (int g = 0; g < RC::IPW; ++g) {
-            const float *src = sw + (g * RC::NCH + row) * 2 * NACC + 2 * slot;
-            sr += src[0];
-            si += src[1];
+        for (int g = 0; g < UL::IPW; ++g) {
+            const float2 v = sw[(g * UL::LPI + ln) * NACC + sq];
+            sr += v.x;
+            si += v.y;
         }
         const float unf = __int_as_float(h.y);  // u_norm times the row scale
         out[e] = make_float2(sr * unf, si * unf);

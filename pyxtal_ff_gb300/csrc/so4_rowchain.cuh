@@ -182,33 +182,6 @@ __device__ __forceinline__ int centre_of(const int32_t *img_ptr, int natoms, int
 // offset of level L in a lane's accumulator: sum_{l<L} (l+1)
 __host__ __device__ constexpr int acc_block(int L) { return L * (L + 1) / 2; }
 
-// Levels L..TWOL of the U recursion (no derivatives); after each level the
-// lane adds w sfac U of its row into its accumulator for that level.
-template <int TWOL, int L>
-struct RcUtot {
-    __device__ __forceinline__ static void run(int mb, const CK<float> &ck, float wsf, float (&ur)[TWOL + 1],
-                                               float (&ui)[TWOL + 1], float (&dr)[3][TWOL + 1],
-                                               float (&di)[3][TWOL + 1], float (&accr)[acc_block(TWOL + 1)],
-                                               float (&acci)[acc_block(TWOL + 1)]) {
-        if ((L & 1) == 0) rc_start<TWOL, L, false>(mb, ur, ui, dr, di);
-        rc_level<TWOL, L, false>(mb, ck, ur, ui, dr, di);
-        if (2 * mb <= L) {
-#pragma unroll
-            for (int ma = 0; ma <= L; ++ma) {
-                accr[acc_block(L) + ma] += wsf * ur[ma];
-                acci[acc_block(L) + ma] += wsf * ui[ma];
-            }
-        }
-        RcUtot<TWOL, L + 1>::run(mb, ck, wsf, ur, ui, dr, di, accr, acci);
-    }
-};
-template <int TWOL>
-struct RcUtot<TWOL, TWOL + 1> {
-    __device__ __forceinline__ static void run(int, const CK<float> &, float, float (&)[TWOL + 1], float (&)[TWOL + 1],
-                                               float (&)[3][TWOL + 1], float (&)[3][TWOL + 1],
-                                               float (&)[acc_block(TWOL + 1)], float (&)[acc_block(TWOL + 1)]) {}
-};
-
 // ---------------------------------------------------------------------------
 // U_tot (no derivatives), rows as (re, im) pairs so that the weighted accumulation is one
 // packed FMA per entry; the recursion and the chain start are rc_level / rc_start's own
@@ -274,6 +247,60 @@ __device__ __forceinline__ void rc2_start(int mb, float2 (&u)[TWOL + 1]) {
     }
 }
 
+// The last chain (H = TWOL/2) at level TWOL, from the previous chain's row of level
+// TWOL-1 held in u (and its derivative along one direction in du), entry by entry and
+// without a row of its own: P[c] = (-1)^(H+c) conj(u[TWOL-1-c]) is the start row, the
+// entries ma <= H are rc_level's recursion, the centre is conjugated and the upper half
+// is the middle-row mirror.  Adds wu V[ma] (+ wd dV[ma]) to acc[ma], ma = 0..TWOL.
+template <int TWOL, bool DERIV>
+__device__ __forceinline__ void rc2_last_chain(const CK<float> &ck, const float2 (&u)[TWOL + 1],
+                                               const float2 (&du)[TWOL + 1], float wu, float wd,
+                                               float2 (&acc)[acc_block(TWOL + 1)]) {
+    constexpr int L = TWOL, H = L / 2;
+    const float2 w2 = make_float2(wu, wu), d2 = make_float2(wd, wd);
+    auto sgn = [](int c) { return ((H + c) & 1) ? -1.f : 1.f; };
+#pragma unroll
+    for (int ma = 0; ma <= H; ++ma) {
+        float vr = 0.f, vi = 0.f, er = 0.f, ei = 0.f;
+        if (ma > 0) {
+            const float s = sgn(ma - 1);
+            const float pr = s * u[L - ma].x, pi = -s * u[L - ma].y;
+            vr = fmaf(ck.cb.im, pi, -ck.cb.re * pr);
+            vi = fmaf(-ck.cb.im, pr, -ck.cb.re * pi);
+            if (DERIV) {
+                const float qr = s * du[L - ma].x, qi = -s * du[L - ma].y;
+                er = -(ck.cdb[0].re * pr - ck.cdb[0].im * pi + ck.cb.re * qr - ck.cb.im * qi);
+                ei = -(ck.cdb[0].re * pi + ck.cdb[0].im * pr + ck.cb.re * qi + ck.cb.im * qr);
+            }
+        }
+        {
+            const float s = sgn(ma);
+            const float pr = s * u[L - 1 - ma].x, pi = -s * u[L - 1 - ma].y;
+            vr = fmaf(ck.ca.re, pr, fmaf(-ck.ca.im, pi, vr));
+            vi = fmaf(ck.ca.re, pi, fmaf(ck.ca.im, pr, vi));
+            if (DERIV) {
+                const float qr = s * du[L - 1 - ma].x, qi = -s * du[L - 1 - ma].y;
+                er += ck.cda[0].re * pr - ck.cda[0].im * pi + ck.ca.re * qr - ck.ca.im * qi;
+                ei += ck.cda[0].re * pi + ck.cda[0].im * pr + ck.ca.re * qi + ck.ca.im * qr;
+            }
+        }
+        if (ma == H) {
+            vi = -vi;
+            ei = -ei;
+        }
+        float2 a = __ffma2_rn(w2, make_float2(vr, vi), acc[ma]);
+        if (DERIV) a = __ffma2_rn(d2, make_float2(er, ei), a);
+        acc[ma] = a;
+        if (ma < H) {
+            // the mirror entry L - ma: (-1)^(H + L - ma) conj(V[ma])
+            const float m = sgn(L - ma);
+            float2 b = __ffma2_rn(w2, make_float2(m * vr, -m * vi), acc[L - ma]);
+            if (DERIV) b = __ffma2_rn(d2, make_float2(m * er, -m * ei), b);
+            acc[L - ma] = b;
+        }
+    }
+}
+
 // Levels L..TWOL of one image's chain mb (lane chain; with UtotLanes::PAIR the lane of
 // chain NCH-2 also runs chain NCH-1 at level TWOL), accumulating wsf times each row.
 template <int TWOL, int L>
@@ -283,20 +310,7 @@ struct RcUtot2 {
                                                float2 (&acc)[acc_block(TWOL + 1)]) {
         const float2 w2 = make_float2(wsf, wsf);
         if constexpr (UL::PAIR && L == TWOL) {
-            // the last chain (c = TWOL/2) from this lane's own row of level TWOL-1 (chain c-1)
-            constexpr int H = L / 2;
-            if (mb == H - 1) {
-                float2 t[TWOL + 1];
-#pragma unroll
-                for (int c = 0; c < L; ++c) {
-                    const float s = ((H + c) & 1) ? -1.f : 1.f;
-                    t[c] = make_float2(s * u[L - 1 - c].x, -s * u[L - 1 - c].y);
-                }
-                t[L] = make_float2(0.f, 0.f);
-                rc2_level<TWOL, L>(H, ck, t);
-#pragma unroll
-                for (int ma = 0; ma <= L; ++ma) acc[ma] = __ffma2_rn(w2, t[ma], acc[ma]);
-            }
+            if (mb == L / 2 - 1) rc2_last_chain<TWOL, false>(ck, u, u, wsf, 0.f, acc);
         } else if constexpr ((L & 1) == 0) {
             rc2_start<TWOL, L>(mb, u);
         }
@@ -314,33 +328,71 @@ struct RcUtot2<TWOL, TWOL + 1> {
                                                float2 (&)[acc_block(TWOL + 1)]) {}
 };
 
-// Levels L..TWOL with the derivative along one direction per image (ck.cda[0],
-// ck.cdb[0] hold d conj(a), d conj(b) along it); after each level the lane adds
-//   a_du U + a_d dU   (a_du = w dsfac (r^ . dr_m), a_d = w sfac)
-// of its row into its accumulator (the tangent of U_tot used by the JVP).
+// rc2_level with the derivative along one direction (ck.cda[0], ck.cdb[0]): du is the
+// row of dV, updated with rc_level's expressions
 template <int TWOL, int L>
-struct RcJvp {
-    __device__ __forceinline__ static void run(int mb, const CK<float> &ck, float a_du, float a_d,
-                                               float (&ur)[TWOL + 1], float (&ui)[TWOL + 1],
-                                               float (&dr)[1][TWOL + 1], float (&di)[1][TWOL + 1],
-                                               float (&accr)[acc_block(TWOL + 1)], float (&acci)[acc_block(TWOL + 1)]) {
-        if ((L & 1) == 0) rc_start<TWOL, L, true, 1>(mb, ur, ui, dr, di);
-        rc_level<TWOL, L, true, 1>(mb, ck, ur, ui, dr, di);
-        if (2 * mb <= L) {
+__device__ __forceinline__ void rc2_level_d(int mb, const CK<float> &ck, float2 (&u)[TWOL + 1],
+                                            float2 (&du)[TWOL + 1]) {
 #pragma unroll
-            for (int ma = 0; ma <= L; ++ma) {
-                accr[acc_block(L) + ma] += a_du * ur[ma] + a_d * dr[0][ma];
-                acci[acc_block(L) + ma] += a_du * ui[ma] + a_d * di[0][ma];
-            }
+    for (int ma = L; ma >= 0; --ma) {
+        float vr = 0.f, vi = 0.f, er = 0.f, ei = 0.f;
+        if (ma > 0) {
+            const float pr = u[ma - 1].x, pi = u[ma - 1].y, qr = du[ma - 1].x, qi = du[ma - 1].y;
+            vr = fmaf(ck.cb.im, pi, -ck.cb.re * pr);
+            vi = fmaf(-ck.cb.im, pr, -ck.cb.re * pi);
+            er = -(ck.cdb[0].re * pr - ck.cdb[0].im * pi + ck.cb.re * qr - ck.cb.im * qi);
+            ei = -(ck.cdb[0].re * pi + ck.cdb[0].im * pr + ck.cb.re * qi + ck.cb.im * qr);
         }
-        RcJvp<TWOL, L + 1>::run(mb, ck, a_du, a_d, ur, ui, dr, di, accr, acci);
+        if (ma < L) {
+            const float pr = u[ma].x, pi = u[ma].y, qr = du[ma].x, qi = du[ma].y;
+            vr = fmaf(ck.ca.re, pr, fmaf(-ck.ca.im, pi, vr));
+            vi = fmaf(ck.ca.re, pi, fmaf(ck.ca.im, pr, vi));
+            er += ck.cda[0].re * pr - ck.cda[0].im * pi + ck.ca.re * qr - ck.ca.im * qi;
+            ei += ck.cda[0].re * pi + ck.cda[0].im * pr + ck.ca.re * qi + ck.ca.im * qr;
+        }
+        u[ma] = make_float2(vr, vi);
+        du[ma] = make_float2(er, ei);
+    }
+    if ((L & 1) == 0 && 2 * mb == L) {
+        constexpr int H = L / 2;
+        u[H].y = -u[H].y;
+        du[H].y = -du[H].y;
+#pragma unroll
+        for (int ma = H + 1; ma <= L; ++ma) {
+            const float s = ((H + ma) & 1) ? -1.f : 1.f;
+            u[ma] = make_float2(s * u[L - ma].x, -s * u[L - ma].y);
+            du[ma] = make_float2(s * du[L - ma].x, -s * du[L - ma].y);
+        }
+    }
+}
+
+// the JVP's tangent of U_tot: levels L..TWOL of chain mb with the derivative along the
+// image's tangent, adding a_du V + a_d dV of each row (lanes as in RcUtot2)
+template <int TWOL, int L>
+struct RcJvp2 {
+    using UL = UtotLanes<TWOL>;
+    __device__ __forceinline__ static void run(int mb, const CK<float> &ck, float a_du, float a_d, float2 (&u)[TWOL + 1],
+                                               float2 (&du)[TWOL + 1], float2 (&acc)[acc_block(TWOL + 1)]) {
+        if constexpr (UL::PAIR && L == TWOL) {
+            if (mb == L / 2 - 1) rc2_last_chain<TWOL, true>(ck, u, du, a_du, a_d, acc);
+        } else if constexpr ((L & 1) == 0) {
+            rc2_start<TWOL, L>(mb, u);
+            rc2_start<TWOL, L>(mb, du);
+        }
+        rc2_level_d<TWOL, L>(mb, ck, u, du);
+        if (2 * mb <= L) {
+            const float2 w2 = make_float2(a_du, a_du), d2 = make_float2(a_d, a_d);
+#pragma unroll
+            for (int ma = 0; ma <= L; ++ma)
+                acc[acc_block(L) + ma] = __ffma2_rn(d2, du[ma], __ffma2_rn(w2, u[ma], acc[acc_block(L) + ma]));
+        }
+        RcJvp2<TWOL, L + 1>::run(mb, ck, a_du, a_d, u, du, acc);
     }
 };
 template <int TWOL>
-struct RcJvp<TWOL, TWOL + 1> {
-    __device__ __forceinline__ static void run(int, const CK<float> &, float, float, float (&)[TWOL + 1],
-                                               float (&)[TWOL + 1], float (&)[1][TWOL + 1], float (&)[1][TWOL + 1],
-                                               float (&)[acc_block(TWOL + 1)], float (&)[acc_block(TWOL + 1)]) {}
+struct RcJvp2<TWOL, TWOL + 1> {
+    __device__ __forceinline__ static void run(int, const CK<float> &, float, float, float2 (&)[TWOL + 1],
+                                               float2 (&)[TWOL + 1], float2 (&)[acc_block(TWOL + 1)]) {}
 };
 
 // ---------------------------------------------------------------------------
