@@ -36,9 +36,10 @@ CONFIG = {"workload": "diamond-Si 20x20x10 (32000 atoms), SO4 lmax=4, rcut=5.0 A
 
 
 # DRAM bytes (read + write) per full launch of each stage's kernel: the figures of the
-# one-kernel captures of a 16,384-atom case (profiles/k_utot_rc_k_zw32_k_deidrj_rev2_si16384_lmax4.md),
-# times 1.95 for the atoms and images of the 32,000-atom workload
-NCU_TRAFFIC = {"utot32": 25.8e6, "linear_by32": 51.0e6, "adjoint_deidrj32": 68.2e6}
+# one-kernel captures of a 16,384-atom case (profiles/k_zw64_k_utot_rc_k_jvp_du_rc_si16384_lmax4.md
+# for the window and U_tot passes, profiles/k_utot_rc_k_zw32_k_deidrj_rev2_si16384_lmax4.md for
+# the per-image pass), times 1.95 for the atoms and images of the 32,000-atom workload
+NCU_TRAFFIC = {"utot32": 25.8e6, "linear_by32": 48.2e6, "adjoint_deidrj32": 68.2e6}
 
 
 def workload():
