@@ -1006,16 +1006,16 @@ __global__ void __launch_bounds__(NT, (TWOL == 8) ? 3 : 2) k_deidrj_rev2(DArgs A
             const int nlines = (A.nh * (int)sizeof(float2) + 127) / 128;
             for (int l = role; l < nlines; l += 2) asm volatile("prefetch.global.L1 [%0];" ::"l"(yb + 128 * l));
         }
-        float ur[NS][W], ui[NS][W];
+        float2 u[NS][W];
 #pragma unroll
         for (int q = 0; q < NS; ++q)
 #pragma unroll
-            for (int e = 0; e < W; ++e) ur[q][e] = ui[q][e] = 0.f;
+            for (int e = 0; e < W; ++e) u[q][e] = make_float2(0.f, 0.f);
         if (role == 0) {
-            ur[0][0] = 1.f;  // level 0 of chain 0
+            u[0][0].x = 1.f;  // level 0 of chain 0
             st[Y::idx(0, 0) * NT] = make_float2(1.f, 0.f);
         }
-        rev2::Fwd<TWOL, 1, NT>::run(role, ch, ck, ur, ui, st);
+        rev2::Fwd<TWOL, 1, NT>::run(role, ch, ck, u, st);
         float2 g[NS][W];
 #pragma unroll
         for (int q = 0; q < NS; ++q)
@@ -1024,7 +1024,7 @@ __global__ void __launch_bounds__(NT, (TWOL == 8) ? 3 : 2) k_deidrj_rev2(DArgs A
         const float2 *Yc = A.Y + (size_t)c_it * A.nh;
         const float2 z2 = make_float2(0.f, 0.f);
         float2 su2 = z2, sa1 = z2, sa2 = z2, sb1 = z2, sb2 = z2;
-        rev2::Back<TWOL, TWOL, NT>::run(role, ch, rv_pairs(ck), Yc, st, ur, ui, g, su2, sa1, sa2, sb1, sb2);
+        rev2::Back<TWOL, TWOL, NT>::run(role, ch, rv_pairs(ck), Yc, st, u, g, su2, sa1, sa2, sb1, sb2);
         float tu = su2.x + su2.y, t0 = sa1.x + sa1.y, t1 = sa2.x - sa2.y;
         float t2 = -(sb1.x + sb1.y), t3 = -(sb2.x - sb2.y);
         // the pair's two lanes: both hold the image's sums

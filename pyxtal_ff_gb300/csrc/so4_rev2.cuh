@@ -70,12 +70,12 @@ struct Layout {
 };
 
 // Forward sweep, levels L..TWOL.  ch[s]: this lane's chain in slot s (-1: none); role: 0 A, 1 B.
+// Rows are (re, im) pairs (rc2_level: rc_level's arithmetic), stored to shared memory as they are.
 template <int TWOL, int L, int NT>
 struct Fwd {
     using Y = Layout<TWOL>;
     __device__ __forceinline__ static void run(int role, const int (&ch)[Y::NS], const CK<float> &ck,
-                                               float (&ur)[Y::NS][TWOL + 1], float (&ui)[Y::NS][TWOL + 1],
-                                               float2 *st) {
+                                               float2 (&u)[Y::NS][TWOL + 1], float2 *st) {
         if constexpr ((L & 1) == 0) {
             // chain c = L/2 starts from chain c - 1's row of level L - 1:
             //   P[k] = (-1)^(c + k) conj(Q[L - 1 - k]),  k = 0 .. L - 1
@@ -84,41 +84,37 @@ struct Fwd {
             const bool take = role == role_of(c);
 #pragma unroll
             for (int k = 0; k < L; ++k) {
-                float qr = ur[ss][L - 1 - k], qi = ui[ss][L - 1 - k];
+                float qr = u[ss][L - 1 - k].x, qi = u[ss][L - 1 - k].y;
                 if (cross) {
                     qr = __shfl_xor_sync(0xffffffffu, qr, 1);
                     qi = __shfl_xor_sync(0xffffffffu, qi, 1);
                 }
                 const float s = ((c + k) & 1) ? -1.f : 1.f;
-                if (take) {
-                    ur[sd][k] = s * qr;
-                    ui[sd][k] = -s * qi;
-                }
+                if (take) u[sd][k] = make_float2(s * qr, -s * qi);
             }
             if (take) {
 #pragma unroll
-                for (int k = 0; k < L; ++k) st[(Y::idx(sd, L - 1) + k) * NT] = make_float2(ur[sd][k], ui[sd][k]);
+                for (int k = 0; k < L; ++k) st[(Y::idx(sd, L - 1) + k) * NT] = u[sd][k];
             }
         }
-        float dr[3][TWOL + 1], di[3][TWOL + 1];  // unused (no derivatives)
 #pragma unroll
         for (int s = 0; s < Y::NS; ++s) {
             if (Y::act(s) <= L) {
-                rc_level<TWOL, L, false>(ch[s], ck, ur[s], ui[s], dr, di);
+                rc2_level<TWOL, L>(ch[s], ck, u[s]);
                 if (L < TWOL && ch[s] >= 0 && 2 * ch[s] <= L) {
 #pragma unroll
-                    for (int ma = 0; ma <= L; ++ma) st[(Y::idx(s, L) + ma) * NT] = make_float2(ur[s][ma], ui[s][ma]);
+                    for (int ma = 0; ma <= L; ++ma) st[(Y::idx(s, L) + ma) * NT] = u[s][ma];
                 }
             }
         }
-        Fwd<TWOL, L + 1, NT>::run(role, ch, ck, ur, ui, st);
+        Fwd<TWOL, L + 1, NT>::run(role, ch, ck, u, st);
     }
 };
 template <int TWOL, int NT>
 struct Fwd<TWOL, TWOL + 1, NT> {
     using Y = Layout<TWOL>;
     __device__ __forceinline__ static void run(int, const int (&)[Y::NS], const CK<float> &,
-                                               float (&)[Y::NS][TWOL + 1], float (&)[Y::NS][TWOL + 1], float2 *) {}
+                                               float2 (&)[Y::NS][TWOL + 1], float2 *) {}
 };
 
 // Backward sweep, level L down to 1, per slot as RvBack does per lane; at a chain start
@@ -128,9 +124,8 @@ struct Back {
     using Y = Layout<TWOL>;
     __device__ __forceinline__ static void run(int role, const int (&ch)[Y::NS], const RvPairs &q,
                                                const float2 *__restrict__ Yc, const float2 *st,
-                                               const float (&ur)[Y::NS][TWOL + 1], const float (&ui)[Y::NS][TWOL + 1],
-                                               float2 (&g)[Y::NS][TWOL + 1], float2 &su, float2 &sa1, float2 &sa2,
-                                               float2 &sb1, float2 &sb2) {
+                                               const float2 (&u)[Y::NS][TWOL + 1], float2 (&g)[Y::NS][TWOL + 1],
+                                               float2 &su, float2 &sa1, float2 &sa2, float2 &sb1, float2 &sb2) {
         constexpr int H = L / 2;
 #pragma unroll
         for (int s = 0; s < Y::NS; ++s) {
@@ -144,7 +139,7 @@ struct Back {
                         const bool none = (L & 1) == 0 && ma > H && mb == H;
                         const float2 y = none ? make_float2(0.f, 0.f) : __ldg(Yr + ma);
                         // level TWOL from the forward sweep's registers, lower levels from shared memory
-                        const float2 row = (L == TWOL) ? make_float2(ur[s][ma], ui[s][ma]) : st[(Y::idx(s, L) + ma) * NT];
+                        const float2 row = (L == TWOL) ? u[s][ma] : st[(Y::idx(s, L) + ma) * NT];
                         su = __ffma2_rn(row, y, su);
                         g[s][ma] = __fadd2_rn(g[s][ma], y);
                     }
@@ -194,7 +189,7 @@ struct Back {
                 }
             }
         }
-        Back<TWOL, L - 1, NT>::run(role, ch, q, Yc, st, ur, ui, g, su, sa1, sa2, sb1, sb2);
+        Back<TWOL, L - 1, NT>::run(role, ch, q, Yc, st, u, g, su, sa1, sa2, sb1, sb2);
     }
 };
 template <int TWOL, int NT>
@@ -202,9 +197,8 @@ struct Back<TWOL, 0, NT> {
     using Y = Layout<TWOL>;
     __device__ __forceinline__ static void run(int role, const int (&)[Y::NS], const RvPairs &,
                                                const float2 *__restrict__ Yc, const float2 *,
-                                               const float (&)[Y::NS][TWOL + 1], const float (&)[Y::NS][TWOL + 1],
-                                               float2 (&)[Y::NS][TWOL + 1], float2 &su, float2 &, float2 &,
-                                               float2 &, float2 &) {
+                                               const float2 (&)[Y::NS][TWOL + 1], float2 (&)[Y::NS][TWOL + 1],
+                                               float2 &su, float2 &, float2 &, float2 &, float2 &) {
         if (role == 0) su.x += __ldg(Yc).x;  // level 0: U = 1 (chain 0, lane A)
     }
 };
