@@ -262,11 +262,20 @@ __global__ void k_scan_images(const so4_geom *geom, const double *pos, const int
         int tb[3], img[3];
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-            const int t = bi[k] + d[k];
+            // the wrapped bin and the image floor(t / nb), by whole periods: t lies within
+            // mshift of [0, nb), so one step at most unless the cell is thinner than rcut
             const int nb = g.nbin[k];
-            const int wk = ((t % nb) + nb) % nb;
+            int wk = bi[k] + d[k], im = 0;
+            while (wk < 0) {
+                wk += nb;
+                --im;
+            }
+            while (wk >= nb) {
+                wk -= nb;
+                ++im;
+            }
             tb[k] = wk;
-            img[k] = (t - wk) / nb;
+            img[k] = im;
         }
         const int bin = g.bin_base + (tb[0] * g.nbin[1] + tb[1]) * g.nbin[2] + tb[2];
         // the next candidate's index is read one ahead, so its loads do not wait on it
