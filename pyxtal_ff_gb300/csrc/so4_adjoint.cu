@@ -1394,8 +1394,11 @@ extern "C" int so4_forward32(const so4_tables *t, const so4_params *p, int natom
     int rc = SO4_OK;
     switch (t->twol) {
         case 2: rc = launch_utot_rc<2>(A, t->tune.utot_warps, st); break;
+        case 3: rc = launch_utot_rc<3>(A, t->tune.utot_warps, st); break;
         case 4: rc = launch_utot_rc<4>(A, t->tune.utot_warps, st); break;
+        case 5: rc = launch_utot_rc<5>(A, t->tune.utot_warps, st); break;
         case 6: rc = launch_utot_rc<6>(A, t->tune.utot_warps, st); break;
+        case 7: rc = launch_utot_rc<7>(A, t->tune.utot_warps, st); break;
         case 8: rc = launch_utot_rc<8>(A, t->tune.utot_warps, st); break;
         case 10: rc = launch_utot_rc<10>(A, t->tune.utot_warps, st); break;
         case 12: rc = launch_utot_rc<12>(A, t->tune.utot_warps, st); break;
@@ -1487,8 +1490,11 @@ extern "C" int so4_adjoint_deidrj32(const so4_tables *t, const so4_params *p, in
     int rc = SO4_OK;
     switch (t->twol) {
         case 2: rc = launch_deidrj_rev<2>(D, nimg, t->tune.rev_threads, t->tune.rev_pair == 1, st); break;
+        case 3: rc = launch_deidrj_rev<3>(D, nimg, t->tune.rev_threads, t->tune.rev_pair == 1, st); break;
         case 4: rc = launch_deidrj_rev<4>(D, nimg, t->tune.rev_threads, t->tune.rev_pair == 1, st); break;
+        case 5: rc = launch_deidrj_rev<5>(D, nimg, t->tune.rev_threads, t->tune.rev_pair == 1, st); break;
         case 6: rc = launch_deidrj_rev<6>(D, nimg, t->tune.rev_threads, t->tune.rev_pair == 1, st); break;
+        case 7: rc = launch_deidrj_rev<7>(D, nimg, t->tune.rev_threads, t->tune.rev_pair == 1, st); break;
         case 8: rc = launch_deidrj_rev<8>(D, nimg, t->tune.rev_threads, t->tune.rev_pair == 1, st); break;
         case 10: rc = launch_deidrj_rev<10>(D, nimg, t->tune.rev_threads, t->tune.rev_pair == 1, st); break;
         case 12: rc = launch_deidrj_rev<12>(D, nimg, t->tune.rev_threads, t->tune.rev_pair == 1, st); break;
@@ -1679,8 +1685,11 @@ extern "C" int so4_utot32(const so4_tables *t, const so4_params *p, int natoms, 
     int rc = SO4_OK;
     switch (t->twol) {
         case 2: rc = launch_utot_rc<2>(A, t->tune.utot_warps, st); break;
+        case 3: rc = launch_utot_rc<3>(A, t->tune.utot_warps, st); break;
         case 4: rc = launch_utot_rc<4>(A, t->tune.utot_warps, st); break;
+        case 5: rc = launch_utot_rc<5>(A, t->tune.utot_warps, st); break;
         case 6: rc = launch_utot_rc<6>(A, t->tune.utot_warps, st); break;
+        case 7: rc = launch_utot_rc<7>(A, t->tune.utot_warps, st); break;
         case 8: rc = launch_utot_rc<8>(A, t->tune.utot_warps, st); break;
         case 10: rc = launch_utot_rc<10>(A, t->tune.utot_warps, st); break;
         case 12: rc = launch_utot_rc<12>(A, t->tune.utot_warps, st); break;

@@ -201,8 +201,11 @@ extern "C" int so4_jvp32(const so4_tables *t, const so4_params *p, const int *d_
     int rc;
     switch (t->twol) {
         case 2: rc = launch_jvp_du<2>(A, st); break;
+        case 3: rc = launch_jvp_du<3>(A, st); break;
         case 4: rc = launch_jvp_du<4>(A, st); break;
+        case 5: rc = launch_jvp_du<5>(A, st); break;
         case 6: rc = launch_jvp_du<6>(A, st); break;
+        case 7: rc = launch_jvp_du<7>(A, st); break;
         case 8: rc = launch_jvp_du<8>(A, st); break;
         case 10: rc = launch_jvp_du<10>(A, st); break;
         case 12: rc = launch_jvp_du<12>(A, st); break;

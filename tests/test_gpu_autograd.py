@@ -42,12 +42,13 @@ def _ctx(lmax=3, rc=4.5):
     return structs, ptr, p, ctx, x
 
 
-@pytest.mark.parametrize("lmax", [2, 3, 4])
+@pytest.mark.parametrize("lmax", [1.5, 2, 2.5, 3, 3.5, 4])
 def test_jvp_matches_oracle_dxdr_and_rdxdr(cuda_device, lmax):
+    # half-integer lmax (SNAP's odd twol) runs the same row-chain kernels at twol 3, 5, 7
     rc = 4.5
     structs, ptr, p, ctx, _ = _ctx(lmax, rc)
     N, S_ = ctx.nb.natoms, ctx.nb.nstruct
-    rng = np.random.default_rng(lmax)
+    rng = np.random.default_rng(int(2 * lmax))
     v = rng.normal(size=(N, 3))
     Gm = rng.normal(size=(S_, 3, 3))
     dB_v = engine.jvp32(ctx.tab, ctx.prm, ctx.nb, ctx.w_nb, ctx.utot, v=torch.from_numpy(v).cuda()).cpu().numpy()
