@@ -34,7 +34,7 @@ struct JArgs {
 
 // tangent of U_tot, one warp per centre (same lanes as k_utot_rc: UtotLanes)
 template <int TWOL, int NW>
-__global__ void __launch_bounds__(NW * 32, (TWOL <= 6) ? 4 : ((TWOL == 8) ? 3 : 1)) k_jvp_du_rc(JArgs A) {
+__global__ void __launch_bounds__(NW * 32, (TWOL <= 4) ? 4 : ((TWOL <= 8) ? 3 : 1)) k_jvp_du_rc(JArgs A) {
     using UL = UtotLanes<TWOL>;
     constexpr int W = TWOL + 1, NACC = acc_block(TWOL + 1);
     extern __shared__ __align__(16) float jv_smem[];
