@@ -136,12 +136,13 @@ class SO4Calculator:
             self._batch_key = batch
         return self
 
-    def capture(self, batch: Batch, model, headroom=1.25, branches=None, pdl=None):
+    def capture(self, batch: Batch, model, headroom=1.25, branches=None, pdl=None, host_io=False):
         """The whole energy / forces / stress step of this batch layout as one CUDA graph
         (see CapturedStep); call the result with new positions.  branches / pdl default to
-        the calculator's tuning (2 and off untuned)."""
+        the calculator's tuning (2 and off untuned); host_io: the graph also copies the
+        positions in from, and the results out to, pinned host buffers of the step."""
         return CapturedStep(self, batch, model, headroom=headroom, branches=self.branches if branches is None else branches,
-                            pdl=self.pdl if pdl is None else pdl)
+                            pdl=self.pdl if pdl is None else pdl, host_io=host_io)
 
     def neighbors(self, batch: Batch, positions):
         return engine.build_neighbors(positions, batch.cells, batch.pbc, batch.atom_ptr, self.rcut, device=self.device)
@@ -233,9 +234,15 @@ class CapturedStep:
     `check()` reads them (one small synchronising copy) and returns False when the
     neighbour list outgrew the buffers, after which the step must be captured again
     (`SO4Calculator.capture`); it raises for non-finite positions like the eager path.
+
+    With host_io=True the step owns pinned host buffers, `host_positions` (N, 3) and
+    `host_out` (energy, forces, stress), and the graph itself copies the positions in
+    and the results out: a step is one graph launch and one wait, with no other call
+    (an MD engine writes its positions into `host_positions` and reads `host_out`).
     """
 
-    def __init__(self, calc: "SO4Calculator", batch: Batch, model, headroom=1.25, branches=2, pdl=False):
+    def __init__(self, calc: "SO4Calculator", batch: Batch, model, headroom=1.25, branches=2, pdl=False,
+                 host_io=False):
         self.linear = isinstance(model, LinearModel)
         # programmatic dependent launch between U_tot, the window pass and the per-image pass
         # (so4_set_pdl): only for a linear energy, whose beta is fixed for the whole step
@@ -306,6 +313,12 @@ class CapturedStep:
         self.energy = torch.empty(max(S, 1), dtype=torch.float64, device=dev)
         self.stress = torch.empty((max(S, 1), 6), dtype=torch.float64, device=dev)
         self._voigt = torch.tensor(VOIGT, device=dev)  # on the device before capture (no copies inside it)
+        self.host_io = bool(host_io)
+        if self.host_io:
+            self.host_positions = torch.from_numpy(np.ascontiguousarray(batch.positions, dtype=np.float64)).pin_memory()
+            self.host_out = dict(energy=torch.empty(S, dtype=torch.float64).pin_memory(),
+                                 forces=torch.empty((N, 3), dtype=torch.float64).pin_memory(),
+                                 stress=torch.empty((S, 6), dtype=torch.float64).pin_memory())
         self.launches = 0
         # eager warm-up on a side stream (sets kernel attributes, lets torch's allocator settle)
         side = torch.cuda.Stream(device=dev)
@@ -321,15 +334,22 @@ class CapturedStep:
         self.launches = int(L.so4_launch_count() - c0)  # kernels of this library in one replay
 
     def _enqueue(self):
+        if self.host_io:  # the positions from the pinned host buffer, as a node of the graph
+            self.pos.copy_(self.host_positions, non_blocking=True)
         if not self.linear:
             self._enqueue_model()
-            return
-        L = engine.lib()
-        prev = L.so4_set_pdl(1 if self.pdl else 0)
-        try:
-            self._enqueue_linear()
-        finally:
-            L.so4_set_pdl(prev)
+        else:
+            L = engine.lib()
+            prev = L.so4_set_pdl(1 if self.pdl else 0)
+            try:
+                self._enqueue_linear()
+            finally:
+                L.so4_set_pdl(prev)
+        if self.host_io:  # and the results back to the pinned host buffers
+            N, S = self.layout.natoms, self.layout.nstruct
+            self.host_out["energy"].copy_(self.energy[:S], non_blocking=True)
+            self.host_out["forces"].copy_(self.forces[:N], non_blocking=True)
+            self.host_out["stress"].copy_(self.stress[:S], non_blocking=True)
 
     def _enqueue_linear(self):
         lay, calc, tab, L = self.layout, self.calc, self.calc.tables, engine.lib()
@@ -429,7 +449,15 @@ class CapturedStep:
     def __call__(self, positions=None):
         """One step; positions (N,3) f64 from the host (pinned for an asynchronous copy)
         or the device, or None to reuse the last ones.  Returns views of the static
-        outputs (valid until the next call)."""
+        outputs (valid until the next call).  With host_io: positions (if given) are first
+        written into `host_positions`, and the call waits for the step and returns
+        `host_out`."""
+        if self.host_io:
+            if positions is not None:
+                self.host_positions.copy_(torch.as_tensor(np.asarray(positions, dtype=np.float64)))
+            self.graph.replay()
+            torch.cuda.current_stream(self.pos.device).synchronize()
+            return self.host_out
         if positions is not None:
             if isinstance(positions, np.ndarray):
                 positions = torch.from_numpy(np.ascontiguousarray(positions, dtype=np.float64))
