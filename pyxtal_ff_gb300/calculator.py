@@ -454,7 +454,9 @@ class CapturedStep:
         `host_out`."""
         if self.host_io:
             if positions is not None:
-                self.host_positions.copy_(torch.as_tensor(np.asarray(positions, dtype=np.float64)))
+                if not isinstance(positions, torch.Tensor):
+                    positions = torch.from_numpy(np.ascontiguousarray(positions, dtype=np.float64))
+                self.host_positions.copy_(positions)
             self.graph.replay()
             torch.cuda.current_stream(self.pos.device).synchronize()
             return self.host_out
