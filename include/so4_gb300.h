@@ -397,7 +397,7 @@ int so4_adjoint_linear32(const so4_tables *t, const so4_params *p, int nstruct, 
  * is not read).  With v = -dL/dF and G = dL/dW it gives dL/dbeta for the forces
  * and virial of so4_adjoint32, i.e. the gradient a force/stress loss sends back
  * into an energy model.  Scratch: so4_jvp_workspace_size() bytes.  Built for twol
- * 2 to 8, 10 and 12; SO4_ERR_UNSUPPORTED at twol 9 and 11. */
+ * 2 to 12; SO4_ERR_UNSUPPORTED at twol 0 and 1. */
 size_t so4_jvp_workspace_size(const so4_tables *t, int natoms);
 int so4_jvp32(const so4_tables *t, const so4_params *p, const int *d_atom_struct, int natoms,
               const double *d_w_nb, const int32_t *d_img_ptr, const int32_t *d_img_j, const double *d_img_r,

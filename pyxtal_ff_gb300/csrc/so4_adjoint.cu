@@ -1400,7 +1400,9 @@ extern "C" int so4_forward32(const so4_tables *t, const so4_params *p, int natom
         case 6: rc = launch_utot_rc<6>(A, t->tune.utot_warps, st); break;
         case 7: rc = launch_utot_rc<7>(A, t->tune.utot_warps, st); break;
         case 8: rc = launch_utot_rc<8>(A, t->tune.utot_warps, st); break;
+        case 9: rc = launch_utot_rc<9>(A, t->tune.utot_warps, st); break;
         case 10: rc = launch_utot_rc<10>(A, t->tune.utot_warps, st); break;
+        case 11: rc = launch_utot_rc<11>(A, t->tune.utot_warps, st); break;
         case 12: rc = launch_utot_rc<12>(A, t->tune.utot_warps, st); break;
         default: {
             const size_t smu =
@@ -1496,7 +1498,9 @@ extern "C" int so4_adjoint_deidrj32(const so4_tables *t, const so4_params *p, in
         case 6: rc = launch_deidrj_rev<6>(D, nimg, t->tune.rev_threads, t->tune.rev_pair == 1, st); break;
         case 7: rc = launch_deidrj_rev<7>(D, nimg, t->tune.rev_threads, t->tune.rev_pair == 1, st); break;
         case 8: rc = launch_deidrj_rev<8>(D, nimg, t->tune.rev_threads, t->tune.rev_pair == 1, st); break;
+        case 9: rc = launch_deidrj_rev<9>(D, nimg, t->tune.rev_threads, t->tune.rev_pair == 1, st); break;
         case 10: rc = launch_deidrj_rev<10>(D, nimg, t->tune.rev_threads, t->tune.rev_pair == 1, st); break;
+        case 11: rc = launch_deidrj_rev<11>(D, nimg, t->tune.rev_threads, t->tune.rev_pair == 1, st); break;
         case 12: rc = launch_deidrj_rev<12>(D, nimg, t->tune.rev_threads, t->tune.rev_pair == 1, st); break;
         default: {
             const size_t smd = sizeof(float) * rootpq_floats(t->ldim) +
@@ -1691,7 +1695,9 @@ extern "C" int so4_utot32(const so4_tables *t, const so4_params *p, int natoms, 
         case 6: rc = launch_utot_rc<6>(A, t->tune.utot_warps, st); break;
         case 7: rc = launch_utot_rc<7>(A, t->tune.utot_warps, st); break;
         case 8: rc = launch_utot_rc<8>(A, t->tune.utot_warps, st); break;
+        case 9: rc = launch_utot_rc<9>(A, t->tune.utot_warps, st); break;
         case 10: rc = launch_utot_rc<10>(A, t->tune.utot_warps, st); break;
+        case 11: rc = launch_utot_rc<11>(A, t->tune.utot_warps, st); break;
         case 12: rc = launch_utot_rc<12>(A, t->tune.utot_warps, st); break;
         default: {
             const size_t smu =

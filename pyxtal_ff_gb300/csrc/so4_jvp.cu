@@ -207,7 +207,9 @@ extern "C" int so4_jvp32(const so4_tables *t, const so4_params *p, const int *d_
         case 6: rc = launch_jvp_du<6>(A, st); break;
         case 7: rc = launch_jvp_du<7>(A, st); break;
         case 8: rc = launch_jvp_du<8>(A, st); break;
+        case 9: rc = launch_jvp_du<9>(A, st); break;
         case 10: rc = launch_jvp_du<10>(A, st); break;
+        case 11: rc = launch_jvp_du<11>(A, st); break;
         case 12: rc = launch_jvp_du<12>(A, st); break;
         default: return SO4_ERR_UNSUPPORTED;
     }

@@ -42,9 +42,9 @@ def _ctx(lmax=3, rc=4.5):
     return structs, ptr, p, ctx, x
 
 
-@pytest.mark.parametrize("lmax", [1.5, 2, 2.5, 3, 3.5, 4])
+@pytest.mark.parametrize("lmax", [1.5, 2, 2.5, 3, 3.5, 4, 4.5, 5.5])
 def test_jvp_matches_oracle_dxdr_and_rdxdr(cuda_device, lmax):
-    # half-integer lmax (SNAP's odd twol) runs the same row-chain kernels at twol 3, 5, 7
+    # half-integer lmax (SNAP's odd twol) runs the same row-chain kernels at twol 3 to 11
     rc = 4.5
     structs, ptr, p, ctx, _ = _ctx(lmax, rc)
     N, S_ = ctx.nb.natoms, ctx.nb.nstruct
